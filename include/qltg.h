@@ -1,0 +1,203 @@
+/*
+ * qltg.h - C ABI of the GB300-native block-sparse hot path of TensorToolkit (qlten).
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an int
+ * status (QLTG_OK = 0) and never exits the process. Device buffers are raw CUDA device
+ * pointers holding a tensor's raw data in the reference's BlockSparseDataTensor layout:
+ * blocks in ascending block index, each block row-major over its degeneracy dims, at
+ * cumulative offsets (reference qltensor/blk_spar_data_ten/blk_spar_data_ten.h:53-572,
+ * data_blk_operations.h:137-145). Complex data is interleaved (re, im) doubles, i.e.
+ * std::complex<double>. Streams are passed as `void*` (a cudaStream_t, NULL = legacy
+ * default stream).
+ *
+ * Ownership: callers own every tensor buffer they pass in. The library owns plans,
+ * workspaces, CUDA graphs and the outputs of decompositions (freed with the matching
+ * *_destroy call). Calls on one context are not thread-safe; use one context per thread.
+ */
+#ifndef QLTG_H_
+#define QLTG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define QLTG_API __attribute__((visibility("default")))
+#else
+#define QLTG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+enum {
+  QLTG_OK = 0,
+  QLTG_ERR_INVALID = 1,      /* malformed descriptor, axes or argument */
+  QLTG_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  QLTG_ERR_OOM = 3,          /* device allocation failed */
+  QLTG_ERR_TIMEOUT = 4,      /* a bounded device-side wait expired */
+  QLTG_ERR_NOCONV = 5,       /* an iterative decomposition did not converge */
+  QLTG_ERR_EMPTY_SVD = 6,    /* no block fits lqndiv: reference EmptySVDResultError */
+  QLTG_ERR_UNSUPPORTED = 7   /* valid input outside what this build implements */
+};
+
+enum { QLTG_F64 = 0, QLTG_C128 = 1 };     /* element types */
+enum { QLTG_IN = 0, QLTG_OUT = 1 };       /* TenIndexDirType */
+
+/* Arithmetic of a contraction.
+ * QLTG_MODE_FP64:  plain FP64 (DMMA / DFMA), the reference's precision.
+ * QLTG_MODE_SPLIT: FP64 emulated with BF16 slices on the tcgen05 tensor cores, FP32
+ *                  accumulation, FP64 recombination; relative error <= 1e-12 of the
+ *                  FP64 result (stated per call by qltg_ctrct_last_error_bound). */
+enum { QLTG_MODE_FP64 = 0, QLTG_MODE_SPLIT = 1 };
+
+/* ---------------------------------------------------------------- descriptors */
+/* Metadata of one block-sparse tensor (QLTensor indexes + block map). All arrays are
+ * host memory borrowed for the duration of the call.
+ * Mirrors: Index / QNSector (reference qltensor/index.h:45-229, qltensor/qnsct.h:34-139)
+ * and the block map of BlockSparseDataTensor (blk_spar_data_ten.h:53-572). */
+typedef struct qltg_tensor_desc {
+  int32_t rank;
+  int32_t dtype;            /* QLTG_F64 or QLTG_C128 */
+  int32_t qn_ncomp;         /* integer components of one quantum number (U1QN: 1, fU1U1QN: 2) */
+  int32_t parity_comp;      /* QN component whose oddness is the fermion parity; -1 = bosonic */
+  const int32_t* dirs;      /* [rank]  QLTG_IN / QLTG_OUT */
+  const int32_t* nsct;      /* [rank]  sectors per leg */
+  const int32_t* qns;       /* [sum(nsct) * qn_ncomp] sector quantum numbers, leg by leg */
+  const int64_t* dims;      /* [sum(nsct)] sector degeneracies, leg by leg */
+  int64_t nblk;             /* stored blocks */
+  const int64_t* coords;    /* [nblk * rank] sector coordinates, ascending block index */
+} qltg_tensor_desc;
+
+/* ---------------------------------------------------------------- context */
+typedef struct qltg_ctx qltg_ctx;
+
+/* Bind a context to CUDA device `device`. Replaces the reference's process-wide
+ * cuBLAS/cuSOLVER/cuTENSOR handle singletons (framework/hp_numeric/gpu_set.h:30-192). */
+QLTG_API int qltg_create(int device, qltg_ctx** ctx);
+QLTG_API int qltg_destroy(qltg_ctx* ctx);
+
+/* Message of the last failing call on this thread (never NULL). */
+QLTG_API const char* qltg_last_error(void);
+
+/* ---------------------------------------------------------------- contraction */
+typedef struct qltg_ctrct_plan qltg_ctrct_plan;
+
+/* Plan C = A . B over axes_a[i] <-> axes_b[i] (i < naxes). Replaces the constructor of
+ * TensorContractionExecutor (reference tensor_manipulation/ten_ctrct.h:177-217): saved
+ * axes, transpose orders, result legs = saved A legs ++ saved B legs, and the sector
+ * pairing / task list of BlockSparseDataTensor::DataBlkGenForTenCtrct
+ * (qltensor/blk_spar_data_ten/data_blk_operations.h:411-578), computed on the device.
+ * Contracted legs must be inverse to each other (same sectors, opposite direction). */
+QLTG_API int qltg_ctrct_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* a, const qltg_tensor_desc* b,
+                           const int64_t* axes_a, const int64_t* axes_b, int32_t naxes,
+                           qltg_ctrct_plan** plan);
+
+/* Result topology: rank, number of blocks and raw-data size (elements) of C. */
+QLTG_API int qltg_ctrct_plan_result(const qltg_ctrct_plan* plan, int32_t* rank, int64_t* nblk, int64_t* size);
+
+/* C's block coordinates [nblk * rank] and offsets [nblk] (either may be NULL). The legs of
+ * C are the saved legs of A followed by the saved legs of B, in order. */
+QLTG_API int qltg_ctrct_plan_result_blocks(const qltg_ctrct_plan* plan, int64_t* coords, int64_t* offsets);
+
+/* The task list in the reference's generation order (A blocks outer, B blocks inner),
+ * 8 int64 per task: a_blk_idx, b_blk_idx, c_blk_idx, m, k, n, fermion sign (+-1),
+ * beta (0 for the task that creates its output block). `tasks` may be NULL to query
+ * *ntasks only. Mirrors RawDataCtrctTask (raw_data_operation_tasks.h:196-248). */
+QLTG_API int qltg_ctrct_plan_tasks(const qltg_ctrct_plan* plan, int64_t* ntasks, int64_t* tasks);
+
+/* Algorithmic FLOPs (sum of 2mkn, 8mkn for complex) and the bytes of A, B and C. */
+QLTG_API int qltg_ctrct_plan_stats(const qltg_ctrct_plan* plan, double* flops, double* bytes);
+
+/* Execute: c_dev (C's raw buffer, size from qltg_ctrct_plan_result) = A . B.
+ * Replaces BlockSparseDataTensor::CtrctTwoBSDTAndAssignIn (global_operations.h:895-992):
+ * per-block transposes, then one persistent grouped GEMM over all tasks, each output tile
+ * accumulating all of its tasks before a single store. Asynchronous on `stream`. */
+QLTG_API int qltg_ctrct_exec(qltg_ctrct_plan* plan, const void* a_dev, const void* b_dev, void* c_dev,
+                    int32_t mode, void* stream);
+
+/* The two stages of qltg_ctrct_exec, separately, for profiling: stage 1 runs only the
+ * operand transposes into the plan's scratch, stage 2 only the grouped GEMM (reading the
+ * operands left by the last stage-1 call on this plan), stage 0 both. */
+QLTG_API int qltg_ctrct_exec_stage(qltg_ctrct_plan* plan, const void* a_dev, const void* b_dev, void* c_dev,
+                                   int32_t mode, int32_t stage, void* stream);
+
+QLTG_API int qltg_ctrct_plan_destroy(qltg_ctrct_plan* plan);
+
+/* ---------------------------------------------------------------- transpose */
+/* dst = A transposed to leg order `perm` (new leg i = old leg perm[i]), blocks reordered to
+ * ascending block index of the permuted tensor, each block multiplied by its fermionic
+ * exchange sign when the tensor is fermionic. Mirrors QLTensor::Transpose /
+ * BlockSparseDataTensor::Transpose (qltensor/qltensor_impl.h:448-464,
+ * global_operations.h:393-441) with DataBlk sign from FermionicInplaceReorder
+ * (utility/utils_inl.h:52-75). dst must hold the same number of elements as src. */
+QLTG_API int qltg_transpose(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev,
+                   const int32_t* perm, void* dst_dev, void* stream);
+
+/* ---------------------------------------------------------------- two-site matvec */
+typedef struct qltg_matvec qltg_matvec;
+
+/* Plan and capture (one CUDA graph) the two-site effective-Hamiltonian product
+ *   t1 = lenv.psi {{0},{0}};  t2 = t1.mpo1 {{0,2},{0,1}};
+ *   t3 = t2.mpo2 {{4,1},{0,1}};  out = t3.renv {{4,1},{1,0}}
+ * exactly as the reference's chain (tests/test_tensor_manipulation/test_ten_ctrct_1sct.cc:253-257).
+ * The operator buffers must stay valid and unchanged while the matvec lives. */
+QLTG_API int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* lenv_dev,
+                       const qltg_tensor_desc* psi, const qltg_tensor_desc* mpo1, const void* mpo1_dev,
+                       const qltg_tensor_desc* mpo2, const void* mpo2_dev,
+                       const qltg_tensor_desc* renv, const void* renv_dev, int32_t mode, void* stream,
+                       qltg_matvec** mv);
+
+/* Topology of the result (rank 4: a', s1', s2', r'). */
+QLTG_API int qltg_matvec_result(const qltg_matvec* mv, int64_t* nblk, int64_t* size);
+QLTG_API int qltg_matvec_result_blocks(const qltg_matvec* mv, int64_t* coords, int64_t* offsets);
+
+/* Algorithmic FLOPs of one product and the number of kernel launches in its graph. */
+QLTG_API int qltg_matvec_stats(const qltg_matvec* mv, double* flops, int64_t* launches);
+
+/* out_dev = H_eff . psi_dev (one graph launch on `stream`). */
+QLTG_API int qltg_matvec_apply(qltg_matvec* mv, const void* psi_dev, void* out_dev, void* stream);
+
+QLTG_API int qltg_matvec_destroy(qltg_matvec* mv);
+
+/* ---------------------------------------------------------------- decompositions */
+typedef struct qltg_decomp qltg_decomp;
+
+/* Truncated block SVD: T (legs 0..ldims-1 | ldims..rank-1) = U S Vt, mirroring
+ * qlten::SVD (tensor_manipulation/ten_decomp/ten_svd.h:244-263): block-matrices grouped by
+ * (left flux, right flux) (ten_decomp/ten_decomp_basic.h:68-106), all block-matrices
+ * decomposed in one batched one-sided Jacobi launch, truncation keeping from Dmin while
+ * the kept weight <= (1 - trunc_err) of the total and <= Dmax (ten_svd.h:281-372),
+ * U with a new OUT leg, S = (IN, OUT) diagonal, Vt with a new IN leg (ten_svd.h:467-582).
+ * `lqndiv` has qn_ncomp components. Returns QLTG_ERR_EMPTY_SVD when nothing is kept. */
+QLTG_API int qltg_svd(qltg_ctx* ctx, const qltg_tensor_desc* t, const void* t_dev, int32_t ldims,
+             const int32_t* lqndiv, double trunc_err, int64_t dmin, int64_t dmax, void* stream,
+             qltg_decomp** out);
+
+/* Block QR: T = Q R (Householder, one batched launch), mirroring qlten::QR
+ * (tensor_manipulation/ten_decomp/ten_qr.h:152-162): mid leg dim min(rows, cols) per
+ * block-matrix, Q with a new OUT leg, R with a new IN leg, LAPACK sign convention. */
+QLTG_API int qltg_qr(qltg_ctx* ctx, const qltg_tensor_desc* t, const void* t_dev, int32_t ldims,
+            const int32_t* lqndiv, void* stream, qltg_decomp** out);
+
+/* SVD: actual truncation error and kept dimension D (QR: 0 and the mid dimension). */
+QLTG_API int qltg_decomp_info(const qltg_decomp* d, double* trunc_err, int64_t* kept_dim);
+
+/* Result tensors: SVD which = 0 U, 1 S, 2 Vt; QR which = 0 Q, 1 R.
+ * info[0..5] = rank, qn_ncomp, dtype, nblk, size, total sectors. */
+QLTG_API int qltg_decomp_tensor_info(const qltg_decomp* d, int32_t which, int64_t* info);
+
+/* Copy the metadata of a result tensor into caller arrays sized from the info call and
+ * return its library-owned device buffer in *dev (valid until qltg_decomp_destroy). */
+QLTG_API int qltg_decomp_tensor_export(const qltg_decomp* d, int32_t which, int32_t* dirs, int32_t* nsct,
+                              int32_t* qns, int64_t* dims, int64_t* coords, int64_t* offsets,
+                              const void** dev);
+
+QLTG_API int qltg_decomp_destroy(qltg_decomp* d);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* QLTG_H_ */

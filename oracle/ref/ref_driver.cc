@@ -1,0 +1,279 @@
+// Runs the reference implementation (header-only qlten, CPU path) on synthetic inputs
+// from tensortoolkit_gb300/csrc/synth.h and writes inputs, task lists and results to a
+// QTB1 file. Built only where the reference sources are present, by oracle/ref/Makefile;
+// its outputs pin the CPU restatement (oracle/oracle.cc) and become the committed golden
+// fixtures under tests/golden/. Test infrastructure only.
+//
+// Usage: ref_driver <case> <out.qtb> [args...]
+//   cfg1                          Contract(A, B, {{2},{0}}) of the rank-3 U(1) case
+//   matvec_u1 qmax sigma D seed   four-step two-site chain, U(1), FP64
+//   matvec_f half D seed          four-step chain, fermionic U(1)xU(1), complex128
+//   ctrct_misc seed               extra axis patterns incl. scalar results and IN-leg contractions
+//   svd_u1 qmax sigma D seed trunc Dmin Dmax   SVD of a spectrum-controlled psi (ldims 2)
+//   svd_stress nb lo hi seed trunc Dmin Dmax   SVD of a rank-2 block-diagonal tensor
+//   svd_f half D seed trunc Dmin Dmax          SVD of a fermionic complex psi
+//   qr_u1 qmax sigma D seed                     QR of psi (ldims 2)
+//   qr_f half D seed                            QR of a fermionic complex psi
+//   time_matvec_u1 qmax sigma D seed threads iters   wall time of the chain (no dump)
+#include "qlten/qlten.h"
+#include "synth.h"
+#include "../qtb_io.h"
+
+#include <chrono>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+using namespace qlten;
+using qlten::special_qn::U1QN;
+using qlten::special_qn::fU1U1QN;
+namespace sy = qltg_synth;
+
+template <typename QNT> QNT make_qn(const int32_t* q);
+template <> U1QN make_qn<U1QN>(const int32_t* q) { return U1QN(q[0]); }
+template <> fU1U1QN make_qn<fU1U1QN>(const int32_t* q) { return fU1U1QN(q[0], q[1]); }
+
+template <typename QNT> constexpr int qn_ncomp() { return std::is_same<QNT, U1QN>::value ? 1 : 2; }
+
+template <typename QNT>
+Index<QNT> to_index(const sy::Leg& l) {
+  std::vector<QNSector<QNT>> s;
+  for (int64_t i = 0; i < l.nsct(); ++i) s.emplace_back(make_qn<QNT>(&l.qns[i * l.ncomp]), (size_t)l.dims[i]);
+  return Index<QNT>(s, l.dir == sy::DIR_IN ? TenIndexDirType::IN : TenIndexDirType::OUT);
+}
+
+template <typename ElemT, typename QNT>
+QLTensor<ElemT, QNT> to_qlten(const sy::Tensor& t) {
+  IndexVec<QNT> idx;
+  for (auto& l : t.legs) idx.push_back(to_index<QNT>(l));
+  QLTensor<ElemT, QNT> q(idx);
+  std::vector<int32_t> zero(qn_ncomp<QNT>(), 0);
+  q.Fill(make_qn<QNT>(zero.data()), ElemT(0));
+  auto& bsdt = q.GetBlkSparDataTen();
+  const auto& blks = bsdt.GetBlkIdxDataBlkMap();
+  if ((int64_t)blks.size() != t.nblk()) throw std::runtime_error("block count mismatch");
+  int64_t b = 0;
+  for (auto& kv : blks) {
+    if ((int64_t)kv.second.data_offset != t.offsets[b]) throw std::runtime_error("offset mismatch");
+    for (int i = 0; i < t.rank(); ++i)
+      if ((int64_t)kv.second.blk_coors[i] != t.coords[b * t.rank() + i]) throw std::runtime_error("coords mismatch");
+    ++b;
+  }
+  if ((int64_t)bsdt.GetActualRawDataSize() != t.size) throw std::runtime_error("size mismatch");
+  std::memcpy(bsdt.GetActualRawDataPtr(), t.data.data(), t.data.size() * sizeof(double));
+  return q;
+}
+
+template <typename ElemT, typename QNT>
+void dump(qtb::Writer& w, const std::string& name, const QLTensor<ElemT, QNT>& t) {
+  const auto& idxs = t.GetIndexes();
+  std::vector<int32_t> dirs, nsct, qns;
+  std::vector<int64_t> dims;
+  for (auto& ix : idxs) {
+    dirs.push_back(ix.GetDir() == TenIndexDirType::IN ? sy::DIR_IN : sy::DIR_OUT);
+    nsct.push_back((int32_t)ix.GetQNSctNum());
+    for (auto& s : ix.GetQNScts()) {
+      for (int k = 0; k < qn_ncomp<QNT>(); ++k) qns.push_back(s.GetQn().GetQNVal(k).GetVal());
+      dims.push_back((int64_t)s.GetDegeneracy());
+    }
+  }
+  w.i32(name + ".dirs", dirs);
+  w.i32(name + ".nsct", nsct);
+  w.i32(name + ".qns", qns);
+  w.i64(name + ".dims", dims);
+  w.scalar_i64(name + ".ncomp", qn_ncomp<QNT>());
+  const auto& bsdt = t.GetBlkSparDataTen();
+  std::vector<int64_t> coords, offsets;
+  for (auto& kv : bsdt.GetBlkIdxDataBlkMap()) {
+    for (auto c : kv.second.blk_coors) coords.push_back((int64_t)c);
+    offsets.push_back((int64_t)kv.second.data_offset);
+  }
+  w.i64(name + ".coords", coords);
+  w.i64(name + ".offsets", offsets);
+  size_t n = bsdt.GetActualRawDataSize();
+  if (t.IsScalar() && n == 0) n = 0;
+  const double* p = reinterpret_cast<const double*>(bsdt.GetActualRawDataPtr());
+  const size_t per = std::is_same<ElemT, double>::value ? 1 : 2;
+  std::vector<double> data(p ? p : nullptr, p ? p + n * per : nullptr);
+  w.f64(name + ".data", data);
+}
+
+// The task list the reference would execute: DataBlkGenForTenCtrct then
+// SortTasksByCBlkIdx, as TensorContractionExecutor and CtrctTwoBSDTAndAssignIn do
+// (tensor_manipulation/ten_ctrct.h:177-235; global_operations.h:895-992).
+template <typename ElemT, typename QNT>
+void dump_tasks(qtb::Writer& w, const std::string& name, const QLTensor<ElemT, QNT>& a,
+                const QLTensor<ElemT, QNT>& b, const std::vector<std::vector<size_t>>& axes) {
+  auto saved = TenCtrctGenSavedAxesSet(a.Rank(), b.Rank(), axes);
+  QLTensor<ElemT, QNT> c;
+  TenCtrctInitResTen(&a, &b, saved, &c);
+  auto tasks = c.GetBlkSparDataTen().DataBlkGenForTenCtrct(a.GetBlkSparDataTen(), b.GetBlkSparDataTen(), axes, saved);
+  std::vector<int64_t> gen;   // generation order (a_blk, b_blk, c_blk, m, k, n, sign, beta)
+  for (auto& t : tasks) {
+    gen.insert(gen.end(), {(int64_t)t.a_blk_idx, (int64_t)t.b_blk_idx, (int64_t)t.c_blk_idx, (int64_t)t.m,
+                           (int64_t)t.k, (int64_t)t.n, (int64_t)t.f_ex_sign, (int64_t)t.beta});
+  }
+  w.put(name + ".tasks", 1, {tasks.size(), 8}, gen.data(), 8);
+}
+
+template <typename ElemT, typename QNT>
+void contract_case(qtb::Writer& w, const std::string& tag, const QLTensor<ElemT, QNT>& a,
+                   const QLTensor<ElemT, QNT>& b, const std::vector<std::vector<size_t>>& axes,
+                   QLTensor<ElemT, QNT>* out = nullptr) {
+  std::vector<int64_t> ax;
+  for (auto x : axes[0]) ax.push_back((int64_t)x);
+  for (auto x : axes[1]) ax.push_back((int64_t)x);
+  w.i64(tag + ".axes", ax);
+  dump(w, tag + ".A", a);
+  dump(w, tag + ".B", b);
+  dump_tasks(w, tag, a, b, axes);
+  QLTensor<ElemT, QNT> c;
+  Contract(&a, &b, axes, &c);
+  dump(w, tag + ".C", c);
+  if (out) *out = c;
+}
+
+template <typename ElemT, typename QNT>
+void matvec_case(qtb::Writer& w, const sy::Matvec& mv) {
+  auto L = to_qlten<ElemT, QNT>(mv.lenv);
+  auto P = to_qlten<ElemT, QNT>(mv.psi);
+  auto W1 = to_qlten<ElemT, QNT>(mv.mpo1);
+  auto W2 = to_qlten<ElemT, QNT>(mv.mpo2);
+  auto R = to_qlten<ElemT, QNT>(mv.renv);
+  QLTensor<ElemT, QNT> t1, t2, t3, out;
+  contract_case(w, "s1", L, P, {{0}, {0}}, &t1);
+  contract_case(w, "s2", t1, W1, {{0, 2}, {0, 1}}, &t2);
+  contract_case(w, "s3", t2, W2, {{4, 1}, {0, 1}}, &t3);
+  contract_case(w, "s4", t3, R, {{4, 1}, {1, 0}}, &out);
+}
+
+template <typename ElemT, typename QNT>
+void svd_case(qtb::Writer& w, const sy::Tensor& st, size_t ldims, double trunc, size_t dmin, size_t dmax) {
+  auto t = to_qlten<ElemT, QNT>(st);
+  dump(w, "T", t);
+  std::vector<int32_t> zero(qn_ncomp<QNT>(), 0);
+  QLTensor<ElemT, QNT> u, vt;
+  QLTensor<QLTEN_Double, QNT> s;
+  double err = 0;
+  size_t D = 0;
+  SVD(&t, ldims, make_qn<QNT>(zero.data()), trunc, dmin, dmax, &u, &s, &vt, &err, &D);
+  dump(w, "U", u);
+  dump(w, "S", s);
+  dump(w, "Vt", vt);
+  w.scalar_f64("err", err);
+  w.scalar_i64("D", (int64_t)D);
+  w.scalar_i64("ldims", (int64_t)ldims);
+  w.scalar_f64("trunc", trunc);
+  w.scalar_i64("Dmin", (int64_t)dmin);
+  w.scalar_i64("Dmax", (int64_t)dmax);
+}
+
+template <typename ElemT, typename QNT>
+void qr_case(qtb::Writer& w, const sy::Tensor& st, size_t ldims) {
+  auto t = to_qlten<ElemT, QNT>(st);
+  dump(w, "T", t);
+  std::vector<int32_t> zero(qn_ncomp<QNT>(), 0);
+  QLTensor<ElemT, QNT> q, r;
+  QR(&t, ldims, make_qn<QNT>(zero.data()), &q, &r);
+  dump(w, "Q", q);
+  dump(w, "R", r);
+  w.scalar_i64("ldims", (int64_t)ldims);
+}
+
+static sy::Tensor random_like(const std::vector<sy::Leg>& legs, const std::vector<int32_t>& div, bool cplx,
+                              sy::Normal& rng) {
+  auto t = sy::make_tensor(legs, div, cplx);
+  sy::fill_normal(t, rng);
+  return t;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) { std::fprintf(stderr, "usage: ref_driver <case> <out> [args]\n"); return 2; }
+  std::string cs = argv[1];
+  auto A = [&](int i) { return std::string(argv[i]); };
+  try {
+    if (cs == "time_matvec_u1") {
+      auto mv = sy::heisenberg_u1_random(std::stoi(A(2)), std::stod(A(3)), std::stoll(A(4)), std::stoull(A(5)));
+      hp_numeric::SetTensorManipulationThreads(std::stoi(A(6)));
+      int iters = std::stoi(A(7));
+      auto L = to_qlten<double, U1QN>(mv.lenv);
+      auto P = to_qlten<double, U1QN>(mv.psi);
+      auto W = to_qlten<double, U1QN>(mv.mpo1);
+      auto R = to_qlten<double, U1QN>(mv.renv);
+      for (int it = 0; it < iters; ++it) {
+        auto t0 = std::chrono::steady_clock::now();
+        QLTensor<double, U1QN> t1, t2, t3, out;
+        Contract(&L, &P, {{0}, {0}}, &t1);
+        Contract(&t1, &W, {{0, 2}, {0, 1}}, &t2);
+        Contract(&t2, &W, {{4, 1}, {0, 1}}, &t3);
+        Contract(&t3, &R, {{4, 1}, {1, 0}}, &out);
+        double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        std::printf("iter %d %.6f s\n", it, dt);
+      }
+      return 0;
+    }
+    qtb::Writer w(argv[2]);
+    if (cs == "cfg1") {
+      auto p = sy::config1(0);
+      contract_case(w, "c", to_qlten<double, U1QN>(p.a), to_qlten<double, U1QN>(p.b), {{2}, {0}});
+    } else if (cs == "matvec_u1") {
+      auto mv = sy::heisenberg_u1_random(std::stoi(A(3)), std::stod(A(4)), std::stoll(A(5)), std::stoull(A(6)));
+      matvec_case<double, U1QN>(w, mv);
+    } else if (cs == "matvec_u1h") {
+      auto mv = sy::heisenberg_u1_hermitian(std::stoi(A(3)), std::stod(A(4)), std::stoll(A(5)), std::stoull(A(6)));
+      matvec_case<double, U1QN>(w, mv);
+    } else if (cs == "matvec_f") {
+      auto mv = sy::hubbard_u1u1(std::stoi(A(3)), std::stoll(A(4)), std::stoull(A(5)));
+      matvec_case<std::complex<double>, fU1U1QN>(w, mv);
+    } else if (cs == "ctrct_misc") {
+      sy::Normal rng(std::stoull(A(3)));
+      // U(1): scalar result (full contraction), two-leg contraction with transposed B,
+      // contraction over a middle leg.
+      auto mv = sy::heisenberg_u1_random(3, 1.5, 20, std::stoull(A(3)));
+      auto P = to_qlten<double, U1QN>(mv.psi);
+      std::vector<sy::Leg> inv;
+      for (auto& l : mv.psi.legs) inv.push_back(l.inverse());
+      auto Pd = to_qlten<double, U1QN>(random_like(inv, {0}, false, rng));
+      contract_case(w, "u_scalar", P, Pd, {{0, 1, 2, 3}, {0, 1, 2, 3}});
+      contract_case(w, "u_perm", P, Pd, {{3, 1}, {3, 1}});
+      auto L = to_qlten<double, U1QN>(mv.lenv);
+      contract_case(w, "u_mid", L, P, {{2}, {3}});
+      // Fermionic U(1)xU(1) complex: IN-direction contracted legs, several axis orders.
+      auto fm = sy::hubbard_u1u1(1, 6, std::stoull(A(3)));
+      auto FP = to_qlten<std::complex<double>, fU1U1QN>(fm.psi);
+      std::vector<sy::Leg> finv;
+      for (auto& l : fm.psi.legs) finv.push_back(l.inverse());
+      auto FPd = to_qlten<std::complex<double>, fU1U1QN>(random_like(finv, {0, 0}, true, rng));
+      contract_case(w, "f_scalar", FP, FPd, {{0, 1, 2, 3}, {0, 1, 2, 3}});
+      contract_case(w, "f_in", FP, FPd, {{0, 2}, {0, 2}});
+      contract_case(w, "f_rev", FP, FPd, {{3, 1, 0}, {3, 1, 0}});
+      auto FL = to_qlten<std::complex<double>, fU1U1QN>(fm.lenv);
+      auto FW = to_qlten<std::complex<double>, fU1U1QN>(fm.mpo1);
+      contract_case(w, "f_env", FL, FP, {{2}, {0}});
+      contract_case(w, "f_mpo", FW, FW, {{3}, {0}});
+    } else if (cs == "svd_u1") {
+      auto t = sy::svd_psi(std::stoi(A(3)), std::stod(A(4)), std::stoll(A(5)), std::stoull(A(6)));
+      svd_case<double, U1QN>(w, t, 2, std::stod(A(7)), std::stoull(A(8)), std::stoull(A(9)));
+    } else if (cs == "svd_stress") {
+      auto t = sy::svd_stress(std::stoi(A(3)), std::stoll(A(4)), std::stoll(A(5)), std::stoull(A(6)));
+      svd_case<double, U1QN>(w, t, 1, std::stod(A(7)), std::stoull(A(8)), std::stoull(A(9)));
+    } else if (cs == "svd_f") {
+      auto mv = sy::hubbard_u1u1(std::stoi(A(3)), std::stoll(A(4)), std::stoull(A(5)));
+      svd_case<std::complex<double>, fU1U1QN>(w, mv.psi, 2, std::stod(A(6)), std::stoull(A(7)), std::stoull(A(8)));
+    } else if (cs == "qr_u1") {
+      auto mv = sy::heisenberg_u1_random(std::stoi(A(3)), std::stod(A(4)), std::stoll(A(5)), std::stoull(A(6)));
+      qr_case<double, U1QN>(w, mv.psi, 2);
+    } else if (cs == "qr_f") {
+      auto mv = sy::hubbard_u1u1(std::stoi(A(3)), std::stoll(A(4)), std::stoull(A(5)));
+      qr_case<std::complex<double>, fU1U1QN>(w, mv.psi, 2);
+    } else {
+      std::fprintf(stderr, "unknown case %s\n", cs.c_str());
+      return 2;
+    }
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "ref_driver: %s\n", e.what());
+    return 1;
+  }
+  return 0;
+}

@@ -1,0 +1,21 @@
+"""GB300-native block-sparse hot path of TensorToolkit (qlten): Contract, SVD, QR and the
+two-site H*psi matvec, computed by hand-written sm_103a CUDA kernels in libqltg.so behind
+the C ABI declared in include/qltg.h.
+
+Submodules:
+  tensor     host-side block-sparse metadata (BSTensor, Leg)
+  capi       ctypes declarations of the C ABI
+  api        Contract / Transpose / SVD / QR / Matvec over device-resident tensors
+  lanczos    Lanczos ground-state solver driving the captured matvec
+  workloads  deterministic synthetic workloads with the reference's shapes
+"""
+from .tensor import BSTensor, Leg, IN, OUT  # noqa: F401
+
+_API = {"Contract", "ContractionPlan", "Transpose", "SVD", "QR", "Matvec", "DTensor", "Context", "context"}
+
+
+def __getattr__(name):
+    if name in _API:
+        from . import api
+        return getattr(api, name)
+    raise AttributeError(name)

@@ -1,0 +1,328 @@
+"""User-facing Python API over the C ABI, with the reference's names and semantics.
+
+`Contract`, `SVD`, `QR` and `Transpose` take and return `DTensor`s: block-sparse tensors
+whose metadata lives on the host (`BSTensor`) and whose raw buffer lives in HBM (a torch
+CUDA tensor used only as device storage). Every computation runs in libqltg.so; nothing
+here falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import capi
+from .capi import check, lib
+from .tensor import BSTensor, Leg
+
+MODES = {"fp64": capi.QLTG_MODE_FP64, "split": capi.QLTG_MODE_SPLIT}
+
+
+def _mode(m) -> int:
+    return MODES[m] if isinstance(m, str) else int(m)
+
+
+class Context:
+    """A qltg context bound to one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        h = C.c_void_p()
+        check(lib().qltg_create(device, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().qltg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_ctx = {}
+
+
+def context(device: int = 0) -> Context:
+    if device not in _ctx:
+        _ctx[device] = Context(device)
+    return _ctx[device]
+
+
+def stream_ptr(device: int = 0) -> C.c_void_p:
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+class _Desc:
+    """A TensorDesc plus the numpy arrays it points into."""
+
+    def __init__(self, t: BSTensor):
+        self.dirs, self.nsct, self.qns, self.dims = t.meta_arrays()
+        self.coords = np.ascontiguousarray(t.coords.reshape(-1), dtype=np.int64)
+        p = lambda a: a.ctypes.data if a.size else None
+        self.s = capi.TensorDesc(t.rank, capi.QLTG_C128 if t.is_complex else capi.QLTG_F64, t.ncomp,
+                                 t.parity_comp, p(self.dirs), p(self.nsct), p(self.qns), p(self.dims),
+                                 t.nblk if t.rank else (1 if t.size else 0), p(self.coords))
+
+    @property
+    def ref(self):
+        return C.byref(self.s)
+
+
+class DTensor:
+    """Block-sparse tensor with its raw buffer resident on a CUDA device."""
+
+    def __init__(self, meta: BSTensor, buf: torch.Tensor):
+        n = meta.size * (2 if meta.is_complex else 1)
+        if buf.dtype != torch.float64 or buf.numel() < n or not buf.is_cuda:
+            raise ValueError("raw buffer must be a CUDA float64 tensor of the layout's size")
+        self.meta = meta
+        self.buf = buf
+
+    @staticmethod
+    def empty(meta: BSTensor, device: int = 0) -> "DTensor":
+        n = meta.size * (2 if meta.is_complex else 1)
+        return DTensor(meta, torch.empty(max(n, 1), dtype=torch.float64, device=f"cuda:{device}"))
+
+    @staticmethod
+    def from_host(t: BSTensor, device: int = 0) -> "DTensor":
+        meta = BSTensor(t.legs, t.coords, t.dtype, None, offsets=t.offsets, size=t.size)
+        d = DTensor.empty(meta, device)
+        if t.size:
+            d.buf[: t.size * (2 if t.is_complex else 1)].copy_(torch.from_numpy(t.raw_f64()))
+        return d
+
+    def to_host(self) -> BSTensor:
+        n = self.meta.size * (2 if self.meta.is_complex else 1)
+        raw = self.buf[:n].cpu().numpy()
+        data = raw.view(np.complex128) if self.meta.is_complex else raw
+        return BSTensor(self.meta.legs, self.meta.coords, self.meta.dtype, data.copy(),
+                        offsets=self.meta.offsets, size=self.meta.size)
+
+    @property
+    def ptr(self) -> int:
+        return self.buf.data_ptr()
+
+    @property
+    def device(self) -> int:
+        return self.buf.device.index
+
+
+class ContractionPlan:
+    """Planned C = A . B (device sector pairing once, execute many times)."""
+
+    def __init__(self, a: BSTensor, b: BSTensor, axes: Sequence[Sequence[int]], device: int = 0):
+        self.ctx = context(device)
+        self.device = device
+        self.axes = (tuple(int(x) for x in axes[0]), tuple(int(x) for x in axes[1]))
+        da, db = _Desc(a), _Desc(b)
+        axa = np.asarray(self.axes[0], np.int64)
+        axb = np.asarray(self.axes[1], np.int64)
+        h = C.c_void_p()
+        check(lib().qltg_ctrct_plan_create(self.ctx.h, da.ref, db.ref, axa.ctypes.data, axb.ctypes.data,
+                                           len(axa), C.byref(h)))
+        self.h = h
+        rank, nblk, size = C.c_int32(), C.c_int64(), C.c_int64()
+        check(lib().qltg_ctrct_plan_result(h, C.byref(rank), C.byref(nblk), C.byref(size)))
+        coords = np.zeros(max(nblk.value * rank.value, 1), np.int64)
+        offs = np.zeros(max(nblk.value, 1), np.int64)
+        check(lib().qltg_ctrct_plan_result_blocks(h, coords.ctypes.data, offs.ctypes.data))
+        sa = [i for i in range(a.rank) if i not in self.axes[0]]
+        sb = [i for i in range(b.rank) if i not in self.axes[1]]
+        legs = [a.legs[i] for i in sa] + [b.legs[i] for i in sb]
+        if rank.value:
+            self.result = BSTensor(legs, coords[: nblk.value * rank.value].reshape(nblk.value, rank.value),
+                                   a.dtype, None, offsets=offs[: nblk.value])
+        else:
+            self.result = BSTensor([], np.zeros((nblk.value, 0), np.int64), a.dtype, None, size=size.value)
+
+    def tasks(self) -> np.ndarray:
+        n = C.c_int64()
+        check(lib().qltg_ctrct_plan_tasks(self.h, C.byref(n), None))
+        out = np.zeros((n.value, 8), np.int64)
+        if n.value:
+            check(lib().qltg_ctrct_plan_tasks(self.h, C.byref(n), out.ctypes.data))
+        return out
+
+    def stats(self) -> Tuple[float, float]:
+        f, b = C.c_double(), C.c_double()
+        check(lib().qltg_ctrct_plan_stats(self.h, C.byref(f), C.byref(b)))
+        return f.value, b.value
+
+    def execute(self, a: DTensor, b: DTensor, out: Optional[DTensor] = None, mode="fp64") -> DTensor:
+        if out is None:
+            out = DTensor.empty(self.result, self.device)
+        check(lib().qltg_ctrct_exec(self.h, C.c_void_p(a.ptr), C.c_void_p(b.ptr), C.c_void_p(out.ptr),
+                                    _mode(mode), stream_ptr(self.device)))
+        return out
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().qltg_ctrct_plan_destroy(self.h)
+        except Exception:
+            pass
+
+
+def Contract(a: DTensor, b: DTensor, axes: Sequence[Sequence[int]], mode="fp64") -> DTensor:
+    """C = A . B, the reference's qlten::Contract (tensor_manipulation/ten_ctrct.h:276-290).
+
+    The result's legs are the saved legs of A followed by the saved legs of B."""
+    plan = ContractionPlan(a.meta, b.meta, axes, a.device)
+    return plan.execute(a, b, mode=mode)
+
+
+def Transpose(t: DTensor, perm: Sequence[int]) -> DTensor:
+    """QLTensor::Transpose with fermionic block signs (qltensor/qltensor_impl.h:448-464)."""
+    perm = [int(x) for x in perm]
+    m = t.meta
+    legs = [m.legs[i] for i in perm]
+    coords = m.coords[:, perm]
+    tmp = BSTensor(legs, np.zeros((0, len(legs)), np.int64), m.dtype, None)
+    idx = np.zeros(m.nblk, np.int64)
+    for l, leg in enumerate(legs):
+        idx = idx * leg.nsct + coords[:, l]
+    order = np.argsort(idx, kind="stable")
+    meta = BSTensor(legs, coords[order], m.dtype, None)
+    out = DTensor.empty(meta, t.device)
+    d = _Desc(m)
+    p = np.asarray(perm, np.int32)
+    check(lib().qltg_transpose(context(t.device).h, d.ref, C.c_void_p(t.ptr), p.ctypes.data,
+                               C.c_void_p(out.ptr), stream_ptr(t.device)))
+    del tmp
+    return out
+
+
+class Matvec:
+    """The two-site effective Hamiltonian H_eff = lenv . mpo1 . mpo2 . renv as one CUDA graph."""
+
+    def __init__(self, lenv: DTensor, psi_meta: BSTensor, mpo1: DTensor, mpo2: DTensor, renv: DTensor,
+                 mode="fp64"):
+        self.device = lenv.device
+        self.ctx = context(self.device)
+        self._keep = (lenv, mpo1, mpo2, renv)
+        ds = [_Desc(x) for x in (lenv.meta, psi_meta, mpo1.meta, mpo2.meta, renv.meta)]
+        h = C.c_void_p()
+        check(lib().qltg_matvec_create(self.ctx.h, ds[0].ref, C.c_void_p(lenv.ptr), ds[1].ref, ds[2].ref,
+                                       C.c_void_p(mpo1.ptr), ds[3].ref, C.c_void_p(mpo2.ptr), ds[4].ref,
+                                       C.c_void_p(renv.ptr), _mode(mode), stream_ptr(self.device), C.byref(h)))
+        self.h = h
+        nblk, size = C.c_int64(), C.c_int64()
+        check(lib().qltg_matvec_result(h, C.byref(nblk), C.byref(size)))
+        coords = np.zeros(max(nblk.value * 4, 1), np.int64)
+        offs = np.zeros(max(nblk.value, 1), np.int64)
+        check(lib().qltg_matvec_result_blocks(h, coords.ctypes.data, offs.ctypes.data))
+        legs = [lenv.meta.legs[2], mpo1.meta.legs[2], mpo2.meta.legs[2], renv.meta.legs[2]]
+        self.result = BSTensor(legs, coords[: nblk.value * 4].reshape(-1, 4), psi_meta.dtype, None,
+                               offsets=offs[: nblk.value])
+
+    def stats(self) -> Tuple[float, int]:
+        f, n = C.c_double(), C.c_int64()
+        check(lib().qltg_matvec_stats(self.h, C.byref(f), C.byref(n)))
+        return f.value, n.value
+
+    def apply(self, psi: DTensor, out: Optional[DTensor] = None) -> DTensor:
+        if out is None:
+            out = DTensor.empty(self.result, self.device)
+        check(lib().qltg_matvec_apply(self.h, C.c_void_p(psi.ptr), C.c_void_p(out.ptr),
+                                      stream_ptr(self.device)))
+        return out
+
+    def apply_raw(self, psi_ptr: int, out_ptr: int, stream: Optional[int] = None) -> None:
+        s = stream_ptr(self.device) if stream is None else C.c_void_p(stream)
+        check(lib().qltg_matvec_apply(self.h, C.c_void_p(psi_ptr), C.c_void_p(out_ptr), s))
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().qltg_matvec_destroy(self.h)
+        except Exception:
+            pass
+
+
+def _decomp_tensors(h, which_list, device: int, dtype_real_for=()):
+    out = []
+    for w in which_list:
+        info = np.zeros(6, np.int64)
+        check(lib().qltg_decomp_tensor_info(h, w, info.ctypes.data))
+        rank, ncomp, dt, nblk, size, ts = (int(x) for x in info)
+        dirs = np.zeros(max(rank, 1), np.int32)
+        nsct = np.zeros(max(rank, 1), np.int32)
+        qns = np.zeros(max(ts * ncomp, 1), np.int32)
+        dims = np.zeros(max(ts, 1), np.int64)
+        coords = np.zeros(max(nblk * rank, 1), np.int64)
+        offs = np.zeros(max(nblk, 1), np.int64)
+        dev = C.c_void_p()
+        check(lib().qltg_decomp_tensor_export(h, w, dirs.ctypes.data, nsct.ctypes.data, qns.ctypes.data,
+                                              dims.ctypes.data, coords.ctypes.data, offs.ctypes.data,
+                                              C.byref(dev)))
+        legs = []
+        qp = dp = 0
+        for l in range(rank):
+            n = int(nsct[l])
+            legs.append(Leg(int(dirs[l]), qns[qp:qp + n * ncomp].reshape(n, ncomp), dims[dp:dp + n],
+                            -1))
+            qp += n * ncomp
+            dp += n
+        meta = BSTensor(legs, coords[: nblk * rank].reshape(nblk, rank),
+                        np.complex128 if dt == capi.QLTG_C128 else np.float64, None,
+                        offsets=offs[:nblk])
+        t = DTensor.empty(meta, device)
+        nel = size * (2 if dt == capi.QLTG_C128 else 1)
+        if nel:
+            # copy out of the library-owned buffer (device to device, stream ordered)
+            t.buf[:nel].copy_(torch.as_tensor(_DevView(dev.value, nel), device=f"cuda:{device}"))
+        out.append(t)
+    return out
+
+
+class _DevView:
+    """A raw float64 device range exposed through __cuda_array_interface__ (no copy)."""
+
+    def __init__(self, ptr: int, n: int):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False),
+                                         "version": 2, "strides": None}
+
+
+def _set_parity(ts, parity_comp):
+    for t in ts:
+        for l in t.meta.legs:
+            l.parity_comp = parity_comp
+    return ts
+
+
+def SVD(t: DTensor, ldims: int, lqndiv: Sequence[int], trunc_err: float, Dmin: int, Dmax: int):
+    """qlten::SVD (tensor_manipulation/ten_decomp/ten_svd.h:244-263) -> (U, S, Vt, err, D)."""
+    d = _Desc(t.meta)
+    div = np.asarray(lqndiv, np.int32)
+    h = C.c_void_p()
+    check(lib().qltg_svd(context(t.device).h, d.ref, C.c_void_p(t.ptr), int(ldims), div.ctypes.data,
+                         float(trunc_err), int(Dmin), int(Dmax), stream_ptr(t.device), C.byref(h)))
+    try:
+        err, D = C.c_double(), C.c_int64()
+        check(lib().qltg_decomp_info(h, C.byref(err), C.byref(D)))
+        u, s, vt = _set_parity(_decomp_tensors(h, (0, 1, 2), t.device), t.meta.parity_comp)
+        torch.cuda.current_stream(t.device).synchronize()
+        return u, s, vt, err.value, D.value
+    finally:
+        lib().qltg_decomp_destroy(h)
+
+
+def QR(t: DTensor, ldims: int, lqndiv: Sequence[int]):
+    """qlten::QR (tensor_manipulation/ten_decomp/ten_qr.h:152-162) -> (Q, R)."""
+    d = _Desc(t.meta)
+    div = np.asarray(lqndiv, np.int32)
+    h = C.c_void_p()
+    check(lib().qltg_qr(context(t.device).h, d.ref, C.c_void_p(t.ptr), int(ldims), div.ctypes.data,
+                        stream_ptr(t.device), C.byref(h)))
+    try:
+        q, r = _set_parity(_decomp_tensors(h, (0, 1), t.device), t.meta.parity_comp)
+        torch.cuda.current_stream(t.device).synchronize()
+        return q, r
+    finally:
+        lib().qltg_decomp_destroy(h)

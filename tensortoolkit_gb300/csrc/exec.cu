@@ -1,0 +1,71 @@
+// Contraction execution: schedule construction after device pairing, and the launch
+// sequence (operand transposes, then one grouped GEMM).
+#include <algorithm>
+
+#include "ctrct.h"
+#include "split.h"
+
+namespace qltg {
+
+void finalize_plan(CtrctPlan& p, cudaStream_t s) {
+  GemmSchedule& g = p.sched;
+  g.tile.clear();
+  struct Cand { GemmTile t; int64_t cost; };
+  std::vector<Cand> cands;
+  for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q) {
+    const GemmCBlk& cb = g.cblk[q];
+    int64_t ksum = 0;
+    for (int32_t t = cb.t0; t < cb.t1; ++t) ksum += g.task[t].k;
+    const int tm = (cb.m + g.bm - 1) / g.bm, tn = (cb.n + g.bn - 1) / g.bn;
+    QLTG_CHECK(tm < 32768 && tn < 32768, QLTG_ERR_UNSUPPORTED, "output block too large for the tile grid");
+    for (int i = 0; i < tm; ++i)
+      for (int j = 0; j < tn; ++j) {
+        const int64_t rows = std::min(g.bm, cb.m - i * g.bm), cols = std::min(g.bn, cb.n - j * g.bn);
+        cands.push_back({GemmTile{q, (int16_t)i, (int16_t)j}, ksum * rows * cols});
+      }
+  }
+  std::stable_sort(cands.begin(), cands.end(), [](const Cand& x, const Cand& y) { return x.cost > y.cost; });
+  g.tile.reserve(cands.size());
+  for (auto& c : cands) g.tile.push_back(c.t);
+  g.d_cblk = upload(g.cblk, s);
+  g.d_task = upload(g.task, s);
+  g.d_tile = upload(g.tile, s);
+  const size_t eb = p.a.elem_bytes();
+  p.launches_per_exec = g.tile.empty() ? 0 : 1;
+  if (p.a_trans && p.a.size && !g.tile.empty()) {
+    p.a_tl.build(p.a, p.a_order, {}, nullptr, s);
+    p.a_t.alloc(p.a.size * eb);
+    p.launches_per_exec += 1;
+  }
+  if (p.b_trans && p.b.size && !g.tile.empty()) {
+    p.b_tl.build(p.b, p.b_order, {}, nullptr, s);
+    p.b_t.alloc(p.b.size * eb);
+    p.launches_per_exec += 1;
+  }
+  QLTG_CUDA(cudaStreamSynchronize(s));
+}
+
+void exec_contraction(CtrctPlan& p, const void* a, const void* b, void* c, int mode, cudaStream_t s, int stage) {
+  if (p.sched.tile.empty()) return;
+  QLTG_CHECK(a && b && c, QLTG_ERR_INVALID, "null device buffer");
+  QLTG_CHECK(stage >= 0 && stage <= 2, QLTG_ERR_INVALID, "stage must be 0, 1 or 2");
+  QLTG_CHECK(mode == QLTG_MODE_FP64 || mode == QLTG_MODE_SPLIT, QLTG_ERR_INVALID, "unknown arithmetic mode");
+  const int eb = (int)p.a.elem_bytes();
+  const void* ap = a;
+  const void* bp = b;
+  if (p.a_trans && p.a.size) {
+    if (stage != 2) p.a_tl.launch(a, p.a_t.get(), eb, s);
+    ap = p.a_t.get();
+  }
+  if (p.b_trans && p.b.size) {
+    if (stage != 2) p.b_tl.launch(b, p.b_t.get(), eb, s);
+    bp = p.b_t.get();
+  }
+  if (stage == 1) return;
+  if (mode == QLTG_MODE_FP64)
+    launch_gemm_f64(p.sched, ap, bp, c, p.a.dtype == QLTG_C128, p.ctx->num_sms, s);
+  else
+    launch_gemm_split(p, ap, bp, c, s);
+}
+
+}  // namespace qltg

@@ -1,0 +1,159 @@
+// Two-site effective-Hamiltonian matvec: four planned contractions captured as one CUDA
+// graph.
+//
+// The reference's chain is four independent Contract calls, each rebuilding its task
+// list on the host and issuing per-block transposes and per-task GEMMs on the default
+// stream (tests/test_tensor_manipulation/test_ten_ctrct_1sct.cc:253-257). The block
+// topology of a Lanczos matvec never changes, so here the four plans (device pairing,
+// schedules, operand scratch) are built once, the intermediates t1..t3 live in HBM for
+// the life of the object, and the whole chain replays as one graph launch.
+#include <memory>
+
+#include "ctrct.h"
+
+namespace qltg {
+void finalize_plan(CtrctPlan& p, cudaStream_t s);
+}
+
+using namespace qltg;
+
+struct qltg_matvec {
+  qltg_ctx* ctx = nullptr;
+  int mode = QLTG_MODE_FP64;
+  CtrctPlan step[4];
+  DevBuf t[3];
+  const void* lenv = nullptr;
+  const void* mpo1 = nullptr;
+  const void* mpo2 = nullptr;
+  const void* renv = nullptr;
+  int64_t psi_size = 0;
+  struct Graph {
+    const void* in;
+    void* out;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Graph> graphs;
+  cudaStream_t capture_stream = nullptr;
+
+  ~qltg_matvec() {
+    for (auto& g : graphs) {
+      cudaGraphExecDestroy(g.exec);
+      cudaGraphDestroy(g.graph);
+    }
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+  }
+
+  void enqueue(const void* psi, void* out, cudaStream_t s) {
+    exec_contraction(step[0], lenv, psi, t[0].get(), mode, s);
+    exec_contraction(step[1], t[0].get(), mpo1, t[1].get(), mode, s);
+    exec_contraction(step[2], t[1].get(), mpo2, t[2].get(), mode, s);
+    exec_contraction(step[3], t[2].get(), renv, out, mode, s);
+  }
+
+  cudaGraphExec_t graph_for(const void* in, void* out) {
+    for (auto& g : graphs)
+      if (g.in == in && g.out == out) return g.exec;
+    if (graphs.size() >= 8) {
+      cudaGraphExecDestroy(graphs.front().exec);
+      cudaGraphDestroy(graphs.front().graph);
+      graphs.erase(graphs.begin());
+    }
+    Graph g{in, out, nullptr, nullptr};
+    QLTG_CUDA(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue(in, out, capture_stream);
+    } catch (...) {
+      cudaGraph_t junk;
+      cudaStreamEndCapture(capture_stream, &junk);
+      if (junk) cudaGraphDestroy(junk);
+      throw;
+    }
+    QLTG_CUDA(cudaStreamEndCapture(capture_stream, &g.graph));
+    QLTG_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
+    graphs.push_back(g);
+    return g.exec;
+  }
+};
+
+extern "C" {
+
+int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* lenv_dev,
+                       const qltg_tensor_desc* psi, const qltg_tensor_desc* mpo1, const void* mpo1_dev,
+                       const qltg_tensor_desc* mpo2, const void* mpo2_dev, const qltg_tensor_desc* renv,
+                       const void* renv_dev, int32_t mode, void* stream, qltg_matvec** mv) {
+  return guarded([&] {
+    QLTG_CHECK(ctx && mv, QLTG_ERR_INVALID, "null ctx or matvec out-pointer");
+    QLTG_CHECK(lenv_dev && mpo1_dev && mpo2_dev && renv_dev, QLTG_ERR_INVALID, "null operator buffer");
+    QLTG_CHECK(mode == QLTG_MODE_FP64 || mode == QLTG_MODE_SPLIT, QLTG_ERR_INVALID, "unknown arithmetic mode");
+    QLTG_CUDA(cudaSetDevice(ctx->device));
+    auto h = std::make_unique<qltg_matvec>();
+    h->ctx = ctx;
+    h->mode = mode;
+    h->lenv = lenv_dev; h->mpo1 = mpo1_dev; h->mpo2 = mpo2_dev; h->renv = renv_dev;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    QLTG_CUDA(cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking));
+    const Meta ml = meta_from_desc(lenv), mp = meta_from_desc(psi), m1 = meta_from_desc(mpo1),
+               m2 = meta_from_desc(mpo2), mr = meta_from_desc(renv);
+    QLTG_CHECK(ml.rank == 3 && mp.rank == 4 && m1.rank == 4 && m2.rank == 4 && mr.rank == 3, QLTG_ERR_INVALID,
+               "matvec expects lenv rank 3, psi rank 4, mpo rank 4, renv rank 3");
+    h->psi_size = mp.size;
+    const int64_t ax[4][2][2] = {{{0, -1}, {0, -1}}, {{0, 2}, {0, 1}}, {{4, 1}, {0, 1}}, {{4, 1}, {1, 0}}};
+    const int nax[4] = {1, 2, 2, 2};
+    const Meta* rhs[4] = {&mp, &m1, &m2, &mr};
+    for (int i = 0; i < 4; ++i) {
+      CtrctPlan& p = h->step[i];
+      p.ctx = ctx;
+      p.a = (i == 0) ? ml : h->step[i - 1].c;
+      p.b = *rhs[i];
+      p.axa.assign(ax[i][0], ax[i][0] + nax[i]);
+      p.axb.assign(ax[i][1], ax[i][1] + nax[i]);
+      plan_contraction(p, s);
+      finalize_plan(p, s);
+      if (i < 3) h->t[i].alloc(std::max<int64_t>(1, p.c.size) * p.c.elem_bytes());
+    }
+    *mv = h.release();
+  });
+}
+
+int qltg_matvec_result(const qltg_matvec* mv, int64_t* nblk, int64_t* size) {
+  return guarded([&] {
+    QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
+    if (nblk) *nblk = mv->step[3].c.nblk;
+    if (size) *size = mv->step[3].c.size;
+  });
+}
+
+int qltg_matvec_result_blocks(const qltg_matvec* mv, int64_t* coords, int64_t* offsets) {
+  return guarded([&] {
+    QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
+    mv->step[3].c.export_arrays(nullptr, nullptr, nullptr, nullptr, coords, offsets);
+  });
+}
+
+int qltg_matvec_stats(const qltg_matvec* mv, double* flops, int64_t* launches) {
+  return guarded([&] {
+    QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
+    double f = 0;
+    int64_t l = 0;
+    for (auto& p : mv->step) { f += p.flops; l += p.launches_per_exec; }
+    if (flops) *flops = f;
+    if (launches) *launches = l;
+  });
+}
+
+int qltg_matvec_apply(qltg_matvec* mv, const void* psi_dev, void* out_dev, void* stream) {
+  return guarded([&] {
+    QLTG_CHECK(mv && psi_dev && out_dev, QLTG_ERR_INVALID, "null matvec or buffer");
+    QLTG_CUDA(cudaSetDevice(mv->ctx->device));
+    cudaGraphExec_t g = mv->graph_for(psi_dev, out_dev);
+    QLTG_CUDA(cudaGraphLaunch(g, static_cast<cudaStream_t>(stream)));
+  });
+}
+
+int qltg_matvec_destroy(qltg_matvec* mv) {
+  delete mv;
+  return QLTG_OK;
+}
+
+}  // extern "C"
