@@ -250,7 +250,7 @@ int main(int argc, char** argv) {
       contract_case(w, "f_rev", FP, FPd, {{3, 1, 0}, {3, 1, 0}});
       auto FL = to_qlten<std::complex<double>, fU1U1QN>(fm.lenv);
       auto FW = to_qlten<std::complex<double>, fU1U1QN>(fm.mpo1);
-      contract_case(w, "f_env", FL, FP, {{2}, {0}});
+      contract_case(w, "f_env", FP, FL, {{0}, {0}});   // IN leg of A against OUT leg of B
       contract_case(w, "f_mpo", FW, FW, {{3}, {0}});
     } else if (cs == "svd_u1") {
       auto t = sy::svd_psi(std::stoi(A(3)), std::stod(A(4)), std::stoll(A(5)), std::stoull(A(6)));
