@@ -107,6 +107,28 @@ int reorder_sign(std::vector<uint8_t> par, const std::vector<int>& order) {
   return (ex & 1) ? -1 : 1;
 }
 
+// Destination layout of QLTensor::Transpose: blocks in ascending block index of the permuted
+// sector counts, each multiplied by its FermionicInplaceReorder sign.
+void transpose_layout(const Meta& m, const std::vector<int>& order, std::vector<double>& signs,
+                      std::vector<int64_t>& dst_off) {
+  std::vector<std::pair<uint64_t, int64_t>> keyed(m.nblk);
+  signs.assign(m.nblk, 1.0);
+  for (int64_t b = 0; b < m.nblk; ++b) {
+    uint64_t idx = 0;
+    for (int i = 0; i < m.rank; ++i) idx = idx * (uint64_t)m.nsct(order[i]) + (uint64_t)m.coords[b * m.rank + order[i]];
+    keyed[b] = {idx, b};
+    if (m.parity_comp >= 0) {
+      std::vector<uint8_t> par(m.rank);
+      for (int l = 0; l < m.rank; ++l) par[l] = m.parity(l, m.coords[b * m.rank + l]);
+      signs[b] = reorder_sign(par, order);
+    }
+  }
+  std::sort(keyed.begin(), keyed.end());
+  dst_off.assign(m.nblk, 0);
+  int64_t off = 0;
+  for (auto& kv : keyed) { dst_off[kv.second] = off; off += m.blk_size(kv.second); }
+}
+
 }  // namespace qltg
 
 using namespace qltg;
@@ -237,23 +259,9 @@ int qltg_transpose(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev
     }
     QLTG_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    // destination block order: ascending block index over the permuted sector counts
-    std::vector<std::pair<uint64_t, int64_t>> keyed(m.nblk);
-    std::vector<double> signs(m.nblk, 1.0);
-    for (int64_t b = 0; b < m.nblk; ++b) {
-      uint64_t idx = 0;
-      for (int i = 0; i < m.rank; ++i) idx = idx * (uint64_t)m.nsct(order[i]) + (uint64_t)m.coords[b * m.rank + order[i]];
-      keyed[b] = {idx, b};
-      if (m.parity_comp >= 0) {
-        std::vector<uint8_t> par(m.rank);
-        for (int l = 0; l < m.rank; ++l) par[l] = m.parity(l, m.coords[b * m.rank + l]);
-        signs[b] = reorder_sign(par, order);
-      }
-    }
-    std::sort(keyed.begin(), keyed.end());
-    std::vector<int64_t> dst_off(m.nblk);
-    int64_t off = 0;
-    for (auto& kv : keyed) { dst_off[kv.second] = off; off += m.blk_size(kv.second); }
+    std::vector<double> signs;
+    std::vector<int64_t> dst_off;
+    transpose_layout(m, order, signs, dst_off);
     TransposeList tl;
     tl.build(m, order, signs, &dst_off, s);
     tl.launch(src_dev, dst_dev, (int)m.elem_bytes(), s);

@@ -27,6 +27,9 @@ struct TransposeList {
   int64_t nblocks = 0;
   void build(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
              const std::vector<int64_t>* dst_offsets, cudaStream_t s);
+  // host-side descriptors only (fills host / ntiles / nblocks, no device memory)
+  void describe(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
+                const std::vector<int64_t>* dst_offsets);
   void launch(const void* src, void* dst, int elem_bytes, cudaStream_t s) const;
 };
 
@@ -75,6 +78,10 @@ void exec_contraction(CtrctPlan& p, const void* a, const void* b, void* c, int m
 // grouped GEMM launchers (gemm_f64.cu)
 void launch_gemm_f64(const GemmSchedule& g, const void* a, const void* b, void* c, bool cplx, int num_sms,
                      cudaStream_t s);
+
+// Block order, destination offsets and fermionic block signs of QLTensor::Transpose.
+void transpose_layout(const Meta& m, const std::vector<int>& order, std::vector<double>& signs,
+                      std::vector<int64_t>& dst_off);
 
 // Fermionic exchange sign of one block pair (host copy of the device routine).
 int host_exchange_sign(const bool* pa, int ra, const bool* pb, int rb, const int64_t* axa, const int64_t* axb,

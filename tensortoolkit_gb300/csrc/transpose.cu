@@ -116,8 +116,8 @@ __global__ void __launch_bounds__(256) k_permute(const PermDesc* __restrict__ de
 
 }  // namespace
 
-void TransposeList::build(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
-                          const std::vector<int64_t>* dst_offsets, cudaStream_t s) {
+void TransposeList::describe(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
+                             const std::vector<int64_t>* dst_offsets) {
   host.clear();
   ntiles = 0;
   const int r = t.rank;
@@ -178,6 +178,11 @@ void TransposeList::build(const Meta& t, const std::vector<int>& order, const st
     host.push_back(d);
   }
   nblocks = (int64_t)host.size();
+}
+
+void TransposeList::build(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
+                          const std::vector<int64_t>* dst_offsets, cudaStream_t s) {
+  describe(t, order, signs, dst_offsets);
   dev = upload(host, s);
 }
 

@@ -9,6 +9,7 @@ import pytest
 
 from oracle import oracle
 from tensortoolkit_gb300.tensor import BSTensor, rel_frob, same_topology
+from tests.svd_check import check_svd
 
 CTRCT_CASES = [
     ("cfg1", ["c"]),
@@ -79,6 +80,9 @@ def test_svd_matches_reference(golden, case):
         assert same_topology(mine, ref), f"{case}: {name} topology differs"
         # same LAPACK routine on the same dense block-matrices: equal to rounding
         assert rel_frob(mine.data, ref.data) <= 1e-12, f"{case}: {name} values differ"
+    # the gauge-invariant checker used for the GPU Jacobi SVD accepts the oracle's result
+    check_svd(t, u, s, vt, err, D, BSTensor.from_record(rec, "U"), BSTensor.from_record(rec, "S"),
+              BSTensor.from_record(rec, "Vt"), float(rec["err"][0]), int(rec["D"][0]), ldims)
 
 
 @pytest.mark.parametrize("case", ["qr_u1", "qr_f"])
