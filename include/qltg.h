@@ -135,6 +135,18 @@ QLTG_API int qltg_ctrct_plan_destroy(qltg_ctrct_plan* plan);
 QLTG_API int qltg_transpose(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev,
                    const int32_t* perm, void* dst_dev, void* stream);
 
+/* Same result as qltg_transpose, but allocates nothing: no cudaMalloc / cudaFree and no
+ * allocating library call. No counterpart in the reference; it is for callers that cannot
+ * allocate device memory while they run (for example code executing under another
+ * library's stream capture or inside a fixed memory-pool budget). The per-block work list
+ * goes to a fixed table of at most 4096 blocks compiled into the library; larger tensors
+ * are rejected with QLTG_ERR_INVALID. The first call on a device looks up that table's
+ * device address, so make the first call on each device before any stream capture. All
+ * calls share the table: calls that overlap on the GPU race. Returns after its kernel has
+ * finished. */
+QLTG_API int qltg_transpose_noalloc(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev,
+                                    const int32_t* perm, void* dst_dev, void* stream);
+
 /* ---------------------------------------------------------------- two-site matvec */
 typedef struct qltg_matvec qltg_matvec;
 

@@ -37,6 +37,7 @@ _SIGS = {
     "qltg_ctrct_exec_stage": ([_P, _P, _P, _P, C.c_int32, C.c_int32, _P], C.c_int),
     "qltg_ctrct_plan_destroy": ([_P], C.c_int),
     "qltg_transpose": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
+    "qltg_transpose_noalloc": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
     "qltg_matvec_create": ([_P, C.POINTER(TensorDesc), _P, C.POINTER(TensorDesc), C.POINTER(TensorDesc), _P,
                             C.POINTER(TensorDesc), _P, C.POINTER(TensorDesc), _P, C.c_int32, _P,
                             C.POINTER(_P)], C.c_int),

@@ -270,4 +270,30 @@ int qltg_transpose(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev
   });
 }
 
+int qltg_transpose_noalloc(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev, const int32_t* perm,
+                           void* dst_dev, void* stream) {
+  return guarded([&] {
+    QLTG_CHECK(ctx, QLTG_ERR_INVALID, "null ctx");
+    Meta m = meta_from_desc(a);
+    if (m.rank == 0 || m.nblk == 0) return;
+    QLTG_CHECK(perm && src_dev && dst_dev, QLTG_ERR_INVALID, "null perm or buffer");
+    QLTG_CHECK(src_dev != dst_dev, QLTG_ERR_INVALID, "in-place transpose is not supported");
+    QLTG_CHECK(m.nblk <= kNoAllocPermBlocks, QLTG_ERR_INVALID,
+               "qltg_transpose_noalloc: at most 4096 blocks per call (use qltg_transpose)");
+    std::vector<int> order(perm, perm + m.rank);
+    {
+      std::vector<int> chk(order);
+      std::sort(chk.begin(), chk.end());
+      for (int i = 0; i < m.rank; ++i) QLTG_CHECK(chk[i] == i, QLTG_ERR_INVALID, "perm is not a permutation");
+    }
+    QLTG_CUDA(cudaSetDevice(ctx->device));
+    std::vector<double> signs;
+    std::vector<int64_t> dst_off;
+    transpose_layout(m, order, signs, dst_off);
+    TransposeList tl;
+    tl.describe(m, order, signs, &dst_off);
+    launch_permute_noalloc(ctx->device, tl, src_dev, dst_dev, (int)m.elem_bytes(), static_cast<cudaStream_t>(stream));
+  });
+}
+
 }  // extern "C"

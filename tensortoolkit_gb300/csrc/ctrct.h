@@ -83,6 +83,12 @@ void launch_gemm_f64(const GemmSchedule& g, const void* a, const void* b, void* 
 void transpose_layout(const Meta& m, const std::vector<int>& order, std::vector<double>& signs,
                       std::vector<int64_t>& dst_off);
 
+// Allocation-free permute: descriptors go to a fixed device table (at most
+// kNoAllocPermBlocks blocks per call), see transpose.cu.
+constexpr int kNoAllocPermBlocks = 4096;
+void launch_permute_noalloc(int device, const TransposeList& tl, const void* src, void* dst, int elem_bytes,
+                            cudaStream_t s);
+
 // Fermionic exchange sign of one block pair (host copy of the device routine).
 int host_exchange_sign(const bool* pa, int ra, const bool* pb, int rb, const int64_t* axa, const int64_t* axb,
                        int nax, const int32_t* a_ctrct_dirs);

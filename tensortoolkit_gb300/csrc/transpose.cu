@@ -12,6 +12,8 @@
 // staged through shared memory so both the read (along p) and the write (along q) are
 // coalesced. The sign multiply is exact (+-1).
 #include <algorithm>
+#include <mutex>
+#include <string>
 
 #include "ctrct.h"
 
@@ -196,6 +198,59 @@ void TransposeList::launch(const void* src, void* dst, int elem_bytes, cudaStrea
     k_permute<double2><<<grid, 256, 0, s>>>(dev.as<PermDesc>(), (int)nblocks, ntiles,
                                             static_cast<const double2*>(src), static_cast<double2*>(dst));
   QLTG_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant (qltg_transpose_noalloc). Some callers cannot allocate device
+// memory while they run - a DMRG sweep driven from inside another library's CUDA-graph
+// capture or memory-pool budget, or a host thread that must not take the allocator's
+// locks - so the per-call permutation work list lives in this fixed device table instead
+// of a fresh cudaMalloc. Every GPU that loads the library holds the table (about 600 KB)
+// until the process exits. All calls share it and it keeps the last call's descriptors, so
+// calls that overlap on the GPU (on different streams or devices' queues at once) race;
+// each call waits for its own kernel before returning.
+namespace {
+
+__device__ __align__(256) PermDesc g_noalloc_perm[kNoAllocPermBlocks];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+PermDesc* g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of the table for `device`, looked up once per device with that device
+// current (host code may not use the symbol itself as a device pointer).
+PermDesc* noalloc_table(int device) {
+  QLTG_CHECK(device >= 0 && device < kMaxDevices, QLTG_ERR_UNSUPPORTED, "device ordinal above 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    QLTG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_perm));
+    g_noalloc_addr[device] = static_cast<PermDesc*>(p);
+  }
+  return g_noalloc_addr[device];
+}
+
+}  // namespace
+
+void launch_permute_noalloc(int device, const TransposeList& tl, const void* src, void* dst, int elem_bytes,
+                            cudaStream_t s) {
+  QLTG_CHECK(tl.nblocks <= kNoAllocPermBlocks, QLTG_ERR_INVALID,
+             "qltg_transpose_noalloc: tensor has " + std::to_string(tl.nblocks) + " blocks, the fixed table holds " +
+                 std::to_string(kNoAllocPermBlocks));
+  PermDesc* table = noalloc_table(device);
+  if (tl.ntiles == 0) return;
+  QLTG_CUDA(cudaMemcpyAsync(table, tl.host.data(), tl.host.size() * sizeof(PermDesc), cudaMemcpyHostToDevice, s));
+  const unsigned grid = (unsigned)std::min<int64_t>(tl.ntiles, 152 * 8);
+  if (elem_bytes == 8)
+    k_permute<double><<<grid, 256, 0, s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double*>(src),
+                                           static_cast<double*>(dst));
+  else
+    k_permute<double2><<<grid, 256, 0, s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double2*>(src),
+                                            static_cast<double2*>(dst));
+  QLTG_CUDA(cudaGetLastError());
+  // the descriptors were copied from this call's host memory and the table is shared:
+  // finish before returning
+  QLTG_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace qltg
