@@ -152,6 +152,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mode", choices=["split", "fp64"], default=os.environ.get("QLTG_BENCH_MODE", "fp64"))
     ap.add_argument("--cpu-iters", type=int, default=None, help="CPU baseline sample size")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling run: plan the D=4000 matvec, apply it twice, print nothing else")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -179,6 +181,12 @@ def main():
     mv = Matvec(dl, psi, d1, d2, dr, mode=args.mode)
     flops, launches_per_step = mv.stats()
     out = DTensor.empty(mv.result, local)
+    if args.profile:
+        for _ in range(2):
+            mv.apply(dp, out)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_run": True, "mode": args.mode, "launches_per_step": launches_per_step}))
+        return
     stream = torch.cuda.current_stream(local)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
 

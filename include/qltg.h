@@ -46,10 +46,16 @@ enum { QLTG_F64 = 0, QLTG_C128 = 1 };     /* element types */
 enum { QLTG_IN = 0, QLTG_OUT = 1 };       /* TenIndexDirType */
 
 /* Arithmetic of a contraction.
- * QLTG_MODE_FP64:  plain FP64 (DMMA / DFMA), the reference's precision.
- * QLTG_MODE_SPLIT: FP64 emulated with BF16 slices on the tcgen05 tensor cores, FP32
- *                  accumulation, FP64 recombination; relative error <= 1e-12 of the
- *                  FP64 result (stated per call by qltg_ctrct_last_error_bound). */
+ * QLTG_MODE_FP64:  plain FP64 on the FP64 pipe, the reference's precision.
+ * QLTG_MODE_SPLIT: FP64 emulated with BF16 slices on the tcgen05 tensor cores: every row
+ *                  of A / column of B is scaled by a power of two and cut into seven 7-bit
+ *                  integer slices, the 28 slice products of weight >= 2^-56 accumulate
+ *                  exactly (FP32 integers in tensor memory, drained every 128 k into int64),
+ *                  and each task's sum is rounded to FP64 once. Per element the error is
+ *                  below 2^-48 * sum_k |a_ik| |b_kj| scaled by the row / column maxima
+ *                  (about 1e-14 relative for random data); the tests and the benchmark
+ *                  state the measured relative error against the FP64 result. Real (FP64)
+ *                  tensors only; output blocks with n, k <= 8 stay on the FP64 pipe. */
 enum { QLTG_MODE_FP64 = 0, QLTG_MODE_SPLIT = 1 };
 
 /* ---------------------------------------------------------------- descriptors */
@@ -123,6 +129,11 @@ QLTG_API int qltg_ctrct_exec(qltg_ctrct_plan* plan, const void* a_dev, const voi
 QLTG_API int qltg_ctrct_exec_stage(qltg_ctrct_plan* plan, const void* a_dev, const void* b_dev, void* c_dev,
                                    int32_t mode, int32_t stage, void* stream);
 
+/* Wait for `stream`, then report the device-side status of the plan's kernels: QLTG_OK, or
+ * QLTG_ERR_TIMEOUT if a bounded tensor-core wait expired (the kernel then stopped early and
+ * its output is not valid). */
+QLTG_API int qltg_ctrct_plan_device_status(qltg_ctrct_plan* plan, void* stream);
+
 QLTG_API int qltg_ctrct_plan_destroy(qltg_ctrct_plan* plan);
 
 /* ---------------------------------------------------------------- transpose */
@@ -170,6 +181,9 @@ QLTG_API int qltg_matvec_stats(const qltg_matvec* mv, double* flops, int64_t* la
 
 /* out_dev = H_eff . psi_dev (one graph launch on `stream`). */
 QLTG_API int qltg_matvec_apply(qltg_matvec* mv, const void* psi_dev, void* out_dev, void* stream);
+
+/* Device-side status of the four captured contractions (see qltg_ctrct_plan_device_status). */
+QLTG_API int qltg_matvec_device_status(qltg_matvec* mv, void* stream);
 
 QLTG_API int qltg_matvec_destroy(qltg_matvec* mv);
 

@@ -161,6 +161,9 @@ class ContractionPlan:
                                     _mode(mode), stream_ptr(self.device)))
         return out
 
+    def device_status(self) -> None:
+        check(lib().qltg_ctrct_plan_device_status(self.h, stream_ptr(self.device)))
+
     def __del__(self):
         try:
             if self.h:
@@ -236,6 +239,9 @@ class Matvec:
     def apply_raw(self, psi_ptr: int, out_ptr: int, stream: Optional[int] = None) -> None:
         s = stream_ptr(self.device) if stream is None else C.c_void_p(stream)
         check(lib().qltg_matvec_apply(self.h, C.c_void_p(psi_ptr), C.c_void_p(out_ptr), s))
+
+    def device_status(self) -> None:
+        check(lib().qltg_matvec_device_status(self.h, stream_ptr(self.device)))
 
     def __del__(self):
         try:

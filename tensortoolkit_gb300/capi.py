@@ -35,6 +35,7 @@ _SIGS = {
     "qltg_ctrct_plan_stats": ([_P, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
     "qltg_ctrct_exec": ([_P, _P, _P, _P, C.c_int32, _P], C.c_int),
     "qltg_ctrct_exec_stage": ([_P, _P, _P, _P, C.c_int32, C.c_int32, _P], C.c_int),
+    "qltg_ctrct_plan_device_status": ([_P, _P], C.c_int),
     "qltg_ctrct_plan_destroy": ([_P], C.c_int),
     "qltg_transpose": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
     "qltg_transpose_noalloc": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
@@ -45,6 +46,7 @@ _SIGS = {
     "qltg_matvec_result_blocks": ([_P, _P, _P], C.c_int),
     "qltg_matvec_stats": ([_P, C.POINTER(C.c_double), _I64P], C.c_int),
     "qltg_matvec_apply": ([_P, _P, _P, _P], C.c_int),
+    "qltg_matvec_device_status": ([_P, _P], C.c_int),
     "qltg_matvec_destroy": ([_P], C.c_int),
     "qltg_svd": ([_P, C.POINTER(TensorDesc), _P, C.c_int32, _P, C.c_double, C.c_int64, C.c_int64, _P,
                   C.POINTER(_P)], C.c_int),

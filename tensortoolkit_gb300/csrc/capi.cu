@@ -4,6 +4,7 @@
 #include <numeric>
 
 #include "ctrct.h"
+#include "split.h"
 
 namespace qltg {
 
@@ -235,6 +236,15 @@ int qltg_ctrct_exec_stage(qltg_ctrct_plan* plan, const void* a_dev, const void* 
     QLTG_CHECK(plan, QLTG_ERR_INVALID, "null plan");
     QLTG_CUDA(cudaSetDevice(plan->p.ctx->device));
     exec_contraction(plan->p, a_dev, b_dev, c_dev, mode, static_cast<cudaStream_t>(stream), stage);
+  });
+}
+
+int qltg_ctrct_plan_device_status(qltg_ctrct_plan* plan, void* stream) {
+  return guarded([&] {
+    QLTG_CHECK(plan, QLTG_ERR_INVALID, "null plan");
+    QLTG_CUDA(cudaSetDevice(plan->p.ctx->device));
+    QLTG_CHECK(split_device_error(plan->p, static_cast<cudaStream_t>(stream)) == 0, QLTG_ERR_TIMEOUT,
+               "a bounded tensor-core wait expired in the split-precision GEMM");
   });
 }
 

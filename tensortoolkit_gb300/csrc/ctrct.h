@@ -2,6 +2,8 @@
 // schedule for one C = A . B.
 #pragma once
 
+#include <memory>
+
 #include "qltg_internal.h"
 
 namespace qltg {
@@ -48,13 +50,46 @@ struct GemmTile {
   int32_t cblk;
   int16_t tm, tn;
 };
+struct GemmRowChunk {          // skinny output blocks: 256 consecutive rows of one block
+  int32_t cblk;
+  int32_t chunk;
+};
 
 struct GemmSchedule {
   std::vector<GemmCBlk> cblk;
   std::vector<GemmTask> task;
-  std::vector<GemmTile> tile;
-  DevBuf d_cblk, d_task, d_tile;
-  int bm = 64, bn = 64;
+  std::vector<GemmTile> tile;           // 64 x 64 tiles (DMMA / DFMA kernels)
+  std::vector<GemmRowChunk> skinny;     // row chunks of skinny blocks (n, k <= 8)
+  DevBuf d_cblk, d_task, d_tile, d_skinny, d_counter;
+  int bm = 32, bn = 32;
+};
+
+// Split-precision schedule (gemm_split.cu): operand blocks to slice and pack, per-task
+// packed-tile addresses, output tiles of 128 x 32.
+struct SplitOperand {
+  int64_t src_off;        // element offset of the (transposed) FP64 block
+  int64_t pack_off;       // byte offset of its packed slice tiles
+  int64_t vec_begin;      // prefix over operands of rows (A) / columns (B): exponent work items
+  int64_t chunk_begin;    // prefix over operands of 16-byte packing chunks
+  int32_t rows, cols;     // A: m x k; B: k x n
+  int32_t ktiles;         // 64-wide k tiles
+  int32_t exp_off;        // offset of its row (A) / column (B) exponents
+};
+struct SplitTask {
+  int64_t a_pack, b_pack;
+  int32_t a_exp, b_exp;
+  int32_t ktiles;
+  int32_t sign;
+};
+struct SplitPlan {
+  bool built = false;
+  std::vector<SplitOperand> a_ops, b_ops;
+  std::vector<SplitTask> tasks;   // indexed like GemmSchedule::task
+  std::vector<GemmTile> tiles;    // (output block, 128-row tile, 32-col tile)
+  int64_t n_a_vec = 0, n_b_vec = 0, n_a_chunks = 0, n_b_chunks = 0;
+  DevBuf d_a_ops, d_b_ops, d_tasks, d_tiles, a_packed, b_packed, a_exps, b_exps, counter, error;
+  void build(const struct CtrctPlan& p, cudaStream_t s);
+  int64_t launches() const;
 };
 
 struct CtrctPlan {
@@ -69,15 +104,21 @@ struct CtrctPlan {
   TransposeList a_tl, b_tl;
   DevBuf a_t, b_t;             // transposed operand scratch
   GemmSchedule sched;
+  std::unique_ptr<SplitPlan> split;   // built on first use of QLTG_MODE_SPLIT
   int64_t launches_per_exec = 0;
 };
 
 void plan_contraction(CtrctPlan& p, cudaStream_t s);
+int64_t exec_launches_split(const CtrctPlan& p);
 void exec_contraction(CtrctPlan& p, const void* a, const void* b, void* c, int mode, cudaStream_t s, int stage = 0);
 
 // grouped GEMM launchers (gemm_f64.cu)
+bool skinny_cblk(const GemmSchedule& g, int32_t q);
+int skinny_rows_per_item();
 void launch_gemm_f64(const GemmSchedule& g, const void* a, const void* b, void* c, bool cplx, int num_sms,
                      cudaStream_t s);
+void launch_gemm_f64_skinny(const GemmSchedule& g, const void* a, const void* b, void* c, bool cplx, int num_sms,
+                            cudaStream_t s);
 
 // Block order, destination offsets and fermionic block signs of QLTensor::Transpose.
 void transpose_layout(const Meta& m, const std::vector<int>& order, std::vector<double>& signs,

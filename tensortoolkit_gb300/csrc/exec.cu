@@ -10,10 +10,16 @@ namespace qltg {
 void finalize_plan(CtrctPlan& p, cudaStream_t s) {
   GemmSchedule& g = p.sched;
   g.tile.clear();
+  g.skinny.clear();
+  const int rows_per_item = skinny_rows_per_item();
   struct Cand { GemmTile t; int64_t cost; };
   std::vector<Cand> cands;
   for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q) {
     const GemmCBlk& cb = g.cblk[q];
+    if (skinny_cblk(g, q)) {
+      for (int32_t c = 0; c * (int64_t)rows_per_item < cb.m; ++c) g.skinny.push_back(GemmRowChunk{q, c});
+      continue;
+    }
     int64_t ksum = 0;
     for (int32_t t = cb.t0; t < cb.t1; ++t) ksum += g.task[t].k;
     const int tm = (cb.m + g.bm - 1) / g.bm, tn = (cb.n + g.bn - 1) / g.bn;
@@ -30,14 +36,17 @@ void finalize_plan(CtrctPlan& p, cudaStream_t s) {
   g.d_cblk = upload(g.cblk, s);
   g.d_task = upload(g.task, s);
   g.d_tile = upload(g.tile, s);
+  g.d_skinny = upload(g.skinny, s);
+  g.d_counter.alloc(sizeof(int));
   const size_t eb = p.a.elem_bytes();
-  p.launches_per_exec = g.tile.empty() ? 0 : 1;
-  if (p.a_trans && p.a.size && !g.tile.empty()) {
+  const bool any_work = !g.tile.empty() || !g.skinny.empty();
+  p.launches_per_exec = (g.tile.empty() ? 0 : 2) + (g.skinny.empty() ? 0 : 1);   // memset + GEMM
+  if (p.a_trans && p.a.size && any_work) {
     p.a_tl.build(p.a, p.a_order, {}, nullptr, s);
     p.a_t.alloc(p.a.size * eb);
     p.launches_per_exec += 1;
   }
-  if (p.b_trans && p.b.size && !g.tile.empty()) {
+  if (p.b_trans && p.b.size && any_work) {
     p.b_tl.build(p.b, p.b_order, {}, nullptr, s);
     p.b_t.alloc(p.b.size * eb);
     p.launches_per_exec += 1;
@@ -45,8 +54,16 @@ void finalize_plan(CtrctPlan& p, cudaStream_t s) {
   QLTG_CUDA(cudaStreamSynchronize(s));
 }
 
+// Kernel launches of one split-mode execution: operand transposes plus the split stage.
+int64_t exec_launches_split(const CtrctPlan& p) {
+  int64_t n = split_launches(p);
+  if (p.a_trans && p.a.size) n += 1;
+  if (p.b_trans && p.b.size) n += 1;
+  return n;
+}
+
 void exec_contraction(CtrctPlan& p, const void* a, const void* b, void* c, int mode, cudaStream_t s, int stage) {
-  if (p.sched.tile.empty()) return;
+  if (p.sched.tile.empty() && p.sched.skinny.empty()) return;
   QLTG_CHECK(a && b && c, QLTG_ERR_INVALID, "null device buffer");
   QLTG_CHECK(stage >= 0 && stage <= 2, QLTG_ERR_INVALID, "stage must be 0, 1 or 2");
   QLTG_CHECK(mode == QLTG_MODE_FP64 || mode == QLTG_MODE_SPLIT, QLTG_ERR_INVALID, "unknown arithmetic mode");

@@ -1,12 +1,21 @@
-// Grouped FP64 / complex128 GEMM over all tasks of one contraction, one launch.
+// Grouped FP64 / complex128 GEMM over all tasks of one contraction.
 //
 // Replaces the reference's serial loop of one cblas_dgemm / cublasDgemm per task with
 // beta = 0 for the first task of an output block and beta = 1 after it
 // (global_operations.h:895-992 -> raw_data_operations.h:530-548 -> blas_level3.h:35-56,
-// :797-856). Here every 64 x 64 output tile is owned by one CTA that loops over all
-// tasks of its output block, accumulating C_tile += sign_t * A_t[tile rows, :] B_t[:, tile
-// cols] in registers, and stores the tile once: no read-modify-write of C, no atomics,
-// deterministic. Tiles are issued longest-first over a persistent grid.
+// :797-856). Every output tile is owned by one CTA that loops over all tasks of its output
+// block, accumulating sign_t * A_t[tile rows, :] B_t[:, tile cols] in registers, and stores
+// the tile once: no read-modify-write of C, no atomics, deterministic.
+//
+// Two kernels, chosen per output block when the plan is built:
+//  * k_gemm_dfma   - FP64 / complex128 (4 real FMAs per complex FMA) on 32 x 32 output tiles.
+//                    On this GPU the FP64 tensor path (mma.sync m8n8k4 f64) runs at the same
+//                    rate as DFMA (about 1.05 TFLOP/s each, measured) but pads every block to
+//                    8 x 8 x 4 fragments (48 % useful on the matvec's block shapes), so the
+//                    predicated DFMA tile is the faster FP64 kernel;
+//  * k_gemm_skinny - output blocks with n <= 8 and k <= 8 (the MPO steps of the two-site
+//                    matvec: m up to 3e4, k, n <= 3): one thread per output row, operand B
+//                    in registers, memory-streaming.
 #include <algorithm>
 
 #include "ctrct.h"
@@ -14,9 +23,7 @@
 namespace qltg {
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
-
-struct Cd { double x, y; };
+constexpr int BM = 32, BN = 32, BK = 32, NT = 256;
 
 __device__ __forceinline__ void fma_acc(double& acc, double a, double b) { acc = fma(a, b, acc); }
 __device__ __forceinline__ void fma_acc(double2& acc, double2 a, double2 b) {
@@ -30,37 +37,47 @@ __device__ __forceinline__ double2 zero_of(double2) { return make_double2(0.0, 0
 __device__ __forceinline__ double scale(double x, double s) { return x * s; }
 __device__ __forceinline__ double2 scale(double2 x, double s) { return make_double2(x.x * s, x.y * s); }
 
+// One output tile of BM x BN per work item; 16 x 16 threads, each 2 x 2 outputs at
+// (ty + 16 i, tx + 16 j). Operand tiles are staged through shared memory (A transposed so
+// a warp reads one broadcast row); outputs outside the block are predicated off so no FP64
+// issue slot is spent on padding. Work items are taken longest-first from an atomic
+// counter (the plan zeroes it before each launch), so the few very long tiles start first
+// and the rest fill in behind them.
 template <typename T>
-__global__ void __launch_bounds__(NT) k_gemm_grouped(const GemmCBlk* __restrict__ cblk,
-                                                     const GemmTask* __restrict__ task,
-                                                     const GemmTile* __restrict__ tiles, int ntiles,
-                                                     const T* __restrict__ A, const T* __restrict__ B,
-                                                     T* __restrict__ C) {
-  __shared__ T As[BK][BM];
+__global__ void __launch_bounds__(NT) k_gemm_dfma(const GemmCBlk* __restrict__ cblk, const GemmTask* __restrict__ task,
+                                                  const GemmTile* __restrict__ tiles, int ntiles,
+                                                  const T* __restrict__ A, const T* __restrict__ B,
+                                                  T* __restrict__ C, int* __restrict__ counter) {
+  __shared__ T As[BK][BM + 1];
   __shared__ T Bs[BK][BN];
+  __shared__ int s_ti;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+  while (true) {
+    if (threadIdx.x == 0) s_ti = atomicAdd(counter, 1);
+    __syncthreads();
+    const int ti = s_ti;
+    __syncthreads();
+    if (ti >= ntiles) break;
     const GemmTile tl = tiles[ti];
     const GemmCBlk cb = cblk[tl.cblk];
     const int r0 = tl.tm * BM, c0 = tl.tn * BN;
     const int m = cb.m, n = cb.n;
-    T acc[4][4];
+    T acc[2][2];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 2; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) acc[i][j] = zero_of(T());
-    bool rv[4], cv[4];
+      for (int j = 0; j < 2; ++j) acc[i][j] = zero_of(T());
+    bool rv[2], cv[2];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) { rv[i] = r0 + ty + 16 * i < m; cv[i] = c0 + tx + 16 * i < n; }
+    for (int i = 0; i < 2; ++i) { rv[i] = r0 + ty + 16 * i < m; cv[i] = c0 + tx + 16 * i < n; }
     for (int t = cb.t0; t < cb.t1; ++t) {
       const GemmTask tk = task[t];
+      const int k = tk.k;
       const T* a = A + tk.a_off;
       const T* b = B + tk.b_off;
-      const int k = tk.k;
       const double sg = (double)tk.sign;
       for (int k0 = 0; k0 < k; k0 += BK) {
         const int kc = min(BK, k - k0);
-        // A tile: rows r0.., cols k0.. of the m x k row-major operand
 #pragma unroll
         for (int e = threadIdx.x; e < BM * BK; e += NT) {
           const int row = e / BK, kk = e % BK;
@@ -68,7 +85,6 @@ __global__ void __launch_bounds__(NT) k_gemm_grouped(const GemmCBlk* __restrict_
           if (kk < kc && r0 + row < m) v = scale(a[(int64_t)(r0 + row) * k + k0 + kk], sg);
           As[kk][row] = v;
         }
-        // B tile: rows k0.., cols c0.. of the k x n row-major operand
 #pragma unroll
         for (int e = threadIdx.x; e < BK * BN; e += NT) {
           const int kk = e / BN, col = e % BN;
@@ -77,46 +93,118 @@ __global__ void __launch_bounds__(NT) k_gemm_grouped(const GemmCBlk* __restrict_
           Bs[kk][col] = v;
         }
         __syncthreads();
+#pragma unroll 4
         for (int kk = 0; kk < kc; ++kk) {
-          T av[4], bv[4];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx + 16 * j];
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (rv[i])
-#pragma unroll
-              for (int j = 0; j < 4; ++j)
-                if (cv[j]) fma_acc(acc[i][j], av[i], bv[j]);
+          const T a0 = As[kk][ty], a1 = As[kk][ty + 16];
+          const T b0 = Bs[kk][tx], b1 = Bs[kk][tx + 16];
+          if (rv[0]) {
+            if (cv[0]) fma_acc(acc[0][0], a0, b0);
+            if (cv[1]) fma_acc(acc[0][1], a0, b1);
+          }
+          if (rv[1]) {
+            if (cv[0]) fma_acc(acc[1][0], a1, b0);
+            if (cv[1]) fma_acc(acc[1][1], a1, b1);
+          }
         }
         __syncthreads();
       }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 2; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
+      for (int j = 0; j < 2; ++j)
         if (rv[i] && cv[j]) C[cb.c_off + (int64_t)(r0 + ty + 16 * i) * n + c0 + tx + 16 * j] = acc[i][j];
+  }
+}
+
+// Skinny output blocks (n <= 8, every task k <= 8): thread per output row.
+constexpr int kSkinnyRows = 256;
+constexpr int kSkinnyMax = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(kSkinnyRows) k_gemm_skinny(const GemmCBlk* __restrict__ cblk,
+                                                             const GemmTask* __restrict__ task,
+                                                             const GemmRowChunk* __restrict__ items, int nitems,
+                                                             const T* __restrict__ A, const T* __restrict__ B,
+                                                             T* __restrict__ C) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const GemmRowChunk item = items[it];
+    const GemmCBlk cb = cblk[item.cblk];
+    const int row = item.chunk * kSkinnyRows + threadIdx.x;
+    const int n = cb.n;
+    T acc[kSkinnyMax];
+#pragma unroll
+    for (int j = 0; j < kSkinnyMax; ++j) acc[j] = zero_of(T());
+    if (row < cb.m) {
+      for (int t = cb.t0; t < cb.t1; ++t) {
+        const GemmTask tk = task[t];
+        const int k = tk.k;
+        const T* a = A + tk.a_off + (int64_t)row * k;
+        const T* b = B + tk.b_off;
+        const double sg = (double)tk.sign;
+        for (int kk = 0; kk < k; ++kk) {
+          const T av = scale(__ldg(a + kk), sg);
+#pragma unroll
+          for (int j = 0; j < kSkinnyMax; ++j)
+            if (j < n) fma_acc(acc[j], av, __ldg(b + kk * n + j));
+        }
+      }
+      T* out = C + cb.c_off + (int64_t)row * n;
+#pragma unroll
+      for (int j = 0; j < kSkinnyMax; ++j)
+        if (j < n) out[j] = acc[j];
+    }
   }
 }
 
 }  // namespace
 
+bool skinny_cblk(const GemmSchedule& g, int32_t q) {
+  const GemmCBlk& cb = g.cblk[q];
+  if (cb.n > kSkinnyMax) return false;
+  for (int32_t t = cb.t0; t < cb.t1; ++t)
+    if (g.task[t].k > kSkinnyMax) return false;
+  return true;
+}
+
+int skinny_rows_per_item() { return kSkinnyRows; }
+
+void launch_gemm_f64_skinny(const GemmSchedule& g, const void* a, const void* b, void* c, bool cplx, int num_sms,
+                            cudaStream_t s) {
+  const int ns = (int)g.skinny.size();
+  if (!ns) return;
+  const int grid = std::min(ns, std::max(1, num_sms) * 8);
+  if (cplx)
+    k_gemm_skinny<double2><<<grid, kSkinnyRows, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
+                                                        g.d_skinny.as<GemmRowChunk>(), ns,
+                                                        static_cast<const double2*>(a),
+                                                        static_cast<const double2*>(b), static_cast<double2*>(c));
+  else
+    k_gemm_skinny<double><<<grid, kSkinnyRows, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
+                                                       g.d_skinny.as<GemmRowChunk>(), ns, static_cast<const double*>(a),
+                                                       static_cast<const double*>(b), static_cast<double*>(c));
+  QLTG_CUDA(cudaGetLastError());
+}
+
 void launch_gemm_f64(const GemmSchedule& g, const void* a, const void* b, void* c, bool cplx, int num_sms,
                      cudaStream_t s) {
   const int nt = (int)g.tile.size();
-  if (nt == 0) return;
-  const int grid = std::min(nt, std::max(1, num_sms) * (cplx ? 2 : 3));
-  if (cplx)
-    k_gemm_grouped<double2><<<grid, NT, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
-                                                g.d_tile.as<GemmTile>(), nt, static_cast<const double2*>(a),
-                                                static_cast<const double2*>(b), static_cast<double2*>(c));
-  else
-    k_gemm_grouped<double><<<grid, NT, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
-                                               g.d_tile.as<GemmTile>(), nt, static_cast<const double*>(a),
-                                               static_cast<const double*>(b), static_cast<double*>(c));
-  QLTG_CUDA(cudaGetLastError());
+  launch_gemm_f64_skinny(g, a, b, c, cplx, num_sms, s);
+  if (nt) {
+    QLTG_CUDA(cudaMemsetAsync(g.d_counter.get(), 0, sizeof(int), s));
+    const int grid = std::min(nt, std::max(1, num_sms) * 4);
+    if (cplx)
+      k_gemm_dfma<double2><<<grid, NT, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
+                                               g.d_tile.as<GemmTile>(), nt, static_cast<const double2*>(a),
+                                               static_cast<const double2*>(b), static_cast<double2*>(c),
+                                               g.d_counter.as<int>());
+    else
+      k_gemm_dfma<double><<<grid, NT, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
+                                              g.d_tile.as<GemmTile>(), nt, static_cast<const double*>(a),
+                                              static_cast<const double*>(b), static_cast<double*>(c),
+                                              g.d_counter.as<int>());
+    QLTG_CUDA(cudaGetLastError());
+  }
 }
 
 }  // namespace qltg

@@ -1,10 +1,567 @@
-// Split-precision grouped GEMM (placeholder until the tcgen05 kernel lands).
+// Split-precision grouped GEMM: FP64 emulated with BF16 slices on the tcgen05 tensor
+// cores, FP32 accumulation in tensor memory, exact integer recombination, one FP64
+// rounding per output element.
+//
+// Slicing (per operand block, integer arithmetic only - the FP64 pipe of this GPU runs at
+// about 1 TFLOP/s, so nothing here touches it):
+//   every row i of A (column j of B) gets a scale 2^e with max |x| < 2^e, and each element
+//   x = s 2^e y, |y| < 1, is cut into S = 7 base-2^7 digits of Y = floor(|y| 2^49):
+//   x ~= 2^e sum_p a_p 2^(-7p) with integer slices a_p = s d_p in [-127, 127], exact in BF16.
+//   Truncation error < 2^-49 of the row (column) maximum.
+// Products (the Ozaki scheme, restated): C_ij = 2^(ea_i + eb_j) sum_l 2^(-7l) D_l with
+//   D_l = sum_{p+q=l} (A_p B_q)_ij over the 28 slice pairs with p + q <= 8 (levels 2..8).
+//   Every product a_p b_q is an integer of magnitude < 2^14; level l sums l-1 pairs, so over
+//   at most 128 k the FP32 accumulation of every level is exact (7 * 128 * 127^2 < 2^24).
+//   Each level has its own 128 x 32 FP32 accumulator in tensor memory (7 x 32 = 224
+//   columns); every 128 k the levels are drained to two int64 registers per output
+//   (levels 2-4 -> hi, 5-8 -> lo, both < 2^53), and at the end of a task
+//   C += sign * 2^(ea+eb-56) (hi 2^28 + lo) with one FMA-rounding.
+//
+// Layout for the tensor cores: both operands K-major, no swizzle, in 8 x 16-byte core
+// matrices (leading-byte offset 128 B between the two core matrices of a 16-wide k step,
+// stride-byte offset 256 B between 8-row groups). The pack kernels write each (row tile,
+// k tile, slice) as one contiguous tile in exactly that layout, zero-padded, so the GEMM
+// stages operands with plain 16-byte copies and points the MMA descriptors at them.
+//
+// GEMM (one CTA of 128 threads per 128 x 32 output tile at a time, dynamic tile queue):
+//   for each task of the output block, for each 64-wide k tile: all threads stage the 7 A
+//   slices (7 x 16 KB) and 7 B slices (7 x 4 KB) into shared memory; one thread issues the
+//   4 x 28 tcgen05.mma (M=128, N=32, K=16) and commits them to an mbarrier; after every
+//   second k tile (and at the end of a task) the four warps read their 32 lanes of the 7
+//   level accumulators with tcgen05.ld and fold them into the int64 pair.
+// Every wait on the mbarrier is bounded; on expiry the CTA sets the plan's error word,
+// frees its tensor memory and returns.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
 #include "split.h"
 
 namespace qltg {
+namespace {
 
-void launch_gemm_split(CtrctPlan&, const void*, const void*, void*, cudaStream_t) {
-  throw Error(QLTG_ERR_UNSUPPORTED, "split-precision mode is not built yet");
+constexpr int kS = 7;                      // slices
+constexpr int kPairs = 28;                 // p + q <= kS + 1
+constexpr int kLevels = 7;                 // levels 2..8
+constexpr int kTM = 128, kTN = 32, kTK = 64;
+constexpr int kATile = kTM * kTK * 2;      // bytes of one (row tile, k tile, slice): 16 KB
+constexpr int kBTile = kTN * kTK * 2;      // 4 KB
+constexpr int kThreads = 128;
+constexpr int kDrainK = 128;               // k between drains (exactness bound)
+constexpr uint32_t kTmemCols = 256;        // >= 7 * 32, power of two
+constexpr unsigned long long kWaitNs = 1000000000ull;   // 1 s bound on any wait
+
+// ------------------------------------------------------------------ slicing
+// Row / column scale exponents: e with max |x| < 2^e (0 for an all-zero row).
+__device__ __forceinline__ int exp_of_bits(uint64_t absbits) {
+  if (absbits == 0) return 0;
+  const int ef = (int)(absbits >> 52);
+  return ef == 0 ? -1021 : ef - 1022;     // subnormals: treat as 2^-1022 scale
+}
+
+// A (m x k row-major): one warp per row.
+__global__ void k_row_exp(const double* __restrict__ src, const SplitOperand* __restrict__ ops, int nops,
+                          int32_t* __restrict__ exps, int64_t total_rows) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t rg = warp; rg < total_rows; rg += nw) {
+    int lo = 0, hi = nops - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].vec_begin <= rg) lo = mid; else hi = mid - 1; }
+    const SplitOperand o = ops[lo];
+    const int64_t r = rg - o.vec_begin;
+    const double* row = src + o.src_off + r * o.cols;
+    uint64_t mx = 0;
+    for (int c = lane; c < o.cols; c += 32) {
+      const uint64_t b = (uint64_t)__double_as_longlong(row[c]) & 0x7FFFFFFFFFFFFFFFull;
+      mx = b > mx ? b : mx;
+    }
+    for (int sft = 16; sft > 0; sft >>= 1) {
+      const uint64_t y = __shfl_xor_sync(0xffffffffu, mx, sft);
+      mx = y > mx ? y : mx;
+    }
+    if (lane == 0) exps[o.exp_off + r] = exp_of_bits(mx);
+  }
+}
+
+// B (k x n row-major): one thread per column.
+__global__ void k_col_exp(const double* __restrict__ src, const SplitOperand* __restrict__ ops, int nops,
+                          int32_t* __restrict__ exps, int64_t total_cols) {
+  for (int64_t cg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; cg < total_cols;
+       cg += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nops - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].vec_begin <= cg) lo = mid; else hi = mid - 1; }
+    const SplitOperand o = ops[lo];
+    const int64_t c = cg - o.vec_begin;
+    uint64_t mx = 0;
+    for (int r = 0; r < o.rows; ++r) {
+      const uint64_t b = (uint64_t)__double_as_longlong(src[o.src_off + (int64_t)r * o.cols + c]) & 0x7FFFFFFFFFFFFFFFull;
+      mx = b > mx ? b : mx;
+    }
+    exps[o.exp_off + c] = exp_of_bits(mx);
+  }
+}
+
+// Seven 7-bit digits of x / 2^e (sign-magnitude), as BF16 bit patterns.
+__device__ __forceinline__ void slice7(double x, int e, uint16_t* out) {
+  const uint64_t bits = (uint64_t)__double_as_longlong(x);
+  const uint64_t ab = bits & 0x7FFFFFFFFFFFFFFFull;
+  uint64_t Y = 0;
+  if (ab != 0) {
+    const int ex = (int)(ab >> 52);
+    const uint64_t mant = (ab & 0xFFFFFFFFFFFFFull) | (ex ? (1ull << 52) : 0ull);
+    const int ee = ex ? ex : 1;
+    // |x| = mant 2^(ee - 1075); Y = floor(|x| 2^(49 - e)) = mant >> (1075 + e - 49 - ee)
+    const int sh = 1026 + e - ee;
+    Y = sh >= 64 ? 0 : (mant >> sh);
+  }
+  const uint16_t sgn = (uint16_t)((bits >> 48) & 0x8000u);
+#pragma unroll
+  for (int p = 0; p < kS; ++p) {
+    const uint32_t d = (uint32_t)((Y >> (7 * (kS - 1 - p))) & 127u);
+    // bf16 of the integer d (exact): float bits >> 16
+    const uint32_t f = __float_as_uint((float)d);
+    out[p] = d ? (uint16_t)((f >> 16) | sgn) : (uint16_t)0;
+  }
+}
+
+// Pack A operand tiles. One thread per 16-byte chunk (8 consecutive k of one row) per
+// (row tile, k tile); writes the chunk of every slice plane.
+__global__ void k_pack_a(const double* __restrict__ src, const SplitOperand* __restrict__ ops, int nops,
+                         const int32_t* __restrict__ exps, uint8_t* __restrict__ pack, int64_t total_chunks) {
+  for (int64_t ch = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ch < total_chunks;
+       ch += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nops - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].chunk_begin <= ch) lo = mid; else hi = mid - 1; }
+    const SplitOperand o = ops[lo];
+    const int64_t l = ch - o.chunk_begin;
+    // chunk order inside a (rt, kt) tile: ks (4), m_core (16), k_core (2), r8 (8) = 1024 chunks
+    const int64_t tile = l >> 10;
+    const int w = (int)(l & 1023);
+    const int ks = w >> 8, m_core = (w >> 4) & 15, k_core = (w >> 3) & 1, r8 = w & 7;
+    const int64_t rt = tile / o.ktiles, kt = tile % o.ktiles;
+    const int64_t r = rt * kTM + m_core * 8 + r8;
+    const int64_t k0 = kt * kTK + ks * 16 + k_core * 8;
+    uint16_t sl[8][kS];
+    const int e = r < o.rows ? exps[o.exp_off + r] : 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const double x = (r < o.rows && k0 + j < o.cols) ? src[o.src_off + r * o.cols + k0 + j] : 0.0;
+      slice7(x, e, sl[j]);
+    }
+    const int64_t within = (int64_t)ks * 4096 + m_core * 256 + k_core * 128 + r8 * 16;
+#pragma unroll
+    for (int p = 0; p < kS; ++p) {
+      uint4 v;
+      v.x = (uint32_t)sl[0][p] | ((uint32_t)sl[1][p] << 16);
+      v.y = (uint32_t)sl[2][p] | ((uint32_t)sl[3][p] << 16);
+      v.z = (uint32_t)sl[4][p] | ((uint32_t)sl[5][p] << 16);
+      v.w = (uint32_t)sl[6][p] | ((uint32_t)sl[7][p] << 16);
+      *reinterpret_cast<uint4*>(pack + o.pack_off + (tile * kS + p) * (int64_t)kATile + within) = v;
+    }
+  }
+}
+
+// Pack B operand tiles (k x n row-major source, K-major tiles of 32 columns).
+__global__ void k_pack_b(const double* __restrict__ src, const SplitOperand* __restrict__ ops, int nops,
+                         const int32_t* __restrict__ exps, uint8_t* __restrict__ pack, int64_t total_chunks) {
+  for (int64_t ch = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ch < total_chunks;
+       ch += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nops - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].chunk_begin <= ch) lo = mid; else hi = mid - 1; }
+    const SplitOperand o = ops[lo];
+    const int64_t l = ch - o.chunk_begin;
+    // chunk order inside a (ct, kt) tile: ks (4), n_core (4), k_core (2), n8 (8) = 256 chunks
+    const int64_t tile = l >> 8;
+    const int w = (int)(l & 255);
+    const int ks = w >> 6, n_core = (w >> 4) & 3, k_core = (w >> 3) & 1, n8 = w & 7;
+    const int64_t ct = tile / o.ktiles, kt = tile % o.ktiles;
+    const int64_t c = ct * kTN + n_core * 8 + n8;        // output column (B column)
+    const int64_t k0 = kt * kTK + ks * 16 + k_core * 8;  // B row
+    uint16_t sl[8][kS];
+    const int e = c < o.cols ? exps[o.exp_off + c] : 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const double x = (c < o.cols && k0 + j < o.rows) ? src[o.src_off + (k0 + j) * o.cols + c] : 0.0;
+      slice7(x, e, sl[j]);
+    }
+    const int64_t within = (int64_t)ks * 1024 + n_core * 256 + k_core * 128 + n8 * 16;
+#pragma unroll
+    for (int p = 0; p < kS; ++p) {
+      uint4 v;
+      v.x = (uint32_t)sl[0][p] | ((uint32_t)sl[1][p] << 16);
+      v.y = (uint32_t)sl[2][p] | ((uint32_t)sl[3][p] << 16);
+      v.z = (uint32_t)sl[4][p] | ((uint32_t)sl[5][p] << 16);
+      v.w = (uint32_t)sl[6][p] | ((uint32_t)sl[7][p] << 16);
+      *reinterpret_cast<uint4*>(pack + o.pack_off + (tile * kS + p) * (int64_t)kBTile + within) = v;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ tcgen05 helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  // start >> 4 | LBO (128 B) >> 4 << 16 | SBO (256 B) >> 4 << 32 | fixed 0b001 << 46; no swizzle
+  return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+         ((uint64_t)1 << 46);
+}
+
+// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 32.
+__device__ __forceinline__ uint32_t idesc_bf16() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTN >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t id, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+      "l"(da), "l"(db), "r"(id), "r"(acc));
+}
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for the mbarrier phase with a bounded spin (about 1 s of wall time).
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+  const unsigned long long t0 = gtimer();
+  while (true) {
+    uint32_t done = 0;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(phase));
+    if (done) return true;
+    if (gtimer() - t0 > kWaitNs) return false;
+  }
+}
+
+// 2^n as a double built from its bit pattern (integer ops only), with an ldexp fallback
+// outside the normal range.
+__device__ __forceinline__ double pow2(int n) {
+  if (n >= -1022 && n <= 1023) return __longlong_as_double((long long)(n + 1023) << 52);
+  return ldexp(1.0, n);
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+
+struct SmemLayout {
+  uint8_t a[kS * kATile];   // 112 KB
+  uint8_t b[kS * kBTile];   // 28 KB
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_gemm_split(const GemmCBlk* __restrict__ cblk, const SplitTask* __restrict__ task,
+                 const GemmTile* __restrict__ tiles, int ntiles, const uint8_t* __restrict__ apack,
+                 const uint8_t* __restrict__ bpack, const int32_t* __restrict__ aexp,
+                 const int32_t* __restrict__ bexp, double* __restrict__ C, int* __restrict__ counter,
+                 int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  SmemLayout& sm = *reinterpret_cast<SmemLayout*>(smem_raw);
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int s_ti;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    s_fail = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base;
+  const uint32_t mb = smem_u32(&mbar);
+  const uint32_t sa = smem_u32(sm.a), sb = smem_u32(sm.b);
+  const uint32_t id = idesc_bf16();
+  uint32_t phase = 0;
+  const int row_in_tile = warp * 32 + lane;   // TMEM lane owned by this thread
+  while (true) {
+    if (tid == 0) s_ti = atomicAdd(counter, 1);
+    __syncthreads();
+    const int ti = s_ti;
+    if (ti >= ntiles || s_fail) break;
+    const GemmTile tl = tiles[ti];
+    const GemmCBlk cb = cblk[tl.cblk];
+    const int rt = tl.tm, ct = tl.tn;
+    const int row = rt * kTM + row_in_tile;
+    for (int t = cb.t0; t < cb.t1 && !s_fail; ++t) {
+      const SplitTask tk = task[t];
+      long long hi[kTN], lo[kTN];
+#pragma unroll
+      for (int j = 0; j < kTN; ++j) hi[j] = lo[j] = 0;
+      for (int kt = 0; kt < tk.ktiles; ++kt) {
+        // stage the slices of this k tile (16-byte copies; tiles are contiguous in global)
+        const uint4* ga = reinterpret_cast<const uint4*>(apack + tk.a_pack + ((int64_t)rt * tk.ktiles + kt) * kS * kATile);
+        const uint4* gb = reinterpret_cast<const uint4*>(bpack + tk.b_pack + ((int64_t)ct * tk.ktiles + kt) * kS * kBTile);
+        uint4* da = reinterpret_cast<uint4*>(sm.a);
+        uint4* db = reinterpret_cast<uint4*>(sm.b);
+        for (int i = tid; i < kS * kATile / 16; i += kThreads) da[i] = __ldg(ga + i);
+        for (int i = tid; i < kS * kBTile / 16; i += kThreads) db[i] = __ldg(gb + i);
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const bool first_in_period = (kt % (kDrainK / kTK)) == 0;
+        if (tid == 0) {
+#pragma unroll 1
+          for (int ks = 0; ks < kTK / 16; ++ks) {
+            int lvl_started = 0;   // bit l-2: level already written in this k step / period
+#pragma unroll 1
+            for (int p = 1; p <= kS; ++p) {
+#pragma unroll 1
+              for (int q = 1; p + q <= kS + 1; ++q) {
+                const int l = p + q - 2;
+                const uint64_t adesc = smem_desc(sa + (p - 1) * kATile + ks * 4096);
+                const uint64_t bdesc = smem_desc(sb + (q - 1) * kBTile + ks * 1024);
+                const uint32_t acc = (first_in_period && ks == 0 && !(lvl_started >> l & 1)) ? 0u : 1u;
+                mma_bf16(tmem + (uint32_t)(l * kTN), adesc, bdesc, id, acc);
+                lvl_started |= 1 << l;
+              }
+            }
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb));
+        }
+        const bool ok = mbar_wait(mb, phase);
+        phase ^= 1;
+        if (!ok) {
+          if (lane == 0) atomicExch(err, 1);
+          s_fail = 1;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        __syncthreads();
+        if (s_fail) break;
+        const bool drain = ((kt + 1) % (kDrainK / kTK)) == 0 || kt + 1 == tk.ktiles;
+        if (drain) {
+          const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+          for (int l = 0; l < kLevels; ++l) {
+            uint32_t r[kTN];
+            tmem_ld32(lane_base + (uint32_t)(l * kTN), r);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            // level l+2: hi gets levels 2..4 (weights 2^14, 2^7, 1), lo levels 5..8
+            const int wsh = l < 3 ? 7 * (2 - l) : 7 * (6 - l);
+#pragma unroll
+            for (int j = 0; j < kTN; ++j) {
+              const long long v = (long long)__float2ll_rn(__uint_as_float(r[j])) * (1ll << wsh);
+              if (l < 3) hi[j] += v; else lo[j] += v;
+            }
+          }
+          asm volatile("tcgen05.fence::before_thread_sync;");
+          __syncthreads();
+          asm volatile("tcgen05.fence::after_thread_sync;");
+        }
+      }
+      if (s_fail) break;
+      // C += sign 2^(ea + eb - 56) (hi 2^28 + lo)
+      if (row < cb.m) {
+        const int ea = aexp[tk.a_exp + row];
+        double* out = C + cb.c_off + (int64_t)row * cb.n;
+#pragma unroll
+        for (int j = 0; j < kTN; ++j) {
+          const int col = ct * kTN + j;
+          if (col < cb.n) {
+            const int eb = bexp[tk.b_exp + col];
+            const double v = fma((double)hi[j], 268435456.0, (double)lo[j]);
+            const double sc = tk.sign < 0 ? -pow2(ea + eb - 56) : pow2(ea + eb - 56);
+            if (t == cb.t0) out[col] = v * sc; else out[col] = fma(v, sc, out[col]);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+
+unsigned grid_for(int64_t n, int bs = 256) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + bs - 1) / bs, 152 * 32));
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host side
+void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
+  built = false;
+  const GemmSchedule& g = p.sched;
+  // operand blocks used by non-skinny output blocks
+  std::vector<int32_t> a_of(p.a.nblk, -1), b_of(p.b.nblk, -1);
+  a_ops.clear();
+  b_ops.clear();
+  tasks.clear();
+  tiles.clear();
+  int64_t a_pack = 0, b_pack = 0, a_exp = 0, b_exp = 0, a_vec = 0, b_vec = 0, a_chunks = 0, b_chunks = 0;
+  auto a_index = [&](int64_t a_off) {   // block ordinal from its offset
+    return (int64_t)(std::lower_bound(p.a.offsets.begin(), p.a.offsets.end(), a_off) - p.a.offsets.begin());
+  };
+  auto b_index = [&](int64_t b_off) {
+    return (int64_t)(std::lower_bound(p.b.offsets.begin(), p.b.offsets.end(), b_off) - p.b.offsets.begin());
+  };
+  tasks.resize(g.task.size());
+  for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q) {
+    const GemmCBlk& cb = g.cblk[q];
+    if (skinny_cblk(g, q)) continue;
+    for (int32_t t = cb.t0; t < cb.t1; ++t) {
+      const GemmTask& gt = g.task[t];
+      const int64_t ia = a_index(gt.a_off), ib = b_index(gt.b_off);
+      const int k = gt.k;
+      const int ktiles = (k + kTK - 1) / kTK;
+      if (a_of[ia] < 0) {
+        SplitOperand o{};
+        o.src_off = gt.a_off;
+        o.rows = cb.m;
+        o.cols = k;
+        o.ktiles = ktiles;
+        o.exp_off = (int32_t)a_exp;
+        o.vec_begin = a_vec;
+        o.chunk_begin = a_chunks;
+        o.pack_off = a_pack;
+        const int64_t rtiles = (cb.m + kTM - 1) / kTM;
+        a_exp += cb.m;
+        a_vec += cb.m;
+        a_chunks += rtiles * ktiles * 1024;
+        a_pack += rtiles * ktiles * kS * (int64_t)kATile;
+        a_of[ia] = (int32_t)a_ops.size();
+        a_ops.push_back(o);
+      }
+      if (b_of[ib] < 0) {
+        SplitOperand o{};
+        o.src_off = gt.b_off;
+        o.rows = k;
+        o.cols = cb.n;
+        o.ktiles = ktiles;
+        o.exp_off = (int32_t)b_exp;
+        o.vec_begin = b_vec;
+        o.chunk_begin = b_chunks;
+        o.pack_off = b_pack;
+        const int64_t ctiles = (cb.n + kTN - 1) / kTN;
+        b_exp += cb.n;
+        b_vec += cb.n;
+        b_chunks += ctiles * ktiles * 256;
+        b_pack += ctiles * ktiles * kS * (int64_t)kBTile;
+        b_of[ib] = (int32_t)b_ops.size();
+        b_ops.push_back(o);
+      }
+      const SplitOperand& oa = a_ops[a_of[ia]];
+      const SplitOperand& ob = b_ops[b_of[ib]];
+      QLTG_CHECK(oa.rows == cb.m && oa.cols == k && ob.rows == k && ob.cols == cb.n, QLTG_ERR_INVALID,
+                 "internal: inconsistent operand shapes in the split schedule");
+      tasks[t] = SplitTask{oa.pack_off, ob.pack_off, oa.exp_off, ob.exp_off, ktiles, gt.sign};
+    }
+    const int rtiles = (cb.m + kTM - 1) / kTM, ctiles = (cb.n + kTN - 1) / kTN;
+    for (int i = 0; i < rtiles; ++i)
+      for (int j = 0; j < ctiles; ++j) tiles.push_back(GemmTile{q, (int16_t)i, (int16_t)j});
+  }
+  QLTG_CHECK(tiles.size() < ((size_t)1 << 31), QLTG_ERR_UNSUPPORTED, "too many split tiles");
+  // longest first: tiles of blocks with more k tiles
+  std::vector<int64_t> cost(g.cblk.size(), 0);
+  for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q)
+    for (int32_t t = g.cblk[q].t0; t < g.cblk[q].t1; ++t) cost[q] += tasks[t].ktiles;
+  std::stable_sort(tiles.begin(), tiles.end(), [&](const GemmTile& x, const GemmTile& y) { return cost[x.cblk] > cost[y.cblk]; });
+  n_a_vec = a_vec;
+  n_b_vec = b_vec;
+  n_a_chunks = a_chunks;
+  n_b_chunks = b_chunks;
+  d_a_ops = upload(a_ops, s);
+  d_b_ops = upload(b_ops, s);
+  d_tasks = upload(tasks, s);
+  d_tiles = upload(tiles, s);
+  a_packed.alloc(std::max<int64_t>(a_pack, 16));
+  b_packed.alloc(std::max<int64_t>(b_pack, 16));
+  a_exps.alloc(std::max<int64_t>(a_exp, 1) * 4);
+  b_exps.alloc(std::max<int64_t>(b_exp, 1) * 4);
+  counter.alloc(sizeof(int));
+  error.alloc(sizeof(int));
+  QLTG_CUDA(cudaMemsetAsync(error.get(), 0, sizeof(int), s));
+  static bool attr_set = false;
+  if (!attr_set) {
+    QLTG_CUDA(cudaFuncSetAttribute(k_gemm_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemLayout)));
+    attr_set = true;
+  }
+  QLTG_CUDA(cudaStreamSynchronize(s));
+  built = true;
+}
+
+int64_t SplitPlan::launches() const {
+  if (tiles.empty()) return 0;
+  return 6;   // row exps, col exps, pack A, pack B, counter reset, GEMM
+}
+
+void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cudaStream_t s) {
+  QLTG_CHECK(p.a.dtype == QLTG_F64, QLTG_ERR_UNSUPPORTED, "split-precision mode supports FP64 tensors");
+  if (!p.split) {
+    // first split-mode execution of this plan: build the slice schedule (allocates; not
+    // allowed inside a stream capture - the matvec builds it before capturing)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    QLTG_CUDA(cudaStreamIsCapturing(s, &cs));
+    QLTG_CHECK(cs == cudaStreamCaptureStatusNone, QLTG_ERR_INVALID,
+               "split-precision schedule must be prepared before stream capture (run the plan once first)");
+    prepare_split(p, s);
+  }
+  SplitPlan& sp = *p.split;
+  // skinny output blocks stay on the FP64 skinny kernel (k, n <= 8: the tensor cores would
+  // pad them 8x); everything else goes through the slices
+  launch_gemm_f64_skinny(p.sched, a, b, c, false, p.ctx->num_sms, s);
+  if (sp.tiles.empty()) return;
+  const double* A = static_cast<const double*>(a);
+  const double* B = static_cast<const double*>(b);
+  k_row_exp<<<grid_for(sp.n_a_vec * 32), 256, 0, s>>>(A, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+                                                      sp.a_exps.as<int32_t>(), sp.n_a_vec);
+  k_col_exp<<<grid_for(sp.n_b_vec), 256, 0, s>>>(B, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
+                                                 sp.b_exps.as<int32_t>(), sp.n_b_vec);
+  k_pack_a<<<grid_for(sp.n_a_chunks), 256, 0, s>>>(A, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+                                                   sp.a_exps.as<int32_t>(), sp.a_packed.as<uint8_t>(), sp.n_a_chunks);
+  k_pack_b<<<grid_for(sp.n_b_chunks), 256, 0, s>>>(B, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
+                                                   sp.b_exps.as<int32_t>(), sp.b_packed.as<uint8_t>(), sp.n_b_chunks);
+  QLTG_CUDA(cudaGetLastError());
+  QLTG_CUDA(cudaMemsetAsync(sp.counter.get(), 0, sizeof(int), s));
+  const int grid = (int)std::min<int64_t>((int64_t)sp.tiles.size(), p.ctx->num_sms);
+  k_gemm_split<<<grid, kThreads, sizeof(SmemLayout), s>>>(
+      p.sched.d_cblk.as<GemmCBlk>(), sp.d_tasks.as<SplitTask>(), sp.d_tiles.as<GemmTile>(), (int)sp.tiles.size(),
+      sp.a_packed.as<uint8_t>(), sp.b_packed.as<uint8_t>(), sp.a_exps.as<int32_t>(), sp.b_exps.as<int32_t>(),
+      static_cast<double*>(c), sp.counter.as<int>(), sp.error.as<int>());
+  QLTG_CUDA(cudaGetLastError());
+}
+
+void prepare_split(CtrctPlan& p, cudaStream_t s) {
+  if (p.split && p.split->built) return;
+  if (p.a.dtype != QLTG_F64) return;   // complex operands stay on the FP64 path
+  p.split = std::make_unique<SplitPlan>();
+  p.split->build(p, s);
+}
+
+int64_t split_launches(const CtrctPlan& p) {
+  int64_t n = p.sched.skinny.empty() ? 0 : 1;
+  if (p.split) n += p.split->launches();
+  return n;
+}
+
+int split_device_error(const CtrctPlan& p, cudaStream_t s) {
+  if (!p.split || !p.split->built) return 0;
+  int e = 0;
+  QLTG_CUDA(cudaMemcpyAsync(&e, p.split->error.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+  QLTG_CUDA(cudaStreamSynchronize(s));
+  return e;
 }
 
 }  // namespace qltg

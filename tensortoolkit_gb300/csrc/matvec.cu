@@ -10,6 +10,7 @@
 #include <memory>
 
 #include "ctrct.h"
+#include "split.h"
 
 namespace qltg {
 void finalize_plan(CtrctPlan& p, cudaStream_t s);
@@ -110,6 +111,7 @@ int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* 
       p.axb.assign(ax[i][1], ax[i][1] + nax[i]);
       plan_contraction(p, s);
       finalize_plan(p, s);
+      if (mode == QLTG_MODE_SPLIT) prepare_split(p, s);
       if (i < 3) h->t[i].alloc(std::max<int64_t>(1, p.c.size) * p.c.elem_bytes());
     }
     *mv = h.release();
@@ -136,7 +138,10 @@ int qltg_matvec_stats(const qltg_matvec* mv, double* flops, int64_t* launches) {
     QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
     double f = 0;
     int64_t l = 0;
-    for (auto& p : mv->step) { f += p.flops; l += p.launches_per_exec; }
+    for (auto& p : mv->step) {
+      f += p.flops;
+      l += mv->mode == QLTG_MODE_SPLIT && p.split ? exec_launches_split(p) : p.launches_per_exec;
+    }
     if (flops) *flops = f;
     if (launches) *launches = l;
   });
@@ -148,6 +153,16 @@ int qltg_matvec_apply(qltg_matvec* mv, const void* psi_dev, void* out_dev, void*
     QLTG_CUDA(cudaSetDevice(mv->ctx->device));
     cudaGraphExec_t g = mv->graph_for(psi_dev, out_dev);
     QLTG_CUDA(cudaGraphLaunch(g, static_cast<cudaStream_t>(stream)));
+  });
+}
+
+int qltg_matvec_device_status(qltg_matvec* mv, void* stream) {
+  return guarded([&] {
+    QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
+    QLTG_CUDA(cudaSetDevice(mv->ctx->device));
+    for (auto& p : mv->step)
+      QLTG_CHECK(split_device_error(p, static_cast<cudaStream_t>(stream)) == 0, QLTG_ERR_TIMEOUT,
+                 "a bounded tensor-core wait expired in the split-precision GEMM");
   });
 }
 
