@@ -83,6 +83,8 @@ struct SplitTask {
 };
 struct SplitPlan {
   bool built = false;
+  bool a_static = false, b_static = false;   // operand packed once, unchanged afterwards
+  bool a_ready = false, b_ready = false;
   std::vector<SplitOperand> a_ops, b_ops;
   std::vector<SplitTask> tasks;   // indexed like GemmSchedule::task
   std::vector<GemmTile> tiles;    // (output block, 128-row tile, 32-col tile)

@@ -57,8 +57,8 @@ void finalize_plan(CtrctPlan& p, cudaStream_t s) {
 // Kernel launches of one split-mode execution: operand transposes plus the split stage.
 int64_t exec_launches_split(const CtrctPlan& p) {
   int64_t n = split_launches(p);
-  if (p.a_trans && p.a.size) n += 1;
-  if (p.b_trans && p.b.size) n += 1;
+  if (p.a_trans && p.a.size && !(p.split && p.split->a_static)) n += 1;
+  if (p.b_trans && p.b.size && !(p.split && p.split->b_static)) n += 1;
   return n;
 }
 
@@ -70,12 +70,15 @@ void exec_contraction(CtrctPlan& p, const void* a, const void* b, void* c, int m
   const int eb = (int)p.a.elem_bytes();
   const void* ap = a;
   const void* bp = b;
+  // operands packed once for the split path (constant for the plan's life) need no transpose
+  const bool a_packed = mode == QLTG_MODE_SPLIT && p.split && p.split->a_static && p.split->a_ready;
+  const bool b_packed = mode == QLTG_MODE_SPLIT && p.split && p.split->b_static && p.split->b_ready;
   if (p.a_trans && p.a.size) {
-    if (stage != 2) p.a_tl.launch(a, p.a_t.get(), eb, s);
+    if (stage != 2 && !a_packed) p.a_tl.launch(a, p.a_t.get(), eb, s);
     ap = p.a_t.get();
   }
   if (p.b_trans && p.b.size) {
-    if (stage != 2) p.b_tl.launch(b, p.b_t.get(), eb, s);
+    if (stage != 2 && !b_packed) p.b_tl.launch(b, p.b_t.get(), eb, s);
     bp = p.b_t.get();
   }
   if (stage == 1) return;

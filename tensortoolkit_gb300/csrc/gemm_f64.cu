@@ -34,8 +34,12 @@ __device__ __forceinline__ void fma_acc(double2& acc, double2 a, double2 b) {
 }
 __device__ __forceinline__ double zero_of(double) { return 0.0; }
 __device__ __forceinline__ double2 zero_of(double2) { return make_double2(0.0, 0.0); }
-__device__ __forceinline__ double scale(double x, double s) { return x * s; }
-__device__ __forceinline__ double2 scale(double2 x, double s) { return make_double2(x.x * s, x.y * s); }
+// Multiply by a +-1 sign without touching the FP64 pipe: flip the IEEE sign bit(s).
+__device__ __forceinline__ double flip(double x, unsigned long long m) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)m);
+}
+__device__ __forceinline__ double2 flip(double2 x, unsigned long long m) { return make_double2(flip(x.x, m), flip(x.y, m)); }
+__device__ __forceinline__ unsigned long long sign_mask(int sign) { return sign < 0 ? 0x8000000000000000ull : 0ull; }
 
 // One output tile of BM x BN per work item; 16 x 16 threads, each 2 x 2 outputs at
 // (ty + 16 i, tx + 16 j). Operand tiles are staged through shared memory (A transposed so
@@ -75,14 +79,14 @@ __global__ void __launch_bounds__(NT) k_gemm_dfma(const GemmCBlk* __restrict__ c
       const int k = tk.k;
       const T* a = A + tk.a_off;
       const T* b = B + tk.b_off;
-      const double sg = (double)tk.sign;
+      const unsigned long long sg = sign_mask(tk.sign);
       for (int k0 = 0; k0 < k; k0 += BK) {
         const int kc = min(BK, k - k0);
 #pragma unroll
         for (int e = threadIdx.x; e < BM * BK; e += NT) {
           const int row = e / BK, kk = e % BK;
           T v = zero_of(T());
-          if (kk < kc && r0 + row < m) v = scale(a[(int64_t)(r0 + row) * k + k0 + kk], sg);
+          if (kk < kc && r0 + row < m) v = flip(a[(int64_t)(r0 + row) * k + k0 + kk], sg);
           As[kk][row] = v;
         }
 #pragma unroll
@@ -117,9 +121,33 @@ __global__ void __launch_bounds__(NT) k_gemm_dfma(const GemmCBlk* __restrict__ c
   }
 }
 
-// Skinny output blocks (n <= 8, every task k <= 8): thread per output row.
+// Skinny output blocks (n <= 8, every task k <= 8): thread per output row, the row's n
+// outputs in registers, instantiated per n so no FP64 slot is spent on absent columns.
 constexpr int kSkinnyRows = 256;
 constexpr int kSkinnyMax = 8;
+
+template <typename T, int NN>
+__device__ __forceinline__ void skinny_row(const GemmCBlk& cb, const GemmTask* __restrict__ task, int row,
+                                           const T* __restrict__ A, const T* __restrict__ B, T* __restrict__ C) {
+  T acc[NN];
+#pragma unroll
+  for (int j = 0; j < NN; ++j) acc[j] = zero_of(T());
+  for (int t = cb.t0; t < cb.t1; ++t) {
+    const GemmTask tk = task[t];
+    const int k = tk.k;
+    const T* a = A + tk.a_off + (int64_t)row * k;
+    const T* b = B + tk.b_off;
+    const unsigned long long sg = sign_mask(tk.sign);
+    for (int kk = 0; kk < k; ++kk) {
+      const T av = flip(__ldg(a + kk), sg);
+#pragma unroll
+      for (int j = 0; j < NN; ++j) fma_acc(acc[j], av, __ldg(b + kk * NN + j));
+    }
+  }
+  T* out = C + cb.c_off + (int64_t)row * NN;
+#pragma unroll
+  for (int j = 0; j < NN; ++j) out[j] = acc[j];
+}
 
 template <typename T>
 __global__ void __launch_bounds__(kSkinnyRows) k_gemm_skinny(const GemmCBlk* __restrict__ cblk,
@@ -131,28 +159,16 @@ __global__ void __launch_bounds__(kSkinnyRows) k_gemm_skinny(const GemmCBlk* __r
     const GemmRowChunk item = items[it];
     const GemmCBlk cb = cblk[item.cblk];
     const int row = item.chunk * kSkinnyRows + threadIdx.x;
-    const int n = cb.n;
-    T acc[kSkinnyMax];
-#pragma unroll
-    for (int j = 0; j < kSkinnyMax; ++j) acc[j] = zero_of(T());
-    if (row < cb.m) {
-      for (int t = cb.t0; t < cb.t1; ++t) {
-        const GemmTask tk = task[t];
-        const int k = tk.k;
-        const T* a = A + tk.a_off + (int64_t)row * k;
-        const T* b = B + tk.b_off;
-        const double sg = (double)tk.sign;
-        for (int kk = 0; kk < k; ++kk) {
-          const T av = scale(__ldg(a + kk), sg);
-#pragma unroll
-          for (int j = 0; j < kSkinnyMax; ++j)
-            if (j < n) fma_acc(acc[j], av, __ldg(b + kk * n + j));
-        }
-      }
-      T* out = C + cb.c_off + (int64_t)row * n;
-#pragma unroll
-      for (int j = 0; j < kSkinnyMax; ++j)
-        if (j < n) out[j] = acc[j];
+    if (row >= cb.m) continue;
+    switch (cb.n) {
+      case 1: skinny_row<T, 1>(cb, task, row, A, B, C); break;
+      case 2: skinny_row<T, 2>(cb, task, row, A, B, C); break;
+      case 3: skinny_row<T, 3>(cb, task, row, A, B, C); break;
+      case 4: skinny_row<T, 4>(cb, task, row, A, B, C); break;
+      case 5: skinny_row<T, 5>(cb, task, row, A, B, C); break;
+      case 6: skinny_row<T, 6>(cb, task, row, A, B, C); break;
+      case 7: skinny_row<T, 7>(cb, task, row, A, B, C); break;
+      default: skinny_row<T, 8>(cb, task, row, A, B, C); break;
     }
   }
 }

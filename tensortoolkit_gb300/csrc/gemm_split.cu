@@ -256,137 +256,198 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
       : "r"(taddr));
 }
 
-struct SmemLayout {
-  uint8_t a[kS * kATile];   // 112 KB
-  uint8_t b[kS * kBTile];   // 28 KB
+// Three-stage operand pipeline: a stage holds one 32-wide k slab of all 7 A slices
+// (7 x 8 KB) and all 7 B slices (7 x 2 KB) = 70 KB; 3 stages = 210 KB of shared memory.
+constexpr int kStages = 3;
+constexpr int kKS = 32;                         // k per stage (2 MMA k-steps)
+constexpr int kAStage = kTM * kKS * 2;          // 8 KB per A slice per stage
+constexpr int kBStage = kTN * kKS * 2;          // 2 KB per B slice per stage
+constexpr int kStageBytes = kS * (kAStage + kBStage);
+constexpr int kSmemBytes = kStages * kStageBytes + 1024;
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes));
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
+}
+
+// Cursor over the k stages of the tasks of one output block.
+struct StageCursor {
+  int t, j, nst;
 };
+
+__device__ __forceinline__ int stages_of(const SplitTask& tk, int k) { return (k + kKS - 1) / kKS; }
 
 __global__ void __launch_bounds__(kThreads, 1)
     k_gemm_split(const GemmCBlk* __restrict__ cblk, const SplitTask* __restrict__ task,
-                 const GemmTile* __restrict__ tiles, int ntiles, const uint8_t* __restrict__ apack,
-                 const uint8_t* __restrict__ bpack, const int32_t* __restrict__ aexp,
-                 const int32_t* __restrict__ bexp, double* __restrict__ C, int* __restrict__ counter,
-                 int* __restrict__ err) {
-  extern __shared__ __align__(1024) uint8_t smem_raw[];
-  SmemLayout& sm = *reinterpret_cast<SmemLayout*>(smem_raw);
-  __shared__ __align__(8) uint64_t mbar;
+                 const GemmTask* __restrict__ gtask, const GemmTile* __restrict__ tiles, int ntiles,
+                 const uint8_t* __restrict__ apack, const uint8_t* __restrict__ bpack,
+                 const int32_t* __restrict__ aexp, const int32_t* __restrict__ bexp, double* __restrict__ C,
+                 int* __restrict__ counter, int* __restrict__ err) {
+  extern __shared__ uint8_t smem_dyn[];
+  // 1024-byte aligned stage area
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
+  __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], accum_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int s_ti;
-  __shared__ int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // Failure (an expired bounded wait) is a per-thread flag; every decision to stop goes
+  // through __syncthreads_or so the whole CTA leaves its loops together.
+  int fail = 0;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                  "r"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    for (int s = 0; s < kStages; ++s) { mbar_init(smem_u32(&full_bar[s]), 1); mbar_init(smem_u32(&empty_bar[s]), 1); }
+    mbar_init(smem_u32(&accum_bar), 1);
     asm volatile("fence.mbarrier_init.release.cluster;");
-    s_fail = 0;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_base;
-  const uint32_t mb = smem_u32(&mbar);
-  const uint32_t sa = smem_u32(sm.a), sb = smem_u32(sm.b);
+  const uint32_t sbase = smem_u32(smem);
   const uint32_t id = idesc_bf16();
-  uint32_t phase = 0;
-  const int row_in_tile = warp * 32 + lane;   // TMEM lane owned by this thread
+  // per-stage use counters (control thread only) and the accumulator-barrier phase (all)
+  uint32_t loads[kStages] = {0, 0, 0}, consumed[kStages] = {0, 0, 0};
+  uint32_t accum_phase = 0;
+  const int row_in_tile = warp * 32 + lane;
   while (true) {
     if (tid == 0) s_ti = atomicAdd(counter, 1);
     __syncthreads();
     const int ti = s_ti;
-    if (ti >= ntiles || s_fail) break;
+    if (ti >= ntiles) break;
     const GemmTile tl = tiles[ti];
     const GemmCBlk cb = cblk[tl.cblk];
     const int rt = tl.tm, ct = tl.tn;
     const int row = rt * kTM + row_in_tile;
-    for (int t = cb.t0; t < cb.t1 && !s_fail; ++t) {
+    bool stop = false;
+    // total stages of this tile (all tasks)
+    int G = 0;
+    for (int t = cb.t0; t < cb.t1; ++t) G += stages_of(task[t], gtask[t].k);
+    // control thread: producer cursor and prologue (stages 0 .. kStages-2)
+    StageCursor pc{cb.t0, 0, stages_of(task[cb.t0], gtask[cb.t0].k)};
+    int pg = 0;
+    auto issue_load = [&](int g) {
+      const int s = g % kStages;
+      if (loads[s] > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (loads[s] - 1) & 1)) { atomicExch(err, 1); fail = 1; }
+      loads[s]++;
+      const SplitTask tk = task[pc.t];
+      const int kt = pc.j >> 1, half = pc.j & 1;
+      const uint8_t* ga = apack + tk.a_pack + ((int64_t)rt * tk.ktiles + kt) * kS * kATile + half * kAStage;
+      const uint8_t* gb = bpack + tk.b_pack + ((int64_t)ct * tk.ktiles + kt) * kS * kBTile + half * kBStage;
+      const uint32_t sa = sbase + s * kStageBytes, sb = sa + kS * kAStage;
+      const uint32_t fb = smem_u32(&full_bar[s]);
+      mbar_expect_tx(fb, kStageBytes);
+      for (int p = 0; p < kS; ++p) {
+        bulk_g2s(sa + p * kAStage, ga + (int64_t)p * kATile, kAStage, fb);
+        bulk_g2s(sb + p * kBStage, gb + (int64_t)p * kBTile, kBStage, fb);
+      }
+      if (++pc.j == pc.nst && pc.t + 1 < cb.t1) { ++pc.t; pc.j = 0; pc.nst = stages_of(task[pc.t], gtask[pc.t].k); }
+    };
+    if (tid == 0) {
+      for (; pg < G && pg < kStages - 1; ++pg) issue_load(pg);
+    }
+    int g = 0;
+    for (int t = cb.t0; t < cb.t1; ++t) {
       const SplitTask tk = task[t];
+      const int nst = stages_of(tk, gtask[t].k);
       long long hi[kTN], lo[kTN];
 #pragma unroll
       for (int j = 0; j < kTN; ++j) hi[j] = lo[j] = 0;
-      for (int kt = 0; kt < tk.ktiles; ++kt) {
-        // stage the slices of this k tile (16-byte copies; tiles are contiguous in global)
-        const uint4* ga = reinterpret_cast<const uint4*>(apack + tk.a_pack + ((int64_t)rt * tk.ktiles + kt) * kS * kATile);
-        const uint4* gb = reinterpret_cast<const uint4*>(bpack + tk.b_pack + ((int64_t)ct * tk.ktiles + kt) * kS * kBTile);
-        uint4* da = reinterpret_cast<uint4*>(sm.a);
-        uint4* db = reinterpret_cast<uint4*>(sm.b);
-        for (int i = tid; i < kS * kATile / 16; i += kThreads) da[i] = __ldg(ga + i);
-        for (int i = tid; i < kS * kBTile / 16; i += kThreads) db[i] = __ldg(gb + i);
-        asm volatile("fence.proxy.async.shared::cta;");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const bool first_in_period = (kt % (kDrainK / kTK)) == 0;
+      for (int j = 0; j < nst; ++j, ++g) {
+        const bool first_in_period = (j % (kDrainK / kKS)) == 0;
+        const bool drain = ((j + 1) % (kDrainK / kKS)) == 0 || j + 1 == nst;
         if (tid == 0) {
+          const int s = g % kStages;
+          if (!mbar_wait(smem_u32(&full_bar[s]), consumed[s] & 1)) { atomicExch(err, 1); fail = 1; }
+          consumed[s]++;
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t sa = sbase + s * kStageBytes, sb = sa + kS * kAStage;
 #pragma unroll 1
-          for (int ks = 0; ks < kTK / 16; ++ks) {
-            int lvl_started = 0;   // bit l-2: level already written in this k step / period
+          for (int ks = 0; ks < kKS / 16; ++ks) {
+            int started = 0;
 #pragma unroll 1
             for (int p = 1; p <= kS; ++p) {
 #pragma unroll 1
               for (int q = 1; p + q <= kS + 1; ++q) {
                 const int l = p + q - 2;
-                const uint64_t adesc = smem_desc(sa + (p - 1) * kATile + ks * 4096);
-                const uint64_t bdesc = smem_desc(sb + (q - 1) * kBTile + ks * 1024);
-                const uint32_t acc = (first_in_period && ks == 0 && !(lvl_started >> l & 1)) ? 0u : 1u;
+                const uint64_t adesc = smem_desc(sa + (p - 1) * kAStage + ks * 4096);
+                const uint64_t bdesc = smem_desc(sb + (q - 1) * kBStage + ks * 1024);
+                const uint32_t acc = (first_in_period && ks == 0 && !(started >> l & 1)) ? 0u : 1u;
                 mma_bf16(tmem + (uint32_t)(l * kTN), adesc, bdesc, id, acc);
-                lvl_started |= 1 << l;
+                started |= 1 << l;
               }
             }
           }
-          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb));
+          tc_commit(smem_u32(&empty_bar[s]));
+          if (drain) tc_commit(smem_u32(&accum_bar));
+          // keep kStages - 1 loads in flight
+          if (pg < G) issue_load(pg++);
         }
-        const bool ok = mbar_wait(mb, phase);
-        phase ^= 1;
-        if (!ok) {
-          if (lane == 0) atomicExch(err, 1);
-          s_fail = 1;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        __syncthreads();
-        if (s_fail) break;
-        const bool drain = ((kt + 1) % (kDrainK / kTK)) == 0 || kt + 1 == tk.ktiles;
         if (drain) {
+          if (!mbar_wait(smem_u32(&accum_bar), accum_phase & 1)) {
+            if (lane == 0) atomicExch(err, 1);
+            fail = 1;
+          }
+          accum_phase++;
+          asm volatile("tcgen05.fence::after_thread_sync;");
           const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
           for (int l = 0; l < kLevels; ++l) {
             uint32_t r[kTN];
             tmem_ld32(lane_base + (uint32_t)(l * kTN), r);
             asm volatile("tcgen05.wait::ld.sync.aligned;");
-            // level l+2: hi gets levels 2..4 (weights 2^14, 2^7, 1), lo levels 5..8
             const int wsh = l < 3 ? 7 * (2 - l) : 7 * (6 - l);
 #pragma unroll
-            for (int j = 0; j < kTN; ++j) {
-              const long long v = (long long)__float2ll_rn(__uint_as_float(r[j])) * (1ll << wsh);
-              if (l < 3) hi[j] += v; else lo[j] += v;
+            for (int c = 0; c < kTN; ++c) {
+              const long long v = (long long)__float2ll_rn(__uint_as_float(r[c])) * (1ll << wsh);
+              if (l < 3) hi[c] += v; else lo[c] += v;
             }
           }
           asm volatile("tcgen05.fence::before_thread_sync;");
-          __syncthreads();
+          stop = __syncthreads_or(fail) != 0;
           asm volatile("tcgen05.fence::after_thread_sync;");
+          if (stop) break;
         }
       }
-      if (s_fail) break;
-      // C += sign 2^(ea + eb - 56) (hi 2^28 + lo)
+      if (stop) break;
+      // C (+)= sign 2^(ea + eb - 56) (hi 2^28 + lo)
       if (row < cb.m) {
         const int ea = aexp[tk.a_exp + row];
         double* out = C + cb.c_off + (int64_t)row * cb.n;
 #pragma unroll
-        for (int j = 0; j < kTN; ++j) {
-          const int col = ct * kTN + j;
+        for (int c = 0; c < kTN; ++c) {
+          const int col = ct * kTN + c;
           if (col < cb.n) {
             const int eb = bexp[tk.b_exp + col];
-            const double v = fma((double)hi[j], 268435456.0, (double)lo[j]);
+            const double v = fma((double)hi[c], 268435456.0, (double)lo[c]);
             const double sc = tk.sign < 0 ? -pow2(ea + eb - 56) : pow2(ea + eb - 56);
             if (t == cb.t0) out[col] = v * sc; else out[col] = fma(v, sc, out[col]);
           }
         }
       }
     }
-    __syncthreads();
+    if (__syncthreads_or(fail)) break;
+  }
+  // Leave nothing in flight: wait (bounded) for this CTA's outstanding bulk copies and
+  // tensor-core operations before the tensor memory is freed. A no-op on the normal path.
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s)
+      for (; consumed[s] < loads[s]; ++consumed[s]) mbar_wait(smem_u32(&full_bar[s]), consumed[s] & 1);
+    tc_commit(smem_u32(&accum_bar));
+    mbar_wait(smem_u32(&accum_bar), accum_phase & 1);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -476,7 +537,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   // longest first: tiles of blocks with more k tiles
   std::vector<int64_t> cost(g.cblk.size(), 0);
   for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q)
-    for (int32_t t = g.cblk[q].t0; t < g.cblk[q].t1; ++t) cost[q] += tasks[t].ktiles;
+    for (int32_t t = g.cblk[q].t0; t < g.cblk[q].t1; ++t) cost[q] += (g.task[t].k + 31) / 32;
   std::stable_sort(tiles.begin(), tiles.end(), [&](const GemmTile& x, const GemmTile& y) { return cost[x.cblk] > cost[y.cblk]; });
   n_a_vec = a_vec;
   n_b_vec = b_vec;
@@ -495,7 +556,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   QLTG_CUDA(cudaMemsetAsync(error.get(), 0, sizeof(int), s));
   static bool attr_set = false;
   if (!attr_set) {
-    QLTG_CUDA(cudaFuncSetAttribute(k_gemm_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemLayout)));
+    QLTG_CUDA(cudaFuncSetAttribute(k_gemm_split, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     attr_set = true;
   }
   QLTG_CUDA(cudaStreamSynchronize(s));
@@ -504,7 +565,47 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
 
 int64_t SplitPlan::launches() const {
   if (tiles.empty()) return 0;
-  return 6;   // row exps, col exps, pack A, pack B, counter reset, GEMM
+  return (a_static ? 0 : 2) + (b_static ? 0 : 2) + 2;   // exps + pack per packed side, counter reset, GEMM
+}
+
+// Scale exponents and slice tiles of one operand side (A: rows, B: columns).
+void pack_split_operand(SplitPlan& sp, bool side_a, const void* src, cudaStream_t s) {
+  const double* X = static_cast<const double*>(src);
+  if (side_a) {
+    if (sp.a_ops.empty()) return;
+    k_row_exp<<<grid_for(sp.n_a_vec * 32), 256, 0, s>>>(X, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+                                                        sp.a_exps.as<int32_t>(), sp.n_a_vec);
+    k_pack_a<<<grid_for(sp.n_a_chunks), 256, 0, s>>>(X, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+                                                     sp.a_exps.as<int32_t>(), sp.a_packed.as<uint8_t>(),
+                                                     sp.n_a_chunks);
+  } else {
+    if (sp.b_ops.empty()) return;
+    k_col_exp<<<grid_for(sp.n_b_vec), 256, 0, s>>>(X, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
+                                                   sp.b_exps.as<int32_t>(), sp.n_b_vec);
+    k_pack_b<<<grid_for(sp.n_b_chunks), 256, 0, s>>>(X, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
+                                                     sp.b_exps.as<int32_t>(), sp.b_packed.as<uint8_t>(),
+                                                     sp.n_b_chunks);
+  }
+  QLTG_CUDA(cudaGetLastError());
+  (side_a ? sp.a_ready : sp.b_ready) = true;
+}
+
+void split_prepack_static(CtrctPlan& p, const void* a_static, const void* b_static, cudaStream_t s) {
+  if (!p.split || !p.split->built) return;
+  const int eb = (int)p.a.elem_bytes();
+  if (a_static) {
+    const void* src = a_static;
+    if (p.a_trans && p.a.size) { p.a_tl.launch(a_static, p.a_t.get(), eb, s); src = p.a_t.get(); }
+    p.split->a_static = true;
+    pack_split_operand(*p.split, true, src, s);
+  }
+  if (b_static) {
+    const void* src = b_static;
+    if (p.b_trans && p.b.size) { p.b_tl.launch(b_static, p.b_t.get(), eb, s); src = p.b_t.get(); }
+    p.split->b_static = true;
+    pack_split_operand(*p.split, false, src, s);
+  }
+  QLTG_CUDA(cudaStreamSynchronize(s));
 }
 
 void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cudaStream_t s) {
@@ -523,21 +624,13 @@ void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cuda
   // pad them 8x); everything else goes through the slices
   launch_gemm_f64_skinny(p.sched, a, b, c, false, p.ctx->num_sms, s);
   if (sp.tiles.empty()) return;
-  const double* A = static_cast<const double*>(a);
-  const double* B = static_cast<const double*>(b);
-  k_row_exp<<<grid_for(sp.n_a_vec * 32), 256, 0, s>>>(A, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
-                                                      sp.a_exps.as<int32_t>(), sp.n_a_vec);
-  k_col_exp<<<grid_for(sp.n_b_vec), 256, 0, s>>>(B, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
-                                                 sp.b_exps.as<int32_t>(), sp.n_b_vec);
-  k_pack_a<<<grid_for(sp.n_a_chunks), 256, 0, s>>>(A, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
-                                                   sp.a_exps.as<int32_t>(), sp.a_packed.as<uint8_t>(), sp.n_a_chunks);
-  k_pack_b<<<grid_for(sp.n_b_chunks), 256, 0, s>>>(B, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
-                                                   sp.b_exps.as<int32_t>(), sp.b_packed.as<uint8_t>(), sp.n_b_chunks);
-  QLTG_CUDA(cudaGetLastError());
+  if (!(sp.a_static && sp.a_ready)) pack_split_operand(sp, true, a, s);
+  if (!(sp.b_static && sp.b_ready)) pack_split_operand(sp, false, b, s);
   QLTG_CUDA(cudaMemsetAsync(sp.counter.get(), 0, sizeof(int), s));
   const int grid = (int)std::min<int64_t>((int64_t)sp.tiles.size(), p.ctx->num_sms);
-  k_gemm_split<<<grid, kThreads, sizeof(SmemLayout), s>>>(
-      p.sched.d_cblk.as<GemmCBlk>(), sp.d_tasks.as<SplitTask>(), sp.d_tiles.as<GemmTile>(), (int)sp.tiles.size(),
+  k_gemm_split<<<grid, kThreads, kSmemBytes, s>>>(
+      p.sched.d_cblk.as<GemmCBlk>(), sp.d_tasks.as<SplitTask>(), p.sched.d_task.as<GemmTask>(), sp.d_tiles.as<GemmTile>(),
+      (int)sp.tiles.size(),
       sp.a_packed.as<uint8_t>(), sp.b_packed.as<uint8_t>(), sp.a_exps.as<int32_t>(), sp.b_exps.as<int32_t>(),
       static_cast<double*>(c), sp.counter.as<int>(), sp.error.as<int>());
   QLTG_CUDA(cudaGetLastError());

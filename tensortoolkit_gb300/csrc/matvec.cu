@@ -111,7 +111,12 @@ int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* 
       p.axb.assign(ax[i][1], ax[i][1] + nax[i]);
       plan_contraction(p, s);
       finalize_plan(p, s);
-      if (mode == QLTG_MODE_SPLIT) prepare_split(p, s);
+      if (mode == QLTG_MODE_SPLIT) {
+        prepare_split(p, s);
+        // lenv (A of the first step) and renv (B of the last) are constant for the matvec's life
+        if (i == 0) split_prepack_static(p, h->lenv, nullptr, s);
+        if (i == 3) split_prepack_static(p, nullptr, h->renv, s);
+      }
       if (i < 3) h->t[i].alloc(std::max<int64_t>(1, p.c.size) * p.c.elem_bytes());
     }
     *mv = h.release();

@@ -8,6 +8,8 @@ namespace qltg {
 void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cudaStream_t s);
 // Build the slice schedule of a plan (allocates; call before any stream capture).
 void prepare_split(CtrctPlan& p, cudaStream_t s);
+// Pack an operand that stays constant for the plan's lifetime once, now (either may be NULL).
+void split_prepack_static(CtrctPlan& p, const void* a_static, const void* b_static, cudaStream_t s);
 // Kernel launches of one split-mode execution of the GEMM stage.
 int64_t split_launches(const CtrctPlan& p);
 // Device error word of the split GEMM (1 = a bounded tensor-core wait expired).

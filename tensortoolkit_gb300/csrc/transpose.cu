@@ -55,6 +55,22 @@ __global__ void __launch_bounds__(256) k_permute(const PermDesc* __restrict__ de
     int64_t dstride[kMaxRank];
     dstride[r - 1] = 1;
     for (int i = r - 2; i >= 0; --i) dstride[i] = dstride[i + 1] * d.dims[i + 1];
+    if (d.p < 0) {
+      // gather mode (small inner dims): 1024 consecutive destination elements per work item,
+      // each thread decodes its source offset; writes coalesced, reads in short runs
+      const int64_t total = d.nouter;   // block size for this mode
+      const int64_t e0 = local * kRunChunk;
+      for (int64_t e = e0 + threadIdx.x; e < min(e0 + kRunChunk, total); e += blockDim.x) {
+        int64_t rem = e, soff = 0;
+        for (int i = r - 1; i >= 0; --i) {
+          const int64_t x = rem % d.dims[i];
+          rem /= d.dims[i];
+          soff += x * d.sstride[i];
+        }
+        dst[d.dst_off + e] = mul_sign(src[d.src_off + soff], sign);
+      }
+      continue;
+    }
     if (d.p == q) {
       // copy mode: innermost run of length dims[q] contiguous on both sides
       const int64_t chunks_per_run = (d.dims[q] + kRunChunk - 1) / kRunChunk;
@@ -168,8 +184,12 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
     } else if (d.p == m - 1) {
       const int64_t runs = t.blk_size(b) / dd[m - 1];
       tiles = runs * ((dd[m - 1] + kRunChunk - 1) / kRunChunk);
+    } else if (d.p < 0 || dd[d.p] < 16 || dd[m - 1] < 16) {
+      // inner dims too short for 32 x 32 tiles: destination-ordered gather
+      d.p = -1;
+      d.nouter = t.blk_size(b);
+      tiles = (d.nouter + kRunChunk - 1) / kRunChunk;
     } else {
-      QLTG_CHECK(d.p >= 0, QLTG_ERR_INVALID, "internal: permutation without a unit-stride dim");
       d.tiles_p = (int32_t)((dd[d.p] + kTile - 1) / kTile);
       d.tiles_q = (int32_t)((dd[m - 1] + kTile - 1) / kTile);
       d.nouter = t.blk_size(b) / (dd[d.p] * dd[m - 1]);
