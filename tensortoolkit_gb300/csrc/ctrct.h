@@ -71,6 +71,7 @@ struct SplitOperand {
   int64_t pack_off;       // byte offset of its packed slice tiles
   int64_t vec_begin;      // prefix over operands of rows (A) / columns (B): exponent work items
   int64_t chunk_begin;    // prefix over operands of 16-byte packing chunks
+  int64_t item_begin;     // B only: prefix of (column, 32-row chunk) exponent items
   int32_t rows, cols;     // A: m x k; B: k x n
   int32_t ktiles;         // 64-wide k tiles
   int32_t exp_off;        // offset of its row (A) / column (B) exponents
@@ -88,7 +89,7 @@ struct SplitPlan {
   std::vector<SplitOperand> a_ops, b_ops;
   std::vector<SplitTask> tasks;   // indexed like GemmSchedule::task
   std::vector<GemmTile> tiles;    // (output block, 128-row tile, 32-col tile)
-  int64_t n_a_vec = 0, n_b_vec = 0, n_a_chunks = 0, n_b_chunks = 0;
+  int64_t n_a_vec = 0, n_b_vec = 0, n_a_chunks = 0, n_b_chunks = 0, n_b_items = 0;
   DevBuf d_a_ops, d_b_ops, d_tasks, d_tiles, a_packed, b_packed, a_exps, b_exps, counter, error;
   void build(const struct CtrctPlan& p, cudaStream_t s);
   int64_t launches() const;

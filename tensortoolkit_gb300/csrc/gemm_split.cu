@@ -49,7 +49,6 @@ constexpr int kBTile = kTN * kTK * 2;      // 4 KB
 constexpr int kThreads = 128;
 constexpr int kDrainK = 128;               // k between drains (exactness bound)
 constexpr uint32_t kTmemCols = 256;        // >= 7 * 32, power of two
-constexpr unsigned long long kWaitNs = 1000000000ull;   // 1 s bound on any wait
 
 // ------------------------------------------------------------------ slicing
 // Row / column scale exponents: e with max |x| < 2^e (0 for an all-zero row).
@@ -83,22 +82,33 @@ __global__ void k_row_exp(const double* __restrict__ src, const SplitOperand* __
   }
 }
 
-// B (k x n row-major): one thread per column.
+// B (k x n row-major): the scale of a column only depends on the largest exponent field in
+// it, so threads take (column, 32-row chunk) items and fold into the column with atomicMax
+// on the biased exponent (the array starts at zero); k_col_exp_finish turns fields into
+// scale exponents.
 __global__ void k_col_exp(const double* __restrict__ src, const SplitOperand* __restrict__ ops, int nops,
-                          int32_t* __restrict__ exps, int64_t total_cols) {
-  for (int64_t cg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; cg < total_cols;
-       cg += (int64_t)gridDim.x * blockDim.x) {
+                          int32_t* __restrict__ exps, int64_t total_items) {
+  for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < total_items;
+       it += (int64_t)gridDim.x * blockDim.x) {
     int lo = 0, hi = nops - 1;
-    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].vec_begin <= cg) lo = mid; else hi = mid - 1; }
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].item_begin <= it) lo = mid; else hi = mid - 1; }
     const SplitOperand o = ops[lo];
-    const int64_t c = cg - o.vec_begin;
-    uint64_t mx = 0;
-    for (int r = 0; r < o.rows; ++r) {
-      const uint64_t b = (uint64_t)__double_as_longlong(src[o.src_off + (int64_t)r * o.cols + c]) & 0x7FFFFFFFFFFFFFFFull;
-      mx = b > mx ? b : mx;
+    const int64_t l = it - o.item_begin;
+    const int64_t c = l % o.cols, r0 = (l / o.cols) * 32;
+    int mx = 0;
+    const int64_t r1 = min((int64_t)o.rows, r0 + 32);
+    for (int64_t r = r0; r < r1; ++r) {
+      const uint64_t b = (uint64_t)__double_as_longlong(src[o.src_off + r * o.cols + c]) & 0x7FFFFFFFFFFFFFFFull;
+      const int f = b == 0 ? 0 : max(1, (int)(b >> 52));
+      mx = max(mx, f);
     }
-    exps[o.exp_off + c] = exp_of_bits(mx);
+    if (mx) atomicMax(&exps[o.exp_off + c], mx);
   }
+}
+
+__global__ void k_col_exp_finish(int32_t* __restrict__ exps, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    exps[i] = exps[i] == 0 ? 0 : exps[i] - 1022;
 }
 
 // Seven 7-bit digits of x / 2^e (sign-magnitude), as BF16 bit patterns.
@@ -218,23 +228,27 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db
       "l"(da), "l"(db), "r"(id), "r"(acc));
 }
 
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
+// Wait for the mbarrier phase with a bounded spin: about 1 s of SM clock (2^31 cycles at
+// the 2.07 GHz maximum), checked every 256 polls so the fast path is a bare try_wait.
+constexpr long long kWaitCycles = 1ll << 31;
 
-// Wait for the mbarrier phase with a bounded spin (about 1 s of wall time).
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
-  const unsigned long long t0 = gtimer();
+  uint32_t done = 0;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(mbar), "r"(phase));
+  if (done) return true;
+  const long long t0 = clock64();
   while (true) {
-    uint32_t done = 0;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(done)
-        : "r"(mbar), "r"(phase));
-    if (done) return true;
-    if (gtimer() - t0 > kWaitNs) return false;
+    for (int i = 0; i < 256; ++i) {
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+          : "=r"(done)
+          : "r"(mbar), "r"(phase));
+      if (done) return true;
+    }
+    if (clock64() - t0 > kWaitCycles) return false;
   }
 }
 
@@ -256,20 +270,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
       : "r"(taddr));
 }
 
-// Three-stage operand pipeline: a stage holds one 32-wide k slab of all 7 A slices
-// (7 x 8 KB) and all 7 B slices (7 x 2 KB) = 70 KB; 3 stages = 210 KB of shared memory.
+// Operand pipeline: a stage holds one 32-wide k slab of all 7 A slices (7 x 8 KB) and all
+// 7 B slices (7 x 2 KB) = 70 KB; 3 stages = 210 KB of shared memory.
 constexpr int kStages = 3;
 constexpr int kKS = 32;                         // k per stage (2 MMA k-steps)
 constexpr int kAStage = kTM * kKS * 2;          // 8 KB per A slice per stage
 constexpr int kBStage = kTN * kKS * 2;          // 2 KB per B slice per stage
 constexpr int kStageBytes = kS * (kAStage + kBStage);
 constexpr int kSmemBytes = kStages * kStageBytes + 1024;
+constexpr int kPeriod = kDrainK / kKS;          // stages between drains (4)
+constexpr int kRoleThreads = 192;               // warp 0 producer, warp 1 MMA, warps 2-5 drain
+constexpr uint32_t kTmemAlloc = 512;            // two buffers of 7 levels x 32 columns
 
 __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count));
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes));
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar));
 }
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
@@ -280,130 +300,171 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
 }
 
-// Cursor over the k stages of the tasks of one output block.
-struct StageCursor {
-  int t, j, nst;
-};
+// Bounded wait that also gives up as soon as another role has aborted.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t phase, volatile int* abort_flag) {
+  uint32_t done = 0;
+  const long long t0 = clock64();
+  while (true) {
+    for (int i = 0; i < 256; ++i) {
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+          : "=r"(done)
+          : "r"(mbar), "r"(phase));
+      if (done) return true;
+    }
+    if (*abort_flag || clock64() - t0 > kWaitCycles) return false;
+  }
+}
 
-__device__ __forceinline__ int stages_of(const SplitTask& tk, int k) { return (k + kKS - 1) / kKS; }
-
-__global__ void __launch_bounds__(kThreads, 1)
+// Warp-specialised split GEMM. All roles walk the same static sequence of work items
+// (output tiles ti = blockIdx.x, blockIdx.x + gridDim.x, ...; for each its tasks; for each
+// task its 32-wide k stages), so they agree on stage, period and buffer numbers without
+// talking: the producer fills stage g % 3 once the MMAs of stage g - 3 released it; the
+// MMA thread consumes stage g into TMEM buffer (period d) % 2 once the drain of period
+// d - 2 released that buffer; the drain warps read a buffer after its MMAs completed and
+// release it, and after a task's last period write the task's contribution to C.
+__global__ void __launch_bounds__(kRoleThreads, 1)
     k_gemm_split(const GemmCBlk* __restrict__ cblk, const SplitTask* __restrict__ task,
                  const GemmTask* __restrict__ gtask, const GemmTile* __restrict__ tiles, int ntiles,
                  const uint8_t* __restrict__ apack, const uint8_t* __restrict__ bpack,
                  const int32_t* __restrict__ aexp, const int32_t* __restrict__ bexp, double* __restrict__ C,
-                 int* __restrict__ counter, int* __restrict__ err) {
+                 int* __restrict__ err) {
   extern __shared__ uint8_t smem_dyn[];
-  // 1024-byte aligned stage area
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
-  __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], accum_bar;
+  __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], accf_bar[2], acce_bar[2], fin_bar;
   __shared__ uint32_t tmem_base;
-  __shared__ int s_ti;
+  __shared__ volatile int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // Failure (an expired bounded wait) is a per-thread flag; every decision to stop goes
-  // through __syncthreads_or so the whole CTA leaves its loops together.
-  int fail = 0;
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"(kTmemCols));
+                 "r"(kTmemAlloc));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) { mbar_init(smem_u32(&full_bar[s]), 1); mbar_init(smem_u32(&empty_bar[s]), 1); }
-    mbar_init(smem_u32(&accum_bar), 1);
+    for (int b = 0; b < 2; ++b) { mbar_init(smem_u32(&accf_bar[b]), 1); mbar_init(smem_u32(&acce_bar[b]), 4); }
+    mbar_init(smem_u32(&fin_bar), 1);
     asm volatile("fence.mbarrier_init.release.cluster;");
+    s_abort = 0;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_base;
   const uint32_t sbase = smem_u32(smem);
-  const uint32_t id = idesc_bf16();
-  // per-stage use counters (control thread only) and the accumulator-barrier phase (all)
-  uint32_t loads[kStages] = {0, 0, 0}, consumed[kStages] = {0, 0, 0};
-  uint32_t accum_phase = 0;
-  const int row_in_tile = warp * 32 + lane;
-  while (true) {
-    if (tid == 0) s_ti = atomicAdd(counter, 1);
-    __syncthreads();
-    const int ti = s_ti;
-    if (ti >= ntiles) break;
-    const GemmTile tl = tiles[ti];
-    const GemmCBlk cb = cblk[tl.cblk];
-    const int rt = tl.tm, ct = tl.tn;
-    const int row = rt * kTM + row_in_tile;
-    bool stop = false;
-    // total stages of this tile (all tasks)
-    int G = 0;
-    for (int t = cb.t0; t < cb.t1; ++t) G += stages_of(task[t], gtask[t].k);
-    // control thread: producer cursor and prologue (stages 0 .. kStages-2)
-    StageCursor pc{cb.t0, 0, stages_of(task[cb.t0], gtask[cb.t0].k)};
-    int pg = 0;
-    auto issue_load = [&](int g) {
-      const int s = g % kStages;
-      if (loads[s] > 0 && !mbar_wait(smem_u32(&empty_bar[s]), (loads[s] - 1) & 1)) { atomicExch(err, 1); fail = 1; }
-      loads[s]++;
-      const SplitTask tk = task[pc.t];
-      const int kt = pc.j >> 1, half = pc.j & 1;
-      const uint8_t* ga = apack + tk.a_pack + ((int64_t)rt * tk.ktiles + kt) * kS * kATile + half * kAStage;
-      const uint8_t* gb = bpack + tk.b_pack + ((int64_t)ct * tk.ktiles + kt) * kS * kBTile + half * kBStage;
-      const uint32_t sa = sbase + s * kStageBytes, sb = sa + kS * kAStage;
-      const uint32_t fb = smem_u32(&full_bar[s]);
-      mbar_expect_tx(fb, kStageBytes);
-      for (int p = 0; p < kS; ++p) {
-        bulk_g2s(sa + p * kAStage, ga + (int64_t)p * kATile, kAStage, fb);
-        bulk_g2s(sb + p * kBStage, gb + (int64_t)p * kBTile, kBStage, fb);
-      }
-      if (++pc.j == pc.nst && pc.t + 1 < cb.t1) { ++pc.t; pc.j = 0; pc.nst = stages_of(task[pc.t], gtask[pc.t].k); }
-    };
-    if (tid == 0) {
-      for (; pg < G && pg < kStages - 1; ++pg) issue_load(pg);
-    }
-    int g = 0;
-    for (int t = cb.t0; t < cb.t1; ++t) {
-      const SplitTask tk = task[t];
-      const int nst = stages_of(tk, gtask[t].k);
-      long long hi[kTN], lo[kTN];
-#pragma unroll
-      for (int j = 0; j < kTN; ++j) hi[j] = lo[j] = 0;
-      for (int j = 0; j < nst; ++j, ++g) {
-        const bool first_in_period = (j % (kDrainK / kKS)) == 0;
-        const bool drain = ((j + 1) % (kDrainK / kKS)) == 0 || j + 1 == nst;
-        if (tid == 0) {
+  auto fail = [&]() {
+    s_abort = 1;
+    atomicExch(err, 1);
+  };
+
+  if (warp == 0 && lane == 0) {
+    // ------------------------------------------------------------ producer
+    uint32_t g = 0;
+    for (int ti = blockIdx.x; ti < ntiles && !s_abort; ti += gridDim.x) {
+      const GemmTile tl = tiles[ti];
+      const GemmCBlk cb = cblk[tl.cblk];
+      for (int t = cb.t0; t < cb.t1 && !s_abort; ++t) {
+        const SplitTask tk = task[t];
+        const int nst = (gtask[t].k + kKS - 1) / kKS;
+        for (int j = 0; j < nst; ++j, ++g) {
           const int s = g % kStages;
-          if (!mbar_wait(smem_u32(&full_bar[s]), consumed[s] & 1)) { atomicExch(err, 1); fail = 1; }
-          consumed[s]++;
-          asm volatile("tcgen05.fence::after_thread_sync;");
+          if (g >= (uint32_t)kStages &&
+              !mbar_wait_or_abort(smem_u32(&empty_bar[s]), ((g / kStages) - 1) & 1, &s_abort)) { fail(); break; }
+          const int kt = j >> 1, half = j & 1;
+          const uint8_t* ga = apack + tk.a_pack + ((int64_t)tl.tm * tk.ktiles + kt) * kS * kATile + half * kAStage;
+          const uint8_t* gb = bpack + tk.b_pack + ((int64_t)tl.tn * tk.ktiles + kt) * kS * kBTile + half * kBStage;
           const uint32_t sa = sbase + s * kStageBytes, sb = sa + kS * kAStage;
-#pragma unroll 1
+          const uint32_t fb = smem_u32(&full_bar[s]);
+          mbar_expect_tx(fb, kStageBytes);
+#pragma unroll
+          for (int p = 0; p < kS; ++p) {
+            bulk_g2s(sa + p * kAStage, ga + (int64_t)p * kATile, kAStage, fb);
+            bulk_g2s(sb + p * kBStage, gb + (int64_t)p * kBTile, kBStage, fb);
+          }
+        }
+      }
+    }
+    // copies still in flight are waited for by the MMA thread (every issued stage is
+    // consumed on the normal path); on abort wait for the tail of issued stages here
+    if (s_abort) {
+      for (uint32_t x = (g > (uint32_t)kStages ? g - kStages : 0); x < g; ++x)
+        mbar_wait_or_abort(smem_u32(&full_bar[x % kStages]), (x / kStages) & 1, &s_abort);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ------------------------------------------------------------ MMA issuer
+    const uint32_t id = idesc_bf16();
+    // descriptor of stage 0, slice 1, k-step 0; every other operand is a fixed byte offset
+    const uint64_t da0 = smem_desc(sbase), db0 = smem_desc(sbase + kS * kAStage);
+    uint32_t g = 0, d = 0;
+    for (int ti = blockIdx.x; ti < ntiles && !s_abort; ti += gridDim.x) {
+      const GemmTile tl = tiles[ti];
+      const GemmCBlk cb = cblk[tl.cblk];
+      for (int t = cb.t0; t < cb.t1 && !s_abort; ++t) {
+        const int nst = (gtask[t].k + kKS - 1) / kKS;
+        for (int j = 0; j < nst; ++j, ++g) {
+          const int s = g % kStages;
+          const int buf = d & 1;
+          const bool first = (j % kPeriod) == 0;
+          const bool drain = (j % kPeriod) == kPeriod - 1 || j + 1 == nst;
+          if (first && d >= 2 && !mbar_wait_or_abort(smem_u32(&acce_bar[buf]), ((d / 2) - 1) & 1, &s_abort)) {
+            fail();
+            break;
+          }
+          if (!mbar_wait_or_abort(smem_u32(&full_bar[s]), (g / kStages) & 1, &s_abort)) { fail(); break; }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint64_t soff = (uint64_t)((s * kStageBytes) >> 4);
+          const uint32_t dbuf = tmem + (uint32_t)(buf * kLevels * kTN);
+#pragma unroll
           for (int ks = 0; ks < kKS / 16; ++ks) {
             int started = 0;
-#pragma unroll 1
+#pragma unroll
             for (int p = 1; p <= kS; ++p) {
-#pragma unroll 1
+#pragma unroll
               for (int q = 1; p + q <= kS + 1; ++q) {
                 const int l = p + q - 2;
-                const uint64_t adesc = smem_desc(sa + (p - 1) * kAStage + ks * 4096);
-                const uint64_t bdesc = smem_desc(sb + (q - 1) * kBStage + ks * 1024);
-                const uint32_t acc = (first_in_period && ks == 0 && !(started >> l & 1)) ? 0u : 1u;
-                mma_bf16(tmem + (uint32_t)(l * kTN), adesc, bdesc, id, acc);
+                const uint64_t adesc = da0 + soff + (uint64_t)(((p - 1) * kAStage + ks * 4096) >> 4);
+                const uint64_t bdesc = db0 + soff + (uint64_t)(((q - 1) * kBStage + ks * 1024) >> 4);
+                const uint32_t acc = (first && ks == 0 && !(started >> l & 1)) ? 0u : 1u;
+                mma_bf16(dbuf + (uint32_t)(l * kTN), adesc, bdesc, id, acc);
                 started |= 1 << l;
               }
             }
           }
           tc_commit(smem_u32(&empty_bar[s]));
-          if (drain) tc_commit(smem_u32(&accum_bar));
-          // keep kStages - 1 loads in flight
-          if (pg < G) issue_load(pg++);
+          if (drain) { tc_commit(smem_u32(&accf_bar[buf])); ++d; }
         }
-        if (drain) {
-          if (!mbar_wait(smem_u32(&accum_bar), accum_phase & 1)) {
-            if (lane == 0) atomicExch(err, 1);
-            fail = 1;
+      }
+    }
+    // all MMAs issued by this thread complete before the tensor memory is released
+    tc_commit(smem_u32(&fin_bar));
+    mbar_wait_or_abort(smem_u32(&fin_bar), 0, &s_abort);
+  } else if (warp >= 2) {
+    // ------------------------------------------------------------ drain / epilogue
+    const int quad = warp & 3;                       // TMEM lanes 32 * quad .. + 31
+    const int row_in_tile = quad * 32 + lane;
+    uint32_t d = 0;
+    for (int ti = blockIdx.x; ti < ntiles && !s_abort; ti += gridDim.x) {
+      const GemmTile tl = tiles[ti];
+      const GemmCBlk cb = cblk[tl.cblk];
+      const int row = tl.tm * kTM + row_in_tile;
+      bool stop = false;
+      for (int t = cb.t0; t < cb.t1 && !stop; ++t) {
+        const SplitTask tk = task[t];
+        const int nst = (gtask[t].k + kKS - 1) / kKS;
+        long long hi[kTN], lo[kTN];
+#pragma unroll
+        for (int c = 0; c < kTN; ++c) hi[c] = lo[c] = 0;
+        for (int j = 0; j < nst; ++j) {
+          const bool drain = (j % kPeriod) == kPeriod - 1 || j + 1 == nst;
+          if (!drain) continue;
+          const int buf = d & 1;
+          if (!mbar_wait_or_abort(smem_u32(&accf_bar[buf]), (d / 2) & 1, &s_abort)) {
+            if (lane == 0) fail();
+            stop = true;
+            break;
           }
-          accum_phase++;
           asm volatile("tcgen05.fence::after_thread_sync;");
-          const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+          const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * kLevels * kTN);
 #pragma unroll 1
           for (int l = 0; l < kLevels; ++l) {
             uint32_t r[kTN];
@@ -412,47 +473,40 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int wsh = l < 3 ? 7 * (2 - l) : 7 * (6 - l);
 #pragma unroll
             for (int c = 0; c < kTN; ++c) {
-              const long long v = (long long)__float2ll_rn(__uint_as_float(r[c])) * (1ll << wsh);
+              // exact integer below 2^24: the 32-bit conversion suffices
+              const long long v = (long long)__float2int_rn(__uint_as_float(r[c])) * (1ll << wsh);
               if (l < 3) hi[c] += v; else lo[c] += v;
             }
           }
           asm volatile("tcgen05.fence::before_thread_sync;");
-          stop = __syncthreads_or(fail) != 0;
-          asm volatile("tcgen05.fence::after_thread_sync;");
-          if (stop) break;
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
+          ++d;
         }
-      }
-      if (stop) break;
-      // C (+)= sign 2^(ea + eb - 56) (hi 2^28 + lo)
-      if (row < cb.m) {
-        const int ea = aexp[tk.a_exp + row];
-        double* out = C + cb.c_off + (int64_t)row * cb.n;
+        if (stop) break;
+        // C (+)= sign 2^(ea + eb - 56) (hi 2^28 + lo)
+        if (row < cb.m) {
+          const int ea = aexp[tk.a_exp + row];
+          double* out = C + cb.c_off + (int64_t)row * cb.n;
 #pragma unroll
-        for (int c = 0; c < kTN; ++c) {
-          const int col = ct * kTN + c;
-          if (col < cb.n) {
-            const int eb = bexp[tk.b_exp + col];
-            const double v = fma((double)hi[c], 268435456.0, (double)lo[c]);
-            const double sc = tk.sign < 0 ? -pow2(ea + eb - 56) : pow2(ea + eb - 56);
-            if (t == cb.t0) out[col] = v * sc; else out[col] = fma(v, sc, out[col]);
+          for (int c = 0; c < kTN; ++c) {
+            const int col = tl.tn * kTN + c;
+            if (col < cb.n) {
+              const int eb = bexp[tk.b_exp + col];
+              const double v = fma((double)hi[c], 268435456.0, (double)lo[c]);
+              const double sc = tk.sign < 0 ? -pow2(ea + eb - 56) : pow2(ea + eb - 56);
+              if (t == cb.t0) out[col] = v * sc; else out[col] = fma(v, sc, out[col]);
+            }
           }
         }
       }
+      if (stop) break;
     }
-    if (__syncthreads_or(fail)) break;
-  }
-  // Leave nothing in flight: wait (bounded) for this CTA's outstanding bulk copies and
-  // tensor-core operations before the tensor memory is freed. A no-op on the normal path.
-  if (tid == 0) {
-    for (int s = 0; s < kStages; ++s)
-      for (; consumed[s] < loads[s]; ++consumed[s]) mbar_wait(smem_u32(&full_bar[s]), consumed[s] & 1);
-    tc_commit(smem_u32(&accum_bar));
-    mbar_wait(smem_u32(&accum_bar), accum_phase & 1);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemAlloc));
 }
 
 unsigned grid_for(int64_t n, int bs = 256) {
@@ -471,7 +525,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   b_ops.clear();
   tasks.clear();
   tiles.clear();
-  int64_t a_pack = 0, b_pack = 0, a_exp = 0, b_exp = 0, a_vec = 0, b_vec = 0, a_chunks = 0, b_chunks = 0;
+  int64_t a_pack = 0, b_pack = 0, a_exp = 0, b_exp = 0, a_vec = 0, b_vec = 0, a_chunks = 0, b_chunks = 0, b_items = 0;
   auto a_index = [&](int64_t a_off) {   // block ordinal from its offset
     return (int64_t)(std::lower_bound(p.a.offsets.begin(), p.a.offsets.end(), a_off) - p.a.offsets.begin());
   };
@@ -513,11 +567,13 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
         o.ktiles = ktiles;
         o.exp_off = (int32_t)b_exp;
         o.vec_begin = b_vec;
+        o.item_begin = b_items;
         o.chunk_begin = b_chunks;
         o.pack_off = b_pack;
         const int64_t ctiles = (cb.n + kTN - 1) / kTN;
         b_exp += cb.n;
         b_vec += cb.n;
+        b_items += (int64_t)cb.n * ((k + 31) / 32);
         b_chunks += ctiles * ktiles * 256;
         b_pack += ctiles * ktiles * kS * (int64_t)kBTile;
         b_of[ib] = (int32_t)b_ops.size();
@@ -543,6 +599,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   n_b_vec = b_vec;
   n_a_chunks = a_chunks;
   n_b_chunks = b_chunks;
+  n_b_items = b_items;
   d_a_ops = upload(a_ops, s);
   d_b_ops = upload(b_ops, s);
   d_tasks = upload(tasks, s);
@@ -565,7 +622,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
 
 int64_t SplitPlan::launches() const {
   if (tiles.empty()) return 0;
-  return (a_static ? 0 : 2) + (b_static ? 0 : 2) + 2;   // exps + pack per packed side, counter reset, GEMM
+  return (a_static ? 0 : 2) + (b_static ? 0 : 4) + 1;   // per side: (memset,) exps, (finish,) pack; GEMM
 }
 
 // Scale exponents and slice tiles of one operand side (A: rows, B: columns).
@@ -580,8 +637,10 @@ void pack_split_operand(SplitPlan& sp, bool side_a, const void* src, cudaStream_
                                                      sp.n_a_chunks);
   } else {
     if (sp.b_ops.empty()) return;
-    k_col_exp<<<grid_for(sp.n_b_vec), 256, 0, s>>>(X, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
-                                                   sp.b_exps.as<int32_t>(), sp.n_b_vec);
+    QLTG_CUDA(cudaMemsetAsync(sp.b_exps.get(), 0, sp.n_b_vec * sizeof(int32_t), s));
+    k_col_exp<<<grid_for(sp.n_b_items), 256, 0, s>>>(X, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
+                                                     sp.b_exps.as<int32_t>(), sp.n_b_items);
+    k_col_exp_finish<<<grid_for(sp.n_b_vec), 256, 0, s>>>(sp.b_exps.as<int32_t>(), sp.n_b_vec);
     k_pack_b<<<grid_for(sp.n_b_chunks), 256, 0, s>>>(X, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
                                                      sp.b_exps.as<int32_t>(), sp.b_packed.as<uint8_t>(),
                                                      sp.n_b_chunks);
@@ -626,13 +685,12 @@ void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cuda
   if (sp.tiles.empty()) return;
   if (!(sp.a_static && sp.a_ready)) pack_split_operand(sp, true, a, s);
   if (!(sp.b_static && sp.b_ready)) pack_split_operand(sp, false, b, s);
-  QLTG_CUDA(cudaMemsetAsync(sp.counter.get(), 0, sizeof(int), s));
   const int grid = (int)std::min<int64_t>((int64_t)sp.tiles.size(), p.ctx->num_sms);
-  k_gemm_split<<<grid, kThreads, kSmemBytes, s>>>(
+  k_gemm_split<<<grid, kRoleThreads, kSmemBytes, s>>>(
       p.sched.d_cblk.as<GemmCBlk>(), sp.d_tasks.as<SplitTask>(), p.sched.d_task.as<GemmTask>(), sp.d_tiles.as<GemmTile>(),
       (int)sp.tiles.size(),
       sp.a_packed.as<uint8_t>(), sp.b_packed.as<uint8_t>(), sp.a_exps.as<int32_t>(), sp.b_exps.as<int32_t>(),
-      static_cast<double*>(c), sp.counter.as<int>(), sp.error.as<int>());
+      static_cast<double*>(c), sp.error.as<int>());
   QLTG_CUDA(cudaGetLastError());
 }
 
