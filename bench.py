@@ -103,6 +103,88 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk):
+    """Time the GEMM stage of each of the four contractions alone (CUDA events on the
+    launching stream, L2 flushed before each launch) and relate it to the peak."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from tensortoolkit_gb300 import capi
+    from tensortoolkit_gb300.api import ContractionPlan, DTensor
+    mode_i = capi.QLTG_MODE_SPLIT if mode == "split" else capi.QLTG_MODE_FP64
+    axes = [[[0], [0]], [[0, 2], [0, 1]], [[4, 1], [0, 1]], [[4, 1], [1, 0]]]
+    bs = [dp, d1, d2, dr]
+    cur_a, a_meta = dl, lenv
+    per, gemm_ms, alg_flops, tc_flops = [], 0.0, 0.0, 0.0
+    for i in range(4):
+        p = ContractionPlan(a_meta, bs[i].meta if i else psi, axes[i], local)
+        c = DTensor.empty(p.result, local)
+        p.execute(cur_a, bs[i], c, mode=mode)
+        sp = C.c_void_p(stream.cuda_stream)
+        capi.check(capi.lib().qltg_ctrct_exec_stage(p.h, C.c_void_p(cur_a.ptr), C.c_void_p(bs[i].ptr),
+                                                    C.c_void_p(c.ptr), mode_i, 1, sp))
+        ts = []
+        for r in range(5):
+            flush.fill_(float(r))
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            capi.check(capi.lib().qltg_ctrct_exec_stage(p.h, C.c_void_p(cur_a.ptr), C.c_void_p(bs[i].ptr),
+                                                        C.c_void_p(c.ptr), mode_i, 2, sp))
+            s1.record(stream)
+            ts.append((s0, s1))
+        torch.cuda.synchronize()
+        p.device_status()
+        ms = statistics.median(x.elapsed_time(y) for x, y in ts)
+        f, _ = p.stats()
+        tasks = p.tasks()
+        tcf = 0.0
+        if mode == "split" and len(tasks):
+            # group by output block: (m, n) and its ks
+            cbs = {}
+            for (_, _, cidx, m, k, n, _, _) in tasks:
+                cbs.setdefault(int(cidx), [int(m), int(n), []])[2].append(int(k))
+            for m, n, ks in cbs.values():
+                if n <= 8 and max(ks) <= 8:
+                    continue            # skinny blocks stay on the FP64 pipe
+                tiles = -(-m // 128) * -(-n // 32)
+                stages = sum(-(-k // 32) for k in ks)
+                tcf += tiles * stages * 2 * 28 * (2 * 128 * 32 * 16)
+        per.append({"ms": round(ms, 4), "gflop": round(f / 1e9, 4), "tensor_gflop": round(tcf / 1e9, 2)})
+        gemm_ms += ms
+        alg_flops += f
+        tc_flops += tcf
+        cur_a, a_meta = c, p.result
+    if mode == "split":
+        achieved = tc_flops / (gemm_ms / 1e3) / 1e12
+        peak = pk["bf16_tflops"]
+        src = f"bf16 dense burst, {pk['source']} (MEASURED_PEAKS.json)"
+        what = ("k_gemm_split + slice packing, 4 launches per matvec; achieved = executed BF16 tensor flops "
+                "(28 slice products, 128x32x32 padded tiles) / GEMM-stage time")
+    else:
+        n = 8192
+        x = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
+        y = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
+        torch.matmul(x, y)
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(3):
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            torch.matmul(x, y)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, s0.elapsed_time(s1))
+        peak = 2 * n ** 3 / (best / 1e3) / 1e12
+        del x, y
+        achieved = alg_flops / (gemm_ms / 1e3) / 1e12
+        src = "cuBLAS DGEMM 8192^3 measured in this run (the FP64 pipe)"
+        what = "k_gemm_dfma + k_gemm_skinny, algorithmic flops sum(2mkn) / GEMM-stage time"
+    return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if peak else None, "traffic": None, "kernel": what, "peak_source": src,
+            "per_step": per, "gemm_stage_ms": round(gemm_ms, 4),
+            "fp64_equiv_tflops": alg_flops / (gemm_ms / 1e3) / 1e12}
+
+
 def cpu_matvec_time(tensors, iters: int, threads: int) -> float:
     """Seconds per matvec of the CPU restatement (median of `iters`)."""
     from oracle import oracle
@@ -150,7 +232,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--mode", choices=["split", "fp64"], default=os.environ.get("QLTG_BENCH_MODE", "fp64"))
+    ap.add_argument("--mode", choices=["both", "split", "fp64"], default=os.environ.get("QLTG_BENCH_MODE", "both"),
+                    help="both (default): headline split precision, plain FP64 beside it")
     ap.add_argument("--cpu-iters", type=int, default=None, help="CPU baseline sample size")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: plan the D=4000 matvec, apply it twice, print nothing else")
@@ -178,126 +261,75 @@ def main():
     tensors = workloads.heisenberg(WORKLOAD["D"], WORKLOAD["qmax"], WORKLOAD["sigma"], WORKLOAD["seed"])
     lenv, psi, mpo1, mpo2, renv = tensors
     dl, dp, d1, d2, dr = (DTensor.from_host(x, local) for x in tensors)
-    mv = Matvec(dl, psi, d1, d2, dr, mode=args.mode)
-    flops, launches_per_step = mv.stats()
-    out = DTensor.empty(mv.result, local)
-    if args.profile:
-        for _ in range(2):
-            mv.apply(dp, out)
-        torch.cuda.synchronize()
-        print(json.dumps({"profile_run": True, "mode": args.mode, "launches_per_step": launches_per_step}))
-        return
     stream = torch.cuda.current_stream(local)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+    modes = ["split", "fp64"] if args.mode == "both" else [args.mode]
 
-    # warm-up
-    for _ in range(args.warmup):
-        mv.apply(dp, out)
-    torch.cuda.synchronize()
-
-    # device-resident timed region
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        for i in range(args.steps):
-            flush.fill_(float(i))            # write > L2 between steps
-            evs[i][0].record(stream)
-            mv.apply(dp, out)
-            evs[i][1].record(stream)
-        torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
-    t_step = dev_ms / 1e3 / args.steps
-
-    # end to end through the public API with pinned host buffers
-    h_in = torch.from_numpy(psi.raw_f64()).pin_memory()
-    h_out = torch.empty(mv.result.size * (2 if mv.result.is_complex else 1), dtype=torch.float64).pin_memory()
-    d_in = DTensor.empty(psi, local)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(2):
-        d_in.buf[: h_in.numel()].copy_(h_in, non_blocking=True)
-        mv.apply(d_in, out)
-        h_out.copy_(out.buf[: h_out.numel()], non_blocking=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for i in range(args.steps):
-        d_in.buf[: h_in.numel()].copy_(h_in, non_blocking=True)
-        mv.apply(d_in, out)
-        h_out.copy_(out.buf[: h_out.numel()], non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_step = e0.elapsed_time(e1) / 1e3 / args.steps
-
-    # roofline of the dominant kernel: the grouped GEMM of each step, timed alone
-    pk = peaks()
-    gemm_stats = []
-    plans = []
-    ins = [dl, None, None, None]
-    cur_a = dl
-    bs = [dp, d1, d2, dr]
-    axes = [[[0], [0]], [[0, 2], [0, 1]], [[4, 1], [0, 1]], [[4, 1], [1, 0]]]
-    a_meta = lenv
-    outs = []
-    for i in range(4):
-        p = ContractionPlan(a_meta, bs[i].meta if i else psi, axes[i], local)
-        c = DTensor.empty(p.result, local)
-        p.execute(cur_a, bs[i], c, mode=args.mode)
-        plans.append((p, cur_a, bs[i], c))
-        cur_a, a_meta = c, p.result
-    torch.cuda.synchronize()
-    mode_i = capi.QLTG_MODE_SPLIT if args.mode == "split" else capi.QLTG_MODE_FP64
-    gemm_ms_total, gemm_flops_total = 0.0, 0.0
-    reps = 5
-    for p, a, b, c in plans:
-        sp = C.c_void_p(stream.cuda_stream)
-        capi.check(capi.lib().qltg_ctrct_exec_stage(p.h, C.c_void_p(a.ptr), C.c_void_p(b.ptr), C.c_void_p(c.ptr),
-                                                    mode_i, 1, sp))
-        ts = []
-        for r in range(reps):
-            flush.fill_(float(r))
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            capi.check(capi.lib().qltg_ctrct_exec_stage(p.h, C.c_void_p(a.ptr), C.c_void_p(b.ptr),
-                                                        C.c_void_p(c.ptr), mode_i, 2, sp))
-            s1.record(stream)
-            ts.append((s0, s1))
-        torch.cuda.synchronize()
-        ms = statistics.median(x.elapsed_time(y) for x, y in ts)
-        f, _ = p.stats()
-        gemm_stats.append({"flops": f, "ms": ms})
-        gemm_ms_total += ms
-        gemm_flops_total += f
-    # FP64 peak: cuBLAS DGEMM through torch (the plain-FP64 denominator); tensor peak for split
-    if args.mode == "fp64":
-        n = 8192
-        x = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
-        y = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
-        torch.matmul(x, y)
-        torch.cuda.synchronize()
-        best = 1e9
-        for _ in range(3):
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            torch.matmul(x, y)
-            s1.record(stream)
+    if args.profile:
+        for m in modes:
+            mv = Matvec(dl, psi, d1, d2, dr, mode=m)
+            out = DTensor.empty(mv.result, local)
+            for _ in range(2):
+                mv.apply(dp, out)
             torch.cuda.synchronize()
-            best = min(best, s0.elapsed_time(s1))
-        peak_tf = 2 * n ** 3 / (best / 1e3) / 1e12
-        peak_src = "cuBLAS DGEMM 8192^3 measured in this run (FP64 pipe)"
-        del x, y
-    else:
-        peak_tf = pk["bf16_tflops"]
-        peak_src = f"bf16 dense, {pk['source']} (MEASURED_PEAKS.json)"
-    achieved = gemm_flops_total / (gemm_ms_total / 1e3) / 1e12
-    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
-                "frac": achieved / peak_tf if peak_tf else None, "traffic": None,
-                "kernel": "k_gemm_grouped (4 launches per matvec)", "peak_source": peak_src,
-                "per_step_ms": [round(g["ms"], 4) for g in gemm_stats],
-                "gemm_share_of_step": gemm_ms_total / (t_step * 1e3)}
+        print(json.dumps({"profile_run": True, "modes": modes}))
+        return
 
+    pk = peaks()
+    results = {}
+    clk_summary = None
+    for m in modes:
+        mv = Matvec(dl, psi, d1, d2, dr, mode=m)
+        flops, launches_per_step = mv.stats()
+        out = DTensor.empty(mv.result, local)
+        for _ in range(args.warmup):
+            mv.apply(dp, out)
+        torch.cuda.synchronize()
+        mv.device_status()
+        # device-resident timed region
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            for i in range(args.steps):
+                flush.fill_(float(i))            # write > L2 between steps
+                evs[i][0].record(stream)
+                mv.apply(dp, out)
+                evs[i][1].record(stream)
+            torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        mv.device_status()
+        t_step = sum(a.elapsed_time(b) for a, b in evs) / 1e3 / args.steps
+        if clk_summary is None:
+            clk_summary = clk.summary()
+        # end to end through the public API with pinned host buffers
+        h_in = torch.from_numpy(psi.raw_f64()).pin_memory()
+        h_out = torch.empty(mv.result.size, dtype=torch.float64).pin_memory()
+        d_in = DTensor.empty(psi, local)
+        for _ in range(2):
+            d_in.buf[: h_in.numel()].copy_(h_in, non_blocking=True)
+            mv.apply(d_in, out)
+            h_out.copy_(out.buf[: h_out.numel()], non_blocking=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(args.steps):
+            d_in.buf[: h_in.numel()].copy_(h_in, non_blocking=True)
+            mv.apply(d_in, out)
+            h_out.copy_(out.buf[: h_out.numel()], non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_step = e0.elapsed_time(e1) / 1e3 / args.steps
+        roof = gemm_roofline(m, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
+        results[m] = {"s_per_iter": t_step, "e2e_s_per_iter": e2e_step, "flops": flops,
+                      "launches_per_step": launches_per_step, "roofline": roof,
+                      "h2d": int(h_in.numel() * 8), "d2h": int(h_out.numel() * 8)}
+        del mv, out
+
+    head = results[modes[0]]
+    t_step = head["s_per_iter"]
     # max over ranks
     t_max = t_step
     if world > 1:
@@ -307,10 +339,8 @@ def main():
 
     if rank == 0:
         cpu = None
-        cpu_iters = args.cpu_iters
         try:
-            if cpu_iters is None:
-                cpu_iters = 10
+            cpu_iters = 10 if args.cpu_iters is None else args.cpu_iters
             threads = os.cpu_count() or 1
             v = cpu_matvec_time(tensors, cpu_iters, threads)
             cpu = {"value": v, "unit": "s/iter", "cores": threads, "kind": "port",
@@ -322,21 +352,27 @@ def main():
             "metric": METRIC, "value": t_max / world, "unit": "s/iter", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64",
-            "precision": "split (BF16-slice emulated FP64)" if args.mode == "split" else "plain FP64",
+            "precision": ("split: FP64 emulated with BF16 slices on tcgen05, <=1e-12 rel. err vs FP64"
+                          if modes[0] == "split" else "plain FP64"),
             "data": "synthetic (seeded N(0,1) operands with the reference case's shapes)",
-            "config": {"workload": WORKLOAD_NAME, **WORKLOAD, "mode": args.mode,
+            "config": {"workload": WORKLOAD_NAME, **WORKLOAD, "mode": modes[0],
                        "l2": "512 MiB buffer written between timed steps",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "gflops_fp64_equiv": flops / t_step / 1e9,
-            "algorithmic_gflop_per_step": flops / 1e9,
-            "e2e": {"value": e2e_step, "unit": "s/iter", "h2d_bytes_per_step": int(h_in.numel() * 8),
-                    "d2h_bytes_per_step": int(h_out.numel() * 8)},
-            "gpu_launches": int(launches_per_step * args.steps),
-            "gpu_launches_per_step": int(launches_per_step),
-            "roofline": roofline,
+            "gflops_fp64_equiv": head["flops"] / t_step / 1e9,
+            "algorithmic_gflop_per_step": head["flops"] / 1e9,
+            "e2e": {"value": head["e2e_s_per_iter"], "unit": "s/iter", "h2d_bytes_per_step": head["h2d"],
+                    "d2h_bytes_per_step": head["d2h"]},
+            "gpu_launches": int(head["launches_per_step"] * args.steps),
+            "gpu_launches_per_step": int(head["launches_per_step"]),
+            "roofline": head["roofline"],
             "cpu_baseline": cpu,
-            "clocks": clk.summary(),
+            "clocks": clk_summary,
         }
+        if len(modes) > 1:
+            f = results["fp64"]
+            res["fp64"] = {"s_per_iter": f["s_per_iter"], "e2e_s_per_iter": f["e2e_s_per_iter"],
+                           "roofline": f["roofline"], "gpu_launches_per_step": int(f["launches_per_step"])}
+            res["split_speedup_vs_fp64"] = f["s_per_iter"] / head["s_per_iter"]
         print(json.dumps(res))
     if world > 1:
         dist.destroy_process_group()

@@ -58,14 +58,18 @@ __global__ void __launch_bounds__(256) k_permute(const PermDesc* __restrict__ de
     if (d.p < 0) {
       // gather mode (small inner dims): 1024 consecutive destination elements per work item,
       // each thread decodes its source offset; writes coalesced, reads in short runs
-      const int64_t total = d.nouter;   // block size for this mode
-      const int64_t e0 = local * kRunChunk;
-      for (int64_t e = e0 + threadIdx.x; e < min(e0 + kRunChunk, total); e += blockDim.x) {
-        int64_t rem = e, soff = 0;
+      // block sizes are below 2^31 (checked on the host): 32-bit index arithmetic
+      const uint32_t total = (uint32_t)d.nouter;   // block size for this mode
+      const uint32_t e0 = (uint32_t)local * kRunChunk;
+      const uint32_t e1 = min(e0 + (uint32_t)kRunChunk, total);
+      for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        uint32_t rem = e;
+        int64_t soff = 0;
         for (int i = r - 1; i >= 0; --i) {
-          const int64_t x = rem % d.dims[i];
-          rem /= d.dims[i];
-          soff += x * d.sstride[i];
+          const uint32_t di = (uint32_t)d.dims[i];
+          const uint32_t q = rem / di;
+          soff += (int64_t)(rem - q * di) * d.sstride[i];
+          rem = q;
         }
         dst[d.dst_off + e] = mul_sign(src[d.src_off + soff], sign);
       }
@@ -73,15 +77,18 @@ __global__ void __launch_bounds__(256) k_permute(const PermDesc* __restrict__ de
     }
     if (d.p == q) {
       // copy mode: innermost run of length dims[q] contiguous on both sides
-      const int64_t chunks_per_run = (d.dims[q] + kRunChunk - 1) / kRunChunk;
-      const int64_t run = local / chunks_per_run;
-      const int64_t c0 = (local % chunks_per_run) * kRunChunk;
-      int64_t rem = run, soff = 0, doff = 0;
+      const uint32_t chunks_per_run = ((uint32_t)d.dims[q] + kRunChunk - 1) / kRunChunk;
+      const uint32_t run = (uint32_t)local / chunks_per_run;
+      const int64_t c0 = (int64_t)((uint32_t)local - run * chunks_per_run) * kRunChunk;
+      uint32_t rem = run;
+      int64_t soff = 0, doff = 0;
       for (int i = r - 2; i >= 0; --i) {
-        const int64_t x = rem % d.dims[i];
-        rem /= d.dims[i];
-        soff += x * d.sstride[i];
-        doff += x * dstride[i];
+        const uint32_t di = (uint32_t)d.dims[i];
+        const uint32_t qq = rem / di;
+        const uint32_t x = rem - qq * di;
+        rem = qq;
+        soff += (int64_t)x * d.sstride[i];
+        doff += (int64_t)x * dstride[i];
       }
       const T* s = src + d.src_off + soff;
       T* o = dst + d.dst_off + doff;
@@ -102,17 +109,21 @@ __global__ void __launch_bounds__(256) k_permute(const PermDesc* __restrict__ de
       continue;
     }
     // tile mode over (p, q)
-    const int64_t per_outer = (int64_t)d.tiles_p * d.tiles_q;
-    const int64_t outer = local / per_outer;
-    const int64_t tt = local % per_outer;
-    const int64_t p0 = (tt / d.tiles_q) * kTile, q0 = (tt % d.tiles_q) * kTile;
-    int64_t rem = outer, soff = 0, doff = 0;
+    const uint32_t per_outer = (uint32_t)d.tiles_p * (uint32_t)d.tiles_q;
+    const uint32_t outer = (uint32_t)local / per_outer;
+    const uint32_t tt = (uint32_t)local - outer * per_outer;
+    const uint32_t tq = tt / (uint32_t)d.tiles_q;
+    const int64_t p0 = (int64_t)tq * kTile, q0 = (int64_t)(tt - tq * (uint32_t)d.tiles_q) * kTile;
+    uint32_t rem = outer;
+    int64_t soff = 0, doff = 0;
     for (int i = r - 1; i >= 0; --i) {
       if (i == d.p || i == q) continue;
-      const int64_t x = rem % d.dims[i];
-      rem /= d.dims[i];
-      soff += x * d.sstride[i];
-      doff += x * dstride[i];
+      const uint32_t di = (uint32_t)d.dims[i];
+      const uint32_t qq = rem / di;
+      const uint32_t x = rem - qq * di;
+      rem = qq;
+      soff += (int64_t)x * d.sstride[i];
+      doff += (int64_t)x * dstride[i];
     }
     const T* s = src + d.src_off + soff;
     T* o = dst + d.dst_off + doff;
@@ -177,6 +188,7 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
       d.sstride[i] = ds[i];
       if (ds[i] == 1) d.p = i;
     }
+    QLTG_CHECK(t.blk_size(b) < ((int64_t)1 << 31), QLTG_ERR_UNSUPPORTED, "block with 2^31 or more elements");
     int64_t tiles;
     if (m == 0) {
       d.p = 0;
