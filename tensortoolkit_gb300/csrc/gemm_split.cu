@@ -1,36 +1,37 @@
 // Split-precision grouped GEMM: FP64 emulated with BF16 slices on the tcgen05 tensor
-// cores, FP32 accumulation in tensor memory, exact integer recombination, one FP64
-// rounding per output element.
+// cores, FP32 accumulation in tensor memory, integer recombination, one FP64 rounding per
+// output element (per task of the output block).
 //
 // Slicing (per operand block, integer arithmetic only - the FP64 pipe of this GPU runs at
-// about 1 TFLOP/s, so nothing here touches it):
+// about 1 TFLOP/s, so nothing on the hot path leans on it):
 //   every row i of A (column j of B) gets a scale 2^e with max |x| < 2^e, and each element
 //   x = s 2^e y, |y| < 1, is cut into S = 7 base-2^7 digits of Y = floor(|y| 2^49):
-//   x ~= 2^e sum_p a_p 2^(-7p) with integer slices a_p = s d_p in [-127, 127], exact in BF16.
-//   Truncation error < 2^-49 of the row (column) maximum.
-// Products (the Ozaki scheme, restated): C_ij = 2^(ea_i + eb_j) sum_l 2^(-7l) D_l with
-//   D_l = sum_{p+q=l} (A_p B_q)_ij over the 28 slice pairs with p + q <= 8 (levels 2..8).
-//   Every product a_p b_q is an integer of magnitude < 2^14; level l sums l-1 pairs, so over
-//   at most 128 k the FP32 accumulation of every level is exact (7 * 128 * 127^2 < 2^24).
-//   Each level has its own 128 x 32 FP32 accumulator in tensor memory (7 x 32 = 224
-//   columns); every 128 k the levels are drained to two int64 registers per output
-//   (levels 2-4 -> hi, 5-8 -> lo, both < 2^53), and at the end of a task
-//   C += sign * 2^(ea+eb-56) (hi 2^28 + lo) with one FMA-rounding.
+//   x ~= 2^e sum_p a_p 2^(-7p), digits a_p = s d_p in [-127, 127]. Slice p is stored as
+//   the BF16 number a_p 2^(-7p) (exact: 7 significant bits). Truncation error < 2^-49 of
+//   the row (column) maximum.
+// Products (the Ozaki scheme, restated): C_ij = 2^(ea_i + eb_j) sum over the 28 slice pairs
+//   p + q <= 8 of (A_p B_q)_ij. Level L = p + q sums L - 1 pairs, each an integer multiple
+//   of 2^(-7L) below 2^14 of those units, so over at most 128 k the FP32 sum of one level
+//   is exact (4 * 128 * 127^2 < 2^24 for L <= 5). Levels 2, 3, 4 and 5 get their own
+//   128 x 32 FP32 accumulator in tensor memory; levels 6..8 share a fifth one, where FP32
+//   rounding costs at most 2^-24 of a quantity below 2^-26 of the leading level. Every
+//   128 k the accumulators are drained into int32 level sums (and a float for 6..8); at
+//   the end of a task C (+)= sign 2^(ea+eb-42) Z with Z = sum_L i_L 2^(7(6-L)) + fm 2^42 as one
+//   int64, rounded to FP64 with integer operations.
 //
 // Layout for the tensor cores: both operands K-major, no swizzle, in 8 x 16-byte core
 // matrices (leading-byte offset 128 B between the two core matrices of a 16-wide k step,
 // stride-byte offset 256 B between 8-row groups). The pack kernels write each (row tile,
 // k tile, slice) as one contiguous tile in exactly that layout, zero-padded, so the GEMM
-// stages operands with plain 16-byte copies and points the MMA descriptors at them.
+// stages operands with bulk copies and points the descriptors at them.
 //
-// GEMM (one CTA of 128 threads per 128 x 32 output tile at a time, dynamic tile queue):
-//   for each task of the output block, for each 64-wide k tile: all threads stage the 7 A
-//   slices (7 x 16 KB) and 7 B slices (7 x 4 KB) into shared memory; one thread issues the
-//   4 x 28 tcgen05.mma (M=128, N=32, K=16) and commits them to an mbarrier; after every
-//   second k tile (and at the end of a task) the four warps read their 32 lanes of the 7
-//   level accumulators with tcgen05.ld and fold them into the int64 pair.
-// Every wait on the mbarrier is bounded; on expiry the CTA sets the plan's error word,
-// frees its tensor memory and returns.
+// GEMM: one persistent CTA per SM, warp-specialised (see k_gemm_split). Per 16-wide k step
+// the 7 A slices are copied once into tensor memory and the 28 MMAs (M = 128, N = 32,
+// K = 16) read A from there and only B from shared memory: shared-memory traffic per step
+// is 7 A + 28 B reads of a slice instead of 28 + 28.
+// Every wait on an mbarrier is bounded; on expiry the CTA sets the plan's error word,
+// waits (bounded) for its own copies and tensor-core work, frees its tensor memory and
+// returns.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -41,14 +42,11 @@ namespace qltg {
 namespace {
 
 constexpr int kS = 7;                      // slices
-constexpr int kPairs = 28;                 // p + q <= kS + 1
-constexpr int kLevels = 7;                 // levels 2..8
+constexpr int kLevels = 7;                 // accumulators: levels 2..8
 constexpr int kTM = 128, kTN = 32, kTK = 64;
 constexpr int kATile = kTM * kTK * 2;      // bytes of one (row tile, k tile, slice): 16 KB
 constexpr int kBTile = kTN * kTK * 2;      // 4 KB
-constexpr int kThreads = 128;
 constexpr int kDrainK = 128;               // k between drains (exactness bound)
-constexpr uint32_t kTmemCols = 256;        // >= 7 * 32, power of two
 
 // ------------------------------------------------------------------ slicing
 // Row / column scale exponents: e with max |x| < 2^e (0 for an all-zero row).
@@ -111,7 +109,7 @@ __global__ void k_col_exp_finish(int32_t* __restrict__ exps, int64_t n) {
     exps[i] = exps[i] == 0 ? 0 : exps[i] - 1022;
 }
 
-// Seven 7-bit digits of x / 2^e (sign-magnitude), as BF16 bit patterns.
+// Seven 7-bit digits of x / 2^e (sign-magnitude), slice p weighted 2^(-7(p+1)), as BF16 bit patterns.
 __device__ __forceinline__ void slice7(double x, int e, uint16_t* out) {
   const uint64_t bits = (uint64_t)__double_as_longlong(x);
   const uint64_t ab = bits & 0x7FFFFFFFFFFFFFFFull;
@@ -128,9 +126,9 @@ __device__ __forceinline__ void slice7(double x, int e, uint16_t* out) {
 #pragma unroll
   for (int p = 0; p < kS; ++p) {
     const uint32_t d = (uint32_t)((Y >> (7 * (kS - 1 - p))) & 127u);
-    // bf16 of the integer d (exact): float bits >> 16
-    const uint32_t f = __float_as_uint((float)d);
-    out[p] = d ? (uint16_t)((f >> 16) | sgn) : (uint16_t)0;
+    // bf16 of d 2^(-7(p+1)) (exact): the float's bits >> 16, exponent field lowered by 7(p+1)
+    const uint32_t f = __float_as_uint((float)d) >> 16;
+    out[p] = d ? (uint16_t)((f - ((uint32_t)(7 * (p + 1)) << 7)) | sgn) : (uint16_t)0;
   }
 }
 
@@ -158,7 +156,9 @@ __global__ void k_pack_a(const double* __restrict__ src, const SplitOperand* __r
       const double x = (r < o.rows && k0 + j < o.cols) ? src[o.src_off + r * o.cols + k0 + j] : 0.0;
       slice7(x, e, sl[j]);
     }
-    const int64_t within = (int64_t)ks * 4096 + m_core * 256 + k_core * 128 + r8 * 16;
+    // tile layout [ks][slice][m_core][k_core][8 rows x 16 B]: the 7 slices of a 16-wide k
+    // step are contiguous, so a 32-wide stage is one 56 KB copy
+    const int64_t within = (int64_t)ks * (kS * 4096) + m_core * 256 + k_core * 128 + r8 * 16;
 #pragma unroll
     for (int p = 0; p < kS; ++p) {
       uint4 v;
@@ -166,7 +166,7 @@ __global__ void k_pack_a(const double* __restrict__ src, const SplitOperand* __r
       v.y = (uint32_t)sl[2][p] | ((uint32_t)sl[3][p] << 16);
       v.z = (uint32_t)sl[4][p] | ((uint32_t)sl[5][p] << 16);
       v.w = (uint32_t)sl[6][p] | ((uint32_t)sl[7][p] << 16);
-      *reinterpret_cast<uint4*>(pack + o.pack_off + (tile * kS + p) * (int64_t)kATile + within) = v;
+      *reinterpret_cast<uint4*>(pack + o.pack_off + tile * (int64_t)(kS * kATile) + within + p * 4096) = v;
     }
   }
 }
@@ -194,7 +194,9 @@ __global__ void k_pack_b(const double* __restrict__ src, const SplitOperand* __r
       const double x = (c < o.cols && k0 + j < o.rows) ? src[o.src_off + (k0 + j) * o.cols + c] : 0.0;
       slice7(x, e, sl[j]);
     }
-    const int64_t within = (int64_t)ks * 1024 + n_core * 256 + k_core * 128 + n8 * 16;
+    // tile layout [ks][slice][n_core][k_core][8 columns x 16 B]: the 7 slices of a 16-wide k
+    // step form one 224-row K-major operand (slice q = rows 32 (q-1) .. 32 q - 1)
+    const int64_t within = (int64_t)ks * (kS * 1024) + n_core * 256 + k_core * 128 + n8 * 16;
 #pragma unroll
     for (int p = 0; p < kS; ++p) {
       uint4 v;
@@ -202,7 +204,7 @@ __global__ void k_pack_b(const double* __restrict__ src, const SplitOperand* __r
       v.y = (uint32_t)sl[2][p] | ((uint32_t)sl[3][p] << 16);
       v.z = (uint32_t)sl[4][p] | ((uint32_t)sl[5][p] << 16);
       v.w = (uint32_t)sl[6][p] | ((uint32_t)sl[7][p] << 16);
-      *reinterpret_cast<uint4*>(pack + o.pack_off + (tile * kS + p) * (int64_t)kBTile + within) = v;
+      *reinterpret_cast<uint4*>(pack + o.pack_off + tile * (int64_t)(kS * kBTile) + within + p * 1024) = v;
     }
   }
 }
@@ -216,71 +218,37 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
          ((uint64_t)1 << 46);
 }
 
-// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = 32.
-__device__ __forceinline__ uint32_t idesc_bf16() {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTN >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
+// kind::f16 instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t id, uint32_t acc) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-      "l"(da), "l"(db), "r"(id), "r"(acc));
-}
-
-// Wait for the mbarrier phase with a bounded spin: about 1 s of SM clock (2^31 cycles at
-// the 2.07 GHz maximum), checked every 256 polls so the fast path is a bare try_wait.
+// Bounded waits spin for about 1 s of SM clock (2^31 cycles at the 2.07 GHz maximum),
+// checking the clock every 256 polls so the fast path is a bare try_wait.
 constexpr long long kWaitCycles = 1ll << 31;
 
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
-  uint32_t done = 0;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(done)
-      : "r"(mbar), "r"(phase));
-  if (done) return true;
-  const long long t0 = clock64();
-  while (true) {
-    for (int i = 0; i < 256; ++i) {
-      asm volatile(
-          "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-          : "=r"(done)
-          : "r"(mbar), "r"(phase));
-      if (done) return true;
-    }
-    if (clock64() - t0 > kWaitCycles) return false;
-  }
-}
-
-// 2^n as a double built from its bit pattern (integer ops only), with an ldexp fallback
-// outside the normal range.
-__device__ __forceinline__ double pow2(int n) {
-  if (n >= -1022 && n <= 1023) return __longlong_as_double((long long)(n + 1023) << 52);
-  return ldexp(1.0, n);
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
-      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-}
-
-// Operand pipeline: a stage holds one 32-wide k slab of all 7 A slices (7 x 8 KB) and all
-// 7 B slices (7 x 2 KB) = 70 KB; 3 stages = 210 KB of shared memory.
+// Operand pipeline: a stage holds one 32-wide k slab of all 7 A slices (56 KB) and all 7 B
+// slices (14 KB), each as it lies in the packed tile ([16-wide k step][slice][...]); 3
+// stages = 210 KB of shared memory. Per 16-wide k step the A slices are 4 KB apart and the
+// B slices form one 224-row operand.
 constexpr int kStages = 3;
 constexpr int kKS = 32;                         // k per stage (2 MMA k-steps)
-constexpr int kAStage = kTM * kKS * 2;          // 8 KB per A slice per stage
-constexpr int kBStage = kTN * kKS * 2;          // 2 KB per B slice per stage
-constexpr int kStageBytes = kS * (kAStage + kBStage);
+constexpr int kAStep = kS * kTM * 16 * 2;       // 28 KB: 7 A slices of one k step
+constexpr int kBStep = kS * kTN * 16 * 2;       // 7 KB: 7 B slices of one k step
+constexpr int kABytes = 2 * kAStep, kBBytes = 2 * kBStep;
+constexpr int kStageBytes = kABytes + kBBytes;  // 70 KB
 constexpr int kSmemBytes = kStages * kStageBytes + 1024;
 constexpr int kPeriod = kDrainK / kKS;          // stages between drains (4)
-constexpr int kRoleThreads = 192;               // warp 0 producer, warp 1 MMA, warps 2-5 drain
-constexpr uint32_t kTmemAlloc = 512;            // two buffers of 7 levels x 32 columns
+constexpr int kDrainWarps = 16;                 // four per tensor-memory lane quadrant
+constexpr int kDrainCols = kTN / 4;             // columns per drain thread
+constexpr int kRoleThreads = 64 + 32 * kDrainWarps;   // warp 0 producer, warp 1 MMA, warps 2-17 drain
+// Tensor memory: two accumulator sets, each 7 levels x 32 columns (level L at 32 (L - 2)).
+constexpr int kAccCols = kLevels * kTN;         // 224
+constexpr uint32_t kTmemAlloc = 512;
+static_assert(2 * kAccCols <= (int)kTmemAlloc, "tensor memory budget");
+constexpr int kFlushDrains = 64;                // the int64 sum of a chunk stays below 2^63
+constexpr float kMagic = 12582912.0f;           // 1.5 * 2^23: x + kMagic has the integer x in its low bits
+constexpr int kMagicBits = 0x4B400000;          // for |x| < 2^22
 
 __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count));
@@ -296,12 +264,33 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
                "l"(src), "r"(bytes), "r"(mbar)
                : "memory");
 }
+// One lane of the calling warp (the same one every time for a full warp).
+__device__ __forceinline__ bool elect_one() {
+  uint32_t pred = 0;
+  asm volatile("{\n\t.reg .pred p;\n\telect.sync _|p, 0xffffffff;\n\tselp.u32 %0, 1, 0, p;\n\t}\n" : "=r"(pred));
+  return pred != 0;
+}
+// The tensor-core helpers below are called by a whole warp; the elected lane issues.
 __device__ __forceinline__ void tc_commit(uint32_t mbar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
+  if (elect_one())
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
+}
+// D (+)= A B, both operands from shared memory.
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t da, uint64_t db, uint32_t id, uint32_t acc) {
+  if (elect_one())
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+        "l"(da), "l"(db), "r"(id), "r"(acc));
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
 }
 
 // Bounded wait that also gives up as soon as another role has aborted.
-__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t phase, volatile int* abort_flag) {
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t phase, const volatile int* abort_flag) {
   uint32_t done = 0;
   const long long t0 = clock64();
   while (true) {
@@ -316,13 +305,121 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t phase
   }
 }
 
+// Warp-uniform forms for warps whose lanes run the same loop: the abort flag as lane 0 saw
+// it, and a bounded wait that succeeds only if it succeeded in every lane.
+__device__ __forceinline__ bool aborted(volatile int* abort_flag) {
+  return __shfl_sync(0xffffffffu, *abort_flag, 0) != 0;
+}
+__device__ __forceinline__ bool wait_warp(uint32_t mbar, uint32_t phase, volatile int* abort_flag) {
+  return __all_sync(0xffffffffu, mbar_wait_or_abort(mbar, phase, abort_flag));
+}
+// Bounded wait that ignores the abort flag: for the copies and tensor-core work a CTA issued
+// itself, which must land before it frees or leaves the memory they write.
+__device__ __forceinline__ bool wait_warp_own(uint32_t mbar, uint32_t phase) {
+  const int never = 0;
+  return __all_sync(0xffffffffu, mbar_wait_or_abort(mbar, phase, &never));
+}
+
+// z 2^e (negated when neg) rounded to the nearest double, built with integer operations
+// only (the FP64 pipe of this GPU is slow); outside the normal range it falls back to ldexp.
+__device__ __forceinline__ double scaled_i64(long long z, int e, bool neg) {
+  if (z == 0) return 0.0;
+  const unsigned long long a = z < 0 ? 0ull - (unsigned long long)z : (unsigned long long)z;
+  const unsigned long long sgn = ((z < 0) != neg) ? 0x8000000000000000ull : 0ull;
+  const int lz = __clzll((long long)a);
+  const unsigned long long m = a << lz;                 // leading one at bit 63
+  unsigned long long mant = m >> 11;                    // 53 bits, leading one at bit 52
+  const unsigned long long rem = m & 0x7FFull;
+  mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;   // nearest-even
+  const int be = 1023 + 63 - lz + e;                    // biased exponent of the leading bit
+  // (be - 1) << 52 plus the mantissa with its leading one adds the exponent; a rounding
+  // carry to 2^53 moves into the exponent by itself
+  if (be >= 1 && be < 2046) return __longlong_as_double((long long)(sgn | (((unsigned long long)(be - 1) << 52) + mant)));
+  const double v = ldexp((double)z, e);
+  return neg ? -v : v;
+}
+
+// Fold one drained accumulator set into the int64 sums z (units 2^-49) of this thread's
+// row and 8 columns. Level L holds integers times 2^(-7L) below 2^24 (exact in FP32);
+// levels 2 and 3 stay below 2^22 and convert with the magic-number add, the others with
+// F2I; level 8 is rounded to units of 2^-49.
+__device__ __forceinline__ void drain_set(uint32_t lb, long long (&z)[kDrainCols]) {
+  uint32_t r[kDrainCols];
+  int32_t u[kDrainCols];
+  tmem_ld8(lb, r);                                       // level 2
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+  for (int c = 0; c < kDrainCols; ++c)
+    u[c] = (__float_as_int(fmaf(__uint_as_float(r[c]), 0x1p14f, kMagic)) - kMagicBits) * 128;
+  tmem_ld8(lb + kTN, r);                                 // level 3
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+  for (int c = 0; c < kDrainCols; ++c) {
+    u[c] += __float_as_int(fmaf(__uint_as_float(r[c]), 0x1p21f, kMagic)) - kMagicBits;
+    z[c] += (long long)u[c] << 28;
+  }
+  tmem_ld8(lb + 2 * kTN, r);                             // level 4
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+  for (int c = 0; c < kDrainCols; ++c) u[c] = __float2int_rn(__uint_as_float(r[c]) * 0x1p28f) * 128;
+  tmem_ld8(lb + 3 * kTN, r);                             // level 5
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+  for (int c = 0; c < kDrainCols; ++c) {
+    u[c] += __float2int_rn(__uint_as_float(r[c]) * 0x1p35f);
+    z[c] += (long long)u[c] << 14;
+  }
+  tmem_ld8(lb + 4 * kTN, r);                             // level 6
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+  for (int c = 0; c < kDrainCols; ++c) u[c] = __float2int_rn(__uint_as_float(r[c]) * 0x1p42f) * 128;
+  tmem_ld8(lb + 5 * kTN, r);                             // level 7
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+  for (int c = 0; c < kDrainCols; ++c) u[c] += __float2int_rn(__uint_as_float(r[c]) * 0x1p49f);
+  tmem_ld8(lb + 6 * kTN, r);                             // level 8
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+  for (int c = 0; c < kDrainCols; ++c)
+    z[c] += (long long)(u[c] + ((__float2int_rn(__uint_as_float(r[c]) * 0x1p56f) + 64) >> 7));
+}
+
+// C (+)= sign 2^(ea + eb - 49) z for this thread's row and 8 columns, rounded once to FP64;
+// the first write of a tile stores, later ones add.
+__device__ __forceinline__ void flush_sums(const long long (&z)[kDrainCols], int row, int col0, const GemmCBlk& cb,
+                                           const SplitTask& tk, const int32_t* __restrict__ aexp,
+                                           const int32_t* __restrict__ bexp, double* out, bool& written) {
+  if (row < cb.m) {
+    const int ea = aexp[tk.a_exp + row];
+#pragma unroll
+    for (int c = 0; c < kDrainCols; ++c) {
+      const int col = col0 + c;
+      if (col < cb.n) {
+        const double v = scaled_i64(z[c], ea + bexp[tk.b_exp + col] - 49, tk.sign < 0);
+        out[col] = written ? out[col] + v : v;
+      }
+    }
+  }
+  written = true;
+}
+
 // Warp-specialised split GEMM. All roles walk the same static sequence of work items
 // (output tiles ti = blockIdx.x, blockIdx.x + gridDim.x, ...; for each its tasks; for each
 // task its 32-wide k stages), so they agree on stage, period and buffer numbers without
-// talking: the producer fills stage g % 3 once the MMAs of stage g - 3 released it; the
-// MMA thread consumes stage g into TMEM buffer (period d) % 2 once the drain of period
-// d - 2 released that buffer; the drain warps read a buffer after its MMAs completed and
-// release it, and after a task's last period write the task's contribution to C.
+// talking:
+//  * warp 0 fills shared-memory stage g % 3 with two bulk copies once the MMAs of stage
+//    g - 3 released it;
+//  * warp 1 issues, per 16-wide k step, 7 MMAs into accumulator set (period d) % 2 once
+//    the drain warps released it: MMA p multiplies A slice p by B slices 1..8-p
+//    concatenated along N (N = 32 (8 - p)) into the levels p+1..8, i.e. accumulator
+//    columns 32 (p - 1) .. 223, so every slice pair with p + q <= 8 lands on its level
+//    with no padding and the tensor core sees few wide instructions instead of 28 narrow
+//    ones;
+//  * warps 2-17 (four per tensor-memory lane quadrant, 8 columns each) read a set after its
+//    MMAs completed, fold it into int64 sums and release it; after a task's last period
+//    (or every 64 periods) they write the contribution to C.
+// Warps 0 and 1 run their loops as whole warps (warp-uniform state and descriptors); one
+// elected lane issues each copy / tensor-core instruction.
 __global__ void __launch_bounds__(kRoleThreads, 1)
     k_gemm_split(const GemmCBlk* __restrict__ cblk, const SplitTask* __restrict__ task,
                  const GemmTask* __restrict__ gtask, const GemmTile* __restrict__ tiles, int ntiles,
@@ -342,7 +439,7 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
   }
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) { mbar_init(smem_u32(&full_bar[s]), 1); mbar_init(smem_u32(&empty_bar[s]), 1); }
-    for (int b = 0; b < 2; ++b) { mbar_init(smem_u32(&accf_bar[b]), 1); mbar_init(smem_u32(&acce_bar[b]), 4); }
+    for (int b = 0; b < 2; ++b) { mbar_init(smem_u32(&accf_bar[b]), 1); mbar_init(smem_u32(&acce_bar[b]), kDrainWarps); }
     mbar_init(smem_u32(&fin_bar), 1);
     asm volatile("fence.mbarrier_init.release.cluster;");
     s_abort = 0;
@@ -357,77 +454,74 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
     atomicExch(err, 1);
   };
 
-  if (warp == 0 && lane == 0) {
+  if (warp == 0) {
     // ------------------------------------------------------------ producer
     uint32_t g = 0;
-    for (int ti = blockIdx.x; ti < ntiles && !s_abort; ti += gridDim.x) {
+    for (int ti = blockIdx.x; ti < ntiles && !aborted(&s_abort); ti += gridDim.x) {
       const GemmTile tl = tiles[ti];
       const GemmCBlk cb = cblk[tl.cblk];
-      for (int t = cb.t0; t < cb.t1 && !s_abort; ++t) {
+      for (int t = cb.t0; t < cb.t1 && !aborted(&s_abort); ++t) {
         const SplitTask tk = task[t];
         const int nst = (gtask[t].k + kKS - 1) / kKS;
         for (int j = 0; j < nst; ++j, ++g) {
           const int s = g % kStages;
-          if (g >= (uint32_t)kStages &&
-              !mbar_wait_or_abort(smem_u32(&empty_bar[s]), ((g / kStages) - 1) & 1, &s_abort)) { fail(); break; }
-          const int kt = j >> 1, half = j & 1;
-          const uint8_t* ga = apack + tk.a_pack + ((int64_t)tl.tm * tk.ktiles + kt) * kS * kATile + half * kAStage;
-          const uint8_t* gb = bpack + tk.b_pack + ((int64_t)tl.tn * tk.ktiles + kt) * kS * kBTile + half * kBStage;
-          const uint32_t sa = sbase + s * kStageBytes, sb = sa + kS * kAStage;
-          const uint32_t fb = smem_u32(&full_bar[s]);
-          mbar_expect_tx(fb, kStageBytes);
-#pragma unroll
-          for (int p = 0; p < kS; ++p) {
-            bulk_g2s(sa + p * kAStage, ga + (int64_t)p * kATile, kAStage, fb);
-            bulk_g2s(sb + p * kBStage, gb + (int64_t)p * kBTile, kBStage, fb);
+          if (g >= (uint32_t)kStages && !wait_warp(smem_u32(&empty_bar[s]), ((g / kStages) - 1) & 1, &s_abort)) {
+            if (lane == 0) fail();
+            break;
           }
+          const int kt = j >> 1, half = j & 1;
+          const uint8_t* ga = apack + tk.a_pack + ((int64_t)tl.tm * tk.ktiles + kt) * (kS * kATile) + half * kABytes;
+          const uint8_t* gb = bpack + tk.b_pack + ((int64_t)tl.tn * tk.ktiles + kt) * (kS * kBTile) + half * kBBytes;
+          const uint32_t sa = sbase + s * kStageBytes;
+          const uint32_t fb = smem_u32(&full_bar[s]);
+          if (elect_one()) {
+            mbar_expect_tx(fb, kStageBytes);
+            bulk_g2s(sa, ga, kABytes, fb);
+            bulk_g2s(sa + kABytes, gb, kBBytes, fb);
+          }
+          __syncwarp();
         }
       }
     }
-    // copies still in flight are waited for by the MMA thread (every issued stage is
-    // consumed on the normal path); on abort wait for the tail of issued stages here
-    if (s_abort) {
+    // copies still in flight are waited for by the MMA warp (every issued stage is consumed
+    // on the normal path); on abort wait for the tail of issued stages here
+    if (aborted(&s_abort)) {
       for (uint32_t x = (g > (uint32_t)kStages ? g - kStages : 0); x < g; ++x)
-        mbar_wait_or_abort(smem_u32(&full_bar[x % kStages]), (x / kStages) & 1, &s_abort);
+        wait_warp_own(smem_u32(&full_bar[x % kStages]), (x / kStages) & 1);
     }
-  } else if (warp == 1 && lane == 0) {
-    // ------------------------------------------------------------ MMA issuer
-    const uint32_t id = idesc_bf16();
-    // descriptor of stage 0, slice 1, k-step 0; every other operand is a fixed byte offset
-    const uint64_t da0 = smem_desc(sbase), db0 = smem_desc(sbase + kS * kAStage);
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ tensor-core issuer
+    // descriptor of stage 0 at byte 0; every operand is a fixed byte offset from it
+    const uint64_t sd0 = smem_desc(sbase);
     uint32_t g = 0, d = 0;
-    for (int ti = blockIdx.x; ti < ntiles && !s_abort; ti += gridDim.x) {
+    bool ok = true;
+    for (int ti = blockIdx.x; ti < ntiles && ok && !aborted(&s_abort); ti += gridDim.x) {
       const GemmTile tl = tiles[ti];
       const GemmCBlk cb = cblk[tl.cblk];
-      for (int t = cb.t0; t < cb.t1 && !s_abort; ++t) {
+      for (int t = cb.t0; t < cb.t1 && ok && !aborted(&s_abort); ++t) {
         const int nst = (gtask[t].k + kKS - 1) / kKS;
         for (int j = 0; j < nst; ++j, ++g) {
           const int s = g % kStages;
           const int buf = d & 1;
           const bool first = (j % kPeriod) == 0;
           const bool drain = (j % kPeriod) == kPeriod - 1 || j + 1 == nst;
-          if (first && d >= 2 && !mbar_wait_or_abort(smem_u32(&acce_bar[buf]), ((d / 2) - 1) & 1, &s_abort)) {
-            fail();
+          if (first && d >= 2 && !wait_warp(smem_u32(&acce_bar[buf]), ((d / 2) - 1) & 1, &s_abort)) {
+            ok = false;
             break;
           }
-          if (!mbar_wait_or_abort(smem_u32(&full_bar[s]), (g / kStages) & 1, &s_abort)) { fail(); break; }
+          if (!wait_warp(smem_u32(&full_bar[s]), (g / kStages) & 1, &s_abort)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint64_t soff = (uint64_t)((s * kStageBytes) >> 4);
-          const uint32_t dbuf = tmem + (uint32_t)(buf * kLevels * kTN);
+          const uint32_t dbuf = tmem + (uint32_t)(buf * kAccCols);
 #pragma unroll
           for (int ks = 0; ks < kKS / 16; ++ks) {
-            int started = 0;
+            const uint64_t bdesc = sd0 + soff + (uint64_t)((kABytes + ks * kBStep) >> 4);
 #pragma unroll
             for (int p = 1; p <= kS; ++p) {
-#pragma unroll
-              for (int q = 1; p + q <= kS + 1; ++q) {
-                const int l = p + q - 2;
-                const uint64_t adesc = da0 + soff + (uint64_t)(((p - 1) * kAStage + ks * 4096) >> 4);
-                const uint64_t bdesc = db0 + soff + (uint64_t)(((q - 1) * kBStage + ks * 1024) >> 4);
-                const uint32_t acc = (first && ks == 0 && !(started >> l & 1)) ? 0u : 1u;
-                mma_bf16(dbuf + (uint32_t)(l * kTN), adesc, bdesc, id, acc);
-                started |= 1 << l;
-              }
+              const uint64_t adesc = sd0 + soff + (uint64_t)((ks * kAStep + (p - 1) * kTM * 32) >> 4);
+              // the first MMA of a period (p = 1, all 224 columns) overwrites the set
+              const uint32_t acc = (first && ks == 0 && p == 1) ? 0u : 1u;
+              mma_bf16(dbuf + (uint32_t)((p - 1) * kTN), adesc, bdesc, idesc_bf16(kTN * (kS + 1 - p)), acc);
             }
           }
           tc_commit(smem_u32(&empty_bar[s]));
@@ -435,69 +529,51 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
         }
       }
     }
-    // all MMAs issued by this thread complete before the tensor memory is released
+    if (!ok && lane == 0) fail();
+    // all tensor-core work issued by this warp completes before the memory is released
     tc_commit(smem_u32(&fin_bar));
-    mbar_wait_or_abort(smem_u32(&fin_bar), 0, &s_abort);
+    wait_warp_own(smem_u32(&fin_bar), 0);
   } else if (warp >= 2) {
     // ------------------------------------------------------------ drain / epilogue
-    const int quad = warp & 3;                       // TMEM lanes 32 * quad .. + 31
+    const int quad = warp & 3;                       // tensor-memory lanes 32 * quad .. + 31
+    const int cpart = (warp - 2) >> 2;               // columns 8 * cpart .. + 7 of the tile
     const int row_in_tile = quad * 32 + lane;
     uint32_t d = 0;
-    for (int ti = blockIdx.x; ti < ntiles && !s_abort; ti += gridDim.x) {
+    for (int ti = blockIdx.x; ti < ntiles && !aborted(&s_abort); ti += gridDim.x) {
       const GemmTile tl = tiles[ti];
       const GemmCBlk cb = cblk[tl.cblk];
       const int row = tl.tm * kTM + row_in_tile;
-      bool stop = false;
+      const int col0 = tl.tn * kTN + cpart * kDrainCols;
+      double* out = C + cb.c_off + (int64_t)row * cb.n;
+      bool stop = false, written = false;
       for (int t = cb.t0; t < cb.t1 && !stop; ++t) {
         const SplitTask tk = task[t];
         const int nst = (gtask[t].k + kKS - 1) / kKS;
-        long long hi[kTN], lo[kTN];
+        long long z[kDrainCols];
+        // a task's periods in chunks of kFlushDrains, each written out on its own, so the
+        // int64 sums stay in range for any k
+        for (int j0 = 0; j0 < nst && !stop; j0 += kFlushDrains * kPeriod) {
+          const int j1 = min(nst, j0 + kFlushDrains * kPeriod);
 #pragma unroll
-        for (int c = 0; c < kTN; ++c) hi[c] = lo[c] = 0;
-        for (int j = 0; j < nst; ++j) {
-          const bool drain = (j % kPeriod) == kPeriod - 1 || j + 1 == nst;
-          if (!drain) continue;
-          const int buf = d & 1;
-          if (!mbar_wait_or_abort(smem_u32(&accf_bar[buf]), (d / 2) & 1, &s_abort)) {
-            if (lane == 0) fail();
-            stop = true;
-            break;
-          }
-          asm volatile("tcgen05.fence::after_thread_sync;");
-          const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * kLevels * kTN);
-#pragma unroll 1
-          for (int l = 0; l < kLevels; ++l) {
-            uint32_t r[kTN];
-            tmem_ld32(lane_base + (uint32_t)(l * kTN), r);
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
-            const int wsh = l < 3 ? 7 * (2 - l) : 7 * (6 - l);
-#pragma unroll
-            for (int c = 0; c < kTN; ++c) {
-              // exact integer below 2^24: the 32-bit conversion suffices
-              const long long v = (long long)__float2int_rn(__uint_as_float(r[c])) * (1ll << wsh);
-              if (l < 3) hi[c] += v; else lo[c] += v;
+          for (int c = 0; c < kDrainCols; ++c) z[c] = 0;
+          for (int j = j0; j < j1; ++j) {
+            const bool drain = (j % kPeriod) == kPeriod - 1 || j + 1 == nst;
+            if (!drain) continue;
+            const int buf = d & 1;
+            if (!wait_warp(smem_u32(&accf_bar[buf]), (d / 2) & 1, &s_abort)) {
+              if (lane == 0) fail();
+              stop = true;
+              break;
             }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            drain_set(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * kAccCols + cpart * kDrainCols), z);
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
+            ++d;
           }
-          asm volatile("tcgen05.fence::before_thread_sync;");
-          __syncwarp();
-          if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
-          ++d;
-        }
-        if (stop) break;
-        // C (+)= sign 2^(ea + eb - 56) (hi 2^28 + lo)
-        if (row < cb.m) {
-          const int ea = aexp[tk.a_exp + row];
-          double* out = C + cb.c_off + (int64_t)row * cb.n;
-#pragma unroll
-          for (int c = 0; c < kTN; ++c) {
-            const int col = tl.tn * kTN + c;
-            if (col < cb.n) {
-              const int eb = bexp[tk.b_exp + col];
-              const double v = fma((double)hi[c], 268435456.0, (double)lo[c]);
-              const double sc = tk.sign < 0 ? -pow2(ea + eb - 56) : pow2(ea + eb - 56);
-              if (t == cb.t0) out[col] = v * sc; else out[col] = fma(v, sc, out[col]);
-            }
-          }
+          if (stop) break;
+          flush_sums(z, row, col0, cb, tk, aexp, bexp, out, written);
         }
       }
       if (stop) break;
