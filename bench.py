@@ -103,11 +103,34 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture of
+# `python bench.py --profile --mode <mode>` (summaries: profiles/k_gemm_split_d4000.txt,
+# profiles/k_gemm_dfma_d4000.txt). Keyed by matvec step.
+NCU_TRAFFIC = {
+    "split": {0: 137.0e6, 3: 314.5e6},
+    "fp64": {0: 84.6e6},
+}
+
+
+def _time_events(fn, stream, flush, reps=5):
+    import torch
+    ts = []
+    for r in range(reps):
+        flush.fill_(float(r))                       # write > L2 before each timed launch
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        fn()
+        s1.record(stream)
+        ts.append((s0, s1))
+    torch.cuda.synchronize()
+    return statistics.median(x.elapsed_time(y) for x, y in ts)
+
+
 def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk):
-    """Time the GEMM stage of each of the four contractions alone (CUDA events on the
-    launching stream, L2 flushed before each launch) and relate it to the peak."""
+    """Per matvec step: the GEMM stage (incl. operand slicing) and the GEMM kernels alone,
+    each timed with CUDA events on the launching stream with L2 flushed before every launch;
+    the roofline entry is the largest single launch of the dominant kernel."""
     import ctypes as C
-    import numpy as np
     import torch
     from tensortoolkit_gb300 import capi
     from tensortoolkit_gb300.api import ContractionPlan, DTensor
@@ -115,74 +138,72 @@ def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
     axes = [[[0], [0]], [[0, 2], [0, 1]], [[4, 1], [0, 1]], [[4, 1], [1, 0]]]
     bs = [dp, d1, d2, dr]
     cur_a, a_meta = dl, lenv
-    per, gemm_ms, alg_flops, tc_flops = [], 0.0, 0.0, 0.0
+    lib = capi.lib()
+    sp = C.c_void_p(stream.cuda_stream)
+    per, stage_ms, kern_ms, alg_flops, tc_flops = [], 0.0, 0.0, 0.0, 0.0
+    best = None
     for i in range(4):
         p = ContractionPlan(a_meta, bs[i].meta if i else psi, axes[i], local)
         c = DTensor.empty(p.result, local)
         p.execute(cur_a, bs[i], c, mode=mode)
-        sp = C.c_void_p(stream.cuda_stream)
-        capi.check(capi.lib().qltg_ctrct_exec_stage(p.h, C.c_void_p(cur_a.ptr), C.c_void_p(bs[i].ptr),
-                                                    C.c_void_p(c.ptr), mode_i, 1, sp))
-        ts = []
-        for r in range(5):
-            flush.fill_(float(r))
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            capi.check(capi.lib().qltg_ctrct_exec_stage(p.h, C.c_void_p(cur_a.ptr), C.c_void_p(bs[i].ptr),
-                                                        C.c_void_p(c.ptr), mode_i, 2, sp))
-            s1.record(stream)
-            ts.append((s0, s1))
-        torch.cuda.synchronize()
+        args = (p.h, C.c_void_p(cur_a.ptr), C.c_void_p(bs[i].ptr), C.c_void_p(c.ptr), mode_i)
+        capi.check(lib.qltg_ctrct_exec_stage(*args, 1, sp))
+        ms2 = _time_events(lambda: capi.check(lib.qltg_ctrct_exec_stage(*args, 2, sp)), stream, flush)
+        ms3 = _time_events(lambda: capi.check(lib.qltg_ctrct_exec_stage(*args, 3, sp)), stream, flush)
         p.device_status()
-        ms = statistics.median(x.elapsed_time(y) for x, y in ts)
         f, _ = p.stats()
-        tasks = p.tasks()
         tcf = 0.0
-        if mode == "split" and len(tasks):
-            # group by output block: (m, n) and its ks
+        if mode == "split":
             cbs = {}
-            for (_, _, cidx, m, k, n, _, _) in tasks:
+            for (_, _, cidx, m, k, n, _, _) in p.tasks():
                 cbs.setdefault(int(cidx), [int(m), int(n), []])[2].append(int(k))
             for m, n, ks in cbs.values():
                 if n <= 8 and max(ks) <= 8:
                     continue            # skinny blocks stay on the FP64 pipe
                 tiles = -(-m // 128) * -(-n // 32)
                 stages = sum(-(-k // 32) for k in ks)
-                tcf += tiles * stages * 2 * 28 * (2 * 128 * 32 * 16)
-        per.append({"ms": round(ms, 4), "gflop": round(f / 1e9, 4), "tensor_gflop": round(tcf / 1e9, 2)})
-        gemm_ms += ms
+                # 28 slice pairs on 128 x 32 x 32 padded tiles per 32-wide k stage
+                tcf += tiles * stages * 28 * (2 * 128 * 32 * 32)
+        per.append({"stage_ms": round(ms2, 4), "kernel_ms": round(ms3, 4), "gflop": round(f / 1e9, 4),
+                    "tensor_gflop": round(tcf / 1e9, 2)})
+        stage_ms += ms2
+        kern_ms += ms3
         alg_flops += f
         tc_flops += tcf
+        work = tcf if mode == "split" else f
+        if f > 1e9 and (best is None or ms3 > best[1]):
+            best = (i, ms3, work, f)
         cur_a, a_meta = c, p.result
+    i, ms, work, f = best
     if mode == "split":
-        achieved = tc_flops / (gemm_ms / 1e3) / 1e12
         peak = pk["bf16_tflops"]
         src = f"bf16 dense burst, {pk['source']} (MEASURED_PEAKS.json)"
-        what = ("k_gemm_split + slice packing, 4 launches per matvec; achieved = executed BF16 tensor flops "
-                "(28 slice products, 128x32x32 padded tiles) / GEMM-stage time")
+        what = (f"k_gemm_split, one launch (matvec step {i}): executed BF16 tensor flops "
+                "(28 slice pairs on 128x32x32 padded tiles) / launch time")
     else:
         n = 8192
         x = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
         y = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
         torch.matmul(x, y)
         torch.cuda.synchronize()
-        best = 1e9
+        best_ms = 1e9
         for _ in range(3):
             s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s0.record(stream)
             torch.matmul(x, y)
             s1.record(stream)
             torch.cuda.synchronize()
-            best = min(best, s0.elapsed_time(s1))
-        peak = 2 * n ** 3 / (best / 1e3) / 1e12
+            best_ms = min(best_ms, s0.elapsed_time(s1))
+        peak = 2 * n ** 3 / (best_ms / 1e3) / 1e12
         del x, y
-        achieved = alg_flops / (gemm_ms / 1e3) / 1e12
         src = "cuBLAS DGEMM 8192^3 measured in this run (the FP64 pipe)"
-        what = "k_gemm_dfma + k_gemm_skinny, algorithmic flops sum(2mkn) / GEMM-stage time"
+        what = f"k_gemm_dfma (+ k_gemm_skinny), one launch (matvec step {i}): algorithmic flops sum(2mkn) / launch time"
+    achieved = work / (ms / 1e3) / 1e12
     return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak if peak else None, "traffic": None, "kernel": what, "peak_source": src,
-            "per_step": per, "gemm_stage_ms": round(gemm_ms, 4),
-            "fp64_equiv_tflops": alg_flops / (gemm_ms / 1e3) / 1e12}
+            "frac": achieved / peak if peak else None, "traffic": NCU_TRAFFIC.get(mode, {}).get(i),
+            "kernel": what, "peak_source": src, "launch_ms": round(ms, 4),
+            "fp64_equiv_tflops": f / (ms / 1e3) / 1e12,
+            "per_step": per, "gemm_stage_ms": round(stage_ms, 4), "gemm_kernels_ms": round(kern_ms, 4)}
 
 
 def cpu_matvec_time(tensors, iters: int, threads: int) -> float:

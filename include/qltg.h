@@ -123,9 +123,11 @@ QLTG_API int qltg_ctrct_plan_stats(const qltg_ctrct_plan* plan, double* flops, d
 QLTG_API int qltg_ctrct_exec(qltg_ctrct_plan* plan, const void* a_dev, const void* b_dev, void* c_dev,
                     int32_t mode, void* stream);
 
-/* The two stages of qltg_ctrct_exec, separately, for profiling: stage 1 runs only the
- * operand transposes into the plan's scratch, stage 2 only the grouped GEMM (reading the
- * operands left by the last stage-1 call on this plan), stage 0 both. */
+/* The stages of qltg_ctrct_exec, separately, for profiling: stage 1 runs only the operand
+ * transposes into the plan's scratch, stage 2 only the grouped GEMM (reading the operands
+ * left by the last stage-1 call on this plan; in split mode this includes slicing the
+ * operands), stage 3 only the GEMM kernels (split mode: on the slices packed by the last
+ * stage-2 call; QLTG_ERR_INVALID before any), stage 0 all of it. */
 QLTG_API int qltg_ctrct_exec_stage(qltg_ctrct_plan* plan, const void* a_dev, const void* b_dev, void* c_dev,
                                    int32_t mode, int32_t stage, void* stream);
 

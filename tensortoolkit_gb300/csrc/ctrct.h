@@ -82,15 +82,33 @@ struct SplitTask {
   int32_t ktiles;
   int32_t sign;
 };
+// One (output tile, task) step of the split GEMM; the steps of one CTA are contiguous, in
+// the order it processes them.
+struct SplitWork {
+  int64_t c_off;          // element offset of the output block
+  int64_t a_pack, b_pack; // byte offsets of the operand blocks' packed slice tiles
+  int32_t m, n;           // output block shape
+  int32_t a_exp, b_exp;   // exponent offsets of the operand blocks
+  int32_t ktiles;         // 64-wide k tiles of the task
+  int32_t k;              // contracted extent of the task
+  int16_t tm, tn;         // 128-row / 32-column tile of the output block
+  int8_t sign;            // sign of the task
+  uint8_t flags;          // bit 0: first task of the tile, bit 1: last task of the tile
+  uint8_t pad[10];
+};
+static_assert(sizeof(SplitWork) == 64, "SplitWork is one 64-byte record");
 struct SplitPlan {
   bool built = false;
   bool a_static = false, b_static = false;   // operand packed once, unchanged afterwards
   bool a_ready = false, b_ready = false;
   std::vector<SplitOperand> a_ops, b_ops;
   std::vector<SplitTask> tasks;   // indexed like GemmSchedule::task
-  std::vector<GemmTile> tiles;    // (output block, 128-row tile, 32-col tile)
+  std::vector<GemmTile> tiles;    // (output block, 128-row tile, 32-col tile), longest first
+  std::vector<SplitWork> work;    // per CTA: tiles blockIdx.x, + grid, ...; each its tasks
+  std::vector<int32_t> work_off;  // grid + 1 offsets into work
+  int grid = 0;
   int64_t n_a_vec = 0, n_b_vec = 0, n_a_chunks = 0, n_b_chunks = 0, n_b_items = 0;
-  DevBuf d_a_ops, d_b_ops, d_tasks, d_tiles, a_packed, b_packed, a_exps, b_exps, counter, error;
+  DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error;
   void build(const struct CtrctPlan& p, cudaStream_t s);
   int64_t launches() const;
 };

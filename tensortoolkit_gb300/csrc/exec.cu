@@ -65,7 +65,7 @@ int64_t exec_launches_split(const CtrctPlan& p) {
 void exec_contraction(CtrctPlan& p, const void* a, const void* b, void* c, int mode, cudaStream_t s, int stage) {
   if (p.sched.tile.empty() && p.sched.skinny.empty()) return;
   QLTG_CHECK(a && b && c, QLTG_ERR_INVALID, "null device buffer");
-  QLTG_CHECK(stage >= 0 && stage <= 2, QLTG_ERR_INVALID, "stage must be 0, 1 or 2");
+  QLTG_CHECK(stage >= 0 && stage <= 3, QLTG_ERR_INVALID, "stage must be 0, 1, 2 or 3");
   QLTG_CHECK(mode == QLTG_MODE_FP64 || mode == QLTG_MODE_SPLIT, QLTG_ERR_INVALID, "unknown arithmetic mode");
   const int eb = (int)p.a.elem_bytes();
   const void* ap = a;
@@ -74,18 +74,18 @@ void exec_contraction(CtrctPlan& p, const void* a, const void* b, void* c, int m
   const bool a_packed = mode == QLTG_MODE_SPLIT && p.split && p.split->a_static && p.split->a_ready;
   const bool b_packed = mode == QLTG_MODE_SPLIT && p.split && p.split->b_static && p.split->b_ready;
   if (p.a_trans && p.a.size) {
-    if (stage != 2 && !a_packed) p.a_tl.launch(a, p.a_t.get(), eb, s);
+    if (stage < 2 && !a_packed) p.a_tl.launch(a, p.a_t.get(), eb, s);
     ap = p.a_t.get();
   }
   if (p.b_trans && p.b.size) {
-    if (stage != 2 && !b_packed) p.b_tl.launch(b, p.b_t.get(), eb, s);
+    if (stage < 2 && !b_packed) p.b_tl.launch(b, p.b_t.get(), eb, s);
     bp = p.b_t.get();
   }
   if (stage == 1) return;
   if (mode == QLTG_MODE_FP64)
     launch_gemm_f64(p.sched, ap, bp, c, p.a.dtype == QLTG_C128, p.ctx->num_sms, s);
   else
-    launch_gemm_split(p, ap, bp, c, s);
+    launch_gemm_split(p, ap, bp, c, s, /*pack=*/stage != 3);
 }
 
 }  // namespace qltg

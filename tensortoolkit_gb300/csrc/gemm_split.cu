@@ -35,6 +35,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
 
 #include "split.h"
 
@@ -244,8 +245,10 @@ constexpr int kDrainCols = kTN / 4;             // columns per drain thread
 constexpr int kRoleThreads = 64 + 32 * kDrainWarps;   // warp 0 producer, warp 1 MMA, warps 2-17 drain
 // Tensor memory: two accumulator sets, each 7 levels x 32 columns (level L at 32 (L - 2)).
 constexpr int kAccCols = kLevels * kTN;         // 224
+// Then the tile's running FP64 sum over its tasks: 32 doubles per lane as 64 32-bit columns.
+constexpr int kSumCol = 2 * kAccCols;           // 448
 constexpr uint32_t kTmemAlloc = 512;
-static_assert(2 * kAccCols <= (int)kTmemAlloc, "tensor memory budget");
+static_assert(kSumCol + 2 * kTN <= (int)kTmemAlloc, "tensor memory budget");
 constexpr int kFlushDrains = 64;                // the int64 sum of a chunk stays below 2^63
 constexpr float kMagic = 12582912.0f;           // 1.5 * 2^23: x + kMagic has the integer x in its low bits
 constexpr int kMagicBits = 0x4B400000;          // for |x| < 2^22
@@ -289,6 +292,21 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
                : "r"(taddr));
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]));
+}
+
 // Bounded wait that also gives up as soon as another role has aborted.
 __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t phase, const volatile int* abort_flag) {
   uint32_t done = 0;
@@ -320,23 +338,48 @@ __device__ __forceinline__ bool wait_warp_own(uint32_t mbar, uint32_t phase) {
   return __all_sync(0xffffffffu, mbar_wait_or_abort(mbar, phase, &never));
 }
 
-// z 2^e (negated when neg) rounded to the nearest double, built with integer operations
-// only (the FP64 pipe of this GPU is slow); outside the normal range it falls back to ldexp.
-__device__ __forceinline__ double scaled_i64(long long z, int e, bool neg) {
+// z 2^e (negated when neg) rounded to the nearest double (ties to even), with integer
+// operations only: the FP64 pipe of this GPU is slow, and no path here touches it.
+__host__ __device__ __forceinline__ double scaled_i64(long long z, int e, bool neg) {
   if (z == 0) return 0.0;
   const unsigned long long a = z < 0 ? 0ull - (unsigned long long)z : (unsigned long long)z;
   const unsigned long long sgn = ((z < 0) != neg) ? 0x8000000000000000ull : 0ull;
+#ifdef __CUDA_ARCH__
   const int lz = __clzll((long long)a);
-  const unsigned long long m = a << lz;                 // leading one at bit 63
-  unsigned long long mant = m >> 11;                    // 53 bits, leading one at bit 52
-  const unsigned long long rem = m & 0x7FFull;
-  mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;   // nearest-even
+#else
+  const int lz = __builtin_clzll(a);
+#endif
   const int be = 1023 + 63 - lz + e;                    // biased exponent of the leading bit
-  // (be - 1) << 52 plus the mantissa with its leading one adds the exponent; a rounding
-  // carry to 2^53 moves into the exponent by itself
-  if (be >= 1 && be < 2046) return __longlong_as_double((long long)(sgn | (((unsigned long long)(be - 1) << 52) + mant)));
-  const double v = ldexp((double)z, e);
-  return neg ? -v : v;
+  unsigned long long bits;
+  if (be >= 1) {
+    const unsigned long long m = a << lz;               // leading one at bit 63
+    unsigned long long mant = m >> 11;                  // 53 bits, leading one at bit 52
+    const unsigned long long rem = m & 0x7FFull;
+    mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+    // (be - 1) << 52 plus the mantissa with its leading one adds the exponent; a rounding
+    // carry to 2^53 moves into the exponent by itself, and past 2046 it reaches infinity
+    bits = be < 2047 ? ((unsigned long long)(be - 1) << 52) + mant : 0x7FF0000000000000ull;
+    if (bits > 0x7FF0000000000000ull) bits = 0x7FF0000000000000ull;
+  } else {
+    // subnormal result: a 2^(e + 1074) in units of 2^-1074, rounded to nearest-even
+    const int sh = -(e + 1074);                         // > 0 here unless a is large
+    if (sh <= 0) {
+      bits = a << (-sh);                                // cannot overflow: be < 1
+    } else if (sh >= 64) {
+      bits = (sh == 64 && a > 0x8000000000000000ull) ? 1ull : 0ull;
+    } else {
+      const unsigned long long q = a >> sh, r = a - (q << sh), half = 1ull << (sh - 1);
+      bits = q + ((r > half || (r == half && (q & 1ull))) ? 1ull : 0ull);
+    }
+  }
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)(sgn | bits));
+#else
+  double r;
+  const unsigned long long rb = sgn | bits;
+  memcpy(&r, &rb, sizeof r);
+  return r;
+#endif
 }
 
 // Fold one drained accumulator set into the int64 sums z (units 2^-49) of this thread's
@@ -384,22 +427,31 @@ __device__ __forceinline__ void drain_set(uint32_t lb, long long (&z)[kDrainCols
     z[c] += (long long)(u[c] + ((__float2int_rn(__uint_as_float(r[c]) * 0x1p56f) + 64) >> 7));
 }
 
-// C (+)= sign 2^(ea + eb - 49) z for this thread's row and 8 columns, rounded once to FP64;
-// the first write of a tile stores, later ones add.
-__device__ __forceinline__ void flush_sums(const long long (&z)[kDrainCols], int row, int col0, const GemmCBlk& cb,
-                                           const SplitTask& tk, const int32_t* __restrict__ aexp,
-                                           const int32_t* __restrict__ bexp, double* out, bool& written) {
-  if (row < cb.m) {
-    const int ea = aexp[tk.a_exp + row];
+// sum (+)= sign 2^(ea + eb - 49) z, each term rounded once to FP64; the tile's running sum
+// of this thread's 8 columns lives in tensor memory at tsum (16 columns). The first
+// contribution to a tile sets it, later ones add.
+__device__ __forceinline__ void fold_sums(const long long (&z)[kDrainCols], int ea, const int (&eb)[kDrainCols],
+                                          bool neg, uint32_t tsum, bool& written) {
+  uint32_t v[2 * kDrainCols];
+  if (written) {                                   // warp-uniform: later tasks of the tile add
+    tmem_ld16(tsum, v);
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
     for (int c = 0; c < kDrainCols; ++c) {
-      const int col = col0 + c;
-      if (col < cb.n) {
-        const double v = scaled_i64(z[c], ea + bexp[tk.b_exp + col] - 49, tk.sign < 0);
-        out[col] = written ? out[col] + v : v;
-      }
+      const double x = scaled_i64(z[c], ea + eb[c] - 49, neg) + __hiloint2double((int)v[2 * c + 1], (int)v[2 * c]);
+      v[2 * c] = (uint32_t)__double2loint(x);
+      v[2 * c + 1] = (uint32_t)__double2hiint(x);
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < kDrainCols; ++c) {
+      const double x = scaled_i64(z[c], ea + eb[c] - 49, neg);
+      v[2 * c] = (uint32_t)__double2loint(x);
+      v[2 * c + 1] = (uint32_t)__double2hiint(x);
     }
   }
+  tmem_st16(tsum, v);
+  asm volatile("tcgen05.wait::st.sync.aligned;");
   written = true;
 }
 
@@ -421,8 +473,7 @@ __device__ __forceinline__ void flush_sums(const long long (&z)[kDrainCols], int
 // Warps 0 and 1 run their loops as whole warps (warp-uniform state and descriptors); one
 // elected lane issues each copy / tensor-core instruction.
 __global__ void __launch_bounds__(kRoleThreads, 1)
-    k_gemm_split(const GemmCBlk* __restrict__ cblk, const SplitTask* __restrict__ task,
-                 const GemmTask* __restrict__ gtask, const GemmTile* __restrict__ tiles, int ntiles,
+    k_gemm_split(const SplitWork* __restrict__ items, const int32_t* __restrict__ item_off,
                  const uint8_t* __restrict__ apack, const uint8_t* __restrict__ bpack,
                  const int32_t* __restrict__ aexp, const int32_t* __restrict__ bexp, double* __restrict__ C,
                  int* __restrict__ err) {
@@ -449,6 +500,7 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_base;
   const uint32_t sbase = smem_u32(smem);
+  const int beg = item_off[blockIdx.x], end = item_off[blockIdx.x + 1];
   auto fail = [&]() {
     s_abort = 1;
     atomicExch(err, 1);
@@ -457,31 +509,33 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
   if (warp == 0) {
     // ------------------------------------------------------------ producer
     uint32_t g = 0;
-    for (int ti = blockIdx.x; ti < ntiles && !aborted(&s_abort); ti += gridDim.x) {
-      const GemmTile tl = tiles[ti];
-      const GemmCBlk cb = cblk[tl.cblk];
-      for (int t = cb.t0; t < cb.t1 && !aborted(&s_abort); ++t) {
-        const SplitTask tk = task[t];
-        const int nst = (gtask[t].k + kKS - 1) / kKS;
-        for (int j = 0; j < nst; ++j, ++g) {
-          const int s = g % kStages;
-          if (g >= (uint32_t)kStages && !wait_warp(smem_u32(&empty_bar[s]), ((g / kStages) - 1) & 1, &s_abort)) {
-            if (lane == 0) fail();
-            break;
-          }
-          const int kt = j >> 1, half = j & 1;
-          const uint8_t* ga = apack + tk.a_pack + ((int64_t)tl.tm * tk.ktiles + kt) * (kS * kATile) + half * kABytes;
-          const uint8_t* gb = bpack + tk.b_pack + ((int64_t)tl.tn * tk.ktiles + kt) * (kS * kBTile) + half * kBBytes;
-          const uint32_t sa = sbase + s * kStageBytes;
-          const uint32_t fb = smem_u32(&full_bar[s]);
-          if (elect_one()) {
-            mbar_expect_tx(fb, kStageBytes);
-            bulk_g2s(sa, ga, kABytes, fb);
-            bulk_g2s(sa + kABytes, gb, kBBytes, fb);
-          }
-          __syncwarp();
+    SplitWork nx;
+    if (beg < end) nx = items[beg];
+    for (int it = beg; it < end && !aborted(&s_abort); ++it) {
+      const SplitWork w = nx;
+      if (it + 1 < end) nx = items[it + 1];            // prefetch the next step
+      const int nst = (w.k + kKS - 1) / kKS;
+      bool ok = true;
+      for (int j = 0; j < nst; ++j, ++g) {
+        const int s = g % kStages;
+        if (g >= (uint32_t)kStages && !wait_warp(smem_u32(&empty_bar[s]), ((g / kStages) - 1) & 1, &s_abort)) {
+          if (lane == 0) fail();
+          ok = false;
+          break;
         }
+        const int kt = j >> 1, half = j & 1;
+        const uint8_t* ga = apack + w.a_pack + ((int64_t)w.tm * w.ktiles + kt) * (kS * kATile) + half * kABytes;
+        const uint8_t* gb = bpack + w.b_pack + ((int64_t)w.tn * w.ktiles + kt) * (kS * kBTile) + half * kBBytes;
+        const uint32_t sa = sbase + s * kStageBytes;
+        const uint32_t fb = smem_u32(&full_bar[s]);
+        if (elect_one()) {
+          mbar_expect_tx(fb, kStageBytes);
+          bulk_g2s(sa, ga, kABytes, fb);
+          bulk_g2s(sa + kABytes, gb, kBBytes, fb);
+        }
+        __syncwarp();
       }
+      if (!ok) break;
     }
     // copies still in flight are waited for by the MMA warp (every issued stage is consumed
     // on the normal path); on abort wait for the tail of issued stages here
@@ -495,11 +549,11 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
     const uint64_t sd0 = smem_desc(sbase);
     uint32_t g = 0, d = 0;
     bool ok = true;
-    for (int ti = blockIdx.x; ti < ntiles && ok && !aborted(&s_abort); ti += gridDim.x) {
-      const GemmTile tl = tiles[ti];
-      const GemmCBlk cb = cblk[tl.cblk];
-      for (int t = cb.t0; t < cb.t1 && ok && !aborted(&s_abort); ++t) {
-        const int nst = (gtask[t].k + kKS - 1) / kKS;
+    int nst_next = beg < end ? items[beg].k : 0;
+    for (int it = beg; it < end && ok && !aborted(&s_abort); ++it) {
+      const int nst = (nst_next + kKS - 1) / kKS;
+      if (it + 1 < end) nst_next = items[it + 1].k;   // prefetch the next step
+      {
         for (int j = 0; j < nst; ++j, ++g) {
           const int s = g % kStages;
           const int buf = d & 1;
@@ -539,44 +593,57 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
     const int cpart = (warp - 2) >> 2;               // columns 8 * cpart .. + 7 of the tile
     const int row_in_tile = quad * 32 + lane;
     uint32_t d = 0;
-    for (int ti = blockIdx.x; ti < ntiles && !aborted(&s_abort); ti += gridDim.x) {
-      const GemmTile tl = tiles[ti];
-      const GemmCBlk cb = cblk[tl.cblk];
-      const int row = tl.tm * kTM + row_in_tile;
-      const int col0 = tl.tn * kTN + cpart * kDrainCols;
-      double* out = C + cb.c_off + (int64_t)row * cb.n;
-      bool stop = false, written = false;
-      for (int t = cb.t0; t < cb.t1 && !stop; ++t) {
-        const SplitTask tk = task[t];
-        const int nst = (gtask[t].k + kKS - 1) / kKS;
-        long long z[kDrainCols];
-        // a task's periods in chunks of kFlushDrains, each written out on its own, so the
-        // int64 sums stay in range for any k
-        for (int j0 = 0; j0 < nst && !stop; j0 += kFlushDrains * kPeriod) {
-          const int j1 = min(nst, j0 + kFlushDrains * kPeriod);
+    bool stop = false, written = false;
+    const uint32_t tsum = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(kSumCol + 2 * cpart * kDrainCols);
+    for (int it = beg; it < end && !stop && !aborted(&s_abort); ++it) {
+      const SplitWork w = items[it];
+      const int row = w.tm * kTM + row_in_tile;
+      const int col0 = w.tn * kTN + cpart * kDrainCols;
+      const int nst = (w.k + kKS - 1) / kKS;
+      if (w.flags & 1) written = false;
+      // scale exponents, fetched while the first period is still on the tensor cores
+      const int ea = row < w.m ? aexp[w.a_exp + row] : 0;
+      int eb[kDrainCols];
 #pragma unroll
-          for (int c = 0; c < kDrainCols; ++c) z[c] = 0;
-          for (int j = j0; j < j1; ++j) {
-            const bool drain = (j % kPeriod) == kPeriod - 1 || j + 1 == nst;
-            if (!drain) continue;
-            const int buf = d & 1;
-            if (!wait_warp(smem_u32(&accf_bar[buf]), (d / 2) & 1, &s_abort)) {
-              if (lane == 0) fail();
-              stop = true;
-              break;
-            }
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            drain_set(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * kAccCols + cpart * kDrainCols), z);
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
-            ++d;
+      for (int c = 0; c < kDrainCols; ++c) eb[c] = col0 + c < w.n ? bexp[w.b_exp + col0 + c] : 0;
+      long long z[kDrainCols];
+      // the task's periods in chunks of kFlushDrains, each folded on its own, so the int64
+      // sums stay in range for any k
+      for (int j0 = 0; j0 < nst && !stop; j0 += kFlushDrains * kPeriod) {
+        const int j1 = min(nst, j0 + kFlushDrains * kPeriod);
+#pragma unroll
+        for (int c = 0; c < kDrainCols; ++c) z[c] = 0;
+        for (int j = j0; j < j1; ++j) {
+          const bool drain = (j % kPeriod) == kPeriod - 1 || j + 1 == nst;
+          if (!drain) continue;
+          const int buf = d & 1;
+          if (!wait_warp(smem_u32(&accf_bar[buf]), (d / 2) & 1, &s_abort)) {
+            if (lane == 0) fail();
+            stop = true;
+            break;
           }
-          if (stop) break;
-          flush_sums(z, row, col0, cb, tk, aexp, bexp, out, written);
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          drain_set(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * kAccCols + cpart * kDrainCols), z);
+          asm volatile("tcgen05.fence::before_thread_sync;");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
+          ++d;
+        }
+        if (stop) break;
+        fold_sums(z, ea, eb, w.sign < 0, tsum, written);
+      }
+      // one store per tile after its last task (a C tile belongs to exactly one CTA)
+      if (!stop && (w.flags & 2)) {
+        uint32_t v[2 * kDrainCols];
+        tmem_ld16(tsum, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        if (row < w.m) {
+          double* out = C + w.c_off + (int64_t)row * w.n;
+#pragma unroll
+          for (int c = 0; c < kDrainCols; ++c)
+            if (col0 + c < w.n) out[col0 + c] = __hiloint2double((int)v[2 * c + 1], (int)v[2 * c]);
         }
       }
-      if (stop) break;
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -671,6 +738,38 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q)
     for (int32_t t = g.cblk[q].t0; t < g.cblk[q].t1; ++t) cost[q] += (g.task[t].k + 31) / 32;
   std::stable_sort(tiles.begin(), tiles.end(), [&](const GemmTile& x, const GemmTile& y) { return cost[x.cblk] > cost[y.cblk]; });
+  // per-CTA work lists: CTA b takes tiles b, b + grid, ... (longest first), each with the
+  // tasks of its output block in order
+  grid = (int)std::min<int64_t>((int64_t)tiles.size(), std::max(1, p.ctx->num_sms));
+  work.clear();
+  work_off.assign(grid + 1, 0);
+  for (int b = 0; b < grid; ++b) {
+    work_off[b] = (int32_t)work.size();
+    for (size_t ti = b; ti < tiles.size(); ti += grid) {
+      const GemmTile& tl = tiles[ti];
+      const GemmCBlk& cb = g.cblk[tl.cblk];
+      for (int32_t t = cb.t0; t < cb.t1; ++t) {
+        const SplitTask& tk = tasks[t];
+        SplitWork w{};
+        w.c_off = cb.c_off;
+        w.a_pack = tk.a_pack;
+        w.b_pack = tk.b_pack;
+        w.m = cb.m;
+        w.n = cb.n;
+        w.a_exp = tk.a_exp;
+        w.b_exp = tk.b_exp;
+        w.ktiles = tk.ktiles;
+        w.k = g.task[t].k;
+        w.tm = tl.tm;
+        w.tn = tl.tn;
+        w.sign = (int8_t)(tk.sign < 0 ? -1 : 1);
+        w.flags = (uint8_t)((t == cb.t0 ? 1 : 0) | (t + 1 == cb.t1 ? 2 : 0));
+        work.push_back(w);
+      }
+    }
+    QLTG_CHECK(work.size() < ((size_t)1 << 31), QLTG_ERR_UNSUPPORTED, "too many split work items");
+  }
+  work_off[grid] = (int32_t)work.size();
   n_a_vec = a_vec;
   n_b_vec = b_vec;
   n_a_chunks = a_chunks;
@@ -678,20 +777,16 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   n_b_items = b_items;
   d_a_ops = upload(a_ops, s);
   d_b_ops = upload(b_ops, s);
-  d_tasks = upload(tasks, s);
-  d_tiles = upload(tiles, s);
+  d_work = upload(work, s);
+  d_work_off = upload(work_off, s);
   a_packed.alloc(std::max<int64_t>(a_pack, 16));
   b_packed.alloc(std::max<int64_t>(b_pack, 16));
   a_exps.alloc(std::max<int64_t>(a_exp, 1) * 4);
   b_exps.alloc(std::max<int64_t>(b_exp, 1) * 4);
-  counter.alloc(sizeof(int));
   error.alloc(sizeof(int));
   QLTG_CUDA(cudaMemsetAsync(error.get(), 0, sizeof(int), s));
-  static bool attr_set = false;
-  if (!attr_set) {
-    QLTG_CUDA(cudaFuncSetAttribute(k_gemm_split, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-    attr_set = true;
-  }
+  // per device (the attribute belongs to the current device's copy of the kernel)
+  QLTG_CUDA(cudaFuncSetAttribute(k_gemm_split, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
   QLTG_CUDA(cudaStreamSynchronize(s));
   built = true;
 }
@@ -743,7 +838,7 @@ void split_prepack_static(CtrctPlan& p, const void* a_static, const void* b_stat
   QLTG_CUDA(cudaStreamSynchronize(s));
 }
 
-void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cudaStream_t s) {
+void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cudaStream_t s, bool pack) {
   QLTG_CHECK(p.a.dtype == QLTG_F64, QLTG_ERR_UNSUPPORTED, "split-precision mode supports FP64 tensors");
   if (!p.split) {
     // first split-mode execution of this plan: build the slice schedule (allocates; not
@@ -759,13 +854,15 @@ void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cuda
   // pad them 8x); everything else goes through the slices
   launch_gemm_f64_skinny(p.sched, a, b, c, false, p.ctx->num_sms, s);
   if (sp.tiles.empty()) return;
-  if (!(sp.a_static && sp.a_ready)) pack_split_operand(sp, true, a, s);
-  if (!(sp.b_static && sp.b_ready)) pack_split_operand(sp, false, b, s);
-  const int grid = (int)std::min<int64_t>((int64_t)sp.tiles.size(), p.ctx->num_sms);
-  k_gemm_split<<<grid, kRoleThreads, kSmemBytes, s>>>(
-      p.sched.d_cblk.as<GemmCBlk>(), sp.d_tasks.as<SplitTask>(), p.sched.d_task.as<GemmTask>(), sp.d_tiles.as<GemmTile>(),
-      (int)sp.tiles.size(),
-      sp.a_packed.as<uint8_t>(), sp.b_packed.as<uint8_t>(), sp.a_exps.as<int32_t>(), sp.b_exps.as<int32_t>(),
+  if (pack) {
+    if (!(sp.a_static && sp.a_ready)) pack_split_operand(sp, true, a, s);
+    if (!(sp.b_static && sp.b_ready)) pack_split_operand(sp, false, b, s);
+  } else {
+    QLTG_CHECK(sp.a_ready && sp.b_ready, QLTG_ERR_INVALID, "GEMM-only stage before the operands were ever packed");
+  }
+  k_gemm_split<<<sp.grid, kRoleThreads, kSmemBytes, s>>>(
+      sp.d_work.as<SplitWork>(), sp.d_work_off.as<int32_t>(), sp.a_packed.as<uint8_t>(), sp.b_packed.as<uint8_t>(),
+      sp.a_exps.as<int32_t>(), sp.b_exps.as<int32_t>(),
       static_cast<double*>(c), sp.error.as<int>());
   QLTG_CUDA(cudaGetLastError());
 }
