@@ -15,23 +15,27 @@ struct PermDesc {
   int64_t sstride[kMaxRank];   // source stride of each destination dim
   int32_t dims[kMaxRank];      // destination-order dims
   int32_t rank;
-  int32_t p;                   // destination dim that is innermost in the source
-  int32_t tiles_p, tiles_q;    // 32-wide tiles along p and along the innermost dst dim
-  int64_t nouter;              // product of the remaining dims
-  int64_t tile_begin;          // first global tile of this block
-  double sign;
+  int32_t p;                   // destination dim that is innermost in the source (-1: gather mode)
+  int32_t tp, tq;              // tile extents along p and along the innermost dst dim
+  int32_t tiles_p, tiles_q;    // tiles along p and along the innermost dst dim
+  int64_t nouter;              // product of the remaining dims (gather mode: block size)
+  int64_t tile_begin;          // first global work item of this block
+  uint64_t sign_mask;          // 0, or the sign bit: the block's +-1 sign applied by XOR
 };
 
 struct TransposeList {
   std::vector<PermDesc> host;
+  std::vector<uint8_t> identity;   // per block: its data layout is unchanged by the permutation
   DevBuf dev;
   int64_t ntiles = 0;
   int64_t nblocks = 0;
+  // skip_identity: blocks whose layout the permutation leaves unchanged get no work (the
+  // caller reads them from the source)
   void build(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
-             const std::vector<int64_t>* dst_offsets, cudaStream_t s);
+             const std::vector<int64_t>* dst_offsets, cudaStream_t s, bool skip_identity = false);
   // host-side descriptors only (fills host / ntiles / nblocks, no device memory)
   void describe(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
-                const std::vector<int64_t>* dst_offsets);
+                const std::vector<int64_t>* dst_offsets, bool skip_identity = false);
   void launch(const void* src, void* dst, int elem_bytes, cudaStream_t s) const;
 };
 
@@ -42,10 +46,17 @@ struct GemmCBlk {
   int32_t t0, t1;              // task range
 };
 struct GemmTask {
-  int64_t a_off, b_off;        // offsets of the (transposed) operand blocks
+  int64_t a_off, b_off;        // offsets of the (transposed) operand blocks, | kFromSrc
   int32_t k;
   int32_t sign;                // fermion exchange sign
 };
+// Operand offset flag: the block is read from the untransposed operand, whose layout for
+// this block already matches the transposed one (same offset in both buffers).
+constexpr int64_t kFromSrc = (int64_t)1 << 62;
+template <typename T>
+__host__ __device__ __forceinline__ const T* operand_block(const T* scratch, const T* src, int64_t off) {
+  return (off & kFromSrc) ? src + (off & ~kFromSrc) : scratch + off;
+}
 struct GemmTile {
   int32_t cblk;
   int16_t tm, tn;
@@ -136,9 +147,16 @@ void exec_contraction(CtrctPlan& p, const void* a, const void* b, void* c, int m
 // grouped GEMM launchers (gemm_f64.cu)
 bool skinny_cblk(const GemmSchedule& g, int32_t q);
 int skinny_rows_per_item();
-void launch_gemm_f64(const GemmSchedule& g, const void* a, const void* b, void* c, bool cplx, int num_sms,
-                     cudaStream_t s);
-void launch_gemm_f64_skinny(const GemmSchedule& g, const void* a, const void* b, void* c, bool cplx, int num_sms,
+// Operand buffers of one execution: scratch (transposed blocks) and source (the operands as
+// passed in, for blocks flagged kFromSrc).
+struct Operands {
+  const void* a;
+  const void* a_src;
+  const void* b;
+  const void* b_src;
+};
+void launch_gemm_f64(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms, cudaStream_t s);
+void launch_gemm_f64_skinny(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms,
                             cudaStream_t s);
 
 // Block order, destination offsets and fermionic block signs of QLTensor::Transpose.

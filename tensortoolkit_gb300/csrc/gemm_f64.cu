@@ -50,10 +50,11 @@ __device__ __forceinline__ unsigned long long sign_mask(int sign) { return sign 
 template <typename T>
 __global__ void __launch_bounds__(NT) k_gemm_dfma(const GemmCBlk* __restrict__ cblk, const GemmTask* __restrict__ task,
                                                   const GemmTile* __restrict__ tiles, int ntiles,
-                                                  const T* __restrict__ A, const T* __restrict__ B,
+                                                  const T* __restrict__ A, const T* __restrict__ As,
+                                                  const T* __restrict__ B, const T* __restrict__ Bs,
                                                   T* __restrict__ C, int* __restrict__ counter) {
-  __shared__ T As[BK][BM + 1];
-  __shared__ T Bs[BK][BN];
+  __shared__ T sA[BK][BM + 1];
+  __shared__ T sB[BK][BN];
   __shared__ int s_ti;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   while (true) {
@@ -77,8 +78,8 @@ __global__ void __launch_bounds__(NT) k_gemm_dfma(const GemmCBlk* __restrict__ c
     for (int t = cb.t0; t < cb.t1; ++t) {
       const GemmTask tk = task[t];
       const int k = tk.k;
-      const T* a = A + tk.a_off;
-      const T* b = B + tk.b_off;
+      const T* a = operand_block(A, As, tk.a_off);
+      const T* b = operand_block(B, Bs, tk.b_off);
       const unsigned long long sg = sign_mask(tk.sign);
       for (int k0 = 0; k0 < k; k0 += BK) {
         const int kc = min(BK, k - k0);
@@ -87,20 +88,20 @@ __global__ void __launch_bounds__(NT) k_gemm_dfma(const GemmCBlk* __restrict__ c
           const int row = e / BK, kk = e % BK;
           T v = zero_of(T());
           if (kk < kc && r0 + row < m) v = flip(a[(int64_t)(r0 + row) * k + k0 + kk], sg);
-          As[kk][row] = v;
+          sA[kk][row] = v;
         }
 #pragma unroll
         for (int e = threadIdx.x; e < BK * BN; e += NT) {
           const int kk = e / BN, col = e % BN;
           T v = zero_of(T());
           if (kk < kc && c0 + col < n) v = b[(int64_t)(k0 + kk) * n + c0 + col];
-          Bs[kk][col] = v;
+          sB[kk][col] = v;
         }
         __syncthreads();
 #pragma unroll 4
         for (int kk = 0; kk < kc; ++kk) {
-          const T a0 = As[kk][ty], a1 = As[kk][ty + 16];
-          const T b0 = Bs[kk][tx], b1 = Bs[kk][tx + 16];
+          const T a0 = sA[kk][ty], a1 = sA[kk][ty + 16];
+          const T b0 = sB[kk][tx], b1 = sB[kk][tx + 16];
           if (rv[0]) {
             if (cv[0]) fma_acc(acc[0][0], a0, b0);
             if (cv[1]) fma_acc(acc[0][1], a0, b1);
@@ -128,15 +129,16 @@ constexpr int kSkinnyMax = 8;
 
 template <typename T, int NN>
 __device__ __forceinline__ void skinny_row(const GemmCBlk& cb, const GemmTask* __restrict__ task, int row,
-                                           const T* __restrict__ A, const T* __restrict__ B, T* __restrict__ C) {
+                                           const T* __restrict__ A, const T* __restrict__ As, const T* __restrict__ B,
+                                           const T* __restrict__ Bs, T* __restrict__ C) {
   T acc[NN];
 #pragma unroll
   for (int j = 0; j < NN; ++j) acc[j] = zero_of(T());
   for (int t = cb.t0; t < cb.t1; ++t) {
     const GemmTask tk = task[t];
     const int k = tk.k;
-    const T* a = A + tk.a_off + (int64_t)row * k;
-    const T* b = B + tk.b_off;
+    const T* a = operand_block(A, As, tk.a_off) + (int64_t)row * k;
+    const T* b = operand_block(B, Bs, tk.b_off);
     const unsigned long long sg = sign_mask(tk.sign);
     for (int kk = 0; kk < k; ++kk) {
       const T av = flip(__ldg(a + kk), sg);
@@ -153,7 +155,8 @@ template <typename T>
 __global__ void __launch_bounds__(kSkinnyRows) k_gemm_skinny(const GemmCBlk* __restrict__ cblk,
                                                              const GemmTask* __restrict__ task,
                                                              const GemmRowChunk* __restrict__ items, int nitems,
-                                                             const T* __restrict__ A, const T* __restrict__ B,
+                                                             const T* __restrict__ A, const T* __restrict__ As,
+                                                             const T* __restrict__ B, const T* __restrict__ Bs,
                                                              T* __restrict__ C) {
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const GemmRowChunk item = items[it];
@@ -161,14 +164,14 @@ __global__ void __launch_bounds__(kSkinnyRows) k_gemm_skinny(const GemmCBlk* __r
     const int row = item.chunk * kSkinnyRows + threadIdx.x;
     if (row >= cb.m) continue;
     switch (cb.n) {
-      case 1: skinny_row<T, 1>(cb, task, row, A, B, C); break;
-      case 2: skinny_row<T, 2>(cb, task, row, A, B, C); break;
-      case 3: skinny_row<T, 3>(cb, task, row, A, B, C); break;
-      case 4: skinny_row<T, 4>(cb, task, row, A, B, C); break;
-      case 5: skinny_row<T, 5>(cb, task, row, A, B, C); break;
-      case 6: skinny_row<T, 6>(cb, task, row, A, B, C); break;
-      case 7: skinny_row<T, 7>(cb, task, row, A, B, C); break;
-      default: skinny_row<T, 8>(cb, task, row, A, B, C); break;
+      case 1: skinny_row<T, 1>(cb, task, row, A, As, B, Bs, C); break;
+      case 2: skinny_row<T, 2>(cb, task, row, A, As, B, Bs, C); break;
+      case 3: skinny_row<T, 3>(cb, task, row, A, As, B, Bs, C); break;
+      case 4: skinny_row<T, 4>(cb, task, row, A, As, B, Bs, C); break;
+      case 5: skinny_row<T, 5>(cb, task, row, A, As, B, Bs, C); break;
+      case 6: skinny_row<T, 6>(cb, task, row, A, As, B, Bs, C); break;
+      case 7: skinny_row<T, 7>(cb, task, row, A, As, B, Bs, C); break;
+      default: skinny_row<T, 8>(cb, task, row, A, As, B, Bs, C); break;
     }
   }
 }
@@ -185,40 +188,45 @@ bool skinny_cblk(const GemmSchedule& g, int32_t q) {
 
 int skinny_rows_per_item() { return kSkinnyRows; }
 
-void launch_gemm_f64_skinny(const GemmSchedule& g, const void* a, const void* b, void* c, bool cplx, int num_sms,
+template <typename T>
+void launch_skinny_t(const GemmSchedule& g, const Operands& op, void* c, int grid, cudaStream_t s) {
+  k_gemm_skinny<T><<<grid, kSkinnyRows, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
+                                                g.d_skinny.as<GemmRowChunk>(), (int)g.skinny.size(),
+                                                static_cast<const T*>(op.a), static_cast<const T*>(op.a_src),
+                                                static_cast<const T*>(op.b), static_cast<const T*>(op.b_src),
+                                                static_cast<T*>(c));
+}
+
+template <typename T>
+void launch_dfma_t(const GemmSchedule& g, const Operands& op, void* c, int grid, cudaStream_t s) {
+  k_gemm_dfma<T><<<grid, NT, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(), g.d_tile.as<GemmTile>(),
+                                     (int)g.tile.size(), static_cast<const T*>(op.a), static_cast<const T*>(op.a_src),
+                                     static_cast<const T*>(op.b), static_cast<const T*>(op.b_src), static_cast<T*>(c),
+                                     g.d_counter.as<int>());
+}
+
+void launch_gemm_f64_skinny(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms,
                             cudaStream_t s) {
   const int ns = (int)g.skinny.size();
   if (!ns) return;
   const int grid = std::min(ns, std::max(1, num_sms) * 8);
   if (cplx)
-    k_gemm_skinny<double2><<<grid, kSkinnyRows, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
-                                                        g.d_skinny.as<GemmRowChunk>(), ns,
-                                                        static_cast<const double2*>(a),
-                                                        static_cast<const double2*>(b), static_cast<double2*>(c));
+    launch_skinny_t<double2>(g, op, c, grid, s);
   else
-    k_gemm_skinny<double><<<grid, kSkinnyRows, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
-                                                       g.d_skinny.as<GemmRowChunk>(), ns, static_cast<const double*>(a),
-                                                       static_cast<const double*>(b), static_cast<double*>(c));
+    launch_skinny_t<double>(g, op, c, grid, s);
   QLTG_CUDA(cudaGetLastError());
 }
 
-void launch_gemm_f64(const GemmSchedule& g, const void* a, const void* b, void* c, bool cplx, int num_sms,
-                     cudaStream_t s) {
+void launch_gemm_f64(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms, cudaStream_t s) {
   const int nt = (int)g.tile.size();
-  launch_gemm_f64_skinny(g, a, b, c, cplx, num_sms, s);
+  launch_gemm_f64_skinny(g, op, c, cplx, num_sms, s);
   if (nt) {
     QLTG_CUDA(cudaMemsetAsync(g.d_counter.get(), 0, sizeof(int), s));
     const int grid = std::min(nt, std::max(1, num_sms) * 4);
     if (cplx)
-      k_gemm_dfma<double2><<<grid, NT, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
-                                               g.d_tile.as<GemmTile>(), nt, static_cast<const double2*>(a),
-                                               static_cast<const double2*>(b), static_cast<double2*>(c),
-                                               g.d_counter.as<int>());
+      launch_dfma_t<double2>(g, op, c, grid, s);
     else
-      k_gemm_dfma<double><<<grid, NT, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
-                                              g.d_tile.as<GemmTile>(), nt, static_cast<const double*>(a),
-                                              static_cast<const double*>(b), static_cast<double*>(c),
-                                              g.d_counter.as<int>());
+      launch_dfma_t<double>(g, op, c, grid, s);
     QLTG_CUDA(cudaGetLastError());
   }
 }

@@ -58,8 +58,9 @@ __device__ __forceinline__ int exp_of_bits(uint64_t absbits) {
 }
 
 // A (m x k row-major): one warp per row.
-__global__ void k_row_exp(const double* __restrict__ src, const SplitOperand* __restrict__ ops, int nops,
-                          int32_t* __restrict__ exps, int64_t total_rows) {
+__global__ void k_row_exp(const double* __restrict__ scr, const double* __restrict__ src,
+                          const SplitOperand* __restrict__ ops, int nops, int32_t* __restrict__ exps,
+                          int64_t total_rows) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t rg = warp; rg < total_rows; rg += nw) {
@@ -67,7 +68,7 @@ __global__ void k_row_exp(const double* __restrict__ src, const SplitOperand* __
     while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].vec_begin <= rg) lo = mid; else hi = mid - 1; }
     const SplitOperand o = ops[lo];
     const int64_t r = rg - o.vec_begin;
-    const double* row = src + o.src_off + r * o.cols;
+    const double* row = operand_block(scr, src, o.src_off) + r * o.cols;
     uint64_t mx = 0;
     for (int c = lane; c < o.cols; c += 32) {
       const uint64_t b = (uint64_t)__double_as_longlong(row[c]) & 0x7FFFFFFFFFFFFFFFull;
@@ -85,8 +86,9 @@ __global__ void k_row_exp(const double* __restrict__ src, const SplitOperand* __
 // it, so threads take (column, 32-row chunk) items and fold into the column with atomicMax
 // on the biased exponent (the array starts at zero); k_col_exp_finish turns fields into
 // scale exponents.
-__global__ void k_col_exp(const double* __restrict__ src, const SplitOperand* __restrict__ ops, int nops,
-                          int32_t* __restrict__ exps, int64_t total_items) {
+__global__ void k_col_exp(const double* __restrict__ scr, const double* __restrict__ src,
+                          const SplitOperand* __restrict__ ops, int nops, int32_t* __restrict__ exps,
+                          int64_t total_items) {
   for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < total_items;
        it += (int64_t)gridDim.x * blockDim.x) {
     int lo = 0, hi = nops - 1;
@@ -96,8 +98,9 @@ __global__ void k_col_exp(const double* __restrict__ src, const SplitOperand* __
     const int64_t c = l % o.cols, r0 = (l / o.cols) * 32;
     int mx = 0;
     const int64_t r1 = min((int64_t)o.rows, r0 + 32);
+    const double* blk = operand_block(scr, src, o.src_off);
     for (int64_t r = r0; r < r1; ++r) {
-      const uint64_t b = (uint64_t)__double_as_longlong(src[o.src_off + r * o.cols + c]) & 0x7FFFFFFFFFFFFFFFull;
+      const uint64_t b = (uint64_t)__double_as_longlong(blk[r * o.cols + c]) & 0x7FFFFFFFFFFFFFFFull;
       const int f = b == 0 ? 0 : max(1, (int)(b >> 52));
       mx = max(mx, f);
     }
@@ -135,8 +138,9 @@ __device__ __forceinline__ void slice7(double x, int e, uint16_t* out) {
 
 // Pack A operand tiles. One thread per 16-byte chunk (8 consecutive k of one row) per
 // (row tile, k tile); writes the chunk of every slice plane.
-__global__ void k_pack_a(const double* __restrict__ src, const SplitOperand* __restrict__ ops, int nops,
-                         const int32_t* __restrict__ exps, uint8_t* __restrict__ pack, int64_t total_chunks) {
+__global__ void k_pack_a(const double* __restrict__ scr, const double* __restrict__ src,
+                         const SplitOperand* __restrict__ ops, int nops, const int32_t* __restrict__ exps,
+                         uint8_t* __restrict__ pack, int64_t total_chunks) {
   for (int64_t ch = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ch < total_chunks;
        ch += (int64_t)gridDim.x * blockDim.x) {
     int lo = 0, hi = nops - 1;
@@ -151,10 +155,11 @@ __global__ void k_pack_a(const double* __restrict__ src, const SplitOperand* __r
     const int64_t r = rt * kTM + m_core * 8 + r8;
     const int64_t k0 = kt * kTK + ks * 16 + k_core * 8;
     uint16_t sl[8][kS];
+    const double* blk = operand_block(scr, src, o.src_off);
     const int e = r < o.rows ? exps[o.exp_off + r] : 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      const double x = (r < o.rows && k0 + j < o.cols) ? src[o.src_off + r * o.cols + k0 + j] : 0.0;
+      const double x = (r < o.rows && k0 + j < o.cols) ? blk[r * o.cols + k0 + j] : 0.0;
       slice7(x, e, sl[j]);
     }
     // tile layout [ks][slice][m_core][k_core][8 rows x 16 B]: the 7 slices of a 16-wide k
@@ -173,8 +178,9 @@ __global__ void k_pack_a(const double* __restrict__ src, const SplitOperand* __r
 }
 
 // Pack B operand tiles (k x n row-major source, K-major tiles of 32 columns).
-__global__ void k_pack_b(const double* __restrict__ src, const SplitOperand* __restrict__ ops, int nops,
-                         const int32_t* __restrict__ exps, uint8_t* __restrict__ pack, int64_t total_chunks) {
+__global__ void k_pack_b(const double* __restrict__ scr, const double* __restrict__ src,
+                         const SplitOperand* __restrict__ ops, int nops, const int32_t* __restrict__ exps,
+                         uint8_t* __restrict__ pack, int64_t total_chunks) {
   for (int64_t ch = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ch < total_chunks;
        ch += (int64_t)gridDim.x * blockDim.x) {
     int lo = 0, hi = nops - 1;
@@ -189,10 +195,11 @@ __global__ void k_pack_b(const double* __restrict__ src, const SplitOperand* __r
     const int64_t c = ct * kTN + n_core * 8 + n8;        // output column (B column)
     const int64_t k0 = kt * kTK + ks * 16 + k_core * 8;  // B row
     uint16_t sl[8][kS];
+    const double* blk = operand_block(scr, src, o.src_off);
     const int e = c < o.cols ? exps[o.exp_off + c] : 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      const double x = (c < o.cols && k0 + j < o.rows) ? src[o.src_off + (k0 + j) * o.cols + c] : 0.0;
+      const double x = (c < o.cols && k0 + j < o.rows) ? blk[(k0 + j) * o.cols + c] : 0.0;
       slice7(x, e, sl[j]);
     }
     // tile layout [ks][slice][n_core][k_core][8 columns x 16 B]: the 7 slices of a 16-wide k
@@ -681,7 +688,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
     if (skinny_cblk(g, q)) continue;
     for (int32_t t = cb.t0; t < cb.t1; ++t) {
       const GemmTask& gt = g.task[t];
-      const int64_t ia = a_index(gt.a_off), ib = b_index(gt.b_off);
+      const int64_t ia = a_index(gt.a_off & ~kFromSrc), ib = b_index(gt.b_off & ~kFromSrc);
       const int k = gt.k;
       const int ktiles = (k + kTK - 1) / kTK;
       if (a_of[ia] < 0) {
@@ -796,23 +803,25 @@ int64_t SplitPlan::launches() const {
   return (a_static ? 0 : 2) + (b_static ? 0 : 4) + 1;   // per side: (memset,) exps, (finish,) pack; GEMM
 }
 
-// Scale exponents and slice tiles of one operand side (A: rows, B: columns).
-void pack_split_operand(SplitPlan& sp, bool side_a, const void* src, cudaStream_t s) {
-  const double* X = static_cast<const double*>(src);
+// Scale exponents and slice tiles of one operand side (A: rows, B: columns), reading each
+// operand block from the scratch or, flagged kFromSrc, from the source.
+void pack_split_operand(SplitPlan& sp, bool side_a, const void* scratch, const void* source, cudaStream_t s) {
+  const double* X = static_cast<const double*>(scratch);
+  const double* Xs = static_cast<const double*>(source);
   if (side_a) {
     if (sp.a_ops.empty()) return;
-    k_row_exp<<<grid_for(sp.n_a_vec * 32), 256, 0, s>>>(X, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+    k_row_exp<<<grid_for(sp.n_a_vec * 32), 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
                                                         sp.a_exps.as<int32_t>(), sp.n_a_vec);
-    k_pack_a<<<grid_for(sp.n_a_chunks), 256, 0, s>>>(X, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+    k_pack_a<<<grid_for(sp.n_a_chunks), 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
                                                      sp.a_exps.as<int32_t>(), sp.a_packed.as<uint8_t>(),
                                                      sp.n_a_chunks);
   } else {
     if (sp.b_ops.empty()) return;
     QLTG_CUDA(cudaMemsetAsync(sp.b_exps.get(), 0, sp.n_b_vec * sizeof(int32_t), s));
-    k_col_exp<<<grid_for(sp.n_b_items), 256, 0, s>>>(X, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
+    k_col_exp<<<grid_for(sp.n_b_items), 256, 0, s>>>(X, Xs, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
                                                      sp.b_exps.as<int32_t>(), sp.n_b_items);
     k_col_exp_finish<<<grid_for(sp.n_b_vec), 256, 0, s>>>(sp.b_exps.as<int32_t>(), sp.n_b_vec);
-    k_pack_b<<<grid_for(sp.n_b_chunks), 256, 0, s>>>(X, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
+    k_pack_b<<<grid_for(sp.n_b_chunks), 256, 0, s>>>(X, Xs, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
                                                      sp.b_exps.as<int32_t>(), sp.b_packed.as<uint8_t>(),
                                                      sp.n_b_chunks);
   }
@@ -824,21 +833,21 @@ void split_prepack_static(CtrctPlan& p, const void* a_static, const void* b_stat
   if (!p.split || !p.split->built) return;
   const int eb = (int)p.a.elem_bytes();
   if (a_static) {
-    const void* src = a_static;
-    if (p.a_trans && p.a.size) { p.a_tl.launch(a_static, p.a_t.get(), eb, s); src = p.a_t.get(); }
+    const void* scr = a_static;
+    if (p.a_tl.ntiles) { p.a_tl.launch(a_static, p.a_t.get(), eb, s); scr = p.a_t.get(); }
     p.split->a_static = true;
-    pack_split_operand(*p.split, true, src, s);
+    pack_split_operand(*p.split, true, scr, a_static, s);
   }
   if (b_static) {
-    const void* src = b_static;
-    if (p.b_trans && p.b.size) { p.b_tl.launch(b_static, p.b_t.get(), eb, s); src = p.b_t.get(); }
+    const void* scr = b_static;
+    if (p.b_tl.ntiles) { p.b_tl.launch(b_static, p.b_t.get(), eb, s); scr = p.b_t.get(); }
     p.split->b_static = true;
-    pack_split_operand(*p.split, false, src, s);
+    pack_split_operand(*p.split, false, scr, b_static, s);
   }
   QLTG_CUDA(cudaStreamSynchronize(s));
 }
 
-void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cudaStream_t s, bool pack) {
+void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s, bool pack) {
   QLTG_CHECK(p.a.dtype == QLTG_F64, QLTG_ERR_UNSUPPORTED, "split-precision mode supports FP64 tensors");
   if (!p.split) {
     // first split-mode execution of this plan: build the slice schedule (allocates; not
@@ -852,11 +861,11 @@ void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cuda
   SplitPlan& sp = *p.split;
   // skinny output blocks stay on the FP64 skinny kernel (k, n <= 8: the tensor cores would
   // pad them 8x); everything else goes through the slices
-  launch_gemm_f64_skinny(p.sched, a, b, c, false, p.ctx->num_sms, s);
+  launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, s);
   if (sp.tiles.empty()) return;
   if (pack) {
-    if (!(sp.a_static && sp.a_ready)) pack_split_operand(sp, true, a, s);
-    if (!(sp.b_static && sp.b_ready)) pack_split_operand(sp, false, b, s);
+    if (!(sp.a_static && sp.a_ready)) pack_split_operand(sp, true, op.a, op.a_src, s);
+    if (!(sp.b_static && sp.b_ready)) pack_split_operand(sp, false, op.b, op.b_src, s);
   } else {
     QLTG_CHECK(sp.a_ready && sp.b_ready, QLTG_ERR_INVALID, "GEMM-only stage before the operands were ever packed");
   }

@@ -6,7 +6,7 @@
 namespace qltg {
 
 // pack = false skips slicing the operands (they must have been packed by an earlier call).
-void launch_gemm_split(CtrctPlan& p, const void* a, const void* b, void* c, cudaStream_t s, bool pack = true);
+void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s, bool pack = true);
 // Build the slice schedule of a plan (allocates; call before any stream capture).
 void prepare_split(CtrctPlan& p, cudaStream_t s);
 // Pack an operand that stays constant for the plan's lifetime once, now (either may be NULL).

@@ -8,9 +8,14 @@
 // Per block, unit dims are squeezed and destination-adjacent dims that are also adjacent
 // in the source are merged. If the innermost destination dim is also innermost in the
 // source, the block is a set of contiguous runs copied with 16-byte vector accesses;
-// otherwise 32 x 32 tiles over (source-innermost dim p, destination-innermost dim q) are
-// staged through shared memory so both the read (along p) and the write (along q) are
-// coalesced. The sign multiply is exact (+-1).
+// otherwise tiles over (source-innermost dim p, destination-innermost dim q) are staged
+// through shared memory so both the read (along p) and the write (along q) are coalesced.
+// Tiles are 32 x 32, or Tp x Tq with Tp Tq <= 1024 when one of the two dims is short (an
+// inner dim of 4 elements gets 4 x 256 tiles, whose reads and writes are still long
+// contiguous runs). Only blocks whose two inner dims are both short fall back to a
+// destination-ordered gather. The +-1 block sign is applied by flipping the sign bit (no
+// floating-point multiply). Each CTA takes a contiguous range of work items, so it looks up
+// its first block once and then walks forward.
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -21,34 +26,38 @@ namespace qltg {
 namespace {
 
 constexpr int kTile = 32;
-constexpr int kRunChunk = 1024;   // elements per copy-mode work item
+constexpr int kTileElems = 1024;  // elements per tile (Tp * Tq)
+constexpr int kRunChunk = 1024;   // elements per copy-mode / gather-mode work item
+constexpr int kPermThreads = 256;
+
+__device__ __forceinline__ double flip(double x, uint64_t m) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)m);
+}
+__device__ __forceinline__ double2 flip(double2 x, uint64_t m) { return make_double2(flip(x.x, m), flip(x.y, m)); }
 
 template <typename T>
-__device__ __forceinline__ T mul_sign(T x, double s);
-template <>
-__device__ __forceinline__ double mul_sign<double>(double x, double s) { return x * s; }
-template <>
-__device__ __forceinline__ double2 mul_sign<double2>(double2 x, double s) { return make_double2(x.x * s, x.y * s); }
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_permute(const PermDesc* __restrict__ descs, int nd, int64_t ntiles,
-                                                 const T* __restrict__ src, T* __restrict__ dst) {
-  __shared__ T tile[kTile][kTile + 1];
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    // locate the block owning global tile t
-    int lo = 0, hi = nd - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (descs[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
-    }
+__global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __restrict__ descs, int nd, int64_t ntiles,
+                                                          const T* __restrict__ src, T* __restrict__ dst) {
+  // tile buffer: Tq rows of Tp + 1 (Tp a power of two, so the row stride is odd)
+  __shared__ T tile[kTileElems + kTileElems / 2];
+  const int64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+  const int64_t t_begin = (int64_t)blockIdx.x * per, t_end = min(ntiles, t_begin + per);
+  if (t_begin >= t_end) return;
+  // the block owning the first work item; later items walk forward from it
+  int lo = 0, hi = nd - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (descs[mid].tile_begin <= t_begin) lo = mid; else hi = mid - 1;
+  }
+  for (int64_t t = t_begin; t < t_end; ++t) {
+    while (lo + 1 < nd && descs[lo + 1].tile_begin <= t) ++lo;
     const PermDesc& d = descs[lo];
-    int64_t local = t - d.tile_begin;
+    const int64_t local = t - d.tile_begin;
     const int r = d.rank;
     const int q = r - 1;
-    const double sign = d.sign;
+    const uint64_t sg = d.sign_mask;
     if (r == 0) {   // single element
-      if (threadIdx.x == 0) dst[d.dst_off] = mul_sign(src[d.src_off], sign);
+      if (threadIdx.x == 0) dst[d.dst_off] = flip(src[d.src_off], sg);
       continue;
     }
     // destination strides
@@ -56,10 +65,10 @@ __global__ void __launch_bounds__(256) k_permute(const PermDesc* __restrict__ de
     dstride[r - 1] = 1;
     for (int i = r - 2; i >= 0; --i) dstride[i] = dstride[i + 1] * d.dims[i + 1];
     if (d.p < 0) {
-      // gather mode (small inner dims): 1024 consecutive destination elements per work item,
-      // each thread decodes its source offset; writes coalesced, reads in short runs
-      // block sizes are below 2^31 (checked on the host): 32-bit index arithmetic
-      const uint32_t total = (uint32_t)d.nouter;   // block size for this mode
+      // gather mode (both inner dims short): 1024 consecutive destination elements per work
+      // item, each thread decodes its source offset; block sizes are below 2^31 (checked on
+      // the host), so the index arithmetic is 32-bit
+      const uint32_t total = (uint32_t)d.nouter;
       const uint32_t e0 = (uint32_t)local * kRunChunk;
       const uint32_t e1 = min(e0 + (uint32_t)kRunChunk, total);
       for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
@@ -67,11 +76,11 @@ __global__ void __launch_bounds__(256) k_permute(const PermDesc* __restrict__ de
         int64_t soff = 0;
         for (int i = r - 1; i >= 0; --i) {
           const uint32_t di = (uint32_t)d.dims[i];
-          const uint32_t q = rem / di;
-          soff += (int64_t)(rem - q * di) * d.sstride[i];
-          rem = q;
+          const uint32_t qq = rem / di;
+          soff += (int64_t)(rem - qq * di) * d.sstride[i];
+          rem = qq;
         }
-        dst[d.dst_off + e] = mul_sign(src[d.src_off + soff], sign);
+        dst[d.dst_off + e] = flip(src[d.src_off + soff], sg);
       }
       continue;
     }
@@ -97,23 +106,20 @@ __global__ void __launch_bounds__(256) k_permute(const PermDesc* __restrict__ de
         const int64_t n2 = n >> 1;
         const double2* s2 = reinterpret_cast<const double2*>(s + c0);
         double2* o2 = reinterpret_cast<double2*>(o + c0);
-        for (int64_t e = threadIdx.x; e < n2; e += blockDim.x) {
-          double2 v = __ldg(s2 + e);
-          v.x *= sign; v.y *= sign;
-          o2[e] = v;
-        }
-        if ((n & 1) && threadIdx.x == 0) o[c0 + n - 1] = mul_sign(s[c0 + n - 1], sign);
+        for (int64_t e = threadIdx.x; e < n2; e += blockDim.x) o2[e] = flip(__ldg(s2 + e), sg);
+        if ((n & 1) && threadIdx.x == 0) o[c0 + n - 1] = flip(s[c0 + n - 1], sg);
       } else {
-        for (int64_t e = threadIdx.x; e < n; e += blockDim.x) o[c0 + e] = mul_sign(s[c0 + e], sign);
+        for (int64_t e = threadIdx.x; e < n; e += blockDim.x) o[c0 + e] = flip(s[c0 + e], sg);
       }
       continue;
     }
-    // tile mode over (p, q)
+    // tile mode over (p, q) with Tp x Tq tiles
+    const int tp = d.tp, tq = d.tq;
     const uint32_t per_outer = (uint32_t)d.tiles_p * (uint32_t)d.tiles_q;
     const uint32_t outer = (uint32_t)local / per_outer;
     const uint32_t tt = (uint32_t)local - outer * per_outer;
-    const uint32_t tq = tt / (uint32_t)d.tiles_q;
-    const int64_t p0 = (int64_t)tq * kTile, q0 = (int64_t)(tt - tq * (uint32_t)d.tiles_q) * kTile;
+    const uint32_t tpi = tt / (uint32_t)d.tiles_q;
+    const int64_t p0 = (int64_t)tpi * tp, q0 = (int64_t)(tt - tpi * (uint32_t)d.tiles_q) * tq;
     uint32_t rem = outer;
     int64_t soff = 0, doff = 0;
     for (int i = r - 1; i >= 0; --i) {
@@ -128,33 +134,43 @@ __global__ void __launch_bounds__(256) k_permute(const PermDesc* __restrict__ de
     const T* s = src + d.src_off + soff;
     T* o = dst + d.dst_off + doff;
     const int64_t np_ = d.dims[d.p], nq = d.dims[q];
-    // read: threads along p (stride 1 in the source)
-    for (int j = ty; j < kTile; j += 8) {
-      const int64_t pi = p0 + tx, qi = q0 + j;
-      if (pi < np_ && qi < nq) tile[j][tx] = __ldg(s + pi + qi * d.sstride[q]);
+    const int64_t sq = d.sstride[q], dp = dstride[d.p];
+    const int lp = __ffs(tp) - 1, lq = __ffs(tq) - 1;   // tile extents are powers of two
+    const int n = tp * tq, row = tp + 1;
+    // read: p fastest (stride 1 in the source)
+    for (int e = threadIdx.x; e < n; e += kPermThreads) {
+      const int pi = e & (tp - 1), qi = e >> lp;
+      if (p0 + pi < np_ && q0 + qi < nq) tile[qi * row + pi] = __ldg(s + (p0 + pi) + (q0 + qi) * sq);
     }
     __syncthreads();
-    // write: threads along q (stride 1 in the destination)
-    for (int j = ty; j < kTile; j += 8) {
-      const int64_t qi = q0 + tx, pi = p0 + j;
-      if (pi < np_ && qi < nq) o[qi + pi * dstride[d.p]] = mul_sign(tile[tx][j], sign);
+    // write: q fastest (stride 1 in the destination)
+    for (int e = threadIdx.x; e < n; e += kPermThreads) {
+      const int qi = e & (tq - 1), pi = e >> lq;
+      if (p0 + pi < np_ && q0 + qi < nq) o[(q0 + qi) + (p0 + pi) * dp] = flip(tile[qi * row + pi], sg);
     }
     __syncthreads();
   }
 }
 
+int pow2_at_least(int64_t x) {
+  int v = 1;
+  while (v < x && v < kTileElems) v <<= 1;
+  return v;
+}
+
 }  // namespace
 
 void TransposeList::describe(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
-                             const std::vector<int64_t>* dst_offsets) {
+                             const std::vector<int64_t>* dst_offsets, bool skip_identity) {
   host.clear();
+  identity.assign(t.nblk, 0);
   ntiles = 0;
   const int r = t.rank;
   for (int64_t b = 0; b < t.nblk; ++b) {
     PermDesc d{};
     d.src_off = t.offsets[b];
     d.dst_off = dst_offsets ? (*dst_offsets)[b] : t.offsets[b];
-    d.sign = signs.empty() ? 1.0 : signs[b];
+    d.sign_mask = (!signs.empty() && signs[b] < 0) ? 0x8000000000000000ull : 0ull;
     int64_t sstr[kMaxRank];
     sstr[r - 1] = 1;
     for (int i = r - 2; i >= 0; --i) sstr[i] = sstr[i + 1] * t.dim(b, i + 1);
@@ -189,23 +205,45 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
       if (ds[i] == 1) d.p = i;
     }
     QLTG_CHECK(t.blk_size(b) < ((int64_t)1 << 31), QLTG_ERR_UNSUPPORTED, "block with 2^31 or more elements");
+    // at most one non-unit dim left after merging: the block's data is laid out the same way
+    identity[b] = m <= 1 && d.sign_mask == 0 && d.src_off == d.dst_off;
     int64_t tiles;
-    if (m == 0) {
+    if (identity[b] && skip_identity) {
+      tiles = 0;
+    } else if (m == 0) {
       d.p = 0;
       tiles = 1;
     } else if (d.p == m - 1) {
       const int64_t runs = t.blk_size(b) / dd[m - 1];
       tiles = runs * ((dd[m - 1] + kRunChunk - 1) / kRunChunk);
-    } else if (d.p < 0 || dd[d.p] < 16 || dd[m - 1] < 16) {
-      // inner dims too short for 32 x 32 tiles: destination-ordered gather
-      d.p = -1;
-      d.nouter = t.blk_size(b);
-      tiles = (d.nouter + kRunChunk - 1) / kRunChunk;
     } else {
-      d.tiles_p = (int32_t)((dd[d.p] + kTile - 1) / kTile);
-      d.tiles_q = (int32_t)((dd[m - 1] + kTile - 1) / kTile);
-      d.nouter = t.blk_size(b) / (dd[d.p] * dd[m - 1]);
-      tiles = d.nouter * d.tiles_p * d.tiles_q;
+      // tile extents: 32 x 32, or stretched along the longer dim when the other is short
+      int tp = -1, tq = -1;
+      if (d.p >= 0) {
+        const int a = pow2_at_least(dd[d.p]), c = pow2_at_least(dd[m - 1]);
+        if (a >= kTile && c >= kTile) {
+          tp = tq = kTile;
+        } else if (a < kTile) {
+          tp = a;
+          tq = std::min(c, kTileElems / a);
+        } else {
+          tq = c;
+          tp = std::min(a, kTileElems / c);
+        }
+      }
+      if (tp < 0 || tp * tq < 64) {
+        // both inner dims short: destination-ordered gather
+        d.p = -1;
+        d.nouter = t.blk_size(b);
+        tiles = (d.nouter + kRunChunk - 1) / kRunChunk;
+      } else {
+        d.tp = tp;
+        d.tq = tq;
+        d.tiles_p = (int32_t)((dd[d.p] + tp - 1) / tp);
+        d.tiles_q = (int32_t)((dd[m - 1] + tq - 1) / tq);
+        d.nouter = t.blk_size(b) / (dd[d.p] * dd[m - 1]);
+        tiles = d.nouter * d.tiles_p * d.tiles_q;
+      }
     }
     d.tile_begin = ntiles;
     ntiles += tiles;
@@ -215,8 +253,8 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
 }
 
 void TransposeList::build(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
-                          const std::vector<int64_t>* dst_offsets, cudaStream_t s) {
-  describe(t, order, signs, dst_offsets);
+                          const std::vector<int64_t>* dst_offsets, cudaStream_t s, bool skip_identity) {
+  describe(t, order, signs, dst_offsets, skip_identity);
   dev = upload(host, s);
 }
 
@@ -224,10 +262,10 @@ void TransposeList::launch(const void* src, void* dst, int elem_bytes, cudaStrea
   if (ntiles == 0) return;
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, 152 * 8);
   if (elem_bytes == 8)
-    k_permute<double><<<grid, 256, 0, s>>>(dev.as<PermDesc>(), (int)nblocks, ntiles, static_cast<const double*>(src),
+    k_permute<double><<<grid, kPermThreads, 0, s>>>(dev.as<PermDesc>(), (int)nblocks, ntiles, static_cast<const double*>(src),
                                            static_cast<double*>(dst));
   else
-    k_permute<double2><<<grid, 256, 0, s>>>(dev.as<PermDesc>(), (int)nblocks, ntiles,
+    k_permute<double2><<<grid, kPermThreads, 0, s>>>(dev.as<PermDesc>(), (int)nblocks, ntiles,
                                             static_cast<const double2*>(src), static_cast<double2*>(dst));
   QLTG_CUDA(cudaGetLastError());
 }
@@ -274,10 +312,10 @@ void launch_permute_noalloc(int device, const TransposeList& tl, const void* src
   QLTG_CUDA(cudaMemcpyAsync(table, tl.host.data(), tl.host.size() * sizeof(PermDesc), cudaMemcpyHostToDevice, s));
   const unsigned grid = (unsigned)std::min<int64_t>(tl.ntiles, 152 * 8);
   if (elem_bytes == 8)
-    k_permute<double><<<grid, 256, 0, s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double*>(src),
+    k_permute<double><<<grid, kPermThreads, 0, s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double*>(src),
                                            static_cast<double*>(dst));
   else
-    k_permute<double2><<<grid, 256, 0, s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double2*>(src),
+    k_permute<double2><<<grid, kPermThreads, 0, s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double2*>(src),
                                             static_cast<double2*>(dst));
   QLTG_CUDA(cudaGetLastError());
   // the descriptors were copied from this call's host memory and the table is shared:
