@@ -107,8 +107,8 @@ class ClockSampler:
 # `python bench.py --profile --mode <mode>` (summaries: profiles/k_gemm_split_d4000.txt,
 # profiles/k_gemm_dfma_d4000.txt). Keyed by matvec step.
 NCU_TRAFFIC = {
-    "split": {0: 137.0e6, 3: 314.5e6},
-    "fp64": {0: 84.6e6},
+    "split": {0: 133.3e6, 3: 312.0e6},
+    "fp64": {0: 84.6e6, 3: 167.7e6},
 }
 
 
