@@ -127,8 +127,9 @@ def _time_events(fn, stream, flush, reps=5):
 
 
 def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk):
-    """Per matvec step: the GEMM stage (incl. operand slicing) and the GEMM kernels alone,
-    each timed with CUDA events on the launching stream with L2 flushed before every launch;
+    """Per matvec step: the operand transposes, the GEMM stage (incl. operand slicing) and the
+    GEMM kernels alone, each timed with CUDA events on the launching stream with L2 flushed
+    before every launch;
     the roofline entry is the largest single launch of the dominant kernel."""
     import ctypes as C
     import torch
@@ -147,7 +148,7 @@ def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
         c = DTensor.empty(p.result, local)
         p.execute(cur_a, bs[i], c, mode=mode)
         args = (p.h, C.c_void_p(cur_a.ptr), C.c_void_p(bs[i].ptr), C.c_void_p(c.ptr), mode_i)
-        capi.check(lib.qltg_ctrct_exec_stage(*args, 1, sp))
+        ms1 = _time_events(lambda: capi.check(lib.qltg_ctrct_exec_stage(*args, 1, sp)), stream, flush)
         ms2 = _time_events(lambda: capi.check(lib.qltg_ctrct_exec_stage(*args, 2, sp)), stream, flush)
         ms3 = _time_events(lambda: capi.check(lib.qltg_ctrct_exec_stage(*args, 3, sp)), stream, flush)
         p.device_status()
@@ -164,7 +165,8 @@ def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
                 stages = sum(-(-k // 32) for k in ks)
                 # 28 slice pairs on 128 x 32 x 32 padded tiles per 32-wide k stage
                 tcf += tiles * stages * 28 * (2 * 128 * 32 * 32)
-        per.append({"stage_ms": round(ms2, 4), "kernel_ms": round(ms3, 4), "gflop": round(f / 1e9, 4),
+        per.append({"transpose_ms": round(ms1, 4), "stage_ms": round(ms2, 4), "kernel_ms": round(ms3, 4),
+                    "gflop": round(f / 1e9, 4),
                     "tensor_gflop": round(tcf / 1e9, 2)})
         stage_ms += ms2
         kern_ms += ms3

@@ -18,6 +18,7 @@ struct PermDesc {
   int32_t p;                   // destination dim that is innermost in the source (-1: gather mode)
   int32_t tp, tq;              // tile extents along p and along the innermost dst dim
   int32_t tiles_p, tiles_q;    // tiles along p and along the innermost dst dim
+  int32_t u, tu, tiles_u;      // batched outer dim (-1: none), its tile extent and tile count
   int64_t nouter;              // product of the remaining dims (gather mode: block size)
   int64_t tile_begin;          // first global work item of this block
   uint64_t sign_mask;          // 0, or the sign bit: the block's +-1 sign applied by XOR
@@ -32,10 +33,12 @@ struct TransposeList {
   // skip_identity: blocks whose layout the permutation leaves unchanged get no work (the
   // caller reads them from the source)
   void build(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
-             const std::vector<int64_t>* dst_offsets, cudaStream_t s, bool skip_identity = false);
+             const std::vector<int64_t>* dst_offsets, cudaStream_t s, bool skip_identity = false,
+             const std::vector<uint8_t>* skip = nullptr);
   // host-side descriptors only (fills host / ntiles / nblocks, no device memory)
   void describe(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
-                const std::vector<int64_t>* dst_offsets, bool skip_identity = false);
+                const std::vector<int64_t>* dst_offsets, bool skip_identity = false,
+                const std::vector<uint8_t>* skip = nullptr);
   void launch(const void* src, void* dst, int elem_bytes, cudaStream_t s) const;
 };
 
@@ -49,6 +52,7 @@ struct GemmTask {
   int64_t a_off, b_off;        // offsets of the (transposed) operand blocks, | kFromSrc
   int32_t k;
   int32_t sign;                // fermion exchange sign
+  int32_t a_rs, a_cs;          // skinny tasks: A element (row, kk) at row a_rs + kk a_cs
 };
 // Operand offset flag: the block is read from the untransposed operand, whose layout for
 // this block already matches the transposed one (same offset in both buffers).

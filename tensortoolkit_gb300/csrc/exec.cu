@@ -33,28 +33,81 @@ void finalize_plan(CtrctPlan& p, cudaStream_t s) {
   std::stable_sort(cands.begin(), cands.end(), [](const Cand& x, const Cand& y) { return x.cost > y.cost; });
   g.tile.reserve(cands.size());
   for (auto& c : cands) g.tile.push_back(c.t);
-  // operand transposes: blocks whose layout the permutation leaves unchanged are read from
-  // the operand itself (flagged in the task offsets) and get no transpose work
+  // Operand transposes. A task reads its operand block from the transposed scratch unless
+  // (a) the permutation leaves the block's layout unchanged, or (b) it is a skinny task and
+  // the block, read in place, is a strided matrix (rows and columns each one stride); such
+  // tasks read the operand itself (offset flag kFromSrc) and blocks nobody reads from the
+  // scratch get no transpose work.
   const size_t eb = p.a.elem_bytes();
   const bool any_work = !g.tile.empty() || !g.skinny.empty();
-  auto flag_identity = [&](const Meta& m, const TransposeList& tl, bool side_a) {
-    for (auto& tk : g.task) {
-      int64_t& off = side_a ? tk.a_off : tk.b_off;
-      const int64_t b = std::lower_bound(m.offsets.begin(), m.offsets.end(), off) - m.offsets.begin();
-      QLTG_CHECK(b < m.nblk && m.offsets[b] == off, QLTG_ERR_INVALID, "internal: task operand offset is no block start");
-      if (tl.identity[b]) off |= kFromSrc;
-    }
+  std::vector<uint8_t> skinny_task(g.task.size(), 0);
+  for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q)
+    if (skinny_cblk(g, q))
+      for (int32_t t = g.cblk[q].t0; t < g.cblk[q].t1; ++t) skinny_task[t] = 1;
+  auto block_of = [](const Meta& m, int64_t off) {
+    const int64_t b = std::lower_bound(m.offsets.begin(), m.offsets.end(), off) - m.offsets.begin();
+    QLTG_CHECK(b < m.nblk && m.offsets[b] == off, QLTG_ERR_INVALID, "internal: task operand offset is no block start");
+    return b;
+  };
+  // (row stride, column stride) of block b of A read in place, rows = saved legs, columns =
+  // contracted legs in the transposed order; false if either needs more than one stride
+  auto strided_a = [&](int64_t b, int32_t& rs, int32_t& cs) {
+    const int r = p.a.rank, ns = (int)p.sa.size();
+    std::vector<int64_t> sstr(r);
+    if (r) sstr[r - 1] = 1;
+    for (int i = r - 2; i >= 0; --i) sstr[i] = sstr[i + 1] * p.a.dim(b, i + 1);
+    auto merge = [&](int lo, int hi, int32_t& stride) {
+      int64_t run_dim = 0, run_stride = 1;
+      int n = 0;
+      for (int i = lo; i < hi; ++i) {
+        const int leg = p.a_order[i];
+        const int64_t d = p.a.dim(b, leg);
+        if (d == 1) continue;
+        if (n && run_stride == sstr[leg] * d) {
+          run_dim *= d;
+          run_stride = sstr[leg];
+        } else {
+          if (n) return false;
+          run_dim = d;
+          run_stride = sstr[leg];
+          n = 1;
+        }
+      }
+      if (run_stride >= ((int64_t)1 << 31)) return false;
+      stride = (int32_t)(n ? run_stride : 0);
+      return true;
+    };
+    return merge(0, ns, rs) && merge(ns, r, cs);
   };
   p.a_tl = TransposeList();
   p.b_tl = TransposeList();
   if (p.a_trans && p.a.size && any_work) {
-    p.a_tl.build(p.a, p.a_order, {}, nullptr, s, /*skip_identity=*/true);
-    flag_identity(p.a, p.a_tl, true);
+    TransposeList probe;
+    probe.describe(p.a, p.a_order, {}, nullptr);
+    std::vector<uint8_t> need(p.a.nblk, 0);
+    for (size_t t = 0; t < g.task.size(); ++t) {
+      GemmTask& tk = g.task[t];
+      const int64_t b = block_of(p.a, tk.a_off);
+      int32_t rs = 0, cs = 0;
+      if (probe.identity[b]) {
+        tk.a_off |= kFromSrc;
+      } else if (skinny_task[t] && strided_a(b, rs, cs)) {
+        tk.a_off |= kFromSrc;
+        tk.a_rs = rs;
+        tk.a_cs = cs;
+      } else {
+        need[b] = 1;
+      }
+    }
+    std::vector<uint8_t> skip(p.a.nblk);
+    for (int64_t b = 0; b < p.a.nblk; ++b) skip[b] = !need[b];
+    p.a_tl.build(p.a, p.a_order, {}, nullptr, s, false, &skip);
     if (p.a_tl.ntiles) p.a_t.alloc(p.a.size * eb);
   }
   if (p.b_trans && p.b.size && any_work) {
     p.b_tl.build(p.b, p.b_order, {}, nullptr, s, /*skip_identity=*/true);
-    flag_identity(p.b, p.b_tl, false);
+    for (auto& tk : g.task)
+      if (p.b_tl.identity[block_of(p.b, tk.b_off)]) tk.b_off |= kFromSrc;
     if (p.b_tl.ntiles) p.b_t.alloc(p.b.size * eb);
   }
   g.d_cblk = upload(g.cblk, s);

@@ -137,11 +137,11 @@ __device__ __forceinline__ void skinny_row(const GemmCBlk& cb, const GemmTask* _
   for (int t = cb.t0; t < cb.t1; ++t) {
     const GemmTask tk = task[t];
     const int k = tk.k;
-    const T* a = operand_block(A, As, tk.a_off) + (int64_t)row * k;
+    const T* a = operand_block(A, As, tk.a_off) + (int64_t)row * tk.a_rs;
     const T* b = operand_block(B, Bs, tk.b_off);
     const unsigned long long sg = sign_mask(tk.sign);
     for (int kk = 0; kk < k; ++kk) {
-      const T av = flip(__ldg(a + kk), sg);
+      const T av = flip(__ldg(a + (int64_t)kk * tk.a_cs), sg);
 #pragma unroll
       for (int j = 0; j < NN; ++j) fma_acc(acc[j], av, __ldg(b + kk * NN + j));
     }
@@ -175,6 +175,7 @@ __global__ void __launch_bounds__(kSkinnyRows) k_gemm_skinny(const GemmCBlk* __r
     }
   }
 }
+
 
 }  // namespace
 

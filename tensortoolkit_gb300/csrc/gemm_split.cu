@@ -37,6 +37,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "scaled_int.h"
 #include "split.h"
 
 namespace qltg {
@@ -50,6 +51,27 @@ constexpr int kBTile = kTN * kTK * 2;      // 4 KB
 constexpr int kDrainK = 128;               // k between drains (exactness bound)
 
 // ------------------------------------------------------------------ slicing
+// Work distribution of the slicing kernels: CTA b takes the contiguous item range
+// [b per, (b + 1) per); a thread finds the operand owning its first item once and walks
+// forward from there (items only grow).
+struct ItemRange {
+  int64_t begin, end;
+};
+__device__ __forceinline__ ItemRange cta_range(int64_t total) {
+  const int64_t per = (total + gridDim.x - 1) / gridDim.x;
+  const int64_t b = (int64_t)blockIdx.x * per;
+  return ItemRange{b, min(total, b + per)};
+}
+template <typename F>
+__device__ __forceinline__ int first_op(int nops, int64_t item, F begin_of) {
+  int lo = 0, hi = nops - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (begin_of(mid) <= item) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 // Row / column scale exponents: e with max |x| < 2^e (0 for an all-zero row).
 __device__ __forceinline__ int exp_of_bits(uint64_t absbits) {
   if (absbits == 0) return 0;
@@ -61,17 +83,19 @@ __device__ __forceinline__ int exp_of_bits(uint64_t absbits) {
 __global__ void k_row_exp(const double* __restrict__ scr, const double* __restrict__ src,
                           const SplitOperand* __restrict__ ops, int nops, int32_t* __restrict__ exps,
                           int64_t total_rows) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t rg = warp; rg < total_rows; rg += nw) {
-    int lo = 0, hi = nops - 1;
-    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].vec_begin <= rg) lo = mid; else hi = mid - 1; }
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
+  const ItemRange rr = cta_range(total_rows);
+  auto vb = [&](int i) { return ops[i].vec_begin; };
+  int lo = first_op(nops, rr.begin + wib, vb);
+  for (int64_t rg = rr.begin + wib; rg < rr.end; rg += nwb) {
+    while (lo + 1 < nops && ops[lo + 1].vec_begin <= rg) ++lo;
     const SplitOperand o = ops[lo];
     const int64_t r = rg - o.vec_begin;
     const double* row = operand_block(scr, src, o.src_off) + r * o.cols;
     uint64_t mx = 0;
+#pragma unroll 4
     for (int c = lane; c < o.cols; c += 32) {
-      const uint64_t b = (uint64_t)__double_as_longlong(row[c]) & 0x7FFFFFFFFFFFFFFFull;
+      const uint64_t b = (uint64_t)__double_as_longlong(__ldg(row + c)) & 0x7FFFFFFFFFFFFFFFull;
       mx = b > mx ? b : mx;
     }
     for (int sft = 16; sft > 0; sft >>= 1) {
@@ -89,10 +113,11 @@ __global__ void k_row_exp(const double* __restrict__ scr, const double* __restri
 __global__ void k_col_exp(const double* __restrict__ scr, const double* __restrict__ src,
                           const SplitOperand* __restrict__ ops, int nops, int32_t* __restrict__ exps,
                           int64_t total_items) {
-  for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < total_items;
-       it += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = nops - 1;
-    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].item_begin <= it) lo = mid; else hi = mid - 1; }
+  const ItemRange rr = cta_range(total_items);
+  auto ib = [&](int i) { return ops[i].item_begin; };
+  int lo = first_op(nops, rr.begin + threadIdx.x, ib);
+  for (int64_t it = rr.begin + threadIdx.x; it < rr.end; it += blockDim.x) {
+    while (lo + 1 < nops && ops[lo + 1].item_begin <= it) ++lo;
     const SplitOperand o = ops[lo];
     const int64_t l = it - o.item_begin;
     const int64_t c = l % o.cols, r0 = (l / o.cols) * 32;
@@ -130,8 +155,9 @@ __device__ __forceinline__ void slice7(double x, int e, uint16_t* out) {
 #pragma unroll
   for (int p = 0; p < kS; ++p) {
     const uint32_t d = (uint32_t)((Y >> (7 * (kS - 1 - p))) & 127u);
-    // bf16 of d 2^(-7(p+1)) (exact): the float's bits >> 16, exponent field lowered by 7(p+1)
-    const uint32_t f = __float_as_uint((float)d) >> 16;
+    // bf16 of d 2^(-7(p+1)) (exact): float(d) by the magic-number subtraction (FMA pipe,
+    // not the conversion unit), its bits >> 16, exponent field lowered by 7(p+1)
+    const uint32_t f = __float_as_uint(__uint_as_float(0x4B000000u | d) - 8388608.0f) >> 16;
     out[p] = d ? (uint16_t)((f - ((uint32_t)(7 * (p + 1)) << 7)) | sgn) : (uint16_t)0;
   }
 }
@@ -141,10 +167,11 @@ __device__ __forceinline__ void slice7(double x, int e, uint16_t* out) {
 __global__ void k_pack_a(const double* __restrict__ scr, const double* __restrict__ src,
                          const SplitOperand* __restrict__ ops, int nops, const int32_t* __restrict__ exps,
                          uint8_t* __restrict__ pack, int64_t total_chunks) {
-  for (int64_t ch = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ch < total_chunks;
-       ch += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = nops - 1;
-    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].chunk_begin <= ch) lo = mid; else hi = mid - 1; }
+  const ItemRange rr = cta_range(total_chunks);
+  auto cbg = [&](int i) { return ops[i].chunk_begin; };
+  int lo = first_op(nops, rr.begin + threadIdx.x, cbg);
+  for (int64_t ch = rr.begin + threadIdx.x; ch < rr.end; ch += blockDim.x) {
+    while (lo + 1 < nops && ops[lo + 1].chunk_begin <= ch) ++lo;
     const SplitOperand o = ops[lo];
     const int64_t l = ch - o.chunk_begin;
     // chunk order inside a (rt, kt) tile: ks (4), m_core (16), k_core (2), r8 (8) = 1024 chunks
@@ -154,9 +181,10 @@ __global__ void k_pack_a(const double* __restrict__ scr, const double* __restric
     const int64_t rt = tile / o.ktiles, kt = tile % o.ktiles;
     const int64_t r = rt * kTM + m_core * 8 + r8;
     const int64_t k0 = kt * kTK + ks * 16 + k_core * 8;
+    if (r >= o.rows || k0 >= o.cols) continue;   // padding: the buffer was zeroed once
     uint16_t sl[8][kS];
     const double* blk = operand_block(scr, src, o.src_off);
-    const int e = r < o.rows ? exps[o.exp_off + r] : 0;
+    const int e = exps[o.exp_off + r];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const double x = (r < o.rows && k0 + j < o.cols) ? blk[r * o.cols + k0 + j] : 0.0;
@@ -181,10 +209,11 @@ __global__ void k_pack_a(const double* __restrict__ scr, const double* __restric
 __global__ void k_pack_b(const double* __restrict__ scr, const double* __restrict__ src,
                          const SplitOperand* __restrict__ ops, int nops, const int32_t* __restrict__ exps,
                          uint8_t* __restrict__ pack, int64_t total_chunks) {
-  for (int64_t ch = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ch < total_chunks;
-       ch += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = nops - 1;
-    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (ops[mid].chunk_begin <= ch) lo = mid; else hi = mid - 1; }
+  const ItemRange rr = cta_range(total_chunks);
+  auto cbg = [&](int i) { return ops[i].chunk_begin; };
+  int lo = first_op(nops, rr.begin + threadIdx.x, cbg);
+  for (int64_t ch = rr.begin + threadIdx.x; ch < rr.end; ch += blockDim.x) {
+    while (lo + 1 < nops && ops[lo + 1].chunk_begin <= ch) ++lo;
     const SplitOperand o = ops[lo];
     const int64_t l = ch - o.chunk_begin;
     // chunk order inside a (ct, kt) tile: ks (4), n_core (4), k_core (2), n8 (8) = 256 chunks
@@ -194,9 +223,10 @@ __global__ void k_pack_b(const double* __restrict__ scr, const double* __restric
     const int64_t ct = tile / o.ktiles, kt = tile % o.ktiles;
     const int64_t c = ct * kTN + n_core * 8 + n8;        // output column (B column)
     const int64_t k0 = kt * kTK + ks * 16 + k_core * 8;  // B row
+    if (c >= o.cols || k0 >= o.rows) continue;   // padding: the buffer was zeroed once
     uint16_t sl[8][kS];
     const double* blk = operand_block(scr, src, o.src_off);
-    const int e = c < o.cols ? exps[o.exp_off + c] : 0;
+    const int e = exps[o.exp_off + c];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const double x = (c < o.cols && k0 + j < o.rows) ? blk[(k0 + j) * o.cols + c] : 0.0;
@@ -343,50 +373,6 @@ __device__ __forceinline__ bool wait_warp(uint32_t mbar, uint32_t phase, volatil
 __device__ __forceinline__ bool wait_warp_own(uint32_t mbar, uint32_t phase) {
   const int never = 0;
   return __all_sync(0xffffffffu, mbar_wait_or_abort(mbar, phase, &never));
-}
-
-// z 2^e (negated when neg) rounded to the nearest double (ties to even), with integer
-// operations only: the FP64 pipe of this GPU is slow, and no path here touches it.
-__host__ __device__ __forceinline__ double scaled_i64(long long z, int e, bool neg) {
-  if (z == 0) return 0.0;
-  const unsigned long long a = z < 0 ? 0ull - (unsigned long long)z : (unsigned long long)z;
-  const unsigned long long sgn = ((z < 0) != neg) ? 0x8000000000000000ull : 0ull;
-#ifdef __CUDA_ARCH__
-  const int lz = __clzll((long long)a);
-#else
-  const int lz = __builtin_clzll(a);
-#endif
-  const int be = 1023 + 63 - lz + e;                    // biased exponent of the leading bit
-  unsigned long long bits;
-  if (be >= 1) {
-    const unsigned long long m = a << lz;               // leading one at bit 63
-    unsigned long long mant = m >> 11;                  // 53 bits, leading one at bit 52
-    const unsigned long long rem = m & 0x7FFull;
-    mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
-    // (be - 1) << 52 plus the mantissa with its leading one adds the exponent; a rounding
-    // carry to 2^53 moves into the exponent by itself, and past 2046 it reaches infinity
-    bits = be < 2047 ? ((unsigned long long)(be - 1) << 52) + mant : 0x7FF0000000000000ull;
-    if (bits > 0x7FF0000000000000ull) bits = 0x7FF0000000000000ull;
-  } else {
-    // subnormal result: a 2^(e + 1074) in units of 2^-1074, rounded to nearest-even
-    const int sh = -(e + 1074);                         // > 0 here unless a is large
-    if (sh <= 0) {
-      bits = a << (-sh);                                // cannot overflow: be < 1
-    } else if (sh >= 64) {
-      bits = (sh == 64 && a > 0x8000000000000000ull) ? 1ull : 0ull;
-    } else {
-      const unsigned long long q = a >> sh, r = a - (q << sh), half = 1ull << (sh - 1);
-      bits = q + ((r > half || (r == half && (q & 1ull))) ? 1ull : 0ull);
-    }
-  }
-#ifdef __CUDA_ARCH__
-  return __longlong_as_double((long long)(sgn | bits));
-#else
-  double r;
-  const unsigned long long rb = sgn | bits;
-  memcpy(&r, &rb, sizeof r);
-  return r;
-#endif
 }
 
 // Fold one drained accumulator set into the int64 sums z (units 2^-49) of this thread's
@@ -788,6 +774,10 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   d_work_off = upload(work_off, s);
   a_packed.alloc(std::max<int64_t>(a_pack, 16));
   b_packed.alloc(std::max<int64_t>(b_pack, 16));
+  // tile padding (rows or columns past the block, k past the task) stays zero: the pack
+  // kernels only write the chunks that hold operand data
+  QLTG_CUDA(cudaMemsetAsync(a_packed.get(), 0, std::max<int64_t>(a_pack, 16), s));
+  QLTG_CUDA(cudaMemsetAsync(b_packed.get(), 0, std::max<int64_t>(b_pack, 16), s));
   a_exps.alloc(std::max<int64_t>(a_exp, 1) * 4);
   b_exps.alloc(std::max<int64_t>(b_exp, 1) * 4);
   error.alloc(sizeof(int));

@@ -218,6 +218,47 @@ void plan_contraction(CtrctPlan& p, cudaStream_t s) {
   const int rc = (int)(p.sa.size() + p.sb.size());
   QLTG_CHECK(rc <= kMaxRank, QLTG_ERR_UNSUPPORTED, "result rank above 8");
 
+  // The order of the contracted pairs (a_i, b_i) is internal to the contraction: any
+  // consistent reordering of the pairs gives the same C (the k index of every block pair
+  // is only permuted, in A and B alike). For bosonic tensors pick, among the given order and
+  // the orders sorted by A's or by B's leg numbers, the one whose operand transposes move
+  // the fewest bytes (blocks whose layout a transpose leaves unchanged move none). For
+  // fermionic tensors the exchange sign depends on the order, so the given order stays.
+  if (A.parity_comp < 0 && nax >= 2) {
+    auto order_of = [&](const std::vector<int64_t>& axa, const std::vector<int64_t>& axb, std::vector<int>& oa,
+                        std::vector<int>& ob) {
+      oa.assign(p.sa.begin(), p.sa.end());
+      oa.insert(oa.end(), axa.begin(), axa.end());
+      ob.assign(axb.begin(), axb.end());
+      ob.insert(ob.end(), p.sb.begin(), p.sb.end());
+    };
+    auto moved_bytes = [&](const std::vector<int64_t>& axa, const std::vector<int64_t>& axb) {
+      std::vector<int> oa, ob;
+      order_of(axa, axb, oa, ob);
+      int64_t bytes = 0;
+      TransposeList ta, tb;
+      ta.describe(A, oa, {}, nullptr);
+      tb.describe(B, ob, {}, nullptr);
+      for (int64_t b = 0; b < A.nblk; ++b) if (!ta.identity[b]) bytes += A.blk_size(b);
+      for (int64_t b = 0; b < B.nblk; ++b) if (!tb.identity[b]) bytes += B.blk_size(b);
+      return bytes;
+    };
+    std::vector<int> idx(nax);
+    std::vector<int64_t> best_a = p.axa, best_b = p.axb;
+    int64_t best = moved_bytes(p.axa, p.axb);
+    for (int by_b = 0; by_b < 2; ++by_b) {
+      for (int t = 0; t < nax; ++t) idx[t] = t;
+      const auto& key = by_b ? p.axb : p.axa;
+      std::sort(idx.begin(), idx.end(), [&](int x, int y) { return key[x] < key[y]; });
+      std::vector<int64_t> xa(nax), xb(nax);
+      for (int t = 0; t < nax; ++t) { xa[t] = p.axa[idx[t]]; xb[t] = p.axb[idx[t]]; }
+      const int64_t m = moved_bytes(xa, xb);
+      if (m < best) { best = m; best_a = xa; best_b = xb; }
+    }
+    p.axa = best_a;
+    p.axb = best_b;
+  }
+
   // transpose orders: A -> (saved, contracted), B -> (contracted, saved)
   p.a_order.assign(p.sa.begin(), p.sa.end());
   p.a_order.insert(p.a_order.end(), p.axa.begin(), p.axa.end());
@@ -404,7 +445,7 @@ void plan_contraction(CtrctPlan& p, cudaStream_t s) {
   for (int64_t q = 0; q < np; ++q) {
     const int32_t t = h_perm[q];
     const int32_t i = h_ppa[t], j = h_ppb[t];
-    g.task[q] = GemmTask{A.offsets[i], B.offsets[j], (int32_t)h_ka[i], h_sign[t]};
+    g.task[q] = GemmTask{A.offsets[i], B.offsets[j], (int32_t)h_ka[i], h_sign[t], (int32_t)h_ka[i], 1};
   }
   for (int32_t q = 0; q < ncb; ++q) {
     const int32_t t = h_perm[h_cfirst[q]];

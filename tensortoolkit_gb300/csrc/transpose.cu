@@ -26,9 +26,11 @@ namespace qltg {
 namespace {
 
 constexpr int kTile = 32;
-constexpr int kTileElems = 1024;  // elements per tile (Tp * Tq)
+constexpr int kTileElems = 1024;  // elements per (p, q) tile (Tp * Tq)
+constexpr int kTileMax = 4096;    // elements per batched tile (Tp * Tq * Tu)
 constexpr int kRunChunk = 1024;   // elements per copy-mode / gather-mode work item
 constexpr int kPermThreads = 256;
+constexpr int kLoadBatch = 8;     // tile-mode loads issued per thread before storing
 
 __device__ __forceinline__ double flip(double x, uint64_t m) {
   return __longlong_as_double(__double_as_longlong(x) ^ (long long)m);
@@ -38,8 +40,10 @@ __device__ __forceinline__ double2 flip(double2 x, uint64_t m) { return make_dou
 template <typename T>
 __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __restrict__ descs, int nd, int64_t ntiles,
                                                           const T* __restrict__ src, T* __restrict__ dst) {
-  // tile buffer: Tq rows of Tp + 1 (Tp a power of two, so the row stride is odd)
-  __shared__ T tile[kTileElems + kTileElems / 2];
+  // tile buffer: Tu planes of Tq rows of Tp + 1 (Tp a power of two, so the row stride is
+  // odd); Tp >= 2, so Tu Tq (Tp + 1) <= 1.5 Tp Tq Tu
+  extern __shared__ __align__(16) uint8_t perm_smem[];
+  T* tile = reinterpret_cast<T*>(perm_smem);
   const int64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
   const int64_t t_begin = (int64_t)blockIdx.x * per, t_end = min(ntiles, t_begin + per);
   if (t_begin >= t_end) return;
@@ -113,17 +117,21 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
       }
       continue;
     }
-    // tile mode over (p, q) with Tp x Tq tiles
-    const int tp = d.tp, tq = d.tq;
-    const uint32_t per_outer = (uint32_t)d.tiles_p * (uint32_t)d.tiles_q;
+    // tile mode over (p, q, u) with Tp x Tq x Tu tiles (u: one outer dim batched so a tile
+    // holds up to kTileMax elements even when the inner dims are short)
+    const int tp = d.tp, tq = d.tq, tu = d.tu;
+    const uint32_t per_outer = (uint32_t)d.tiles_p * (uint32_t)d.tiles_q * (uint32_t)d.tiles_u;
     const uint32_t outer = (uint32_t)local / per_outer;
-    const uint32_t tt = (uint32_t)local - outer * per_outer;
+    uint32_t tt = (uint32_t)local - outer * per_outer;
+    const uint32_t tui = tt / ((uint32_t)d.tiles_p * (uint32_t)d.tiles_q);
+    tt -= tui * ((uint32_t)d.tiles_p * (uint32_t)d.tiles_q);
     const uint32_t tpi = tt / (uint32_t)d.tiles_q;
     const int64_t p0 = (int64_t)tpi * tp, q0 = (int64_t)(tt - tpi * (uint32_t)d.tiles_q) * tq;
+    const int64_t u0 = (int64_t)tui * tu;
     uint32_t rem = outer;
     int64_t soff = 0, doff = 0;
     for (int i = r - 1; i >= 0; --i) {
-      if (i == d.p || i == q) continue;
+      if (i == d.p || i == q || i == d.u) continue;
       const uint32_t di = (uint32_t)d.dims[i];
       const uint32_t qq = rem / di;
       const uint32_t x = rem - qq * di;
@@ -131,25 +139,61 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
       soff += (int64_t)x * d.sstride[i];
       doff += (int64_t)x * dstride[i];
     }
-    const T* s = src + d.src_off + soff;
-    T* o = dst + d.dst_off + doff;
+    const int64_t nu = d.u >= 0 ? d.dims[d.u] : 1;
+    const int64_t su = d.u >= 0 ? d.sstride[d.u] : 0, du = d.u >= 0 ? dstride[d.u] : 0;
+    const T* s = src + d.src_off + soff + u0 * su;
+    T* o = dst + d.dst_off + doff + u0 * du;
     const int64_t np_ = d.dims[d.p], nq = d.dims[q];
     const int64_t sq = d.sstride[q], dp = dstride[d.p];
     const int lp = __ffs(tp) - 1, lq = __ffs(tq) - 1;   // tile extents are powers of two
-    const int n = tp * tq, row = tp + 1;
-    // read: p fastest (stride 1 in the source)
-    for (int e = threadIdx.x; e < n; e += kPermThreads) {
-      const int pi = e & (tp - 1), qi = e >> lp;
-      if (p0 + pi < np_ && q0 + qi < nq) tile[qi * row + pi] = __ldg(s + (p0 + pi) + (q0 + qi) * sq);
+    const int n = tp * tq * tu, row = tp + 1, plane = tq * row;
+    const int64_t ulim = nu - u0;
+    // read: p fastest (stride 1 in the source); kLoadBatch independent loads in flight per
+    // thread before any of them is stored to shared memory
+    for (int e0 = threadIdx.x; e0 < n; e0 += kPermThreads * kLoadBatch) {
+      T v[kLoadBatch];
+      int slot[kLoadBatch];
+#pragma unroll
+      for (int i = 0; i < kLoadBatch; ++i) {
+        const int e = e0 + i * kPermThreads;
+        const int pi = e & (tp - 1), qi = (e >> lp) & (tq - 1), ui = e >> (lp + lq);
+        slot[i] = -1;
+        if (e < n && p0 + pi < np_ && q0 + qi < nq && ui < ulim) {
+          v[i] = __ldg(s + (p0 + pi) + (q0 + qi) * sq + ui * su);
+          slot[i] = ui * plane + qi * row + pi;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kLoadBatch; ++i)
+        if (slot[i] >= 0) tile[slot[i]] = v[i];
     }
     __syncthreads();
     // write: q fastest (stride 1 in the destination)
     for (int e = threadIdx.x; e < n; e += kPermThreads) {
-      const int qi = e & (tq - 1), pi = e >> lq;
-      if (p0 + pi < np_ && q0 + qi < nq) o[(q0 + qi) + (p0 + pi) * dp] = flip(tile[qi * row + pi], sg);
+      const int qi = e & (tq - 1), pi = (e >> lq) & (tp - 1), ui = e >> (lp + lq);
+      if (p0 + pi < np_ && q0 + qi < nq && ui < ulim)
+        o[(q0 + qi) + (p0 + pi) * dp + ui * du] = flip(tile[ui * plane + qi * row + pi], sg);
     }
     __syncthreads();
   }
+}
+
+// dynamic shared memory of k_permute (also set as the kernel's maximum, per device)
+size_t perm_smem_bytes(int elem_bytes) { return (size_t)(kTileMax + kTileMax / 2) * elem_bytes; }
+
+// once per device (the attribute belongs to the current device's copy of the kernel)
+void perm_set_smem_attr() {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  QLTG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev >= 0 && dev < 64 && done[dev]) return;
+  QLTG_CUDA(cudaFuncSetAttribute(k_permute<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)perm_smem_bytes(8)));
+  QLTG_CUDA(cudaFuncSetAttribute(k_permute<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)perm_smem_bytes(16)));
+  if (dev >= 0 && dev < 64) done[dev] = true;
 }
 
 int pow2_at_least(int64_t x) {
@@ -161,7 +205,8 @@ int pow2_at_least(int64_t x) {
 }  // namespace
 
 void TransposeList::describe(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
-                             const std::vector<int64_t>* dst_offsets, bool skip_identity) {
+                             const std::vector<int64_t>* dst_offsets, bool skip_identity,
+                             const std::vector<uint8_t>* skip) {
   host.clear();
   identity.assign(t.nblk, 0);
   ntiles = 0;
@@ -208,7 +253,7 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
     // at most one non-unit dim left after merging: the block's data is laid out the same way
     identity[b] = m <= 1 && d.sign_mask == 0 && d.src_off == d.dst_off;
     int64_t tiles;
-    if (identity[b] && skip_identity) {
+    if ((identity[b] && skip_identity) || (skip && (*skip)[b])) {
       tiles = 0;
     } else if (m == 0) {
       d.p = 0;
@@ -241,8 +286,23 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
         d.tq = tq;
         d.tiles_p = (int32_t)((dd[d.p] + tp - 1) / tp);
         d.tiles_q = (int32_t)((dd[m - 1] + tq - 1) / tq);
-        d.nouter = t.blk_size(b) / (dd[d.p] * dd[m - 1]);
-        tiles = d.nouter * d.tiles_p * d.tiles_q;
+        // batch the largest remaining dim when the (p, q) tile holds few valid elements
+        d.u = -1;
+        d.tu = 1;
+        const int64_t valid = std::min<int64_t>(dd[d.p], tp) * std::min<int64_t>(dd[m - 1], tq);
+        int64_t best = 1;
+        for (int i = 0; i < m - 1; ++i)
+          if (i != d.p && dd[i] > best) { best = dd[i]; d.u = i; }
+        if (d.u >= 0 && valid < kTileMax / 2) {
+          int tu = 1;
+          while (tu * 2 <= kTileMax / (tp * tq) && tu * 2 * valid <= kTileMax && tu < dd[d.u]) tu *= 2;
+          d.tu = tu;
+        } else {
+          d.u = -1;
+        }
+        d.tiles_u = (int32_t)(d.u >= 0 ? (dd[d.u] + d.tu - 1) / d.tu : 1);
+        d.nouter = t.blk_size(b) / (dd[d.p] * dd[m - 1] * (d.u >= 0 ? dd[d.u] : 1));
+        tiles = d.nouter * d.tiles_p * d.tiles_q * d.tiles_u;
       }
     }
     d.tile_begin = ntiles;
@@ -253,19 +313,21 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
 }
 
 void TransposeList::build(const Meta& t, const std::vector<int>& order, const std::vector<double>& signs,
-                          const std::vector<int64_t>* dst_offsets, cudaStream_t s, bool skip_identity) {
-  describe(t, order, signs, dst_offsets, skip_identity);
+                          const std::vector<int64_t>* dst_offsets, cudaStream_t s, bool skip_identity,
+                          const std::vector<uint8_t>* skip) {
+  describe(t, order, signs, dst_offsets, skip_identity, skip);
   dev = upload(host, s);
 }
 
 void TransposeList::launch(const void* src, void* dst, int elem_bytes, cudaStream_t s) const {
   if (ntiles == 0) return;
+  perm_set_smem_attr();
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, 152 * 8);
   if (elem_bytes == 8)
-    k_permute<double><<<grid, kPermThreads, 0, s>>>(dev.as<PermDesc>(), (int)nblocks, ntiles, static_cast<const double*>(src),
+    k_permute<double><<<grid, kPermThreads, perm_smem_bytes(8), s>>>(dev.as<PermDesc>(), (int)nblocks, ntiles, static_cast<const double*>(src),
                                            static_cast<double*>(dst));
   else
-    k_permute<double2><<<grid, kPermThreads, 0, s>>>(dev.as<PermDesc>(), (int)nblocks, ntiles,
+    k_permute<double2><<<grid, kPermThreads, perm_smem_bytes(16), s>>>(dev.as<PermDesc>(), (int)nblocks, ntiles,
                                             static_cast<const double2*>(src), static_cast<double2*>(dst));
   QLTG_CUDA(cudaGetLastError());
 }
@@ -308,14 +370,15 @@ void launch_permute_noalloc(int device, const TransposeList& tl, const void* src
              "qltg_transpose_noalloc: tensor has " + std::to_string(tl.nblocks) + " blocks, the fixed table holds " +
                  std::to_string(kNoAllocPermBlocks));
   PermDesc* table = noalloc_table(device);
+  perm_set_smem_attr();
   if (tl.ntiles == 0) return;
   QLTG_CUDA(cudaMemcpyAsync(table, tl.host.data(), tl.host.size() * sizeof(PermDesc), cudaMemcpyHostToDevice, s));
   const unsigned grid = (unsigned)std::min<int64_t>(tl.ntiles, 152 * 8);
   if (elem_bytes == 8)
-    k_permute<double><<<grid, kPermThreads, 0, s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double*>(src),
+    k_permute<double><<<grid, kPermThreads, perm_smem_bytes(8), s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double*>(src),
                                            static_cast<double*>(dst));
   else
-    k_permute<double2><<<grid, kPermThreads, 0, s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double2*>(src),
+    k_permute<double2><<<grid, kPermThreads, perm_smem_bytes(16), s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double2*>(src),
                                             static_cast<double2*>(dst));
   QLTG_CUDA(cudaGetLastError());
   // the descriptors were copied from this call's host memory and the table is shared:
