@@ -189,6 +189,33 @@ QLTG_API int qltg_matvec_device_status(qltg_matvec* mv, void* stream);
 
 QLTG_API int qltg_matvec_destroy(qltg_matvec* mv);
 
+/* ---------------------------------------------------------------- Lanczos (device vectors)
+ * Lanczos on a real FP64 matvec's effective Hamiltonian with every vector operation on the
+ * device in FP64: the reference's BSDT vector primitives (Dot / Norm / ScaleByFactor /
+ * LinearCombine on the raw buffer: framework/hp_numeric/blas_level1.h,
+ * tensor_manipulation/ten_linear_combine.h:186-459, raw_data_operations.h:225-272) applied to
+ * Krylov vectors that share ψ's block topology. Step j: w = H v_j, two passes of classical
+ * Gram-Schmidt against v_0..v_j (alpha_j = <v_j, H v_j> with both corrections),
+ * beta_{j+1} = ||w||, v_{j+1} = w / beta_{j+1}; deterministic reductions. Each step is one
+ * CUDA graph (built on the step's first use; later starts reuse it). alpha and beta stay on
+ * the device until qltg_lanczos_coeffs. The eigenvalues of the tridiagonal matrix are left
+ * to the caller (a small dense FP64 problem). */
+typedef struct qltg_lanczos qltg_lanczos;
+
+/* Krylov space of up to max_iter + 1 vectors (max_iter 1..63) for matvec `mv`, which must
+ * outlive the Lanczos object. */
+QLTG_API int qltg_lanczos_create(qltg_matvec* mv, int32_t max_iter, qltg_lanczos** lz);
+/* v_0 = psi0 / ||psi0|| (psi0 in ψ's raw layout); beta_0 = ||psi0||; resets the step count. */
+QLTG_API int qltg_lanczos_start(qltg_lanczos* lz, const void* psi0_dev, void* stream);
+/* One step (asynchronous on `stream`). QLTG_ERR_INVALID after max_iter steps. */
+QLTG_API int qltg_lanczos_step(qltg_lanczos* lz, void* stream);
+/* Copies alpha_0..alpha_{n-1} and beta_0..beta_n (n = steps taken, written to *nsteps);
+ * synchronises `stream`. A beta of 0 means the Krylov space became invariant. */
+QLTG_API int qltg_lanczos_coeffs(qltg_lanczos* lz, int32_t* nsteps, double* alpha, double* beta, void* stream);
+/* Device address of Krylov vector v_i (0 <= i <= steps), ψ's raw layout. */
+QLTG_API int qltg_lanczos_vector(const qltg_lanczos* lz, int32_t i, const void** v_dev);
+QLTG_API int qltg_lanczos_destroy(qltg_lanczos* lz);
+
 /* ---------------------------------------------------------------- decompositions */
 typedef struct qltg_decomp qltg_decomp;
 

@@ -5,13 +5,13 @@ the C ABI declared in include/qltg.h.
 Submodules:
   tensor     host-side block-sparse metadata (BSTensor, Leg)
   capi       ctypes declarations of the C ABI
-  api        Contract / Transpose / SVD / QR / Matvec over device-resident tensors
-  lanczos    Lanczos ground-state solver driving the captured matvec
+  api        Contract / Transpose / SVD / QR / Matvec / Lanczos over device-resident tensors
   workloads  deterministic synthetic workloads with the reference's shapes
 """
 from .tensor import BSTensor, Leg, IN, OUT  # noqa: F401
 
-_API = {"Contract", "ContractionPlan", "Transpose", "SVD", "QR", "Matvec", "DTensor", "Context", "context"}
+_API = {"Contract", "ContractionPlan", "Transpose", "SVD", "QR", "Matvec", "Lanczos", "DTensor", "Context",
+        "context"}
 
 
 def __getattr__(name):

@@ -251,6 +251,66 @@ class Matvec:
             pass
 
 
+class Lanczos:
+    """Lanczos on a real FP64 `Matvec` with the Krylov vectors and all vector operations on
+    the device (full reorthogonalisation, FP64); one CUDA graph per step. The lowest Ritz
+    value after each step comes from the tridiagonal matrix (host FP64)."""
+
+    def __init__(self, mv: Matvec, max_iter: int = 20):
+        self.mv = mv
+        self.max_iter = int(max_iter)
+        h = C.c_void_p()
+        check(lib().qltg_lanczos_create(mv.h, self.max_iter, C.byref(h)))
+        self.h = h
+
+    def start(self, psi0: DTensor) -> None:
+        check(lib().qltg_lanczos_start(self.h, C.c_void_p(psi0.ptr), stream_ptr(self.mv.device)))
+
+    def step(self, n: int = 1) -> None:
+        for _ in range(n):
+            check(lib().qltg_lanczos_step(self.h, stream_ptr(self.mv.device)))
+
+    def coeffs(self):
+        """(alpha[0:n], beta[0:n+1]) after n steps; beta[0] = ||psi0||."""
+        n = C.c_int32()
+        a = np.zeros(self.max_iter, np.float64)
+        b = np.zeros(self.max_iter + 1, np.float64)
+        check(lib().qltg_lanczos_coeffs(self.h, C.byref(n), a.ctypes.data, b.ctypes.data,
+                                        stream_ptr(self.mv.device)))
+        return a[: n.value].copy(), b[: n.value + 1].copy()
+
+    @staticmethod
+    def ritz_lowest(alpha: np.ndarray, beta: np.ndarray) -> np.ndarray:
+        """Lowest eigenvalue of the leading k x k tridiagonal matrix, k = 1 .. len(alpha)."""
+        out = []
+        for k in range(1, len(alpha) + 1):
+            T = np.diag(alpha[:k]) + np.diag(beta[1:k], 1) + np.diag(beta[1:k], -1)
+            out.append(np.linalg.eigvalsh(T)[0])
+        return np.asarray(out)
+
+    def run(self, psi0: DTensor, n: int) -> np.ndarray:
+        """n steps from psi0; the lowest Ritz value after each step."""
+        self.start(psi0)
+        self.step(n)
+        a, b = self.coeffs()
+        return self.ritz_lowest(a, b)
+
+    def vector(self, i: int) -> torch.Tensor:
+        """Krylov vector v_i as a float64 CUDA tensor viewing the device buffer (no copy)."""
+        p = C.c_void_p()
+        check(lib().qltg_lanczos_vector(self.h, int(i), C.byref(p)))
+        n = self.mv.result.size
+        with torch.cuda.device(self.mv.device):
+            return torch.as_tensor(_DevView(p.value, n), device=f"cuda:{self.mv.device}")
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().qltg_lanczos_destroy(self.h)
+        except Exception:
+            pass
+
+
 def _decomp_tensors(h, which_list, device: int, dtype_real_for=()):
     out = []
     for w in which_list:

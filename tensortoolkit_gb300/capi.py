@@ -48,6 +48,12 @@ _SIGS = {
     "qltg_matvec_apply": ([_P, _P, _P, _P], C.c_int),
     "qltg_matvec_device_status": ([_P, _P], C.c_int),
     "qltg_matvec_destroy": ([_P], C.c_int),
+    "qltg_lanczos_create": ([_P, C.c_int32, C.POINTER(_P)], C.c_int),
+    "qltg_lanczos_start": ([_P, _P, _P], C.c_int),
+    "qltg_lanczos_step": ([_P, _P], C.c_int),
+    "qltg_lanczos_coeffs": ([_P, C.POINTER(C.c_int32), _P, _P, _P], C.c_int),
+    "qltg_lanczos_vector": ([_P, C.c_int32, C.POINTER(_P)], C.c_int),
+    "qltg_lanczos_destroy": ([_P], C.c_int),
     "qltg_svd": ([_P, C.POINTER(TensorDesc), _P, C.c_int32, _P, C.c_double, C.c_int64, C.c_int64, _P,
                   C.POINTER(_P)], C.c_int),
     "qltg_qr": ([_P, C.POINTER(TensorDesc), _P, C.c_int32, _P, _P, C.POINTER(_P)], C.c_int),

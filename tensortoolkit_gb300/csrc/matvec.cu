@@ -9,73 +9,10 @@
 // the life of the object, and the whole chain replays as one graph launch.
 #include <memory>
 
-#include "ctrct.h"
+#include "matvec.h"
 #include "split.h"
 
-namespace qltg {
-void finalize_plan(CtrctPlan& p, cudaStream_t s);
-}
-
 using namespace qltg;
-
-struct qltg_matvec {
-  qltg_ctx* ctx = nullptr;
-  int mode = QLTG_MODE_FP64;
-  CtrctPlan step[4];
-  DevBuf t[3];
-  const void* lenv = nullptr;
-  const void* mpo1 = nullptr;
-  const void* mpo2 = nullptr;
-  const void* renv = nullptr;
-  int64_t psi_size = 0;
-  struct Graph {
-    const void* in;
-    void* out;
-    cudaGraph_t graph;
-    cudaGraphExec_t exec;
-  };
-  std::vector<Graph> graphs;
-  cudaStream_t capture_stream = nullptr;
-
-  ~qltg_matvec() {
-    for (auto& g : graphs) {
-      cudaGraphExecDestroy(g.exec);
-      cudaGraphDestroy(g.graph);
-    }
-    if (capture_stream) cudaStreamDestroy(capture_stream);
-  }
-
-  void enqueue(const void* psi, void* out, cudaStream_t s) {
-    exec_contraction(step[0], lenv, psi, t[0].get(), mode, s);
-    exec_contraction(step[1], t[0].get(), mpo1, t[1].get(), mode, s);
-    exec_contraction(step[2], t[1].get(), mpo2, t[2].get(), mode, s);
-    exec_contraction(step[3], t[2].get(), renv, out, mode, s);
-  }
-
-  cudaGraphExec_t graph_for(const void* in, void* out) {
-    for (auto& g : graphs)
-      if (g.in == in && g.out == out) return g.exec;
-    if (graphs.size() >= 8) {
-      cudaGraphExecDestroy(graphs.front().exec);
-      cudaGraphDestroy(graphs.front().graph);
-      graphs.erase(graphs.begin());
-    }
-    Graph g{in, out, nullptr, nullptr};
-    QLTG_CUDA(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal));
-    try {
-      enqueue(in, out, capture_stream);
-    } catch (...) {
-      cudaGraph_t junk;
-      cudaStreamEndCapture(capture_stream, &junk);
-      if (junk) cudaGraphDestroy(junk);
-      throw;
-    }
-    QLTG_CUDA(cudaStreamEndCapture(capture_stream, &g.graph));
-    QLTG_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
-    graphs.push_back(g);
-    return g.exec;
-  }
-};
 
 extern "C" {
 

@@ -1,0 +1,41 @@
+"""Lanczos with full reorthogonalisation on the CPU oracle's matvec: the checker for the
+device Lanczos (same recurrence: two passes of classical Gram-Schmidt per step,
+alpha_j = <v_j, H v_j> including both corrections, beta_{j+1} = ||w||)."""
+import numpy as np
+
+from oracle import oracle
+
+
+def oracle_apply(ops, psi, x):
+    """H x for a raw vector x in psi's layout (oracle matvec)."""
+    lenv, mpo1, mpo2, renv = ops
+    p = psi.__class__(psi.legs, psi.coords, psi.dtype, np.ascontiguousarray(x), offsets=psi.offsets)
+    out, _ = oracle.matvec(lenv, p, mpo1, mpo2, renv)
+    return out.raw_f64().copy()
+
+
+def lanczos(apply, x0, n):
+    b0 = np.linalg.norm(x0)
+    V = [x0 / b0]
+    alpha, beta = [], [b0]
+    for j in range(n):
+        w = apply(V[j])
+        a = 0.0
+        for _ in range(2):
+            M = np.asarray(V)
+            c = M @ w
+            w = w - M.T @ c
+            a += c[j]
+        alpha.append(a)
+        b = np.linalg.norm(w)
+        beta.append(b)
+        V.append(w / b if b > 0 else np.zeros_like(w))
+    return np.asarray(alpha), np.asarray(beta), np.asarray(V)
+
+
+def ritz_lowest(alpha, beta):
+    out = []
+    for k in range(1, len(alpha) + 1):
+        T = np.diag(alpha[:k]) + np.diag(beta[1:k], 1) + np.diag(beta[1:k], -1)
+        out.append(np.linalg.eigvalsh(T)[0])
+    return np.asarray(out)
