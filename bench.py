@@ -208,6 +208,42 @@ def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
             "per_step": per, "gemm_stage_ms": round(stage_ms, 4), "gemm_kernels_ms": round(kern_ms, 4)}
 
 
+def precision_study(local: int, steps: int = 20):
+    """The precision configuration on the symmetric (Hermitian) variant of the D=4000 workload:
+    relative Frobenius error of the split-precision matvec vs the plain FP64 path (itself
+    parity-tested against the oracle), per block and whole, and the drift of the lowest
+    Lanczos Ritz value over `steps` iterations (FP64 full reorthogonalisation on the device)
+    from the same normalised N(0,1) psi0."""
+    import numpy as np
+    from tensortoolkit_gb300 import workloads
+    from tensortoolkit_gb300.api import DTensor, Lanczos, Matvec
+    tensors = workloads.heisenberg(WORKLOAD["D"], WORKLOAD["qmax"], WORKLOAD["sigma"], WORKLOAD["seed"],
+                                   hermitian=True)
+    lenv, psi, mpo1, mpo2, renv = tensors
+    dl, dp, d1, d2, dr = (DTensor.from_host(x, local) for x in tensors)
+    out = {}
+    for m in ("fp64", "split"):
+        mv = Matvec(dl, psi, d1, d2, dr, mode=m)
+        y = mv.apply(dp).to_host()
+        e = Lanczos(mv, steps).run(dp, steps)
+        mv.device_status()
+        out[m] = (y, e)
+        del mv
+    (y64, e64), (ys, es) = out["fp64"], out["split"]
+    blk = []
+    for b in range(y64.nblk):
+        n = np.linalg.norm(y64.block(b))
+        if n > 0:
+            blk.append(float(np.linalg.norm(ys.block(b) - y64.block(b)) / n))
+    drift = np.abs(es - e64)
+    return {"workload": WORKLOAD_NAME + ", symmetric lenv/renv (Hermitian H_eff)",
+            "matvec_rel_err": float(np.linalg.norm(ys.raw_f64() - y64.raw_f64()) / np.linalg.norm(y64.raw_f64())),
+            "max_block_rel_err": max(blk), "median_block_rel_err": float(np.median(blk)), "blocks": len(blk),
+            "lanczos_steps": steps, "e0_fp64": float(e64[-1]), "e0_split": float(es[-1]),
+            "max_energy_drift": float(drift.max()), "max_rel_energy_drift": float((drift / np.abs(e64)).max()),
+            "energy_drift_per_step": [float(x) for x in drift]}
+
+
 def cpu_matvec_time(tensors, iters: int, threads: int) -> float:
     """Seconds per matvec of the CPU restatement (median of `iters`)."""
     from oracle import oracle
@@ -396,6 +432,7 @@ def main():
             res["fp64"] = {"s_per_iter": f["s_per_iter"], "e2e_s_per_iter": f["e2e_s_per_iter"],
                            "roofline": f["roofline"], "gpu_launches_per_step": int(f["launches_per_step"])}
             res["split_speedup_vs_fp64"] = f["s_per_iter"] / head["s_per_iter"]
+            res["precision_study"] = precision_study(local)
         print(json.dumps(res))
     if world > 1:
         dist.destroy_process_group()
