@@ -244,6 +244,108 @@ def precision_study(local: int, steps: int = 20):
             "energy_drift_per_step": [float(x) for x in drift]}
 
 
+def svd_group_shapes(t, ldims: int):
+    """(rows, cols) of the block-diagonal matrices SVD(t, ldims) factors: blocks grouped by
+    the quantum-number flux of their left legs (the reference's grouping key)."""
+    import numpy as np
+    sgn = [1 if l.dir == 0 else -1 for l in t.legs]
+    groups = {}
+    for b in range(t.nblk):
+        c = t.coords[b]
+        flux = tuple(np.sum([sgn[l] * t.legs[l].qns[c[l]] for l in range(ldims)], axis=0).tolist())
+        g = groups.setdefault(flux, [set(), set()])
+        g[0].add(tuple(c[:ldims].tolist()))
+        g[1].add(tuple(c[ldims:].tolist()))
+    shapes = []
+    for rows, cols in groups.values():
+        r = sum(int(np.prod([t.legs[l].dims[x[l]] for l in range(ldims)])) for x in rows)
+        cc = sum(int(np.prod([t.legs[ldims + l].dims[x[l]] for l in range(t.rank - ldims)])) for x in cols)
+        shapes.append((r, cc))
+    return shapes
+
+
+def time_call(fn, reps: int = 5) -> float:
+    """Median wall time of fn() in seconds, device synchronised around each call."""
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts)
+
+
+def run_aux(local: int):
+    """Measurements beside the headline: the batched permute's achieved HBM bandwidth, the
+    batched block SVD / QR (Config 3) against a per-block cuSOLVER loop on the same shapes
+    (the reference GPU build's pattern), and the matvec of Configs 2 and 5."""
+    import numpy as np
+    import torch
+    from tensortoolkit_gb300 import workloads
+    from tensortoolkit_gb300.api import Contract, DTensor, Matvec, QR, SVD, Transpose
+    pk = peaks()
+    out = {"aux": True, "gpu": torch.cuda.get_device_name(local)}
+    dev = f"cuda:{local}"
+    # 1. permute: t0 of the D=4000 matvec (80 MB) to the order a contraction over its legs
+    #    (0, 2) would use; every block moves (Transpose copies identity layouts too)
+    lenv, psi, mpo1, mpo2, renv = workloads.heisenberg(WORKLOAD["D"], WORKLOAD["qmax"], WORKLOAD["sigma"],
+                                                       WORKLOAD["seed"])
+    t0 = Contract(DTensor.from_host(lenv, local), DTensor.from_host(psi, local), [[0], [0]])
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(local)
+    for name, perm in (("t0 (w,l,p1,p2,r) -> (l,p2,r,w,p1)", (1, 3, 4, 0, 2)),
+                       ("t0 (w,l,p1,p2,r) -> (r,p2,p1,l,w)", (4, 3, 2, 1, 0))):
+        Transpose(t0, perm)
+        ms = _time_events(lambda: Transpose(t0, perm), stream, flush)
+        nbytes = 2 * 8 * t0.meta.size
+        out.setdefault("transpose", []).append(
+            {"case": name, "mbytes_moved": nbytes / 1e6, "ms": round(ms, 4), "gbs": nbytes / (ms / 1e3) / 1e9,
+             "frac_of_hbm": nbytes / (ms / 1e3) / 1e9 / pk["hbm_gbs"],
+             "note": "time includes building the block list on the host and its upload"})
+    del t0
+    # 2. batched SVD / QR (Config 3 and the 41-block stress variant) vs per-block cuSOLVER
+    for name, t, ldims in (("Config 3: psi D=2000, 41 block-matrices", workloads.svd_psi(2000, 20, 6.0, 3), 2),
+                           ("stress: 41 square blocks 10..800", workloads.svd_stress(41, 10, 800, 3), 1)):
+        dt = DTensor.from_host(t, local)
+        sv = time_call(lambda: SVD(dt, ldims, [0], 1e-9, 1, 2000))
+        qr = time_call(lambda: QR(dt, ldims, [0]))
+        shapes = svd_group_shapes(t, ldims)
+        mats = [torch.randn(r, c, dtype=torch.float64, device=dev) for r, c in shapes]
+        loop = time_call(lambda: [torch.linalg.svd(m, full_matrices=False) for m in mats])
+        qloop = time_call(lambda: [torch.linalg.qr(m) for m in mats])
+        out.setdefault("svd", []).append(
+            {"case": name, "groups": len(shapes), "max_rows": max(r for r, _ in shapes),
+             "max_cols": max(c for _, c in shapes), "batched_svd_ms": sv * 1e3,
+             "per_block_cusolver_svd_ms": loop * 1e3, "batched_qr_ms": qr * 1e3,
+             "per_block_cusolver_qr_ms": qloop * 1e3,
+             "note": "batched = the whole qltg_svd / qltg_qr call (grouping, kernels, truncation, U/S/Vt "
+                     "or Q/R tensors); per-block = torch.linalg.svd / qr (cuSOLVER) on dense matrices of "
+                     "the same shapes, kernels only"})
+        del dt, mats
+    # 3. matvec of Config 2 (U(1), D=2000) in both forms, and Config 5 (fermionic complex128,
+    #    D=6000, plain FP64: complex operands have no split form)
+    def mv_time(tensors, mode):
+        lenv_, psi_, mpo1_, mpo2_, renv_ = tensors
+        dl_, dp_, d1_, d2_, dr_ = (DTensor.from_host(x, local) for x in tensors)
+        t_create = time.perf_counter()
+        mv = Matvec(dl_, psi_, d1_, d2_, dr_, mode=mode)
+        torch.cuda.synchronize()
+        t_create = time.perf_counter() - t_create
+        o = DTensor.empty(mv.result, local)
+        ms = _time_events(lambda: mv.apply(dp_, o), stream, flush, reps=10)
+        mv.device_status()
+        f, _ = mv.stats()
+        return {"mode": mode, "ms": round(ms, 4), "gflops": f / (ms / 1e3) / 1e9, "plan_s": round(t_create, 3)}
+    c2 = workloads.heisenberg(2000, 20, 6.0, 1)
+    out["config2_matvec_d2000"] = [mv_time(c2, "fp64"), mv_time(c2, "split")]
+    c5 = workloads.hubbard(6000, 10, 4)
+    out["config5_matvec_d6000_complex"] = [mv_time(c5, "fp64")]
+    print(json.dumps(out))
+
+
 def cpu_matvec_time(tensors, iters: int, threads: int) -> float:
     """Seconds per matvec of the CPU restatement (median of `iters`)."""
     from oracle import oracle
@@ -294,6 +396,9 @@ def main():
     ap.add_argument("--mode", choices=["both", "split", "fp64"], default=os.environ.get("QLTG_BENCH_MODE", "both"),
                     help="both (default): headline split precision, plain FP64 beside it")
     ap.add_argument("--cpu-iters", type=int, default=None, help="CPU baseline sample size")
+    ap.add_argument("--aux", action="store_true",
+                    help="measurements beside the headline: permute GB/s, batched SVD/QR vs per-block, "
+                         "Config 2 and Config 5 matvecs (one JSON line)")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: plan the D=4000 matvec, apply it twice, print nothing else")
     args = ap.parse_args()
@@ -323,6 +428,9 @@ def main():
     stream = torch.cuda.current_stream(local)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
     modes = ["split", "fp64"] if args.mode == "both" else [args.mode]
+
+    if args.aux:
+        return run_aux(local)
 
     if args.profile:
         for m in modes:
