@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <numeric>
 
 #include "ctrct.h"
@@ -32,9 +33,9 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxSweeps = 60;
 constexpr int kBigCluster = 8;
+constexpr int kJacobiSmem = 200 * 1024;   // dynamic shared memory of k_jacobi (two column blocks)
 
 // ------------------------------------------------------------------ complex helpers
-__device__ __forceinline__ double conj_mul_re(double a, double b) { return a * b; }
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 __device__ __forceinline__ double2 cconjmul(double2 a, double2 b) {   // conj(a) * b
   return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
@@ -124,24 +125,28 @@ __device__ __forceinline__ int rr_player(int slot, int r, int qq) {
   return slot == 0 ? 0 : ((slot - 1 + r) % (qq - 1)) + 1;
 }
 
+// Rotate stacked columns xi, xj (length L: the p entries of W, then the q of V) so that
+// their first p entries become orthogonal, unless they already are to `tol` (relative).
+// Convergence: a pair is rotated only if |<wi, wj>| > tol ||wi|| ||wj|| (relative
+// orthogonality) and |<wi, wj>| > tol ||A||_F max(||wi||, ||wj||) (absolute floor: pairs whose
+// inner product is at the rounding level of the whole matrix are left alone, which bounds the
+// singular-value change to about tol ||A|| absolute - the accuracy LAPACK's ?gesvd gives).
 template <typename T>
-__device__ void rotate_pair(T* __restrict__ W, T* __restrict__ V, int p, int q, int i, int j, double tol,
-                            int lane, int* rotated) {
-  T* wi = W + (int64_t)i * p;
-  T* wj = W + (int64_t)j * p;
+__device__ __forceinline__ void rotate_cols(T* __restrict__ xi, T* __restrict__ xj, int p, int L, double tol,
+                                            double tol_abs, int lane, int* rotated) {
   double a = 0, b = 0;
   T g;
   if constexpr (sizeof(T) == 8) {
     double gg = 0;
     for (int e = lane; e < p; e += 32) {
-      const double x = wi[e], y = wj[e];
-      a += x * x; b += y * y; gg += x * y;
+      const double x = xi[e], y = xj[e];
+      a = fma(x, x, a); b = fma(y, y, b); gg = fma(x, y, gg);
     }
     g = warp_sum(gg);
   } else {
     double gr = 0, gi = 0;
     for (int e = lane; e < p; e += 32) {
-      const double2 x = wi[e], y = wj[e];
+      const double2 x = xi[e], y = xj[e];
       a += abs2(x); b += abs2(y);
       const double2 t = cconjmul(x, y);
       gr += t.x; gi += t.y;
@@ -151,97 +156,186 @@ __device__ void rotate_pair(T* __restrict__ W, T* __restrict__ V, int p, int q, 
   a = warp_sum(a);
   b = warp_sum(b);
   const double gabs = sqrt(abs2(g));
-  if (!(gabs > tol * sqrt(a) * sqrt(b)) || gabs == 0.0) return;
+  if (!(gabs > tol * sqrt(a) * sqrt(b)) || !(gabs > tol_abs * sqrt(fmax(a, b))) || gabs == 0.0) return;
   if (lane == 0) *rotated = 1;
   const double zeta = (b - a) / (2.0 * gabs);
   const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
   const double c = 1.0 / sqrt(1.0 + t * t);
-  const double s = c * t;
+  const double sn = c * t;
   if constexpr (sizeof(T) == 8) {
-    const double sg = g >= 0 ? s : -s;   // e^{i phi} = sign(g)
-    for (int e = lane; e < p; e += 32) {
-      const double x = wi[e], y = wj[e];
-      wi[e] = c * x - sg * y;
-      wj[e] = sg * x + c * y;
-    }
-    T* vi = V + (int64_t)i * q;
-    T* vj = V + (int64_t)j * q;
-    for (int e = lane; e < q; e += 32) {
-      const double x = vi[e], y = vj[e];
-      vi[e] = c * x - sg * y;
-      vj[e] = sg * x + c * y;
+    const double sg = g >= 0 ? sn : -sn;   // e^{i phi} = sign(g)
+    for (int e = lane; e < L; e += 32) {
+      const double x = xi[e], y = xj[e];
+      xi[e] = c * x - sg * y;
+      xj[e] = sg * x + c * y;
     }
   } else {
-    // [wi', wj'] = [wi, wj] [[c, s e^{i phi}], [-s e^{-i phi}, c]],  e^{i phi} = g / |g|
+    // [xi', xj'] = [xi, xj] [[c, s e^{i phi}], [-s e^{-i phi}, c]],  e^{i phi} = g / |g|
     const double2 ph = make_double2(g.x / gabs, g.y / gabs);
-    const double2 sp = make_double2(s * ph.x, s * ph.y);          // s e^{i phi}
-    const double2 sm = make_double2(s * ph.x, -s * ph.y);         // s e^{-i phi}
-    for (int e = lane; e < p; e += 32) {
-      const double2 x = wi[e], y = wj[e];
+    const double2 sp = make_double2(sn * ph.x, sn * ph.y);          // s e^{i phi}
+    const double2 sm = make_double2(sn * ph.x, -sn * ph.y);         // s e^{-i phi}
+    for (int e = lane; e < L; e += 32) {
+      const double2 x = xi[e], y = xj[e];
       const double2 a1 = cmul(sm, y), b1 = cmul(sp, x);
-      wi[e] = make_double2(c * x.x - a1.x, c * x.y - a1.y);
-      wj[e] = make_double2(b1.x + c * y.x, b1.y + c * y.y);
-    }
-    T* vi = V + (int64_t)i * q;
-    T* vj = V + (int64_t)j * q;
-    for (int e = lane; e < q; e += 32) {
-      const double2 x = vi[e], y = vj[e];
-      const double2 a1 = cmul(sm, y), b1 = cmul(sp, x);
-      vi[e] = make_double2(c * x.x - a1.x, c * x.y - a1.y);
-      vj[e] = make_double2(b1.x + c * y.x, b1.y + c * y.y);
+      xi[e] = make_double2(c * x.x - a1.x, c * x.y - a1.y);
+      xj[e] = make_double2(b1.x + c * y.x, b1.y + c * y.y);
     }
   }
 }
 
-// One cluster (size = gridDim.x / njobs) per job. Sweeps until a sweep performs no rotation
-// (bounded by kMaxSweeps; status[job] = sweeps used, or -1 if not converged).
+// Blocked one-sided Jacobi. The q columns of the stacked matrix [W; V] (W: p x q, V: q x q
+// accumulated rotations, both vector-major in global memory) are cut into 2M blocks of nb
+// columns, nb chosen so that two blocks fit in shared memory. A sweep is the 2M - 1 steps
+// of a round-robin tournament over the blocks; in each step a CTA takes block pairs
+// (a, b), loads their columns into shared memory, runs a full round-robin sweep over those
+// columns there (only __syncthreads between rounds) and writes them back. With M = 1 all
+// columns stay in shared memory for every sweep. One cluster of cl CTAs per job; the
+// cluster barrier separates steps, so a sweep costs 2M - 1 barriers instead of q - 1.
+// Sweeps stop after one without a rotation (bounded by kMaxSweeps; status[job] = sweeps
+// used, or -1 if not converged).
+struct JacobiShape {
+  int nb;   // columns per block
+  int M;    // block pairs per step (2M blocks)
+};
+
+template <typename T>
+__host__ __device__ inline JacobiShape jacobi_shape(int p, int q, int smem_bytes) {
+  const int L = p + q;
+  int nb = smem_bytes / (2 * L * (int)sizeof(T));
+  if (nb < 1) nb = 1;
+  if (2 * nb >= q) return JacobiShape{(q + 1) / 2, 1};
+  // block pairs per step: a multiple of the cluster size, so no CTA of the cluster idles
+  int M = (q + 2 * nb - 1) / (2 * nb);
+  M = (M + kBigCluster - 1) / kBigCluster * kBigCluster;
+  return JacobiShape{(q + 2 * M - 1) / (2 * M), M};
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_jacobi(const JacobiJob* __restrict__ jobs, int cl, T* __restrict__ ws,
                                                      T* __restrict__ vs, int* __restrict__ sweep_rot,
-                                                     int* __restrict__ status, double tol) {
+                                                     int* __restrict__ status, double tol, int smem_bytes) {
+  extern __shared__ __align__(16) uint8_t jac_smem[];
+  T* X = reinterpret_cast<T*>(jac_smem);
   cg::cluster_group cluster = cg::this_cluster();
   const int job = blockIdx.x / cl;
   const int rank = blockIdx.x % cl;
   const JacobiJob jb = jobs[job];
   T* W = ws + jb.w_off;
   T* V = vs + jb.v_off;
-  const int p = jb.p, q = jb.q;
+  const int p = jb.p, q = jb.q, L = p + q;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __shared__ int rotated;
-  // V = identity (vector-major storage of the q x q matrix)
-  for (int64_t e = (int64_t)rank * kThreads + threadIdx.x; e < (int64_t)q * q; e += (int64_t)cl * kThreads) {
-    T one, zero;
-    if constexpr (sizeof(T) == 8) { one = 1.0; zero = 0.0; } else { one = make_double2(1, 0); zero = make_double2(0, 0); }
+  T one, zero;
+  if constexpr (sizeof(T) == 8) { one = 1.0; zero = 0.0; } else { one = make_double2(1, 0); zero = make_double2(0, 0); }
+  auto barrier = [&]() {
+    __threadfence();
+    if (cl > 1) cluster.sync(); else __syncthreads();
+  };
+  // V = identity
+  for (int64_t e = (int64_t)rank * kThreads + threadIdx.x; e < (int64_t)q * q; e += (int64_t)cl * kThreads)
     V[e] = (e / q == e % q) ? one : zero;
-  }
-  __threadfence();
-  if (cl > 1) cluster.sync(); else __syncthreads();
+  // ||A||_F (every CTA of the cluster computes it, in the same order)
+  __shared__ double red[kWarps];
+  double f2 = 0.0;
+  for (int64_t e = threadIdx.x; e < (int64_t)p * q; e += kThreads) f2 += abs2(W[e]);
+  f2 = warp_sum(f2);
+  if (lane == 0) red[warp] = f2;
+  __syncthreads();
+  double normA = 0.0;
+  for (int w = 0; w < kWarps; ++w) normA += red[w];
+  normA = sqrt(normA);
+  const double tol_abs = tol * normA;
+  barrier();
   if (q < 2) {
     if (rank == 0 && threadIdx.x == 0) status[job] = 0;
     return;
   }
-  const int qq = q + (q & 1);
-  const int npairs = qq / 2;
-  const int gw = rank * kWarps + warp, nw = cl * kWarps;
-  int sweep = 0;
-  for (; sweep < kMaxSweeps; ++sweep) {
-    if (threadIdx.x == 0) rotated = 0;
-    __syncthreads();
-    for (int r = 0; r < qq - 1; ++r) {
-      for (int k = gw; k < npairs; k += nw) {
-        int i = rr_player(k, r, qq), j = rr_player(qq - 1 - k, r, qq);
-        if (i > j) { int t = i; i = j; j = t; }
-        if (j < q) rotate_pair<T>(W, V, p, q, i, j, tol, lane, &rotated);
-      }
-      __threadfence();
-      if (cl > 1) cluster.sync(); else __syncthreads();
+  const JacobiShape sh = jacobi_shape<T>(p, q, smem_bytes);
+  const int nb = sh.nb, M = sh.M, nblk = 2 * sh.M;
+  // global column c of block `blk` and its count
+  auto block_cols = [&](int blk, int& c0) {
+    c0 = blk * nb;
+    return max(0, min(q, c0 + nb) - c0);
+  };
+  auto load = [&](int c0, int n, int x0) {   // columns c0 .. c0+n-1 into shared slots x0 ..
+    for (int e = threadIdx.x; e < n * L; e += kThreads) {
+      const int c = e / L, r = e - c * L;
+      X[(int64_t)(x0 + c) * L + r] = r < p ? W[(int64_t)(c0 + c) * p + r] : V[(int64_t)(c0 + c) * q + (r - p)];
     }
+  };
+  auto store = [&](int c0, int n, int x0) {
+    for (int e = threadIdx.x; e < n * L; e += kThreads) {
+      const int c = e / L, r = e - c * L;
+      const T x = X[(int64_t)(x0 + c) * L + r];
+      if (r < p) W[(int64_t)(c0 + c) * p + r] = x; else V[(int64_t)(c0 + c) * q + (r - p)] = x;
+    }
+  };
+  // one full round-robin sweep over the lc columns in shared memory
+  auto local_sweep = [&](int lc) {
+    const int lcc = lc + (lc & 1);
+    for (int r = 0; r < lcc - 1; ++r) {
+      for (int k = warp; k < lcc / 2; k += kWarps) {
+        int i = rr_player(k, r, lcc), j = rr_player(lcc - 1 - k, r, lcc);
+        if (i > j) { const int t = i; i = j; j = t; }
+        if (j < lc) rotate_cols<T>(X + (int64_t)i * L, X + (int64_t)j * L, p, L, tol, tol_abs, lane, &rotated);
+      }
+      __syncthreads();
+    }
+  };
+  // every pair (i in the first na columns, j in the next nbb): max(na, nbb) rounds in which
+  // column i meets column (i + r) mod max of the other block
+  auto cross_sweep = [&](int na, int nbb) {
+    const int nm = max(na, nbb);
+    for (int r = 0; r < nm; ++r) {
+      for (int i = warp; i < nm; i += kWarps) {
+        const int j = (i + r) % nm;
+        if (i < na && j < nbb)
+          rotate_cols<T>(X + (int64_t)i * L, X + (int64_t)(na + j) * L, p, L, tol, tol_abs, lane, &rotated);
+      }
+      __syncthreads();
+    }
+  };
+  int sweep = 0;
+  if (M == 1) {
+    // every column in shared memory for all sweeps (one CTA: cl == 1 for these jobs)
+    load(0, q, 0);
     __syncthreads();
-    if (threadIdx.x == 0 && rotated) atomicAdd(&sweep_rot[job * kMaxSweeps + sweep], 1);
-    __threadfence();
-    if (cl > 1) cluster.sync(); else __syncthreads();
-    const int any = *((volatile int*)&sweep_rot[job * kMaxSweeps + sweep]);
-    if (any == 0) break;
+    for (; sweep < kMaxSweeps; ++sweep) {
+      if (threadIdx.x == 0) rotated = 0;
+      __syncthreads();
+      local_sweep(q);
+      const int any = rotated;
+      __syncthreads();
+      if (!any) break;
+    }
+    store(0, q, 0);
+    barrier();
+  } else {
+    for (; sweep < kMaxSweeps; ++sweep) {
+      if (threadIdx.x == 0) rotated = 0;
+      __syncthreads();
+      for (int st = 0; st < nblk - 1; ++st) {
+        for (int k = rank; k < M; k += cl) {
+          const int ba = rr_player(k, st, nblk), bb = rr_player(nblk - 1 - k, st, nblk);
+          int ca, cb;
+          const int na = block_cols(ba, ca), nbb = block_cols(bb, cb);
+          if (na + nbb < 2) continue;
+          load(ca, na, 0);
+          load(cb, nbb, na);
+          __syncthreads();
+          // the first step of a sweep also orthogonalises the columns inside each block
+          if (st == 0) local_sweep(na + nbb); else cross_sweep(na, nbb);
+          store(ca, na, 0);
+          store(cb, nbb, na);
+          __syncthreads();
+        }
+        barrier();
+      }
+      if (threadIdx.x == 0 && rotated) atomicAdd(&sweep_rot[job * kMaxSweeps + sweep], 1);
+      barrier();
+      const int any = *((volatile int*)&sweep_rot[job * kMaxSweeps + sweep]);
+      if (any == 0) break;
+    }
   }
   if (rank == 0 && threadIdx.x == 0) status[job] = sweep < kMaxSweeps ? sweep + 1 : -1;
 }
@@ -303,7 +397,6 @@ __device__ __forceinline__ double re_of(double2 x) { return x.x; }
 __device__ __forceinline__ double im_of(double) { return 0.0; }
 __device__ __forceinline__ double im_of(double2 x) { return x.y; }
 
-__device__ __forceinline__ double dot_part(double a, double b) { return a * b; }
 
 template <typename T>
 __device__ __forceinline__ T conjT(T x) {
@@ -545,6 +638,82 @@ namespace qltg {
 namespace {
 
 
+// ---- QR preconditioning of the one-sided Jacobi (the Drmac-Veselic scheme, restated):
+// M = Q R (Householder, k_householder), Jacobi on X = R^H, then M = (Q J) S Xn^H with
+// Xn the normalised columns of X and J the accumulated rotations. On graded spectra (the
+// decaying singular values of a DMRG bond) this cuts the sweeps from ~30 to ~8.
+struct PrecondJob {
+  int64_t a_off;   // R in the upper triangle of the factorised p x q matrix (column-major, ld p)
+  int64_t q_off;   // Q, p x q column-major
+  int64_t x_off;   // X = R^H, q vectors of length q (vector i = conj of row i of R)
+  int64_t j_off;   // J, q x q vector-major
+  int64_t w_off;   // output Q J, q vectors of length p
+  int32_t p, q;
+};
+
+template <typename T>
+__global__ void k_r_to_x(const PrecondJob* __restrict__ jobs, int njobs, const T* __restrict__ as,
+                         T* __restrict__ xs) {
+  const PrecondJob jb = jobs[blockIdx.x];
+  const int p = jb.p, q = jb.q;
+  for (int64_t e = threadIdx.x; e < (int64_t)q * q; e += blockDim.x) {
+    const int i = (int)(e / q), c = (int)(e - (int64_t)i * q);   // vector i, element c = conj(R[i, c])
+    T v{};
+    if (c >= i) {
+      v = as[jb.a_off + (int64_t)c * p + i];
+      if constexpr (sizeof(T) == 16) v.y = -v.y;
+    }
+    xs[jb.x_off + e] = v;
+  }
+}
+
+// W = Q J per job: 32 x 32 output tiles (tile list flattened over jobs), FP64 FMA.
+struct QjTile {
+  int32_t job, tm, tn;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_qj(const PrecondJob* __restrict__ jobs, const QjTile* __restrict__ tiles,
+                                            int ntiles, const T* __restrict__ qs, const T* __restrict__ js,
+                                            T* __restrict__ ws) {
+  __shared__ T sq[32][33];
+  __shared__ T sj[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+  for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+    const QjTile tl = tiles[ti];
+    const PrecondJob jb = jobs[tl.job];
+    const int p = jb.p, q = jb.q;
+    const int r0 = tl.tm * 32, c0 = tl.tn * 32;
+    T acc[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] = T{};
+    for (int k0 = 0; k0 < q; k0 += 32) {
+      // Q[r0 + tx, k0 + kk] (column-major) and J[k0 + kk, c0 + col] (vector-major: J[col * q + kk])
+      for (int kk = ty; kk < 32; kk += 8) {
+        sq[kk][tx] = (r0 + tx < p && k0 + kk < q) ? qs[jb.q_off + (int64_t)(k0 + kk) * p + r0 + tx] : T{};
+        sj[tx][kk] = (c0 + tx < q && k0 + kk < q) ? js[jb.j_off + (int64_t)(c0 + tx) * q + k0 + kk] : T{};
+      }
+      __syncthreads();
+#pragma unroll 8
+      for (int kk = 0; kk < 32; ++kk) {
+        const T a = sq[kk][tx];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const T b = sj[ty + 8 * u][kk];
+          if constexpr (sizeof(T) == 8) acc[u] = fma(a, b, acc[u]);
+          else acc[u] = make_double2(acc[u].x + a.x * b.x - a.y * b.y, acc[u].y + a.x * b.y + a.y * b.x);
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int c = c0 + ty + 8 * u, r = r0 + tx;
+      if (r < p && c < q) ws[jb.w_off + (int64_t)c * p + r] = acc[u];
+    }
+  }
+}
+
 template <typename T>
 void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int32_t>& lqndiv, double trunc,
               int64_t dmin, int64_t dmax, cudaStream_t s, qltg_decomp& out) {
@@ -589,9 +758,49 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   DevBuf d_svoff = upload(sv_off, s);
   if (woff) QLTG_CUDA(cudaMemsetAsync(ws.get(), 0, woff * eb, s));
   launch_gather<T>(cd, eoff, t_dev, ws.get(), s, keep_g);
-  // big groups on 8-CTA clusters (8 SMs each), the others one CTA each
+  // QR preconditioning: M = Q R (Householder, in place in the W region), X = R^H into the
+  // V region; the Jacobi below works on X with its rotations J in their own buffer
+  std::vector<QrJob> qjobs(ng);
+  std::vector<PrecondJob> pre(ng);
+  std::vector<JacobiJob> xjobs(ng);
+  std::vector<QjTile> qtiles;
+  int64_t qoff = 0, toff = 0, joff = 0;
+  for (int g = 0; g < ng; ++g) {
+    const JacobiJob& j = jobs[g];
+    qjobs[g] = QrJob{j.w_off, toff, qoff, j.p, j.q};
+    pre[g] = PrecondJob{j.w_off, qoff, j.v_off, joff, j.w_off, j.p, j.q};
+    xjobs[g] = JacobiJob{j.v_off, joff, j.q, j.q};
+    qoff += (int64_t)j.p * j.q;
+    toff += j.q;
+    joff += (int64_t)j.q * j.q;
+    for (int tm = 0; tm * 32 < j.p; ++tm)
+      for (int tn = 0; tn * 32 < j.q; ++tn) qtiles.push_back(QjTile{g, tm, tn});
+  }
+  DevBuf qbuf(std::max<int64_t>(1, qoff) * eb), taubuf(std::max<int64_t>(1, toff) * eb),
+      jbuf(std::max<int64_t>(1, joff) * eb);
+  DevBuf d_qjobs = upload(qjobs, s), d_pre = upload(pre, s), d_qtiles = upload(qtiles, s);
+  if (ng) {
+    k_householder<T><<<ng, kThreads, 0, s>>>(d_qjobs.as<QrJob>(), ws.as<T>(), taubuf.as<T>(), qbuf.as<T>());
+    k_r_to_x<T><<<ng, kThreads, 0, s>>>(d_pre.as<PrecondJob>(), ng, ws.as<T>(), ws.as<T>());
+    QLTG_CUDA(cudaGetLastError());
+  }
+  // groups whose columns all fit in one CTA's shared memory: one CTA each; the others on
+  // 8-CTA clusters stepping through block pairs
   std::vector<JacobiJob> big, small;
-  for (int g = 0; g < ng; ++g) (jobs[g].q >= 96 ? big : small).push_back(jobs[g]);
+  for (int g = 0; g < ng; ++g)
+    (jacobi_shape<T>(xjobs[g].p, xjobs[g].q, kJacobiSmem).M > 1 ? big : small).push_back(xjobs[g]);
+  {
+    static std::mutex mu;
+    static bool done[2][64] = {};
+    int dev = 0;
+    QLTG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64 || !done[sizeof(T) == 16][dev]) {
+      QLTG_CUDA(cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kJacobiSmem));
+      QLTG_CUDA(cudaFuncSetAttribute(k_jacobi<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      if (dev >= 0 && dev < 64) done[sizeof(T) == 16][dev] = true;
+    }
+  }
   DevBuf d_big = upload(big, s), d_small = upload(small, s);
   DevBuf st_big(std::max<size_t>(1, big.size()) * 4), st_small(std::max<size_t>(1, small.size()) * 4);
   DevBuf sr_big(std::max<size_t>(1, big.size()) * kMaxSweeps * 4);
@@ -600,10 +809,30 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   QLTG_CUDA(cudaMemsetAsync(sr_small.get(), 0, sr_small.bytes(), s));
   // rotate while |<wi, wj>| > tol ||wi|| ||wj||: columns orthogonal to a few ulps
   const double tol = 64.0 * 2.220446049250313e-16;
-  if (!big.empty()) {
+  // the single-CTA jobs run beside the clusters: on a second stream forked before the
+  // cluster launch and joined after it
+  cudaStream_t s2 = s;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  const bool two = !big.empty() && !small.empty();
+  if (two) {
+    QLTG_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+    QLTG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    QLTG_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+    QLTG_CUDA(cudaEventRecord(fork, s));
+    QLTG_CUDA(cudaStreamWaitEvent(s2, fork, 0));
+  }
+  cudaError_t le = cudaSuccess;
+  if (!small.empty()) {
+    k_jacobi<T><<<(unsigned)small.size(), kThreads, kJacobiSmem, s2>>>(d_small.as<const JacobiJob>(), 1, ws.as<T>(),
+                                                                        jbuf.as<T>(), sr_small.as<int>(),
+                                                                        st_small.as<int>(), tol, (int)kJacobiSmem);
+    le = cudaGetLastError();
+  }
+  if (!big.empty() && le == cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(big.size() * kBigCluster));
     cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = kJacobiSmem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -612,16 +841,23 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    QLTG_CUDA(cudaLaunchKernelEx(&cfg, k_jacobi<T>, d_big.as<const JacobiJob>(), (int)kBigCluster, ws.as<T>(),
-                                 ws.as<T>(), sr_big.as<int>(), st_big.as<int>(), tol));
+    le = cudaLaunchKernelEx(&cfg, k_jacobi<T>, d_big.as<const JacobiJob>(), (int)kBigCluster, ws.as<T>(),
+                            jbuf.as<T>(), sr_big.as<int>(), st_big.as<int>(), tol, (int)kJacobiSmem);
   }
-  if (!small.empty()) {
-    k_jacobi<T><<<(unsigned)small.size(), kThreads, 0, s>>>(d_small.as<const JacobiJob>(), 1, ws.as<T>(), ws.as<T>(),
-                                                             sr_small.as<int>(), st_small.as<int>(), tol);
-    QLTG_CUDA(cudaGetLastError());
+  if (two) {
+    cudaEventRecord(join, s2);
+    cudaStreamWaitEvent(s, join, 0);
+    cudaEventDestroy(fork);
+    cudaEventDestroy(join);
+    cudaStreamDestroy(s2);   // released by the driver once its work is done
   }
-  DevBuf d_jobs = upload(jobs, s);
+  QLTG_CUDA(le);
+  // singular values and the right vectors from X; the left vectors W = Q J
+  DevBuf d_jobs = upload(xjobs, s);
   if (ng) {
+    k_qj<T><<<(unsigned)std::min<size_t>(std::max<size_t>(1, qtiles.size()), 152 * 8), 256, 0, s>>>(
+        d_pre.as<PrecondJob>(), d_qtiles.as<QjTile>(), (int)qtiles.size(), qbuf.as<T>(), jbuf.as<T>(), ws.as<T>());
+    QLTG_CUDA(cudaGetLastError());
     k_svd_finish<T><<<ng, kThreads, 0, s>>>(d_jobs.as<JacobiJob>(), ws.as<T>(), sv.as<double>(),
                                              d_svoff.as<int64_t>(), order.as<int32_t>());
     QLTG_CUDA(cudaGetLastError());
@@ -717,8 +953,10 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   out.buf[2].alloc(std::max<int64_t>(1, Vt.size) * eb);
 
   // ---- scatter U / Vt from the dense factors (one launch each); S from the host -----
-  // rows >= cols: W = A G, so U = normalised W and Vt = G^H.
-  // rows <  cols: W = A^T G, so A = conj(G) S W^T: U = conj(G) and Vt = W^T (normalised).
+  // With M = A (rows >= cols) or A^T (rows < cols) factorised as M = W S G^H (W = Q J in the
+  // W region, G = the normalised X in the V region):
+  // rows >= cols: U = W and Vt = G^H.
+  // rows <  cols: A = conj(G) S W^T: U = conj(G) and Vt = W^T.
   std::vector<ScatterDesc> su, sd;
   std::vector<int32_t> list;
   int64_t eu = 0, ev = 0;
