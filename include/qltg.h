@@ -148,6 +148,17 @@ QLTG_API int qltg_ctrct_plan_destroy(qltg_ctrct_plan* plan);
 QLTG_API int qltg_transpose(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev,
                    const int32_t* perm, void* dst_dev, void* stream);
 
+/* Reusable permute plan: the per-block work list of qltg_transpose for one tensor layout and
+ * permutation is built and uploaded once; each exec is one asynchronous kernel launch
+ * (no host work, no allocation). Replaces building an HPTT / cuTENSOR plan per block per
+ * call (framework/hp_numeric/ten_trans.h:56-114, :245-349). Same result as qltg_transpose
+ * (fermionic block signs included). */
+typedef struct qltg_transpose_plan qltg_transpose_plan;
+QLTG_API int qltg_transpose_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* a, const int32_t* perm, void* stream,
+                                        qltg_transpose_plan** plan);
+QLTG_API int qltg_transpose_plan_exec(qltg_transpose_plan* plan, const void* src_dev, void* dst_dev, void* stream);
+QLTG_API int qltg_transpose_plan_destroy(qltg_transpose_plan* plan);
+
 /* Same result as qltg_transpose, but allocates nothing: no cudaMalloc / cudaFree and no
  * allocating library call. No counterpart in the reference; it is for callers that cannot
  * allocate device memory while they run (for example code executing under another

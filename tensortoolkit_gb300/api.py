@@ -180,24 +180,57 @@ def Contract(a: DTensor, b: DTensor, axes: Sequence[Sequence[int]], mode="fp64")
     return plan.execute(a, b, mode=mode)
 
 
-def Transpose(t: DTensor, perm: Sequence[int]) -> DTensor:
-    """QLTensor::Transpose with fermionic block signs (qltensor/qltensor_impl.h:448-464)."""
-    perm = [int(x) for x in perm]
-    m = t.meta
+def _transposed_meta(m: BSTensor, perm: Sequence[int]) -> BSTensor:
     legs = [m.legs[i] for i in perm]
     coords = m.coords[:, perm]
-    tmp = BSTensor(legs, np.zeros((0, len(legs)), np.int64), m.dtype, None)
     idx = np.zeros(m.nblk, np.int64)
     for l, leg in enumerate(legs):
         idx = idx * leg.nsct + coords[:, l]
     order = np.argsort(idx, kind="stable")
-    meta = BSTensor(legs, coords[order], m.dtype, None)
+    return BSTensor(legs, coords[order], m.dtype, None)
+
+
+class TransposePlan:
+    """A reusable Transpose for one tensor layout and permutation: the block work list is
+    built once; `execute` is one asynchronous kernel launch."""
+
+    def __init__(self, meta: BSTensor, perm: Sequence[int], device: int = 0):
+        self.perm = [int(x) for x in perm]
+        self.device = device
+        self.meta = meta
+        self.result = _transposed_meta(meta, self.perm)
+        d = _Desc(meta)
+        p = np.asarray(self.perm, np.int32)
+        h = C.c_void_p()
+        check(lib().qltg_transpose_plan_create(context(device).h, d.ref, p.ctypes.data, stream_ptr(device),
+                                               C.byref(h)))
+        self.h = h
+
+    def execute(self, t: DTensor, out: Optional[DTensor] = None) -> DTensor:
+        if out is None:
+            out = DTensor.empty(self.result, self.device)
+        check(lib().qltg_transpose_plan_exec(self.h, C.c_void_p(t.ptr), C.c_void_p(out.ptr),
+                                             stream_ptr(self.device)))
+        return out
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().qltg_transpose_plan_destroy(self.h)
+        except Exception:
+            pass
+
+
+def Transpose(t: DTensor, perm: Sequence[int]) -> DTensor:
+    """QLTensor::Transpose with fermionic block signs (qltensor/qltensor_impl.h:448-464)."""
+    perm = [int(x) for x in perm]
+    m = t.meta
+    meta = _transposed_meta(m, perm)
     out = DTensor.empty(meta, t.device)
     d = _Desc(m)
     p = np.asarray(perm, np.int32)
     check(lib().qltg_transpose(context(t.device).h, d.ref, C.c_void_p(t.ptr), p.ctypes.data,
                                C.c_void_p(out.ptr), stream_ptr(t.device)))
-    del tmp
     return out
 
 

@@ -39,6 +39,9 @@ _SIGS = {
     "qltg_ctrct_plan_destroy": ([_P], C.c_int),
     "qltg_transpose": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
     "qltg_transpose_noalloc": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
+    "qltg_transpose_plan_create": ([_P, C.POINTER(TensorDesc), _P, _P, C.POINTER(_P)], C.c_int),
+    "qltg_transpose_plan_exec": ([_P, _P, _P, _P], C.c_int),
+    "qltg_transpose_plan_destroy": ([_P], C.c_int),
     "qltg_matvec_create": ([_P, C.POINTER(TensorDesc), _P, C.POINTER(TensorDesc), C.POINTER(TensorDesc), _P,
                             C.POINTER(TensorDesc), _P, C.POINTER(TensorDesc), _P, C.c_int32, _P,
                             C.POINTER(_P)], C.c_int),

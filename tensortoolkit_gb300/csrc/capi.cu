@@ -280,6 +280,48 @@ int qltg_transpose(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev
   });
 }
 
+int qltg_transpose_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* a, const int32_t* perm, void* stream,
+                               qltg_transpose_plan** plan) {
+  return guarded([&] {
+    QLTG_CHECK(ctx && plan, QLTG_ERR_INVALID, "null ctx or plan out-pointer");
+    Meta m = meta_from_desc(a);
+    QLTG_CHECK(m.rank == 0 || perm, QLTG_ERR_INVALID, "null perm");
+    std::vector<int> order(perm, perm + m.rank);
+    {
+      std::vector<int> chk(order);
+      std::sort(chk.begin(), chk.end());
+      for (int i = 0; i < m.rank; ++i) QLTG_CHECK(chk[i] == i, QLTG_ERR_INVALID, "perm is not a permutation");
+    }
+    QLTG_CUDA(cudaSetDevice(ctx->device));
+    auto h = std::make_unique<qltg_transpose_plan>();
+    h->ctx = ctx;
+    h->elem_bytes = (int)m.elem_bytes();
+    if (m.rank && m.nblk) {
+      std::vector<double> signs;
+      std::vector<int64_t> dst_off;
+      transpose_layout(m, order, signs, dst_off);
+      h->tl.build(m, order, signs, &dst_off, static_cast<cudaStream_t>(stream));
+      QLTG_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    }
+    *plan = h.release();
+  });
+}
+
+int qltg_transpose_plan_exec(qltg_transpose_plan* plan, const void* src_dev, void* dst_dev, void* stream) {
+  return guarded([&] {
+    QLTG_CHECK(plan, QLTG_ERR_INVALID, "null plan");
+    if (plan->tl.ntiles == 0) return;
+    QLTG_CHECK(src_dev && dst_dev && src_dev != dst_dev, QLTG_ERR_INVALID, "null or identical buffers");
+    QLTG_CUDA(cudaSetDevice(plan->ctx->device));
+    plan->tl.launch(src_dev, dst_dev, plan->elem_bytes, static_cast<cudaStream_t>(stream));
+  });
+}
+
+int qltg_transpose_plan_destroy(qltg_transpose_plan* plan) {
+  delete plan;
+  return QLTG_OK;
+}
+
 int qltg_transpose_noalloc(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev, const int32_t* perm,
                            void* dst_dev, void* stream) {
   return guarded([&] {

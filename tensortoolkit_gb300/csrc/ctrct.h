@@ -179,6 +179,12 @@ int host_exchange_sign(const bool* pa, int ra, const bool* pb, int rb, const int
 
 }  // namespace qltg
 
+struct qltg_transpose_plan {
+  qltg_ctx* ctx = nullptr;
+  int elem_bytes = 8;
+  qltg::TransposeList tl;
+};
+
 struct qltg_ctrct_plan {
   qltg::CtrctPlan p;
 };

@@ -178,3 +178,21 @@ def test_transpose_large_blocks(gpu):
         c = lenv.coords[b]
         ob = np.where((out.coords == c[[2, 1, 0]]).all(axis=1))[0][0]
         np.testing.assert_array_equal(out.block(int(ob)), np.transpose(lenv.block(b), (2, 1, 0)))
+
+
+@pytest.mark.parametrize("perm", [(0, 2, 3, 1), (3, 2, 1, 0)])
+def test_transpose_plan_matches_transpose(gpu, perm):
+    """A reusable plan gives Transpose's result bit for bit, on repeated executions and on a
+    second tensor of the same layout (fermionic complex tensor: block signs included)."""
+    from tensortoolkit_gb300.api import TransposePlan
+    lenv, psi, *_ = workloads.hubbard(300, 4, 9)
+    d = DTensor.from_host(psi)
+    plan = TransposePlan(psi, perm)
+    ref = Transpose(d, perm).to_host()
+    for _ in range(2):
+        got = plan.execute(d).to_host()
+        np.testing.assert_array_equal(got.coords, ref.coords)
+        np.testing.assert_array_equal(got.data, ref.data)
+    psi2 = BSTensor(psi.legs, psi.coords, psi.dtype, psi.data * 2.0)
+    got2 = plan.execute(DTensor.from_host(psi2)).to_host()
+    np.testing.assert_array_equal(got2.data, ref.data * 2.0)
