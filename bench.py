@@ -278,7 +278,7 @@ def time_call(fn, reps: int = 5) -> float:
     return statistics.median(ts)
 
 
-def run_aux(local: int):
+def run_aux(local: int, part: str = "all"):
     """Measurements beside the headline: the batched permute's achieved HBM bandwidth, the
     batched block SVD / QR (Config 3) against a per-block cuSOLVER loop on the same shapes
     (the reference GPU build's pattern), and the matvec of Configs 2 and 5."""
@@ -289,14 +289,14 @@ def run_aux(local: int):
     pk = peaks()
     out = {"aux": True, "gpu": torch.cuda.get_device_name(local)}
     dev = f"cuda:{local}"
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(local)
     # 1. permute: t0 of the D=4000 matvec (80 MB) to the order a contraction over its legs
     #    (0, 2) would use; every block moves (Transpose copies identity layouts too)
     lenv, psi, mpo1, mpo2, renv = workloads.heisenberg(WORKLOAD["D"], WORKLOAD["qmax"], WORKLOAD["sigma"],
                                                        WORKLOAD["seed"])
     t0 = Contract(DTensor.from_host(lenv, local), DTensor.from_host(psi, local), [[0], [0]])
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    stream = torch.cuda.current_stream(local)
-    for name, perm in (("t0 (w,l,p1,p2,r) -> (l,p2,r,w,p1)", (1, 3, 4, 0, 2)),
+    for name, perm in () if part not in ("all", "transpose") else (("t0 (w,l,p1,p2,r) -> (l,p2,r,w,p1)", (1, 3, 4, 0, 2)),
                        ("t0 (w,l,p1,p2,r) -> (r,p2,p1,l,w)", (4, 3, 2, 1, 0)),
                        ("t0 (w,l,p1,p2,r) -> (l,w,r,p1,p2)", (1, 0, 4, 2, 3))):
         plan = TransposePlan(t0.meta, perm, local)
@@ -314,8 +314,9 @@ def run_aux(local: int):
         del dst, plan
     del t0
     # 2. batched SVD / QR (Config 3 and the 41-block stress variant) vs per-block cuSOLVER
-    for name, t, ldims in (("Config 3: psi D=2000, 41 block-matrices", workloads.svd_psi(2000, 20, 6.0, 3), 2),
-                           ("stress: 41 square blocks 10..800", workloads.svd_stress(41, 10, 800, 3), 1)):
+    svd_cases = (("Config 3: psi D=2000, 41 block-matrices", workloads.svd_psi(2000, 20, 6.0, 3), 2),
+                 ("stress: 41 square blocks 10..800", workloads.svd_stress(41, 10, 800, 3), 1))
+    for name, t, ldims in svd_cases if part in ("all", "svd") else ():
         dt = DTensor.from_host(t, local)
         sv = time_call(lambda: SVD(dt, ldims, [0], 1e-9, 1, 2000))
         qr = time_call(lambda: QR(dt, ldims, [0]))
@@ -346,10 +347,11 @@ def run_aux(local: int):
         mv.device_status()
         f, _ = mv.stats()
         return {"mode": mode, "ms": round(ms, 4), "gflops": f / (ms / 1e3) / 1e9, "plan_s": round(t_create, 3)}
-    c2 = workloads.heisenberg(2000, 20, 6.0, 1)
-    out["config2_matvec_d2000"] = [mv_time(c2, "fp64"), mv_time(c2, "split")]
-    c5 = workloads.hubbard(6000, 10, 4)
-    out["config5_matvec_d6000_complex"] = [mv_time(c5, "fp64")]
+    if part in ("all", "matvec"):
+        c2 = workloads.heisenberg(2000, 20, 6.0, 1)
+        out["config2_matvec_d2000"] = [mv_time(c2, "fp64"), mv_time(c2, "split")]
+        c5 = workloads.hubbard(6000, 10, 4)
+        out["config5_matvec_d6000_complex"] = [mv_time(c5, "fp64")]
     print(json.dumps(out))
 
 
@@ -406,6 +408,7 @@ def main():
     ap.add_argument("--aux", action="store_true",
                     help="measurements beside the headline: permute GB/s, batched SVD/QR vs per-block, "
                          "Config 2 and Config 5 matvecs (one JSON line)")
+    ap.add_argument("--aux-part", choices=["all", "transpose", "svd", "matvec"], default="all")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: plan the D=4000 matvec, apply it twice, print nothing else")
     args = ap.parse_args()
@@ -437,7 +440,7 @@ def main():
     modes = ["split", "fp64"] if args.mode == "both" else [args.mode]
 
     if args.aux:
-        return run_aux(local)
+        return run_aux(local, args.aux_part)
 
     if args.profile:
         for m in modes:
