@@ -26,9 +26,8 @@ namespace qltg {
 namespace {
 
 constexpr int kTile = 32;
-constexpr int kTileElems = 1024;  // elements per (p, q) tile (Tp * Tq)
 constexpr int kTileMax = 4096;    // elements per batched tile (Tp * Tq * Tu)
-constexpr int kRunChunk = 1024;   // elements per copy-mode / gather-mode work item
+constexpr int kRunChunk = 4096;   // elements per copy-mode / gather-mode work item
 constexpr int kPermThreads = 256;
 constexpr int kLoadBatch = 8;     // tile-mode loads issued per thread before storing
 
@@ -53,9 +52,18 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
     const int mid = (lo + hi + 1) >> 1;
     if (descs[mid].tile_begin <= t_begin) lo = mid; else hi = mid - 1;
   }
+  // the current block's descriptor, staged in shared memory when the walk reaches a new block
+  __shared__ PermDesc sdesc;
+  int cur = -1;
   for (int64_t t = t_begin; t < t_end; ++t) {
     while (lo + 1 < nd && descs[lo + 1].tile_begin <= t) ++lo;
-    const PermDesc& d = descs[lo];
+    if (lo != cur) {   // uniform across the CTA: every thread walks the same items
+      __syncthreads();
+      if (threadIdx.x == 0) sdesc = descs[lo];
+      __syncthreads();
+      cur = lo;
+    }
+    const PermDesc& d = sdesc;
     const int64_t local = t - d.tile_begin;
     const int r = d.rank;
     const int q = r - 1;
@@ -88,6 +96,39 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
       }
       continue;
     }
+    if (d.p == q && d.tq > 1) {
+      // copy mode with short runs: a work item is d.tq consecutive runs (of dims[q] elements,
+      // contiguous on both sides); each warp copies whole runs, decoding one run's offsets
+      const uint32_t len = (uint32_t)d.dims[q];
+      const uint32_t nruns = (uint32_t)(d.nouter);
+      const uint32_t r0 = (uint32_t)local * (uint32_t)d.tq;
+      const uint32_t r1 = min(nruns, r0 + (uint32_t)d.tq);
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (uint32_t run = r0 + warp; run < r1; run += kPermThreads / 32) {
+        uint32_t rem = run;
+        int64_t soff = 0, doff = 0;
+        for (int i = r - 2; i >= 0; --i) {
+          const uint32_t di = (uint32_t)d.dims[i];
+          const uint32_t qq = rem / di;
+          const uint32_t x = rem - qq * di;
+          rem = qq;
+          soff += (int64_t)x * d.sstride[i];
+          doff += (int64_t)x * dstride[i];
+        }
+        const T* s = src + d.src_off + soff;
+        T* o = dst + d.dst_off + doff;
+        for (uint32_t e0 = lane; e0 < len; e0 += 32 * 4) {
+          T v[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if (e0 + 32 * i < len) v[i] = __ldg(s + e0 + 32 * i);
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if (e0 + 32 * i < len) o[e0 + 32 * i] = flip(v[i], sg);
+        }
+      }
+      continue;
+    }
     if (d.p == q) {
       // copy mode: innermost run of length dims[q] contiguous on both sides
       const uint32_t chunks_per_run = ((uint32_t)d.dims[q] + kRunChunk - 1) / kRunChunk;
@@ -107,13 +148,38 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
       T* o = dst + d.dst_off + doff;
       const int64_t n = min((int64_t)kRunChunk, (int64_t)d.dims[q] - c0);
       if (sizeof(T) == 8 && ((((uintptr_t)(s + c0)) | ((uintptr_t)(o + c0))) & 15) == 0) {
+        // 16-byte vectors, kLoadBatch loads in flight per thread before the stores
         const int64_t n2 = n >> 1;
         const double2* s2 = reinterpret_cast<const double2*>(s + c0);
         double2* o2 = reinterpret_cast<double2*>(o + c0);
-        for (int64_t e = threadIdx.x; e < n2; e += blockDim.x) o2[e] = flip(__ldg(s2 + e), sg);
+        for (int64_t e0 = threadIdx.x; e0 < n2; e0 += (int64_t)blockDim.x * kLoadBatch) {
+          double2 v[kLoadBatch];
+#pragma unroll
+          for (int i = 0; i < kLoadBatch; ++i) {
+            const int64_t e = e0 + (int64_t)i * blockDim.x;
+            if (e < n2) v[i] = __ldg(s2 + e);
+          }
+#pragma unroll
+          for (int i = 0; i < kLoadBatch; ++i) {
+            const int64_t e = e0 + (int64_t)i * blockDim.x;
+            if (e < n2) o2[e] = flip(v[i], sg);
+          }
+        }
         if ((n & 1) && threadIdx.x == 0) o[c0 + n - 1] = flip(s[c0 + n - 1], sg);
       } else {
-        for (int64_t e = threadIdx.x; e < n; e += blockDim.x) o[c0 + e] = flip(s[c0 + e], sg);
+        for (int64_t e0 = threadIdx.x; e0 < n; e0 += (int64_t)blockDim.x * kLoadBatch) {
+          T v[kLoadBatch];
+#pragma unroll
+          for (int i = 0; i < kLoadBatch; ++i) {
+            const int64_t e = e0 + (int64_t)i * blockDim.x;
+            if (e < n) v[i] = __ldg(s + c0 + e);
+          }
+#pragma unroll
+          for (int i = 0; i < kLoadBatch; ++i) {
+            const int64_t e = e0 + (int64_t)i * blockDim.x;
+            if (e < n) o[c0 + e] = flip(v[i], sg);
+          }
+        }
       }
       continue;
     }
@@ -198,7 +264,7 @@ void perm_set_smem_attr() {
 
 int pow2_at_least(int64_t x) {
   int v = 1;
-  while (v < x && v < kTileElems) v <<= 1;
+  while (v < x && v < kTileMax) v <<= 1;
   return v;
 }
 
@@ -260,7 +326,15 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
       tiles = 1;
     } else if (d.p == m - 1) {
       const int64_t runs = t.blk_size(b) / dd[m - 1];
-      tiles = runs * ((dd[m - 1] + kRunChunk - 1) / kRunChunk);
+      if (dd[m - 1] * 2 <= kRunChunk) {
+        // short runs: several per work item (tq = runs per item)
+        d.tq = (int32_t)std::max<int64_t>(2, kRunChunk / dd[m - 1]);
+        d.nouter = runs;
+        tiles = (runs + d.tq - 1) / d.tq;
+      } else {
+        d.tq = 1;
+        tiles = runs * ((dd[m - 1] + kRunChunk - 1) / kRunChunk);
+      }
     } else {
       // tile extents: 32 x 32, or stretched along the longer dim when the other is short
       int tp = -1, tq = -1;
@@ -270,10 +344,10 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
           tp = tq = kTile;
         } else if (a < kTile) {
           tp = a;
-          tq = std::min(c, kTileElems / a);
+          tq = std::min(c, kTileMax / a);
         } else {
           tq = c;
-          tp = std::min(a, kTileElems / c);
+          tp = std::min(a, kTileMax / c);
         }
       }
       if (tp < 0 || tp * tq < 64) {
