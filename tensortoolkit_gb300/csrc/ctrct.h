@@ -84,12 +84,10 @@ struct GemmSchedule {
 struct SplitOperand {
   int64_t src_off;        // element offset of the (transposed) FP64 block
   int64_t pack_off;       // byte offset of its packed slice tiles
-  int64_t vec_begin;      // prefix over operands of rows (A) / columns (B): exponent work items
-  int64_t chunk_begin;    // prefix over operands of 16-byte packing chunks
-  int64_t item_begin;     // B only: prefix of (column, 32-row chunk) exponent items
   int32_t rows, cols;     // A: m x k; B: k x n
   int32_t ktiles;         // 64-wide k tiles
-  int32_t exp_off;        // offset of its row (A) / column (B) exponents
+  int32_t exp_off;        // offset of its row (A) / column (B) exponent fields
+  int64_t chunk_begin;    // A: prefix over operands of 8-element chunks (row-scale kernel)
 };
 struct SplitTask {
   int64_t a_pack, b_pack;
@@ -122,8 +120,12 @@ struct SplitPlan {
   std::vector<SplitWork> work;    // per CTA: tiles blockIdx.x, + grid, ...; each its tasks
   std::vector<int32_t> work_off;  // grid + 1 offsets into work
   int grid = 0;
-  int64_t n_a_vec = 0, n_b_vec = 0, n_a_chunks = 0, n_b_chunks = 0, n_b_items = 0;
-  DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error;
+  std::vector<int2> a_row_tiles;  // (A operand, 128-row tile) items of the row-scale kernel
+  std::vector<int4> a_tiles;      // (A operand, 128-row tile, 64-wide k tile) items of the A pack
+  std::vector<int2> b_col_tiles;  // (B operand, 32-column tile) items of the B packing kernel
+  int row_exp_grid = 1, pack_a_grid = 1, pack_b_grid = 1;   // one wave of resident CTAs of each
+  int64_t n_a_chunks = 0, n_a_rows = 0;
+  DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_a_row_tiles, d_a_tiles, d_b_col_tiles;
   void build(const struct CtrctPlan& p, cudaStream_t s);
   int64_t launches() const;
 };
@@ -151,6 +153,9 @@ void exec_contraction(CtrctPlan& p, const void* a, const void* b, void* c, int m
 // grouped GEMM launchers (gemm_f64.cu)
 bool skinny_cblk(const GemmSchedule& g, int32_t q);
 int skinny_rows_per_item();
+// Grid of the skinny kernel: one full wave of resident CTAs (the first call queries the
+// occupancy; call it once outside any stream capture).
+int skinny_grid(int items, bool cplx, int num_sms);
 // Operand buffers of one execution: scratch (transposed blocks) and source (the operands as
 // passed in, for blocks flagged kFromSrc).
 struct Operands {

@@ -110,6 +110,7 @@ void finalize_plan(CtrctPlan& p, cudaStream_t s) {
       if (p.b_tl.identity[block_of(p.b, tk.b_off)]) tk.b_off |= kFromSrc;
     if (p.b_tl.ntiles) p.b_t.alloc(p.b.size * eb);
   }
+  if (!g.skinny.empty()) (void)skinny_grid((int)g.skinny.size(), p.a.dtype == QLTG_C128, p.ctx->num_sms);
   g.d_cblk = upload(g.cblk, s);
   g.d_task = upload(g.task, s);
   g.d_tile = upload(g.tile, s);

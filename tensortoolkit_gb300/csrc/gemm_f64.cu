@@ -151,8 +151,13 @@ __device__ __forceinline__ void skinny_row(const GemmCBlk& cb, const GemmTask* _
   for (int j = 0; j < NN; ++j) out[j] = acc[j];
 }
 
+// Resident CTAs per SM the kernel is compiled for: 6 for real operands (40 registers, no
+// spills); complex ones need their registers (1).
+template <typename T> struct SkinnyMinBlocks { static constexpr int value = 1; };
+template <> struct SkinnyMinBlocks<double> { static constexpr int value = 6; };
+
 template <typename T>
-__global__ void __launch_bounds__(kSkinnyRows) k_gemm_skinny(const GemmCBlk* __restrict__ cblk,
+__global__ void __launch_bounds__(kSkinnyRows, SkinnyMinBlocks<T>::value) k_gemm_skinny(const GemmCBlk* __restrict__ cblk,
                                                              const GemmTask* __restrict__ task,
                                                              const GemmRowChunk* __restrict__ items, int nitems,
                                                              const T* __restrict__ A, const T* __restrict__ As,
@@ -206,11 +211,26 @@ void launch_dfma_t(const GemmSchedule& g, const Operands& op, void* c, int grid,
                                      g.d_counter.as<int>());
 }
 
+// CTAs of one full wave: the grid-stride loop then has no partial second wave.
+template <typename T>
+int skinny_wave(int num_sms) {
+  static int per_sm = [] {
+    int n = 0;
+    QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_gemm_skinny<T>, kSkinnyRows, 0));
+    return std::max(1, n);
+  }();
+  return std::max(1, num_sms) * per_sm;
+}
+
+int skinny_grid(int items, bool cplx, int num_sms) {
+  return std::max(1, std::min(items, cplx ? skinny_wave<double2>(num_sms) : skinny_wave<double>(num_sms)));
+}
+
 void launch_gemm_f64_skinny(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms,
                             cudaStream_t s) {
   const int ns = (int)g.skinny.size();
   if (!ns) return;
-  const int grid = std::min(ns, std::max(1, num_sms) * 8);
+  const int grid = skinny_grid(ns, cplx, num_sms);
   if (cplx)
     launch_skinny_t<double2>(g, op, c, grid, s);
   else

@@ -54,196 +54,232 @@ constexpr int kDrainK = 128;               // k between drains (exactness bound)
 // Work distribution of the slicing kernels: CTA b takes the contiguous item range
 // [b per, (b + 1) per); a thread finds the operand owning its first item once and walks
 // forward from there (items only grow).
-struct ItemRange {
-  int64_t begin, end;
-};
-__device__ __forceinline__ ItemRange cta_range(int64_t total) {
-  const int64_t per = (total + gridDim.x - 1) / gridDim.x;
-  const int64_t b = (int64_t)blockIdx.x * per;
-  return ItemRange{b, min(total, b + per)};
+// Row / column scales are kept as exponent fields F: 0 for an all-zero row (column), else
+// max(1, largest biased exponent field of |x|), so that atomicMax can fold them. The scale
+// exponent is e = F - 1022 (max |x| < 2^e; subnormal-only rows use 2^-1021), 0 for F = 0.
+__device__ __forceinline__ int field_of_bits(uint64_t absbits) {
+  return absbits == 0 ? 0 : max(1, (int)(absbits >> 52));
 }
-template <typename F>
-__device__ __forceinline__ int first_op(int nops, int64_t item, F begin_of) {
-  int lo = 0, hi = nops - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (begin_of(mid) <= item) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
+__device__ __forceinline__ int exp_of_field(int f) { return f ? f - 1022 : 0; }
 
-// Row / column scale exponents: e with max |x| < 2^e (0 for an all-zero row).
-__device__ __forceinline__ int exp_of_bits(uint64_t absbits) {
-  if (absbits == 0) return 0;
-  const int ef = (int)(absbits >> 52);
-  return ef == 0 ? -1021 : ef - 1022;     // subnormals: treat as 2^-1022 scale
-}
-
-// A (m x k row-major): one warp per row.
-__global__ void k_row_exp(const double* __restrict__ scr, const double* __restrict__ src,
-                          const SplitOperand* __restrict__ ops, int nops, int32_t* __restrict__ exps,
-                          int64_t total_rows) {
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
-  const ItemRange rr = cta_range(total_rows);
-  auto vb = [&](int i) { return ops[i].vec_begin; };
-  int lo = first_op(nops, rr.begin + wib, vb);
-  for (int64_t rg = rr.begin + wib; rg < rr.end; rg += nwb) {
-    while (lo + 1 < nops && ops[lo + 1].vec_begin <= rg) ++lo;
-    const SplitOperand o = ops[lo];
-    const int64_t r = rg - o.vec_begin;
-    const double* row = operand_block(scr, src, o.src_off) + r * o.cols;
-    uint64_t mx = 0;
-#pragma unroll 4
-    for (int c = lane; c < o.cols; c += 32) {
-      const uint64_t b = (uint64_t)__double_as_longlong(__ldg(row + c)) & 0x7FFFFFFFFFFFFFFFull;
-      mx = b > mx ? b : mx;
-    }
-    for (int sft = 16; sft > 0; sft >>= 1) {
-      const uint64_t y = __shfl_xor_sync(0xffffffffu, mx, sft);
-      mx = y > mx ? y : mx;
-    }
-    if (lane == 0) exps[o.exp_off + r] = exp_of_bits(mx);
-  }
-}
-
-// B (k x n row-major): the scale of a column only depends on the largest exponent field in
-// it, so threads take (column, 32-row chunk) items and fold into the column with atomicMax
-// on the biased exponent (the array starts at zero); k_col_exp_finish turns fields into
-// scale exponents.
-__global__ void k_col_exp(const double* __restrict__ scr, const double* __restrict__ src,
-                          const SplitOperand* __restrict__ ops, int nops, int32_t* __restrict__ exps,
-                          int64_t total_items) {
-  const ItemRange rr = cta_range(total_items);
-  auto ib = [&](int i) { return ops[i].item_begin; };
-  int lo = first_op(nops, rr.begin + threadIdx.x, ib);
-  for (int64_t it = rr.begin + threadIdx.x; it < rr.end; it += blockDim.x) {
-    while (lo + 1 < nops && ops[lo + 1].item_begin <= it) ++lo;
-    const SplitOperand o = ops[lo];
-    const int64_t l = it - o.item_begin;
-    const int64_t c = l % o.cols, r0 = (l / o.cols) * 32;
-    int mx = 0;
-    const int64_t r1 = min((int64_t)o.rows, r0 + 32);
-    const double* blk = operand_block(scr, src, o.src_off);
-    for (int64_t r = r0; r < r1; ++r) {
-      const uint64_t b = (uint64_t)__double_as_longlong(blk[r * o.cols + c]) & 0x7FFFFFFFFFFFFFFFull;
-      const int f = b == 0 ? 0 : max(1, (int)(b >> 52));
-      mx = max(mx, f);
-    }
-    if (mx) atomicMax(&exps[o.exp_off + c], mx);
-  }
-}
-
-__global__ void k_col_exp_finish(int32_t* __restrict__ exps, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    exps[i] = exps[i] == 0 ? 0 : exps[i] - 1022;
-}
-
-// Seven 7-bit digits of x / 2^e (sign-magnitude), slice p weighted 2^(-7(p+1)), as BF16 bit patterns.
-__device__ __forceinline__ void slice7(double x, int e, uint16_t* out) {
+// |x| / 2^e as the 49-bit integer Y = floor(|x| 2^(49 - e)) and the sign as a BF16 sign bit.
+__device__ __forceinline__ uint64_t scaled_y(double x, int e, uint32_t& sgn) {
   const uint64_t bits = (uint64_t)__double_as_longlong(x);
   const uint64_t ab = bits & 0x7FFFFFFFFFFFFFFFull;
-  uint64_t Y = 0;
-  if (ab != 0) {
-    const int ex = (int)(ab >> 52);
-    const uint64_t mant = (ab & 0xFFFFFFFFFFFFFull) | (ex ? (1ull << 52) : 0ull);
-    const int ee = ex ? ex : 1;
-    // |x| = mant 2^(ee - 1075); Y = floor(|x| 2^(49 - e)) = mant >> (1075 + e - 49 - ee)
-    const int sh = 1026 + e - ee;
-    Y = sh >= 64 ? 0 : (mant >> sh);
+  sgn = (uint32_t)(bits >> 48) & 0x8000u;
+  if (ab == 0) return 0;
+  const int ex = (int)(ab >> 52);
+  const uint64_t mant = (ab & 0xFFFFFFFFFFFFFull) | (ex ? (1ull << 52) : 0ull);
+  const int sh = 1026 + e - (ex ? ex : 1);
+  return sh >= 64 ? 0 : (mant >> sh);
+}
+// Slice p of two elements as one word of two BF16 values: digit d = bits 7 (kS - 1 - p) ..
+// + 6 of Y, value d 2^(-7(p+1)) with the element's sign. The digit is or-ed into the
+// mantissa of 2^23 (float 2^23 + d), one FMA scales and removes the 2^23 exactly (d has at
+// most 7 significant bits, so the float's low 16 bits are zero and its high half is the
+// exact BF16), one byte permute takes both high halves.
+template <int P>
+__device__ __forceinline__ uint32_t digit_magic(uint64_t y) {
+  const uint32_t hi = (uint32_t)(y >> 32), lo = (uint32_t)y;
+  constexpr int sh = 7 * (kS - 1 - P);
+  uint32_t x;
+  if constexpr (sh >= 32) x = hi >> (sh - 32);
+  else if constexpr (sh + 7 > 32) x = __funnelshift_r(lo, hi, sh);
+  else x = lo >> sh;
+  return (x & 127u) | 0x4B000000u;
+}
+template <int P>
+__device__ __forceinline__ uint32_t plane_pair(uint64_t y0, uint64_t y1, uint32_t sgn_pair) {
+  const float scale = __uint_as_float((uint32_t)(127 - 7 * (P + 1)) << 23);
+  const float f0 = __fmaf_rn(__uint_as_float(digit_magic<P>(y0)), scale, -8388608.0f * scale);
+  const float f1 = __fmaf_rn(__uint_as_float(digit_magic<P>(y1)), scale, -8388608.0f * scale);
+  return __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632) | sgn_pair;
+}
+// The 7 slice planes of 8 consecutive elements, written as 16-byte words at dst + p stride.
+__device__ __forceinline__ void store_planes(const uint64_t* y, const uint32_t* sg, uint8_t* dst, int stride) {
+  const uint32_t s01 = sg[0] | (sg[1] << 16), s23 = sg[2] | (sg[3] << 16), s45 = sg[4] | (sg[5] << 16),
+                 s67 = sg[6] | (sg[7] << 16);
+#define QLTG_PLANE(P)                                                                           \
+  {                                                                                             \
+    uint4 v;                                                                                    \
+    v.x = plane_pair<P>(y[0], y[1], s01);                                                       \
+    v.y = plane_pair<P>(y[2], y[3], s23);                                                       \
+    v.z = plane_pair<P>(y[4], y[5], s45);                                                       \
+    v.w = plane_pair<P>(y[6], y[7], s67);                                                       \
+    *reinterpret_cast<uint4*>(dst + P * stride) = v;                                            \
   }
-  const uint16_t sgn = (uint16_t)((bits >> 48) & 0x8000u);
+  QLTG_PLANE(0) QLTG_PLANE(1) QLTG_PLANE(2) QLTG_PLANE(3) QLTG_PLANE(4) QLTG_PLANE(5) QLTG_PLANE(6)
+#undef QLTG_PLANE
+}
+
+// Row scales of A as exponent fields: every thread takes 8 consecutive elements of one
+// operand block (blocks are dense row-major m x k), folds the exponent fields of each row it
+// touches and adds them with atomicMax (one or two per thread unless the rows are short).
+// Operand blocks are laid end to end in units of 8-element chunks (chunk_begin).
+__global__ void __launch_bounds__(256) k_row_field(const double* __restrict__ scr, const double* __restrict__ src,
+                                                   const SplitOperand* __restrict__ ops, int nops,
+                                                   int64_t total_chunks, int32_t* __restrict__ fields) {
+  // contiguous chunk range per CTA, so a thread's chunks stay in one operand block or move
+  // to the next ones: one binary search, then a forward scan
+  const int64_t per = (total_chunks + gridDim.x - 1) / gridDim.x;
+  const int64_t cbeg = (int64_t)blockIdx.x * per, cend = min(total_chunks, cbeg + per);
+  int lo = 0;
+  {
+    int hi = nops - 1;
+    const int64_t first = cbeg + threadIdx.x;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ops[mid].chunk_begin <= first) lo = mid; else hi = mid - 1;
+    }
+  }
+  // uniform trip count across the CTA: the warp-wide match below needs all 32 lanes
+  for (int64_t base = cbeg; base < cend; base += blockDim.x) {
+    const int64_t ch = base + threadIdx.x;
+    const bool valid = ch < cend;
+    int k1 = -1, v1 = 0, k2 = -2, v2 = 0;
+    if (valid) {
+      while (lo + 1 < nops && ops[lo + 1].chunk_begin <= ch) ++lo;
+      const SplitOperand o = ops[lo];
+      const int n = o.rows * o.cols;   // one block: below 2^31 elements (checked on the host)
+      const int e0 = (int)(ch - o.chunk_begin) * 8;
+      const double* blk = operand_block(scr, src, o.src_off);
+      uint64_t v[8];
 #pragma unroll
-  for (int p = 0; p < kS; ++p) {
-    const uint32_t d = (uint32_t)((Y >> (7 * (kS - 1 - p))) & 127u);
-    // bf16 of d 2^(-7(p+1)) (exact): float(d) by the magic-number subtraction (FMA pipe,
-    // not the conversion unit), its bits >> 16, exponent field lowered by 7(p+1)
-    const uint32_t f = __float_as_uint(__uint_as_float(0x4B000000u | d) - 8388608.0f) >> 16;
-    out[p] = d ? (uint16_t)((f - ((uint32_t)(7 * (p + 1)) << 7)) | sgn) : (uint16_t)0;
+      for (int j = 0; j < 8; ++j) v[j] = e0 + j < n ? (uint64_t)__double_as_longlong(__ldg(blk + e0 + j)) : 0ull;
+      int r = e0 / o.cols;
+      int c = e0 - r * o.cols;
+      // the chunk's first row (r0, f0) and last row (r, f); rows strictly between (blocks
+      // with fewer than 8 columns) are added directly
+      const int r0 = r;
+      int f = 0, f0 = -1;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (e0 + j < n) {
+          if (c == o.cols) {
+            if (f0 < 0) f0 = f;
+            else if (f) atomicMax(fields + o.exp_off + r, f);
+            f = 0;
+            ++r;
+            c = 0;
+          }
+          f = max(f, field_of_bits(v[j] & 0x7FFFFFFFFFFFFFFFull));
+          ++c;
+        }
+      }
+      k1 = o.exp_off + r0;
+      v1 = f0 < 0 ? f : f0;
+      if (f0 >= 0) {
+        k2 = o.exp_off + r;
+        v2 = f;
+      }
+    }
+    // warp aggregation: lanes adding to the same row combine first, one lane adds
+    const int lane = threadIdx.x & 31;
+    const unsigned m1 = __match_any_sync(0xffffffffu, k1);
+    const int x1 = (int)__reduce_max_sync(m1, (unsigned)v1);
+    if (k1 >= 0 && x1 && lane == __ffs(m1) - 1) atomicMax(fields + k1, x1);
+    const unsigned m2 = __match_any_sync(0xffffffffu, k2);
+    const int x2 = (int)__reduce_max_sync(m2, (unsigned)v2);
+    if (k2 >= 0 && x2 && lane == __ffs(m2) - 1) atomicMax(fields + k2, x2);
   }
 }
 
-// Pack A operand tiles. One thread per 16-byte chunk (8 consecutive k of one row) per
-// (row tile, k tile); writes the chunk of every slice plane.
-__global__ void k_pack_a(const double* __restrict__ scr, const double* __restrict__ src,
-                         const SplitOperand* __restrict__ ops, int nops, const int32_t* __restrict__ exps,
-                         uint8_t* __restrict__ pack, int64_t total_chunks) {
-  const ItemRange rr = cta_range(total_chunks);
-  auto cbg = [&](int i) { return ops[i].chunk_begin; };
-  int lo = first_op(nops, rr.begin + threadIdx.x, cbg);
-  for (int64_t ch = rr.begin + threadIdx.x; ch < rr.end; ch += blockDim.x) {
-    while (lo + 1 < nops && ops[lo + 1].chunk_begin <= ch) ++lo;
-    const SplitOperand o = ops[lo];
-    const int64_t l = ch - o.chunk_begin;
-    // chunk order inside a (rt, kt) tile: ks (4), m_core (16), k_core (2), r8 (8) = 1024 chunks
-    const int64_t tile = l >> 10;
-    const int w = (int)(l & 1023);
-    const int ks = w >> 8, m_core = (w >> 4) & 15, k_core = (w >> 3) & 1, r8 = w & 7;
-    const int64_t rt = tile / o.ktiles, kt = tile % o.ktiles;
-    const int64_t r = rt * kTM + m_core * 8 + r8;
-    const int64_t k0 = kt * kTK + ks * 16 + k_core * 8;
-    if (r >= o.rows || k0 >= o.cols) continue;   // padding: the buffer was zeroed once
-    uint16_t sl[8][kS];
+// Slices of A, one CTA per (operand block, 128-row tile, 64-wide k tile): one thread per
+// 16-byte chunk (8 consecutive k of one row) writes the chunk of every slice plane. Runs
+// right after k_row_exp, whose pass over A left it in L2.
+__global__ void __launch_bounds__(256) k_pack_a(const double* __restrict__ scr, const double* __restrict__ src,
+                                                const SplitOperand* __restrict__ ops, const int4* __restrict__ tiles,
+                                                int ntiles, const int32_t* __restrict__ exps,
+                                                uint8_t* __restrict__ pack) {
+  for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+    const int4 tt = tiles[ti];   // operand, row tile, k tile
+    const SplitOperand o = ops[tt.x];
     const double* blk = operand_block(scr, src, o.src_off);
-    const int e = exps[o.exp_off + r];
+    for (int w = threadIdx.x; w < 1024; w += blockDim.x) {
+      // chunk order inside a (row tile, k tile): ks (4), m_core (16), k_core (2), r8 (8)
+      const int ks = w >> 8, m_core = (w >> 4) & 15, k_core = (w >> 3) & 1, r8 = w & 7;
+      const int64_t r = (int64_t)tt.y * kTM + m_core * 8 + r8;
+      const int64_t k0 = (int64_t)tt.z * kTK + ks * 16 + k_core * 8;
+      if (r >= o.rows || k0 >= o.cols) continue;   // padding: the buffer was zeroed once
+      const int e = exp_of_field(__ldg(exps + o.exp_off + r));
+      uint64_t y[8];
+      uint32_t sg[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const double x = (r < o.rows && k0 + j < o.cols) ? blk[r * o.cols + k0 + j] : 0.0;
-      slice7(x, e, sl[j]);
-    }
-    // tile layout [ks][slice][m_core][k_core][8 rows x 16 B]: the 7 slices of a 16-wide k
-    // step are contiguous, so a 32-wide stage is one 56 KB copy
-    const int64_t within = (int64_t)ks * (kS * 4096) + m_core * 256 + k_core * 128 + r8 * 16;
-#pragma unroll
-    for (int p = 0; p < kS; ++p) {
-      uint4 v;
-      v.x = (uint32_t)sl[0][p] | ((uint32_t)sl[1][p] << 16);
-      v.y = (uint32_t)sl[2][p] | ((uint32_t)sl[3][p] << 16);
-      v.z = (uint32_t)sl[4][p] | ((uint32_t)sl[5][p] << 16);
-      v.w = (uint32_t)sl[6][p] | ((uint32_t)sl[7][p] << 16);
-      *reinterpret_cast<uint4*>(pack + o.pack_off + tile * (int64_t)(kS * kATile) + within + p * 4096) = v;
+      for (int j = 0; j < 8; ++j) y[j] = scaled_y((k0 + j < o.cols) ? blk[r * o.cols + k0 + j] : 0.0, e, sg[j]);
+      // tile layout [ks][slice][m_core][k_core][8 rows x 16 B]: the 7 slices of a 16-wide k
+      // step are contiguous, so a 32-wide stage is one 56 KB copy
+      const int64_t tile = (int64_t)tt.y * o.ktiles + tt.z;
+      store_planes(y, sg, pack + o.pack_off + tile * (int64_t)(kS * kATile) + (int64_t)ks * (kS * 4096) + m_core * 256 +
+                              k_core * 128 + r8 * 16, 4096);
     }
   }
 }
 
-// Pack B operand tiles (k x n row-major source, K-major tiles of 32 columns).
-__global__ void k_pack_b(const double* __restrict__ scr, const double* __restrict__ src,
-                         const SplitOperand* __restrict__ ops, int nops, const int32_t* __restrict__ exps,
-                         uint8_t* __restrict__ pack, int64_t total_chunks) {
-  const ItemRange rr = cta_range(total_chunks);
-  auto cbg = [&](int i) { return ops[i].chunk_begin; };
-  int lo = first_op(nops, rr.begin + threadIdx.x, cbg);
-  for (int64_t ch = rr.begin + threadIdx.x; ch < rr.end; ch += blockDim.x) {
-    while (lo + 1 < nops && ops[lo + 1].chunk_begin <= ch) ++lo;
-    const SplitOperand o = ops[lo];
-    const int64_t l = ch - o.chunk_begin;
-    // chunk order inside a (ct, kt) tile: ks (4), n_core (4), k_core (2), n8 (8) = 256 chunks
-    const int64_t tile = l >> 8;
-    const int w = (int)(l & 255);
-    const int ks = w >> 6, n_core = (w >> 4) & 3, k_core = (w >> 3) & 1, n8 = w & 7;
-    const int64_t ct = tile / o.ktiles, kt = tile % o.ktiles;
-    const int64_t c = ct * kTN + n_core * 8 + n8;        // output column (B column)
-    const int64_t k0 = kt * kTK + ks * 16 + k_core * 8;  // B row
-    if (c >= o.cols || k0 >= o.rows) continue;   // padding: the buffer was zeroed once
-    uint16_t sl[8][kS];
+// Column scales and slices of B (k x n row-major), one CTA per (operand block, 32-column
+// tile). Phase 1: thread (row group g, column c) folds rows g, g + 8, ... of its column (a
+// warp reads 32 consecutive columns of one row); the 8 partial maxima per column meet in
+// shared memory. Phase 2: one thread per 16-byte chunk (8 consecutive k of one column) of
+// every 64-wide k tile writes the chunk of every slice plane.
+__global__ void __launch_bounds__(256) k_pack_b_cols(const double* __restrict__ scr, const double* __restrict__ src,
+                                                     const SplitOperand* __restrict__ ops,
+                                                     const int2* __restrict__ col_tiles, int ntiles,
+                                                     int32_t* __restrict__ exps, uint8_t* __restrict__ pack) {
+  __shared__ uint64_t smx[8][kTN];
+  __shared__ int se[kTN];
+  const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+    const int2 tt = col_tiles[ti];
+    const SplitOperand o = ops[tt.x];
     const double* blk = operand_block(scr, src, o.src_off);
-    const int e = exps[o.exp_off + c];
+    const int c0 = tt.y * kTN;
+    const int nc = min(kTN, o.cols - c0);
+    uint64_t mx = 0;
+    if (lane < nc) {
+      const double* col = blk + c0 + lane;
+      for (int r = g; r < o.rows; r += 32) {
+        uint64_t v[4];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const double x = (c < o.cols && k0 + j < o.rows) ? blk[(k0 + j) * o.cols + c] : 0.0;
-      slice7(x, e, sl[j]);
-    }
-    // tile layout [ks][slice][n_core][k_core][8 columns x 16 B]: the 7 slices of a 16-wide k
-    // step form one 224-row K-major operand (slice q = rows 32 (q-1) .. 32 q - 1)
-    const int64_t within = (int64_t)ks * (kS * 1024) + n_core * 256 + k_core * 128 + n8 * 16;
+        for (int u = 0; u < 4; ++u)
+          v[u] = r + 8 * u < o.rows ? (uint64_t)__double_as_longlong(__ldg(col + (int64_t)(r + 8 * u) * o.cols)) : 0ull;
 #pragma unroll
-    for (int p = 0; p < kS; ++p) {
-      uint4 v;
-      v.x = (uint32_t)sl[0][p] | ((uint32_t)sl[1][p] << 16);
-      v.y = (uint32_t)sl[2][p] | ((uint32_t)sl[3][p] << 16);
-      v.z = (uint32_t)sl[4][p] | ((uint32_t)sl[5][p] << 16);
-      v.w = (uint32_t)sl[6][p] | ((uint32_t)sl[7][p] << 16);
-      *reinterpret_cast<uint4*>(pack + o.pack_off + tile * (int64_t)(kS * kBTile) + within + p * 1024) = v;
+        for (int u = 0; u < 4; ++u) {
+          const uint64_t b1 = v[u] & 0x7FFFFFFFFFFFFFFFull;
+          mx = b1 > mx ? b1 : mx;
+        }
+      }
     }
+    smx[g][lane] = mx;
+    __syncthreads();
+    if (threadIdx.x < kTN) {
+      uint64_t m = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) m = smx[q][threadIdx.x] > m ? smx[q][threadIdx.x] : m;
+      const int f = field_of_bits(m);
+      se[threadIdx.x] = exp_of_field(f);
+      if ((int)threadIdx.x < nc) exps[o.exp_off + c0 + threadIdx.x] = f;
+    }
+    __syncthreads();
+    const int nch = o.ktiles * 256;
+    for (int l = threadIdx.x; l < nch; l += blockDim.x) {
+      // chunk order inside a (column tile, k tile): ks (4), n_core (4), k_core (2), n8 (8)
+      const int kt = l >> 8, w = l & 255;
+      const int ks = w >> 6, n_core = (w >> 4) & 3, k_core = (w >> 3) & 1, n8 = w & 7;
+      const int cc = n_core * 8 + n8;
+      const int64_t k0 = (int64_t)kt * kTK + ks * 16 + k_core * 8;
+      if (cc >= nc || k0 >= o.rows) continue;   // padding: the buffer was zeroed once
+      const int e = se[cc];
+      const double* col = blk + c0 + cc;
+      uint64_t y[8];
+      uint32_t sg[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) y[j] = scaled_y((k0 + j < o.rows) ? col[(k0 + j) * o.cols] : 0.0, e, sg[j]);
+      // tile layout [ks][slice][n_core][k_core][8 columns x 16 B]: the 7 slices of a 16-wide k
+      // step form one 224-row K-major operand (slice q = rows 32 (q-1) .. 32 q - 1)
+      const int64_t tile = (int64_t)tt.y * o.ktiles + kt;
+      store_planes(y, sg, pack + o.pack_off + tile * (int64_t)(kS * kBTile) + (int64_t)ks * (kS * 1024) + n_core * 256 +
+                              k_core * 128 + n8 * 16, 1024);
+    }
+    __syncthreads();   // smx / se are rewritten by the next column tile
   }
 }
 
@@ -595,10 +631,10 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
       const int nst = (w.k + kKS - 1) / kKS;
       if (w.flags & 1) written = false;
       // scale exponents, fetched while the first period is still on the tensor cores
-      const int ea = row < w.m ? aexp[w.a_exp + row] : 0;
+      const int ea = row < w.m ? exp_of_field(aexp[w.a_exp + row]) : 0;
       int eb[kDrainCols];
 #pragma unroll
-      for (int c = 0; c < kDrainCols; ++c) eb[c] = col0 + c < w.n ? bexp[w.b_exp + col0 + c] : 0;
+      for (int c = 0; c < kDrainCols; ++c) eb[c] = col0 + c < w.n ? exp_of_field(bexp[w.b_exp + col0 + c]) : 0;
       long long z[kDrainCols];
       // the task's periods in chunks of kFlushDrains, each folded on its own, so the int64
       // sums stay in range for any k
@@ -645,9 +681,6 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemAlloc));
 }
 
-unsigned grid_for(int64_t n, int bs = 256) {
-  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + bs - 1) / bs, 152 * 32));
-}
 
 }  // namespace
 
@@ -661,7 +694,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   b_ops.clear();
   tasks.clear();
   tiles.clear();
-  int64_t a_pack = 0, b_pack = 0, a_exp = 0, b_exp = 0, a_vec = 0, b_vec = 0, a_chunks = 0, b_chunks = 0, b_items = 0;
+  int64_t a_pack = 0, b_pack = 0, a_exp = 0, b_exp = 0, a_chunks = 0;
   auto a_index = [&](int64_t a_off) {   // block ordinal from its offset
     return (int64_t)(std::lower_bound(p.a.offsets.begin(), p.a.offsets.end(), a_off) - p.a.offsets.begin());
   };
@@ -684,13 +717,12 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
         o.cols = k;
         o.ktiles = ktiles;
         o.exp_off = (int32_t)a_exp;
-        o.vec_begin = a_vec;
-        o.chunk_begin = a_chunks;
         o.pack_off = a_pack;
+        o.chunk_begin = a_chunks;
+        QLTG_CHECK((int64_t)cb.m * k < ((int64_t)1 << 31) - 8, QLTG_ERR_UNSUPPORTED, "operand block too large");
         const int64_t rtiles = (cb.m + kTM - 1) / kTM;
         a_exp += cb.m;
-        a_vec += cb.m;
-        a_chunks += rtiles * ktiles * 1024;
+        a_chunks += ((int64_t)cb.m * k + 7) / 8;
         a_pack += rtiles * ktiles * kS * (int64_t)kATile;
         a_of[ia] = (int32_t)a_ops.size();
         a_ops.push_back(o);
@@ -702,15 +734,9 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
         o.cols = cb.n;
         o.ktiles = ktiles;
         o.exp_off = (int32_t)b_exp;
-        o.vec_begin = b_vec;
-        o.item_begin = b_items;
-        o.chunk_begin = b_chunks;
         o.pack_off = b_pack;
         const int64_t ctiles = (cb.n + kTN - 1) / kTN;
         b_exp += cb.n;
-        b_vec += cb.n;
-        b_items += (int64_t)cb.n * ((k + 31) / 32);
-        b_chunks += ctiles * ktiles * 256;
         b_pack += ctiles * ktiles * kS * (int64_t)kBTile;
         b_of[ib] = (int32_t)b_ops.size();
         b_ops.push_back(o);
@@ -763,11 +789,30 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
     QLTG_CHECK(work.size() < ((size_t)1 << 31), QLTG_ERR_UNSUPPORTED, "too many split work items");
   }
   work_off[grid] = (int32_t)work.size();
-  n_a_vec = a_vec;
-  n_b_vec = b_vec;
+  a_row_tiles.clear();
+  for (int i = 0; i < (int)a_ops.size(); ++i)
+    for (int rt = 0; rt * kTM < a_ops[i].rows; ++rt) a_row_tiles.push_back(make_int2(i, rt));
+  d_a_row_tiles = upload(a_row_tiles, s);
+  b_col_tiles.clear();
+  for (int i = 0; i < (int)b_ops.size(); ++i)
+    for (int ct = 0; ct * kTN < b_ops[i].cols; ++ct) b_col_tiles.push_back(make_int2(i, ct));
+  d_b_col_tiles = upload(b_col_tiles, s);
   n_a_chunks = a_chunks;
-  n_b_chunks = b_chunks;
-  n_b_items = b_items;
+  a_tiles.clear();
+  for (int i = 0; i < (int)a_ops.size(); ++i)
+    for (int rt = 0; rt * kTM < a_ops[i].rows; ++rt)
+      for (int kt = 0; kt < a_ops[i].ktiles; ++kt) a_tiles.push_back(make_int4(i, rt, kt, 0));
+  d_a_tiles = upload(a_tiles, s);
+  {
+    int per_sm = 0;
+    QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_field, 256, 0));
+    row_exp_grid = (int)std::max<int64_t>(1, std::min<int64_t>((n_a_chunks + 255) / 256,
+                                                               (int64_t)std::max(1, per_sm) * p.ctx->num_sms));
+    QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pack_a, 256, 0));
+    pack_a_grid = std::max(1, std::min((int)a_tiles.size(), std::max(1, per_sm) * p.ctx->num_sms));
+    QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pack_b_cols, 256, 0));
+    pack_b_grid = std::max(1, std::min((int)b_col_tiles.size(), std::max(1, per_sm) * p.ctx->num_sms));
+  }
   d_a_ops = upload(a_ops, s);
   d_b_ops = upload(b_ops, s);
   d_work = upload(work, s);
@@ -778,6 +823,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   // kernels only write the chunks that hold operand data
   QLTG_CUDA(cudaMemsetAsync(a_packed.get(), 0, std::max<int64_t>(a_pack, 16), s));
   QLTG_CUDA(cudaMemsetAsync(b_packed.get(), 0, std::max<int64_t>(b_pack, 16), s));
+  n_a_rows = a_exp;
   a_exps.alloc(std::max<int64_t>(a_exp, 1) * 4);
   b_exps.alloc(std::max<int64_t>(b_exp, 1) * 4);
   error.alloc(sizeof(int));
@@ -790,7 +836,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
 
 int64_t SplitPlan::launches() const {
   if (tiles.empty()) return 0;
-  return (a_static ? 0 : 2) + (b_static ? 0 : 4) + 1;   // per side: (memset,) exps, (finish,) pack; GEMM
+  return (a_static ? 0 : 3) + (b_static ? 0 : 1) + 1;   // A: memset, row scales, pack; B: pack; GEMM
 }
 
 // Scale exponents and slice tiles of one operand side (A: rows, B: columns), reading each
@@ -799,21 +845,23 @@ void pack_split_operand(SplitPlan& sp, bool side_a, const void* scratch, const v
   const double* X = static_cast<const double*>(scratch);
   const double* Xs = static_cast<const double*>(source);
   if (side_a) {
-    if (sp.a_ops.empty()) return;
-    k_row_exp<<<grid_for(sp.n_a_vec * 32), 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
-                                                        sp.a_exps.as<int32_t>(), sp.n_a_vec);
-    k_pack_a<<<grid_for(sp.n_a_chunks), 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
-                                                     sp.a_exps.as<int32_t>(), sp.a_packed.as<uint8_t>(),
-                                                     sp.n_a_chunks);
+    if (sp.a_ops.empty()) {
+      sp.a_ready = true;
+      return;
+    }
+    QLTG_CUDA(cudaMemsetAsync(sp.a_exps.get(), 0, sp.n_a_rows * sizeof(int32_t), s));
+    k_row_field<<<sp.row_exp_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+                                                sp.n_a_chunks, sp.a_exps.as<int32_t>());
+    k_pack_a<<<sp.pack_a_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), sp.d_a_tiles.as<int4>(),
+                                            (int)sp.a_tiles.size(), sp.a_exps.as<int32_t>(), sp.a_packed.as<uint8_t>());
   } else {
-    if (sp.b_ops.empty()) return;
-    QLTG_CUDA(cudaMemsetAsync(sp.b_exps.get(), 0, sp.n_b_vec * sizeof(int32_t), s));
-    k_col_exp<<<grid_for(sp.n_b_items), 256, 0, s>>>(X, Xs, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
-                                                     sp.b_exps.as<int32_t>(), sp.n_b_items);
-    k_col_exp_finish<<<grid_for(sp.n_b_vec), 256, 0, s>>>(sp.b_exps.as<int32_t>(), sp.n_b_vec);
-    k_pack_b<<<grid_for(sp.n_b_chunks), 256, 0, s>>>(X, Xs, sp.d_b_ops.as<SplitOperand>(), (int)sp.b_ops.size(),
-                                                     sp.b_exps.as<int32_t>(), sp.b_packed.as<uint8_t>(),
-                                                     sp.n_b_chunks);
+    if (sp.b_ops.empty()) {
+      sp.b_ready = true;
+      return;
+    }
+    const int nt = (int)sp.b_col_tiles.size();
+    k_pack_b_cols<<<sp.pack_b_grid, 256, 0, s>>>(X, Xs, sp.d_b_ops.as<SplitOperand>(), sp.d_b_col_tiles.as<int2>(), nt,
+                                                 sp.b_exps.as<int32_t>(), sp.b_packed.as<uint8_t>());
   }
   QLTG_CUDA(cudaGetLastError());
   (side_a ? sp.a_ready : sp.b_ready) = true;
@@ -850,7 +898,8 @@ void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s
   }
   SplitPlan& sp = *p.split;
   // skinny output blocks stay on the FP64 skinny kernel (k, n <= 8: the tensor cores would
-  // pad them 8x); everything else goes through the slices
+  // pad them 8x, and exact integer emulation of these rows measured slower than the FP64
+  // pipe); everything else goes through the slices
   launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, s);
   if (sp.tiles.empty()) return;
   if (pack) {

@@ -50,8 +50,11 @@ int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* 
       finalize_plan(p, s);
       if (mode == QLTG_MODE_SPLIT) {
         prepare_split(p, s);
-        // lenv (A of the first step) and renv (B of the last) are constant for the matvec's life
+        // lenv (A of the first step), the MPO tensors and renv (B of the later steps) are
+        // constant for the matvec's life
         if (i == 0) split_prepack_static(p, h->lenv, nullptr, s);
+        if (i == 1) split_prepack_static(p, nullptr, h->mpo1, s);
+        if (i == 2) split_prepack_static(p, nullptr, h->mpo2, s);
         if (i == 3) split_prepack_static(p, nullptr, h->renv, s);
       }
       if (i < 3) h->t[i].alloc(std::max<int64_t>(1, p.c.size) * p.c.elem_bytes());
