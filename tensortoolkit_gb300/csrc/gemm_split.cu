@@ -35,6 +35,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <queue>
 #include <cstring>
 
 #include "scaled_int.h"
@@ -752,19 +753,32 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
       for (int j = 0; j < ctiles; ++j) tiles.push_back(GemmTile{q, (int16_t)i, (int16_t)j});
   }
   QLTG_CHECK(tiles.size() < ((size_t)1 << 31), QLTG_ERR_UNSUPPORTED, "too many split tiles");
-  // longest first: tiles of blocks with more k tiles
+  // Per-CTA work lists by longest processing time first: tiles in decreasing cost, each to
+  // the CTA with the least work so far. Cost of a tile: 2 per 32-wide k stage plus 1 per
+  // task (the drain and rounding that end a task).
   std::vector<int64_t> cost(g.cblk.size(), 0);
   for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q)
-    for (int32_t t = g.cblk[q].t0; t < g.cblk[q].t1; ++t) cost[q] += (g.task[t].k + 31) / 32;
+    for (int32_t t = g.cblk[q].t0; t < g.cblk[q].t1; ++t) cost[q] += 2 * ((g.task[t].k + 31) / 32) + 1;
   std::stable_sort(tiles.begin(), tiles.end(), [&](const GemmTile& x, const GemmTile& y) { return cost[x.cblk] > cost[y.cblk]; });
-  // per-CTA work lists: CTA b takes tiles b, b + grid, ... (longest first), each with the
-  // tasks of its output block in order
   grid = (int)std::min<int64_t>((int64_t)tiles.size(), std::max(1, p.ctx->num_sms));
+  std::vector<std::vector<int32_t>> owned(grid);
+  {
+    using Load = std::pair<int64_t, int>;   // (work so far, CTA)
+    std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
+    for (int b = 0; b < grid; ++b) heap.push({0, b});
+    for (size_t ti = 0; ti < tiles.size(); ++ti) {
+      Load l = heap.top();
+      heap.pop();
+      owned[l.second].push_back((int32_t)ti);
+      l.first += cost[tiles[ti].cblk];
+      heap.push(l);
+    }
+  }
   work.clear();
   work_off.assign(grid + 1, 0);
   for (int b = 0; b < grid; ++b) {
     work_off[b] = (int32_t)work.size();
-    for (size_t ti = b; ti < tiles.size(); ti += grid) {
+    for (const int32_t ti : owned[b]) {
       const GemmTile& tl = tiles[ti];
       const GemmCBlk& cb = g.cblk[tl.cblk];
       for (int32_t t = cb.t0; t < cb.t1; ++t) {
