@@ -39,7 +39,10 @@ enum {
   QLTG_ERR_TIMEOUT = 4,      /* a bounded device-side wait expired */
   QLTG_ERR_NOCONV = 5,       /* an iterative decomposition did not converge */
   QLTG_ERR_EMPTY_SVD = 6,    /* no block fits lqndiv: reference EmptySVDResultError */
-  QLTG_ERR_UNSUPPORTED = 7   /* valid input outside what this build implements */
+  QLTG_ERR_UNSUPPORTED = 7,  /* valid input outside what this build implements */
+  QLTG_ERR_LAYOUT = 8        /* accumulate: the output's indexes differ from the contraction
+                                result, or it lacks result blocks and expansion is off
+                                (reference ContractAccumulateLayoutMismatch) */
 };
 
 enum { QLTG_F64 = 0, QLTG_C128 = 1 };     /* element types */
@@ -137,6 +140,48 @@ QLTG_API int qltg_ctrct_exec_stage(qltg_ctrct_plan* plan, const void* a_dev, con
 QLTG_API int qltg_ctrct_plan_device_status(qltg_ctrct_plan* plan, void* stream);
 
 QLTG_API int qltg_ctrct_plan_destroy(qltg_ctrct_plan* plan);
+
+/* ------------------------------------------------ contiguous-axes contraction, accumulation */
+enum { QLTG_SIDE_HEAD = 0, QLTG_SIDE_TAIL = 1 };
+
+/* Plan for ContractContiguousAxes<ASide, BSide>(A, B, a_start, b_start, n, C) (reference
+ * tensor_manipulation/contract_contiguous_axes.h:849-868): A's axes (a_start + i) mod rank_A
+ * against B's (b_start + i) mod rank_B, i < n; C's legs are A's saved legs then B's, each in
+ * cyclic order from the end of its contracted range (a fermionic block whose saved legs leave
+ * ascending order takes that reordering's sign, as the reference's residue sign,
+ * qltensor/blk_spar_data_ten/data_blk_operations.h:580-611). a_side / b_side
+ * (QLTG_SIDE_HEAD / QLTG_SIDE_TAIL) are the reference's layout hints; the result does not
+ * depend on them. The returned plan is a contraction plan: query and execute it with
+ * qltg_ctrct_plan_result / _result_blocks / qltg_ctrct_exec. */
+QLTG_API int qltg_ctrct_plan_create_contiguous(qltg_ctx* ctx, const qltg_tensor_desc* a, const qltg_tensor_desc* b,
+                                               int64_t a_start, int64_t b_start, int32_t n, int32_t a_side,
+                                               int32_t b_side, qltg_ctrct_plan** plan);
+
+typedef struct qltg_accum_plan qltg_accum_plan;
+
+/* Plan for C = beta C + alpha A.B with the tail/head contiguous contraction of
+ * ContractTailHeadContiguousAccumulate (allow_expand = 1) or
+ * TryContractTailHeadContiguousAccumulate (allow_expand = 0)
+ * (contract_contiguous_axes.h:953-1040; executor :333-472, :557-783).
+ * c_in NULL: C is default (exec then needs beta == 0) and the output is the contraction's
+ * topology. Otherwise c_in's legs must equal the contraction result's (else
+ * QLTG_ERR_LAYOUT); its blocks may be a superset. If it lacks result blocks the output is
+ * the union topology (*expanded = 1) or, with allow_expand = 0, QLTG_ERR_LAYOUT and no plan
+ * (the reference's Try form returning false). */
+QLTG_API int qltg_accum_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* a, const qltg_tensor_desc* b,
+                                    int64_t a_start, int64_t b_start, int32_t n, const qltg_tensor_desc* c_in,
+                                    int32_t allow_expand, qltg_accum_plan** plan, int32_t* expanded);
+/* Output topology: rank, blocks, elements (scalar outputs: 1 element). */
+QLTG_API int qltg_accum_plan_result(const qltg_accum_plan* plan, int32_t* rank, int64_t* nblk, int64_t* size);
+QLTG_API int qltg_accum_plan_result_blocks(const qltg_accum_plan* plan, int64_t* coords, int64_t* offsets);
+/* c_out_dev = beta c_in_dev + alpha A.B (alpha, beta: {re, im}; imaginary parts must be 0
+ * for FP64 tensors). Blocks of the old C the contraction does not touch are scaled by beta,
+ * new blocks get alpha A.B; beta == 0 never reads c_in_dev. c_out_dev may be c_in_dev unless
+ * the output was expanded. mode: QLTG_MODE_FP64 or QLTG_MODE_SPLIT (real tensors). */
+QLTG_API int qltg_accum_exec(qltg_accum_plan* plan, const void* a_dev, const void* b_dev, const void* c_in_dev,
+                             void* c_out_dev, const double* alpha, const double* beta, int32_t mode, void* stream);
+QLTG_API int qltg_accum_plan_device_status(qltg_accum_plan* plan, void* stream);
+QLTG_API int qltg_accum_plan_destroy(qltg_accum_plan* plan);
 
 /* ---------------------------------------------------------------- transpose */
 /* dst = A transposed to leg order `perm` (new leg i = old leg perm[i]), blocks reordered to

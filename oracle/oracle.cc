@@ -20,6 +20,15 @@
 //    C_blk = sign * A_t B_t + beta * C_blk with a row-major dgemm/zgemm
 //      raw_data_operation_tasks.h:250-269, global_operations.h:895-992,
 //      raw_data_operations.h:530-548, framework/hp_numeric/blas_level3.h:35-56
+//  * contiguous-axes contraction: contracted axes (start + i) mod rank, saved axes in the
+//    cyclic order from the end of the contracted range; a fermionic block whose saved legs
+//    come out of ascending order takes the sign of that reordering (-1 per pair of odd legs
+//    that trade places: the residue sign of the reference's rotated matrix view)
+//      tensor_manipulation/contract_contiguous_axes.h:305-472, :849-868,
+//      qltensor/blk_spar_data_ten/data_blk_operations.h:580-611
+//  * accumulate: C = beta C + alpha A.B over the union of C's blocks and the contraction's;
+//    beta = 0 never reads C; a missing block is an error unless expansion is allowed
+//      tensor_manipulation/contract_contiguous_axes.h:557-783, :953-1040
 //  * SVD: block-matrices grouped by (left flux, right flux) in first-appearance order,
 //    dense gather, LAPACKE ?gesvd('S','S'), global descending sort, keep from Dmin while
 //    kept_sv2 <= (1 - eps) total and <= Dmax, result tensors U / S / Vt
@@ -275,6 +284,15 @@ std::vector<int64_t> saved_axes(int rank, const std::vector<int64_t>& ctrct) {
   return s;
 }
 
+// Sign of reordering a block's saved legs from ascending leg order to `order`.
+int saved_order_sign(const std::vector<bool>& par, const std::vector<int64_t>& order) {
+  int n = 0;
+  for (size_t i = 0; i < order.size(); ++i)
+    for (size_t j = i + 1; j < order.size(); ++j)
+      if (order[i] > order[j] && par[order[i]] && par[order[j]]) ++n;
+  return (n & 1) ? -1 : 1;
+}
+
 bool is_identity(const std::vector<int64_t>& first, const std::vector<int64_t>& second) {
   for (size_t i = 0; i < first.size(); ++i) if (first[i] != (int64_t)i) return false;
   for (size_t i = 0; i < second.size(); ++i) if (second[i] != (int64_t)(i + first.size())) return false;
@@ -283,9 +301,8 @@ bool is_identity(const std::vector<int64_t>& first, const std::vector<int64_t>& 
 
 template <typename T>
 void run_tasks(const Tensor& a, const Tensor& b, const std::vector<int64_t>& axa, const std::vector<int64_t>& axb,
-               CtrctOut& out) {
+               const std::vector<int64_t>& sa, const std::vector<int64_t>& sb, CtrctOut& out) {
   Tensor& c = out.c;
-  const auto sa = saved_axes(a.rank(), axa), sb = saved_axes(b.rank(), axb);
   std::vector<int64_t> a_order = sa, b_order = axb;
   a_order.insert(a_order.end(), axa.begin(), axa.end());
   b_order.insert(b_order.end(), sb.begin(), sb.end());
@@ -333,7 +350,9 @@ void run_tasks(const Tensor& a, const Tensor& b, const std::vector<int64_t>& axa
   }
 }
 
-CtrctOut contract(const Tensor& a, const Tensor& b, const std::vector<int64_t>& axa, const std::vector<int64_t>& axb) {
+// sa_order / sb_order: the saved legs in the order they take in C (empty: ascending).
+CtrctOut contract(const Tensor& a, const Tensor& b, const std::vector<int64_t>& axa, const std::vector<int64_t>& axb,
+                  const std::vector<int64_t>& sa_order = {}, const std::vector<int64_t>& sb_order = {}) {
   if (axa.size() != axb.size()) throw std::runtime_error("oracle: axes size mismatch");
   if (a.is_complex != b.is_complex) throw std::runtime_error("oracle: mixed element types");
   CtrctOut out;
@@ -341,7 +360,8 @@ CtrctOut contract(const Tensor& a, const Tensor& b, const std::vector<int64_t>& 
   c.ncomp = a.ncomp;
   c.parity_comp = a.parity_comp;
   c.is_complex = a.is_complex;
-  const auto sa = saved_axes(a.rank(), axa), sb = saved_axes(b.rank(), axb);
+  const auto sa = sa_order.empty() ? saved_axes(a.rank(), axa) : sa_order;
+  const auto sb = sb_order.empty() ? saved_axes(b.rank(), axb) : sb_order;
   for (auto i : sa) c.legs.push_back(a.legs[i]);
   for (auto i : sb) c.legs.push_back(b.legs[i]);
   const bool fermionic = a.parity_comp >= 0;
@@ -356,7 +376,7 @@ CtrctOut contract(const Tensor& a, const Tensor& b, const std::vector<int64_t>& 
     return p;
   };
   auto finish = [&]() {
-    if (c.is_complex) run_tasks<cplx>(a, b, axa, axb, out); else run_tasks<double>(a, b, axa, axb, out);
+    if (c.is_complex) run_tasks<cplx>(a, b, axa, axb, sa, sb, out); else run_tasks<double>(a, b, axa, axb, sa, sb, out);
   };
   auto prod = [](const Tensor& t, int64_t blk, const std::vector<int64_t>& axes) {
     int64_t s = 1;
@@ -388,7 +408,11 @@ CtrctOut contract(const Tensor& a, const Tensor& b, const std::vector<int64_t>& 
       const uint64_t cidx = c.blk_idx(cc.data());
       int beta = 1;
       if (!cblocks.count(cidx)) { cblocks[cidx] = cc; beta = 0; }
-      int sign = fermionic ? exchange_sign(parities(a, i), parities(b, j), axa, axb, a_dir) : 1;
+      int sign = 1;
+      if (fermionic) {
+        const auto pa = parities(a, i), pb = parities(b, j);
+        sign = exchange_sign(pa, pb, axa, axb, a_dir) * saved_order_sign(pa, sa) * saved_order_sign(pb, sb);
+      }
       out.tasks.push_back({i, j, cidx, m, k, n, sign, beta});
     }
   }
@@ -748,6 +772,111 @@ void* orc_contract(const OrcTensorIn* a, const OrcTensorIn* b, const int64_t* ax
                                        (int64_t)tb.blk_idx(&tb.coords[t.b * tb.rank()]), (int64_t)t.c_idx, t.m,
                                        t.k, t.n, (int64_t)t.sign, (int64_t)t.beta});
     return r;
+  } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
+}
+
+// ContractContiguousAxes: axes (start + i) mod rank, saved legs cyclic from the range end.
+static void contiguous_axes(int ra, int rb, int64_t a0, int64_t b0, int n, std::vector<int64_t>& axa,
+                            std::vector<int64_t>& axb, std::vector<int64_t>& sa, std::vector<int64_t>& sb) {
+  if (n < 1 || n > ra || n > rb || a0 < 0 || a0 >= ra || b0 < 0 || b0 >= rb)
+    throw std::runtime_error("oracle: contiguous axis range out of bounds");
+  for (int i = 0; i < n; ++i) { axa.push_back((a0 + i) % ra); axb.push_back((b0 + i) % rb); }
+  for (int i = 0; i < ra - n; ++i) sa.push_back((a0 + n + i) % ra);
+  for (int i = 0; i < rb - n; ++i) sb.push_back((b0 + n + i) % rb);
+}
+
+void* orc_contract_contiguous(const OrcTensorIn* a, const OrcTensorIn* b, int64_t a0, int64_t b0, int n) {
+  try {
+    Tensor ta = from_in(a), tb = from_in(b);
+    std::vector<int64_t> axa, axb, sa, sb;
+    contiguous_axes(ta.rank(), tb.rank(), a0, b0, n, axa, axb, sa, sb);
+    auto out = contract(ta, tb, axa, axb, sa, sb);
+    auto* r = new Result;
+    r->tensors.emplace_back(new Tensor(std::move(out.c)));
+    return r;
+  } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
+}
+
+// C = beta C + alpha A.B (tail/head contiguous contraction) over the union topology.
+// c_in NULL: the default output (beta must be 0). *status: 0 done, 1 layout mismatch (the
+// indexes differ, or blocks are missing and expansion is not allowed; nothing computed).
+void* orc_accumulate(const OrcTensorIn* a, const OrcTensorIn* b, int64_t a0, int64_t b0, int n,
+                     const double* alpha, const double* beta, const OrcTensorIn* c_in, int allow_expand,
+                     int* status) {
+  try {
+    *status = 0;
+    Tensor ta = from_in(a), tb = from_in(b);
+    std::vector<int64_t> axa, axb, sa, sb;
+    contiguous_axes(ta.rank(), tb.rank(), a0, b0, n, axa, axb, sa, sb);
+    Tensor t = contract(ta, tb, axa, axb, sa, sb).c;
+    const cplx al(alpha[0], alpha[1]), be(beta[0], beta[1]);
+    if (!c_in && be != cplx(0.0)) throw std::runtime_error("oracle: accumulate into a default output needs beta == 0");
+    Tensor c0;
+    if (c_in) {
+      c0 = from_in(c_in);
+      bool same = c0.rank() == t.rank() && c0.ncomp == t.ncomp && c0.is_complex == t.is_complex;
+      for (int l = 0; same && l < t.rank(); ++l)
+        same = c0.legs[l].dir == t.legs[l].dir && c0.legs[l].qns == t.legs[l].qns && c0.legs[l].dims == t.legs[l].dims;
+      if (!same) { *status = 1; return nullptr; }
+    }
+    // union topology
+    std::map<uint64_t, std::pair<int64_t, int64_t>> blocks;   // blk_idx -> (ordinal in c0, ordinal in t)
+    const int r = t.rank();
+    if (c_in)
+      for (int64_t i = 0; i < c0.nblk(); ++i) blocks[r ? c0.blk_idx(&c0.coords[i * r]) : 0] = {i, -1};
+    bool missing = false;
+    for (int64_t i = 0; i < t.nblk(); ++i) {
+      const uint64_t k = r ? t.blk_idx(&t.coords[i * r]) : 0;
+      auto it = blocks.find(k);
+      if (it == blocks.end()) { blocks[k] = {-1, i}; missing = true; }
+      else it->second.second = i;
+    }
+    if (c_in && missing && !allow_expand) { *status = 1; return nullptr; }
+    Tensor c;
+    c.ncomp = t.ncomp;
+    c.parity_comp = t.parity_comp;
+    c.is_complex = t.is_complex;
+    c.legs = t.legs;
+    if (r == 0) {   // scalar output: one value
+      c.size = 1;
+      c.offsets = {0};
+    } else {
+      for (auto& kv : blocks) {
+        const Tensor& src = kv.second.first >= 0 ? c0 : t;
+        const int64_t ord = kv.second.first >= 0 ? kv.second.first : kv.second.second;
+        c.coords.insert(c.coords.end(), src.coords.begin() + ord * r, src.coords.begin() + (ord + 1) * r);
+      }
+      c.refresh_offsets();
+    }
+    const int per = c.is_complex ? 2 : 1;
+    c.data.assign((size_t)per * c.size, 0.0);
+    auto get = [&](const Tensor& x, int64_t e) {
+      return x.is_complex ? cplx(x.data[2 * e], x.data[2 * e + 1]) : cplx(x.data[e], 0.0);
+    };
+    auto put = [&](int64_t e, cplx v) {
+      if (c.is_complex) { c.data[2 * e] = v.real(); c.data[2 * e + 1] = v.imag(); } else c.data[e] = v.real();
+    };
+    auto combine = [&](int64_t dst, int64_t n_el, int64_t old_off, int64_t t_off) {
+      for (int64_t e = 0; e < n_el; ++e) {
+        cplx v(0.0);
+        if (old_off >= 0 && be != cplx(0.0)) v += be * get(c0, old_off + e);
+        if (t_off >= 0) v += al * get(t, t_off + e);
+        put(dst + e, v);
+      }
+    };
+    if (r == 0) {
+      combine(0, 1, c_in && c0.size ? 0 : -1, t.size ? 0 : -1);
+    } else {
+      int64_t q = 0;
+      for (auto& kv : blocks) {
+        const int64_t o = kv.second.first, ti = kv.second.second;
+        combine(c.offsets[q], c.blk_size(q), o >= 0 ? c0.offsets[o] : -1, ti >= 0 ? t.offsets[ti] : -1);
+        ++q;
+      }
+    }
+    auto* res = new Result;
+    res->tensors.emplace_back(new Tensor(std::move(c)));
+    return res;
   } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
 }
 

@@ -65,6 +65,12 @@ def lib():
         L.orc_load_blas.argtypes = [C.c_char_p]
         L.orc_contract.restype = C.c_void_p
         L.orc_contract.argtypes = [C.POINTER(_TensorIn), C.POINTER(_TensorIn), C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_contract_contiguous.restype = C.c_void_p
+        L.orc_contract_contiguous.argtypes = [C.POINTER(_TensorIn), C.POINTER(_TensorIn), C.c_int64, C.c_int64,
+                                              C.c_int]
+        L.orc_accumulate.restype = C.c_void_p
+        L.orc_accumulate.argtypes = [C.POINTER(_TensorIn), C.POINTER(_TensorIn), C.c_int64, C.c_int64, C.c_int,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         L.orc_svd.restype = C.c_void_p
         L.orc_svd.argtypes = [C.POINTER(_TensorIn), C.c_int, C.c_void_p, C.c_double, C.c_int64, C.c_int64]
         L.orc_qr.restype = C.c_void_p
@@ -136,6 +142,45 @@ def contract(a: BSTensor, b: BSTensor, axes: Sequence[Sequence[int]]):
         if nt:
             L.orc_tasks(r, tasks.ctypes.data)
         return c, tasks
+    finally:
+        L.orc_free(r)
+
+
+def contract_contiguous(a: BSTensor, b: BSTensor, a_start: int, b_start: int, n: int) -> BSTensor:
+    """Reference-semantics ContractContiguousAxes(a, b, a_start, b_start, n): contracted axes
+    (start + i) mod rank, C legs = the saved legs of A then of B, each cyclic from the end of
+    its contracted range."""
+    L = lib()
+    ia, ib = _In(a), _In(b)
+    r = L.orc_contract_contiguous(C.byref(ia.s), C.byref(ib.s), int(a_start), int(b_start), int(n))
+    if not r:
+        raise RuntimeError(L.orc_last_error().decode())
+    try:
+        return _export(L, r, 0)
+    finally:
+        L.orc_free(r)
+
+
+def accumulate(a: BSTensor, b: BSTensor, a_start: int, b_start: int, n: int, alpha, beta,
+               c: Optional[BSTensor] = None, allow_expand: bool = True):
+    """Reference-semantics ContractTailHeadContiguousAccumulate (allow_expand) /
+    TryContractTailHeadContiguousAccumulate: (True, beta c + alpha a.b over the union
+    topology), or (False, None) when the layout does not fit."""
+    L = lib()
+    ia, ib = _In(a), _In(b)
+    ic = _In(c) if c is not None else None
+    al = np.array([complex(alpha).real, complex(alpha).imag])
+    be = np.array([complex(beta).real, complex(beta).imag])
+    st = np.zeros(1, np.int32)
+    r = L.orc_accumulate(C.byref(ia.s), C.byref(ib.s), int(a_start), int(b_start), int(n), al.ctypes.data,
+                         be.ctypes.data, C.byref(ic.s) if ic is not None else None, int(allow_expand),
+                         st.ctypes.data)
+    if not r:
+        if st[0] == 1:
+            return False, None
+        raise RuntimeError(L.orc_last_error().decode())
+    try:
+        return True, _export(L, r, 0)
     finally:
         L.orc_free(r)
 

@@ -9,6 +9,10 @@
 //   matvec_u1 qmax sigma D seed   four-step two-site chain, U(1), FP64
 //   matvec_f half D seed          four-step chain, fermionic U(1)xU(1), complex128
 //   ctrct_misc seed               extra axis patterns incl. scalar results and IN-leg contractions
+//   ctrct_contig seed             ContractContiguousAxes (all side pairs, wrapped and middle
+//                                 ranges) and ContractTailHeadContiguousAccumulate /
+//                                 TryContractTailHeadContiguousAccumulate (default, same,
+//                                 expanded and superset outputs), U(1) real and fermionic complex
 //   svd_u1 qmax sigma D seed trunc Dmin Dmax   SVD of a spectrum-controlled psi (ldims 2)
 //   svd_stress nb lo hi seed trunc Dmin Dmax   SVD of a rank-2 block-diagonal tensor
 //   svd_f half D seed trunc Dmin Dmax          SVD of a fermionic complex psi
@@ -44,12 +48,13 @@ Index<QNT> to_index(const sy::Leg& l) {
 }
 
 template <typename ElemT, typename QNT>
-QLTensor<ElemT, QNT> to_qlten(const sy::Tensor& t) {
+QLTensor<ElemT, QNT> to_qlten(const sy::Tensor& t, const std::vector<int32_t>& div = {}) {
   IndexVec<QNT> idx;
   for (auto& l : t.legs) idx.push_back(to_index<QNT>(l));
   QLTensor<ElemT, QNT> q(idx);
-  std::vector<int32_t> zero(qn_ncomp<QNT>(), 0);
-  q.Fill(make_qn<QNT>(zero.data()), ElemT(0));
+  std::vector<int32_t> d(qn_ncomp<QNT>(), 0);
+  for (size_t i = 0; i < div.size() && i < d.size(); ++i) d[i] = div[i];
+  q.Fill(make_qn<QNT>(d.data()), ElemT(0));
   auto& bsdt = q.GetBlkSparDataTen();
   const auto& blks = bsdt.GetBlkIdxDataBlkMap();
   if ((int64_t)blks.size() != t.nblk()) throw std::runtime_error("block count mismatch");
@@ -134,6 +139,100 @@ void contract_case(qtb::Writer& w, const std::string& tag, const QLTensor<ElemT,
   if (out) *out = c;
 }
 
+static sy::Tensor random_like(const std::vector<sy::Leg>& legs, const std::vector<int32_t>& div, bool cplx,
+                              sy::Normal& rng) {
+  auto t = sy::make_tensor(legs, div, cplx);
+  sy::fill_normal(t, rng);
+  return t;
+}
+
+// ContractContiguousAxes<ASide, BSide> (tensor_manipulation/contract_contiguous_axes.h:849-868)
+template <typename ElemT, typename QNT, CtrctSide SA, CtrctSide SB>
+QLTensor<ElemT, QNT> contig(const QLTensor<ElemT, QNT>& a, const QLTensor<ElemT, QNT>& b, size_t a0, size_t b0,
+                            size_t n) {
+  QLTensor<ElemT, QNT> c;
+  ContractContiguousAxes<ElemT, QNT, SA, SB>(a, b, a0, b0, n, c);
+  return c;
+}
+
+template <typename ElemT, typename QNT>
+void contig_case(qtb::Writer& w, const std::string& tag, const QLTensor<ElemT, QNT>& a,
+                 const QLTensor<ElemT, QNT>& b, size_t a0, size_t b0, size_t n, bool a_tail, bool b_head) {
+  w.i64(tag + ".params", {(int64_t)a0, (int64_t)b0, (int64_t)n, a_tail ? 1 : 0, b_head ? 1 : 0});
+  dump(w, tag + ".A", a);
+  dump(w, tag + ".B", b);
+  QLTensor<ElemT, QNT> c;
+  using S = CtrctSide;
+  if (a_tail && b_head) c = contig<ElemT, QNT, S::Tail, S::Head>(a, b, a0, b0, n);
+  else if (a_tail) c = contig<ElemT, QNT, S::Tail, S::Tail>(a, b, a0, b0, n);
+  else if (b_head) c = contig<ElemT, QNT, S::Head, S::Head>(a, b, a0, b0, n);
+  else c = contig<ElemT, QNT, S::Head, S::Tail>(a, b, a0, b0, n);
+  dump(w, tag + ".C", c);
+}
+
+template <typename ElemT> std::vector<double> re_im(ElemT x);
+template <> std::vector<double> re_im<double>(double x) { return {x, 0.0}; }
+template <> std::vector<double> re_im<std::complex<double>>(std::complex<double> x) { return {x.real(), x.imag()}; }
+
+// ContractTailHeadContiguousAccumulate / TryContractTailHeadContiguousAccumulate
+// (tensor_manipulation/contract_contiguous_axes.h:953-1040). c0 == nullptr: default output.
+template <typename ElemT, typename QNT>
+void accum_case(qtb::Writer& w, const std::string& tag, const QLTensor<ElemT, QNT>& a,
+                const QLTensor<ElemT, QNT>& b, size_t a0, size_t b0, size_t n, ElemT alpha, ElemT beta,
+                const QLTensor<ElemT, QNT>* c0, bool try_only, QLTensor<ElemT, QNT>* out = nullptr) {
+  w.i64(tag + ".params", {(int64_t)a0, (int64_t)b0, (int64_t)n, 1, 1});
+  w.f64(tag + ".alpha", re_im(alpha));
+  w.f64(tag + ".beta", re_im(beta));
+  dump(w, tag + ".A", a);
+  dump(w, tag + ".B", b);
+  QLTensor<ElemT, QNT> c;
+  if (c0) {
+    dump(w, tag + ".C0", *c0);
+    c = *c0;
+  }
+  if (try_only) {
+    const bool ok = TryContractTailHeadContiguousAccumulate(a, b, a0, b0, n, alpha, beta, c);
+    w.scalar_i64(tag + ".ok", ok ? 1 : 0);
+  } else {
+    ContractTailHeadContiguousAccumulate(a, b, a0, b0, n, alpha, beta, c);
+  }
+  dump(w, tag + ".C", c);
+  if (out) *out = c;
+}
+
+template <typename ElemT, typename QNT>
+void contig_suite(qtb::Writer& w, const std::string& pre, const sy::Matvec& mv, const std::vector<int32_t>& div0,
+                  const std::vector<int32_t>& div1, ElemT alpha, ElemT beta, sy::Normal& rng) {
+  const bool cplx = !std::is_same<ElemT, double>::value;
+  auto P = to_qlten<ElemT, QNT>(mv.psi);
+  auto L = to_qlten<ElemT, QNT>(mv.lenv);
+  std::vector<sy::Leg> inv;
+  for (auto& l : mv.psi.legs) inv.push_back(l.inverse());
+  auto Pd = to_qlten<ElemT, QNT>(random_like(inv, div0, cplx, rng));
+  const auto& pl = mv.psi.legs;
+  auto Q = to_qlten<ElemT, QNT>(random_like({pl[2].inverse(), pl[3].inverse(), pl[0].inverse(), pl[1].inverse()},
+                                            div0, cplx, rng));
+  contig_case(w, pre + "hh", L, P, 0, 0, 1, false, true);     // lenv leg 0 . psi leg 0
+  contig_case(w, pre + "wrap", P, Pd, 3, 3, 2, true, true);   // axes {3, 0} . {3, 0}
+  contig_case(w, pre + "mid", P, Pd, 1, 1, 2, true, true);    // axes {1, 2}: saved order 3, 0
+  contig_case(w, pre + "tt", P, Pd, 2, 2, 2, true, false);
+  contig_case(w, pre + "ht", P, Q, 0, 2, 2, false, false);
+  // accumulate: A = lenv with its legs rotated (last leg = inverse of psi leg 0), tail . head
+  const auto& ll = mv.lenv.legs;
+  auto A1 = to_qlten<ElemT, QNT>(random_like({ll[1], ll[2], ll[0]}, div0, cplx, rng));
+  auto A2 = to_qlten<ElemT, QNT>(random_like({ll[1], ll[2], ll[0]}, div0, cplx, rng));
+  std::vector<sy::Leg> cl = {ll[1], ll[2], pl[1], pl[2], pl[3]};
+  auto Csame = contig<ElemT, QNT, CtrctSide::Tail, CtrctSide::Head>(A2, P, 2, 0, 1);
+  auto Cother = to_qlten<ElemT, QNT>(random_like(cl, div1, cplx, rng), div1);
+  accum_case(w, pre + "acc_default", A1, P, 2, 0, 1, alpha, ElemT(0), (const QLTensor<ElemT, QNT>*)nullptr, false);
+  accum_case(w, pre + "acc_same", A1, P, 2, 0, 1, alpha, beta, &Csame, false);
+  QLTensor<ElemT, QNT> Cunion;
+  accum_case(w, pre + "acc_expand", A1, P, 2, 0, 1, alpha, beta, &Cother, false, &Cunion);
+  accum_case(w, pre + "acc_superset", A2, P, 2, 0, 1, beta, alpha, &Cunion, false);
+  accum_case(w, pre + "try_fail", A1, P, 2, 0, 1, alpha, beta, &Cother, true);
+  accum_case(w, pre + "try_ok", A2, P, 2, 0, 1, alpha, beta, &Cunion, true);
+}
+
 template <typename ElemT, typename QNT>
 void matvec_case(qtb::Writer& w, const sy::Matvec& mv) {
   auto L = to_qlten<ElemT, QNT>(mv.lenv);
@@ -179,13 +278,6 @@ void qr_case(qtb::Writer& w, const sy::Tensor& st, size_t ldims) {
   dump(w, "Q", q);
   dump(w, "R", r);
   w.scalar_i64("ldims", (int64_t)ldims);
-}
-
-static sy::Tensor random_like(const std::vector<sy::Leg>& legs, const std::vector<int32_t>& div, bool cplx,
-                              sy::Normal& rng) {
-  auto t = sy::make_tensor(legs, div, cplx);
-  sy::fill_normal(t, rng);
-  return t;
 }
 
 int main(int argc, char** argv) {
@@ -252,6 +344,13 @@ int main(int argc, char** argv) {
       auto FW = to_qlten<std::complex<double>, fU1U1QN>(fm.mpo1);
       contract_case(w, "f_env", FP, FL, {{0}, {0}});   // IN leg of A against OUT leg of B
       contract_case(w, "f_mpo", FW, FW, {{3}, {0}});
+    } else if (cs == "ctrct_contig") {
+      sy::Normal rng(std::stoull(A(3)));
+      auto mv = sy::heisenberg_u1_random(3, 1.5, 20, std::stoull(A(3)));
+      contig_suite<double, U1QN>(w, "u_", mv, {0}, {1}, 2.0, -1.5, rng);
+      auto fm = sy::hubbard_u1u1(1, 6, std::stoull(A(3)));
+      contig_suite<std::complex<double>, fU1U1QN>(w, "f_", fm, {0, 0}, {2, 0}, std::complex<double>(0.5, 0.25),
+                                                  std::complex<double>(-1.0, 0.5), rng);
     } else if (cs == "svd_u1") {
       auto t = sy::svd_psi(std::stoi(A(3)), std::stod(A(4)), std::stoll(A(5)), std::stoull(A(6)));
       svd_case<double, U1QN>(w, t, 2, std::stod(A(7)), std::stoull(A(8)), std::stoull(A(9)));

@@ -10,7 +10,9 @@ Submodules:
 """
 from .tensor import BSTensor, Leg, IN, OUT  # noqa: F401
 
-_API = {"Contract", "ContractionPlan", "Transpose", "SVD", "QR", "Matvec", "Lanczos", "DTensor", "Context",
+_API = {"Contract", "ContractionPlan", "ContractContiguousAxes", "ContiguousContractionPlan",
+        "ContractTailHeadContiguous", "ContractTailHeadContiguousAccumulate",
+        "TryContractTailHeadContiguousAccumulate", "AccumulatePlan", "Transpose", "SVD", "QR", "Matvec", "Lanczos", "DTensor", "Context",
         "context"}
 
 

@@ -180,6 +180,139 @@ def Contract(a: DTensor, b: DTensor, axes: Sequence[Sequence[int]], mode="fp64")
     return plan.execute(a, b, mode=mode)
 
 
+_SIDES = {"head": capi.QLTG_SIDE_HEAD, "tail": capi.QLTG_SIDE_TAIL}
+
+
+def _contiguous_axes(ra: int, rb: int, a_start: int, b_start: int, n: int):
+    """Contracted axes and cyclic saved orders of ContractContiguousAxes."""
+    axa = [(a_start + i) % ra for i in range(n)]
+    axb = [(b_start + i) % rb for i in range(n)]
+    sa = [(a_start + n + i) % ra for i in range(ra - n)]
+    sb = [(b_start + n + i) % rb for i in range(rb - n)]
+    return axa, axb, sa, sb
+
+
+def _result_meta(h, result_fn, blocks_fn, legs, dtype) -> BSTensor:
+    rank, nblk, size = C.c_int32(), C.c_int64(), C.c_int64()
+    check(result_fn(h, C.byref(rank), C.byref(nblk), C.byref(size)))
+    coords = np.zeros(max(nblk.value * rank.value, 1), np.int64)
+    offs = np.zeros(max(nblk.value, 1), np.int64)
+    check(blocks_fn(h, coords.ctypes.data, offs.ctypes.data))
+    if rank.value:
+        return BSTensor(legs, coords[: nblk.value * rank.value].reshape(nblk.value, rank.value), dtype, None,
+                        offsets=offs[: nblk.value])
+    return BSTensor([], np.zeros((nblk.value, 0), np.int64), dtype, None, size=size.value)
+
+
+class ContiguousContractionPlan(ContractionPlan):
+    """Planned ContractContiguousAxes<ASide, BSide>(A, B, a_start, b_start, n, C)
+    (reference tensor_manipulation/contract_contiguous_axes.h:849-868): A's axes
+    (a_start + i) mod rank against B's (b_start + i) mod rank; C's legs are A's saved legs
+    then B's, each cyclic from the end of its contracted range. The sides are the
+    reference's layout hints ("head" / "tail"); the result does not depend on them."""
+
+    def __init__(self, a: BSTensor, b: BSTensor, a_start: int, b_start: int, n: int, a_side: str = "tail",
+                 b_side: str = "head", device: int = 0):
+        self.ctx = context(device)
+        self.device = device
+        axa, axb, sa, sb = _contiguous_axes(a.rank, b.rank, int(a_start), int(b_start), int(n))
+        self.axes = (tuple(axa), tuple(axb))
+        da, db = _Desc(a), _Desc(b)
+        h = C.c_void_p()
+        check(lib().qltg_ctrct_plan_create_contiguous(self.ctx.h, da.ref, db.ref, int(a_start), int(b_start), int(n),
+                                                      _SIDES[a_side], _SIDES[b_side], C.byref(h)))
+        self.h = h
+        legs = [a.legs[i] for i in sa] + [b.legs[i] for i in sb]
+        self.result = _result_meta(h, lib().qltg_ctrct_plan_result, lib().qltg_ctrct_plan_result_blocks, legs,
+                                   a.dtype)
+
+
+def ContractContiguousAxes(a: DTensor, b: DTensor, a_start: int, b_start: int, n: int, a_side: str = "tail",
+                           b_side: str = "head", mode="fp64") -> DTensor:
+    """The reference's ContractContiguousAxes (contract_contiguous_axes.h:849-868)."""
+    plan = ContiguousContractionPlan(a.meta, b.meta, a_start, b_start, n, a_side, b_side, a.device)
+    return plan.execute(a, b, mode=mode)
+
+
+def ContractTailHeadContiguous(a: DTensor, b: DTensor, a_start: int, b_start: int, n: int, mode="fp64") -> DTensor:
+    """The reference's ContractTailHeadContiguous (contract_contiguous_axes.h:914-928)."""
+    return ContractContiguousAxes(a, b, a_start, b_start, n, "tail", "head", mode)
+
+
+class AccumulatePlan:
+    """Planned C = beta C + alpha A.B (tail/head contiguous contraction) over the union of C's
+    blocks and the contraction's, the reference's ContractTailHeadContiguousAccumulate
+    (allow_expand) / TryContractTailHeadContiguousAccumulate (contract_contiguous_axes.h:
+    953-1040). Raises ContractAccumulateLayoutMismatch when C's indexes differ from the
+    result's, or it lacks result blocks and allow_expand is False."""
+
+    def __init__(self, a: BSTensor, b: BSTensor, a_start: int, b_start: int, n: int, c: Optional[BSTensor],
+                 allow_expand: bool = True, device: int = 0):
+        self.h = None
+        self.ctx = context(device)
+        self.device = device
+        self.has_c = c is not None
+        _, _, sa, sb = _contiguous_axes(a.rank, b.rank, int(a_start), int(b_start), int(n))
+        da, db = _Desc(a), _Desc(b)
+        dc = _Desc(c) if c is not None else None
+        h = C.c_void_p()
+        exp = C.c_int32()
+        check(lib().qltg_accum_plan_create(self.ctx.h, da.ref, db.ref, int(a_start), int(b_start), int(n),
+                                           dc.ref if dc is not None else None, int(bool(allow_expand)), C.byref(h),
+                                           C.byref(exp)))
+        self.h = h
+        self.expanded = bool(exp.value)
+        legs = [a.legs[i] for i in sa] + [b.legs[i] for i in sb]
+        self.result = _result_meta(h, lib().qltg_accum_plan_result, lib().qltg_accum_plan_result_blocks, legs,
+                                   a.dtype)
+
+    def execute(self, a: DTensor, b: DTensor, c: Optional[DTensor], alpha, beta, out: Optional[DTensor] = None,
+                mode="fp64") -> DTensor:
+        """out = beta c + alpha a.b. Without `out` the result goes over c's buffer when the
+        topology did not grow, else into a new tensor."""
+        if out is None:
+            out = c if (c is not None and not self.expanded) else DTensor.empty(self.result, self.device)
+        al = np.array([complex(alpha).real, complex(alpha).imag])
+        be = np.array([complex(beta).real, complex(beta).imag])
+        check(lib().qltg_accum_exec(self.h, C.c_void_p(a.ptr), C.c_void_p(b.ptr),
+                                    C.c_void_p(c.ptr) if c is not None else None, C.c_void_p(out.ptr),
+                                    al.ctypes.data, be.ctypes.data, _mode(mode), stream_ptr(self.device)))
+        if out is c:
+            out.meta = self.result
+        return out
+
+    def device_status(self) -> None:
+        check(lib().qltg_accum_plan_device_status(self.h, stream_ptr(self.device)))
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().qltg_accum_plan_destroy(self.h)
+        except Exception:
+            pass
+
+
+def ContractTailHeadContiguousAccumulate(a: DTensor, b: DTensor, a_start: int, b_start: int, n: int, alpha, beta,
+                                         c: Optional[DTensor] = None, mode="fp64") -> DTensor:
+    """c = beta c + alpha A.B; returns the updated tensor (c itself unless its topology grew).
+    c None is the reference's default output (beta must be 0)."""
+    plan = AccumulatePlan(a.meta, b.meta, a_start, b_start, n, c.meta if c is not None else None, True, a.device)
+    return plan.execute(a, b, c, alpha, beta, mode=mode)
+
+
+def TryContractTailHeadContiguousAccumulate(a: DTensor, b: DTensor, a_start: int, b_start: int, n: int, alpha,
+                                            beta, c: Optional[DTensor] = None,
+                                            mode="fp64") -> Tuple[bool, Optional[DTensor]]:
+    """(True, updated c) when c already holds every result block (or is default with
+    beta == 0); (False, c unchanged) when the layout does not fit."""
+    try:
+        plan = AccumulatePlan(a.meta, b.meta, a_start, b_start, n, c.meta if c is not None else None, False,
+                              a.device)
+    except capi.ContractAccumulateLayoutMismatch:
+        return False, c
+    return True, plan.execute(a, b, c, alpha, beta, mode=mode)
+
+
 def _transposed_meta(m: BSTensor, perm: Sequence[int]) -> BSTensor:
     legs = [m.legs[i] for i in perm]
     coords = m.coords[:, perm]

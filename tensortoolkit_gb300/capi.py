@@ -8,7 +8,8 @@ import re
 from . import _native
 
 QLTG_OK, QLTG_ERR_INVALID, QLTG_ERR_CUDA, QLTG_ERR_OOM, QLTG_ERR_TIMEOUT, QLTG_ERR_NOCONV, \
-    QLTG_ERR_EMPTY_SVD, QLTG_ERR_UNSUPPORTED = range(8)
+    QLTG_ERR_EMPTY_SVD, QLTG_ERR_UNSUPPORTED, QLTG_ERR_LAYOUT = range(9)
+QLTG_SIDE_HEAD, QLTG_SIDE_TAIL = 0, 1
 QLTG_F64, QLTG_C128 = 0, 1
 QLTG_MODE_FP64, QLTG_MODE_SPLIT = 0, 1
 
@@ -37,6 +38,15 @@ _SIGS = {
     "qltg_ctrct_exec_stage": ([_P, _P, _P, _P, C.c_int32, C.c_int32, _P], C.c_int),
     "qltg_ctrct_plan_device_status": ([_P, _P], C.c_int),
     "qltg_ctrct_plan_destroy": ([_P], C.c_int),
+    "qltg_ctrct_plan_create_contiguous": ([_P, C.POINTER(TensorDesc), C.POINTER(TensorDesc), C.c_int64,
+                                           C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.POINTER(_P)], C.c_int),
+    "qltg_accum_plan_create": ([_P, C.POINTER(TensorDesc), C.POINTER(TensorDesc), C.c_int64, C.c_int64,
+                                C.c_int32, _P, C.c_int32, C.POINTER(_P), C.POINTER(C.c_int32)], C.c_int),
+    "qltg_accum_plan_result": ([_P, C.POINTER(C.c_int32), _I64P, _I64P], C.c_int),
+    "qltg_accum_plan_result_blocks": ([_P, _P, _P], C.c_int),
+    "qltg_accum_exec": ([_P, _P, _P, _P, _P, _P, _P, C.c_int32, _P], C.c_int),
+    "qltg_accum_plan_device_status": ([_P, _P], C.c_int),
+    "qltg_accum_plan_destroy": ([_P], C.c_int),
     "qltg_transpose": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
     "qltg_transpose_noalloc": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
     "qltg_transpose_plan_create": ([_P, C.POINTER(TensorDesc), _P, _P, C.POINTER(_P)], C.c_int),
@@ -84,6 +94,11 @@ class EmptySVDResultError(QltgError):
     """Mirror of qlten::EmptySVDResultError (reference framework/exceptions.h)."""
 
 
+class ContractAccumulateLayoutMismatch(QltgError):
+    """Mirror of qlten::detail::ContractAccumulateLayoutMismatch (reference
+    tensor_manipulation/contract_contiguous_axes.h:84-88)."""
+
+
 _lib = None
 
 
@@ -104,4 +119,6 @@ def check(code: int) -> None:
         msg = lib().qltg_last_error().decode()
         if code == QLTG_ERR_EMPTY_SVD:
             raise EmptySVDResultError(code, msg)
+        if code == QLTG_ERR_LAYOUT:
+            raise ContractAccumulateLayoutMismatch(code, msg)
         raise QltgError(code, msg)

@@ -85,7 +85,6 @@ bool inverse_leg(const Meta& a, int la, const Meta& b, int lb) {
   return a.dirs[la] != b.dirs[lb] && a.qns[la] == b.qns[lb] && a.dims[la] == b.dims[lb];
 }
 
-void finalize_plan(CtrctPlan& p, cudaStream_t s);
 
 // FermionicInplaceReorder (reference utility/utils_inl.h:52-75): sign of moving the legs
 // into `order` by the cycle-following in-place reorder, counting odd legs passed over.

@@ -134,6 +134,9 @@ struct CtrctPlan {
   qltg_ctx* ctx = nullptr;
   Meta a, b, c;
   std::vector<int64_t> axa, axb, sa, sb;
+  // Optional order of the saved legs in C (empty: ascending, as Contract). A fermionic block
+  // whose saved legs leave ascending order takes that reordering's sign (ContractContiguousAxes).
+  std::vector<int64_t> sa_order, sb_order;
   bool a_trans = false, b_trans = false;
   std::vector<int> a_order, b_order;
   // tasks in the reference's generation order: a, b, c_blk_idx, m, k, n, sign, beta
@@ -147,6 +150,8 @@ struct CtrctPlan {
 };
 
 void plan_contraction(CtrctPlan& p, cudaStream_t s);
+// Grouped-GEMM schedule, operand transposes and device buffers of a planned contraction.
+void finalize_plan(CtrctPlan& p, cudaStream_t s);
 int64_t exec_launches_split(const CtrctPlan& p);
 void exec_contraction(CtrctPlan& p, const void* a, const void* b, void* c, int mode, cudaStream_t s, int stage = 0);
 

@@ -7,7 +7,6 @@
 #include "ctrct.h"
 
 namespace qltg {
-void finalize_plan(CtrctPlan& p, cudaStream_t s);
 }
 
 using qltg::CtrctPlan;

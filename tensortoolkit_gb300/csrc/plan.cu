@@ -76,6 +76,17 @@ __global__ void k_match(const uint64_t* __restrict__ key_a, int64_t na, const ui
   cnt[i] = lo - l;
 }
 
+// Sign of reordering a block's saved legs from ascending leg order to `order` (n legs):
+// -1 per pair of odd legs that trade places. +1 for the ascending order of Contract; for the
+// cyclic order of ContractContiguousAxes it is the residue sign of the reference's rotated
+// matrix view (qltensor/blk_spar_data_ten/data_blk_operations.h:580-611).
+__host__ __device__ inline int saved_order_sign(const uint8_t* par, const int* order, int n) {
+  int c = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j) c += (order[i] > order[j]) & par[order[i]] & par[order[j]];
+  return (c & 1) ? -1 : 1;
+}
+
 // Fermionic exchange sign of one pair, the reference's FermionExchangeSignForCtrct
 // (data_blk_operations.h:351-401): bring each contracted B leg next to its A partner,
 // counting odd legs passed over, plus one exchange per odd IN-direction A leg.
@@ -126,7 +137,8 @@ __global__ void k_emit(const int32_t* __restrict__ ca, const int32_t* __restrict
     int sign = 1;
     if (P.fermionic) {
       for (int l = 0; l < P.rb; ++l) pb_l[l] = par_b[P.b_leg_off[l] + c2[l]];
-      sign = exchange_sign(pa_l, P.ra, pb_l, P.rb, P.axa, P.axb, P.nax, P.a_ctrct_in);
+      sign = exchange_sign(pa_l, P.ra, pb_l, P.rb, P.axa, P.axb, P.nax, P.a_ctrct_in) *
+             saved_order_sign(pa_l, P.sa, P.nsa) * saved_order_sign(pb_l, P.sb, P.nsb);
     }
     pa[p] = (int32_t)i;
     pb[p] = j;
@@ -215,6 +227,15 @@ void plan_contraction(CtrctPlan& p, cudaStream_t s) {
   }
   p.sa = saved_axes(A.rank, p.axa);
   p.sb = saved_axes(B.rank, p.axb);
+  auto reorder = [](std::vector<int64_t>& saved, const std::vector<int64_t>& order) {
+    if (order.empty()) return;
+    std::vector<int64_t> x = order, y = saved;
+    std::sort(x.begin(), x.end());
+    QLTG_CHECK(x == y, QLTG_ERR_INVALID, "saved-leg order is not a permutation of the saved legs");
+    saved = order;
+  };
+  reorder(p.sa, p.sa_order);
+  reorder(p.sb, p.sb_order);
   const int rc = (int)(p.sa.size() + p.sb.size());
   QLTG_CHECK(rc <= kMaxRank, QLTG_ERR_UNSUPPORTED, "result rank above 8");
 

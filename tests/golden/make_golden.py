@@ -1,6 +1,7 @@
 """Regenerate the committed golden fixtures from the reference implementation itself.
 
-Runs oracle/_ref/ref_driver (the reference's own Contract / SVD / QR, built from the
+Runs oracle/_ref/ref_driver (the reference's own Contract / ContractContiguousAxes /
+ContractTailHeadContiguousAccumulate / SVD / QR, built from the
 reference sources by oracle/ref/Makefile) on inputs from the deterministic workload
 generator and stores inputs, task lists and outputs as compressed .npz files here.
 
@@ -26,6 +27,7 @@ CASES = {
     "matvec_u1_small": (["matvec_u1", "4", "2.0", "40", "1"], -1),
     "matvec_f_small": (["matvec_f", "2", "24", "4"], 0),
     "ctrct_misc_u1": (["ctrct_misc", "7"], None),
+    "ctrct_contig": (["ctrct_contig", "11"], None),
     "svd_u1_full": (["svd_u1", "4", "2.0", "40", "3", "1e-9", "1", "1000"], -1),
     "svd_u1_trunc": (["svd_u1", "4", "2.0", "40", "3", "1e-2", "1", "1000"], -1),
     "svd_u1_dmax": (["svd_u1", "4", "2.0", "40", "3", "1e-12", "1", "12"], -1),
@@ -40,7 +42,7 @@ CASES = {
 def parity_for(name, key, default):
     if default is not None:
         return default
-    return 0 if key.startswith("f_") else -1   # ctrct_misc: f_* cases are fermionic
+    return 0 if key.startswith("f_") else -1   # ctrct_misc / ctrct_contig: f_* cases are fermionic
 
 
 def main():
