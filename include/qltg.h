@@ -216,6 +216,33 @@ QLTG_API int qltg_transpose_plan_destroy(qltg_transpose_plan* plan);
 QLTG_API int qltg_transpose_noalloc(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev,
                                     const int32_t* perm, void* dst_dev, void* stream);
 
+/* ---------------------------------------------------------------- .qlten stream I/O
+ * The reference's QLTensor serialisation (qltensor/qltensor_impl.h:799-830, index.h:170-188,
+ * qnsct.h:106-115, special_qn/u1qn.h / u1u1qn.h, blk_spar_data_ten.h:791-830,
+ * raw_data_operations.h:583-640): text header (rank; per index its sectors with quantum
+ * numbers, degeneracies and hashes, direction, dimension, hash; the block coordinates), then
+ * the raw buffer. Quantum number types: qn_ncomp 1 = U1QN, 2 = U1U1QN (parity_comp -1) or
+ * fU1U1QN (parity_comp 0). */
+typedef struct qltg_qlten_file qltg_qlten_file;
+
+/* Parse a file's header; every stored hash is checked (a wrong quantum number type fails). */
+QLTG_API int qltg_qlten_open(const char* path, int32_t qn_ncomp, int32_t parity_comp, int32_t elem_type,
+                             qltg_qlten_file** file);
+/* rank, sum of sector counts over the legs, blocks (a scalar: 1), elements. */
+QLTG_API int qltg_qlten_info(const qltg_qlten_file* file, int32_t* rank, int64_t* total_sectors, int64_t* nblk,
+                             int64_t* size);
+/* Descriptor arrays (as qltg_tensor_desc; qns / dims leg by leg). */
+QLTG_API int qltg_qlten_meta(const qltg_qlten_file* file, int32_t* dirs, int32_t* nsct, int32_t* qns,
+                             int64_t* dims, int64_t* coords);
+/* The raw buffer into device memory (dst_is_device = 1: through a pinned staging buffer,
+ * copied on `stream`, complete on return) or host memory. */
+QLTG_API int qltg_qlten_read_data(qltg_qlten_file* file, void* dst, int32_t dst_is_device, void* stream);
+QLTG_API int qltg_qlten_close(qltg_qlten_file* file);
+/* Write tensor `t` with raw buffer `data` (device or host memory) as a .qlten stream that the
+ * reference reads with operator>>; byte-identical to what the reference writes. */
+QLTG_API int qltg_qlten_write(const char* path, const qltg_tensor_desc* t, const void* data, int32_t data_is_device,
+                              void* stream);
+
 /* ---------------------------------------------------------------- two-site matvec */
 typedef struct qltg_matvec qltg_matvec;
 

@@ -13,6 +13,9 @@
 //                                 ranges) and ContractTailHeadContiguousAccumulate /
 //                                 TryContractTailHeadContiguousAccumulate (default, same,
 //                                 expanded and superset outputs), U(1) real and fermionic complex
+//   qlten_io seed dir             tensors written by the reference's QLTensor stream operator
+//                                 (dir/<tag>.qlten) and dumped to <out>: U(1) real, fermionic
+//                                 complex, a scalar, a tensor with no blocks
 //   svd_u1 qmax sigma D seed trunc Dmin Dmax   SVD of a spectrum-controlled psi (ldims 2)
 //   svd_stress nb lo hi seed trunc Dmin Dmax   SVD of a rank-2 block-diagonal tensor
 //   svd_f half D seed trunc Dmin Dmax          SVD of a fermionic complex psi
@@ -27,6 +30,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <string>
 
 using namespace qlten;
@@ -351,6 +355,29 @@ int main(int argc, char** argv) {
       auto fm = sy::hubbard_u1u1(1, 6, std::stoull(A(3)));
       contig_suite<std::complex<double>, fU1U1QN>(w, "f_", fm, {0, 0}, {2, 0}, std::complex<double>(0.5, 0.25),
                                                   std::complex<double>(-1.0, 0.5), rng);
+    } else if (cs == "qlten_io") {
+      // QLTensor::StreamWrite (qltensor/qltensor_impl.h:825-830) through operator<<
+      const std::string dir = A(4);
+      auto save = [&](const std::string& tag, const auto& t) {
+        std::ofstream ofs(dir + "/" + tag + ".qlten", std::ios::binary);
+        ofs << t;
+        dump(w, tag, t);
+      };
+      auto mv = sy::heisenberg_u1_random(2, 1.0, 8, std::stoull(A(3)));
+      save("u_psi", to_qlten<double, U1QN>(mv.psi));
+      save("u_lenv", to_qlten<double, U1QN>(mv.lenv));
+      auto fm = sy::hubbard_u1u1(1, 4, std::stoull(A(3)));
+      save("f_psi", to_qlten<std::complex<double>, fU1U1QN>(fm.psi));
+      auto P = to_qlten<double, U1QN>(mv.psi);
+      QLTensor<double, U1QN> sc;
+      Contract(&P, &P, {{0, 1, 2, 3}, {0, 1, 2, 3}}, &sc);   // not a valid pairing: an empty scalar
+      std::vector<sy::Leg> inv;
+      for (auto& l : mv.psi.legs) inv.push_back(l.inverse());
+      sy::Normal rng(std::stoull(A(3)));
+      auto Pd = to_qlten<double, U1QN>(random_like(inv, {0}, false, rng));
+      QLTensor<double, U1QN> sc2;
+      Contract(&P, &Pd, {{0, 1, 2, 3}, {0, 1, 2, 3}}, &sc2);
+      save("u_scalar", sc2);
     } else if (cs == "svd_u1") {
       auto t = sy::svd_psi(std::stoi(A(3)), std::stod(A(4)), std::stoll(A(5)), std::stoull(A(6)));
       svd_case<double, U1QN>(w, t, 2, std::stod(A(7)), std::stoull(A(8)), std::stoull(A(9)));

@@ -313,6 +313,26 @@ def TryContractTailHeadContiguousAccumulate(a: DTensor, b: DTensor, a_start: int
     return True, plan.execute(a, b, c, alpha, beta, mode=mode)
 
 
+def read_qlten(path: str, qn: str = "U1QN", dtype: str = "f64", device: int = 0) -> DTensor:
+    """Read a .qlten file (the reference's QLTensor stream format) straight into device
+    memory: header parsed in libqltg.so, raw buffer through a pinned staging buffer."""
+    from .qlten_io import QltenFile
+    f = QltenFile(path, qn, dtype)
+    try:
+        meta = BSTensor(f.meta.legs, f.meta.coords, f.meta.dtype, None, offsets=f.meta.offsets, size=f.meta.size)
+        out = DTensor.empty(meta, device)
+        check(lib().qltg_qlten_read_data(f.h, C.c_void_p(out.ptr), 1, stream_ptr(device)))
+        return out
+    finally:
+        f.close()
+
+
+def write_qlten(path: str, t: DTensor) -> None:
+    """Write a device tensor as a .qlten file the reference reads with operator>>."""
+    d = _Desc(t.meta)
+    check(lib().qltg_qlten_write(path.encode(), d.ref, C.c_void_p(t.ptr), 1, stream_ptr(t.device)))
+
+
 def _transposed_meta(m: BSTensor, perm: Sequence[int]) -> BSTensor:
     legs = [m.legs[i] for i in perm]
     coords = m.coords[:, perm]

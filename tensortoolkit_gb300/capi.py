@@ -47,6 +47,12 @@ _SIGS = {
     "qltg_accum_exec": ([_P, _P, _P, _P, _P, _P, _P, C.c_int32, _P], C.c_int),
     "qltg_accum_plan_device_status": ([_P, _P], C.c_int),
     "qltg_accum_plan_destroy": ([_P], C.c_int),
+    "qltg_qlten_open": ([C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(_P)], C.c_int),
+    "qltg_qlten_info": ([_P, C.POINTER(C.c_int32), _I64P, _I64P, _I64P], C.c_int),
+    "qltg_qlten_meta": ([_P, _P, _P, _P, _P, _P], C.c_int),
+    "qltg_qlten_read_data": ([_P, _P, C.c_int32, _P], C.c_int),
+    "qltg_qlten_close": ([_P], C.c_int),
+    "qltg_qlten_write": ([C.c_char_p, C.POINTER(TensorDesc), _P, C.c_int32, _P], C.c_int),
     "qltg_transpose": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
     "qltg_transpose_noalloc": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
     "qltg_transpose_plan_create": ([_P, C.POINTER(TensorDesc), _P, _P, C.POINTER(_P)], C.c_int),

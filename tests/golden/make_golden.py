@@ -28,6 +28,8 @@ CASES = {
     "matvec_f_small": (["matvec_f", "2", "24", "4"], 0),
     "ctrct_misc_u1": (["ctrct_misc", "7"], None),
     "ctrct_contig": (["ctrct_contig", "11"], None),
+    # also writes tests/golden/qlten/<tag>.qlten with the reference's stream operator
+    "qlten_io": (["qlten_io", "5", "{qlten_dir}"], None),
     "svd_u1_full": (["svd_u1", "4", "2.0", "40", "3", "1e-9", "1", "1000"], -1),
     "svd_u1_trunc": (["svd_u1", "4", "2.0", "40", "3", "1e-2", "1", "1000"], -1),
     "svd_u1_dmax": (["svd_u1", "4", "2.0", "40", "3", "1e-12", "1", "12"], -1),
@@ -51,7 +53,10 @@ def main():
     for name, (args, pc) in CASES.items():
         with tempfile.TemporaryDirectory() as td:
             path = os.path.join(td, "out.qtb")
-            subprocess.check_call([DRIVER, args[0], path] + args[1:])
+            qdir = os.path.join(HERE, "qlten")
+            os.makedirs(qdir, exist_ok=True)
+            run_args = [a.replace("{qlten_dir}", qdir) for a in args]
+            subprocess.check_call([DRIVER, run_args[0], path] + run_args[1:])
             rec = read_qtb(path)
         prefixes = sorted({k.rsplit(".", 1)[0] for k in rec if k.endswith(".dirs")})
         for p in prefixes:
