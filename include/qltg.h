@@ -216,6 +216,40 @@ QLTG_API int qltg_transpose_plan_destroy(qltg_transpose_plan* plan);
 QLTG_API int qltg_transpose_noalloc(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev,
                                     const int32_t* perm, void* dst_dev, void* stream);
 
+/* ---------------------------------------------------------------- dmrg axis primitives
+ * The reference's bosonic qlten::dmrg axis operations (tensor_manipulation/dmrg/axis_ops.h);
+ * fermionic tensors are rejected with QLTG_ERR_UNSUPPORTED, as there. */
+
+/* out = beta out + alpha D(in): ApplyAxisDiagonal (axis_ops.h:2370-2547); with out_dev ==
+ * in_dev, alpha 1, beta 0 it is ApplyAxisDiagonalInPlace (:2549-2582). values: one per
+ * degeneracy of `axis`, sectors in index order (AxisDiagonalOp::values flattened; complex
+ * interleaved). beta == 0 never reads out_dev. The output has the input's topology. */
+QLTG_API int qltg_axis_diagonal(qltg_ctx* ctx, const qltg_tensor_desc* t, int32_t axis, const double* values,
+                                const void* in_dev, void* out_dev, const double* alpha, const double* beta,
+                                void* stream);
+/* out = in with every block times the value of its sector on `axis`:
+ * ApplyAxisSectorScalarsPreserveOrder (axis_ops.h:2655-2744). out_dev may be in_dev. */
+QLTG_API int qltg_axis_sector_scalars(qltg_ctx* ctx, const qltg_tensor_desc* t, int32_t axis,
+                                      const double* values_by_sector, const void* in_dev, void* out_dev,
+                                      void* stream);
+
+typedef struct qltg_axis_plan qltg_axis_plan;
+/* ApplyRank2ToAxisPreserveOrder (axis_ops.h:2862-2993): `axis` of t contracted with op's index
+ * 0 (op index 0 must be the inverse of t's leg), op's index 1 takes the axis' place. */
+QLTG_API int qltg_axis_rank2_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* t, const qltg_tensor_desc* op,
+                                         int32_t axis, qltg_axis_plan** plan);
+/* ApplyTwoRank2ToAxesPreserveOrder (axis_ops.h:2995-3126): op1 on axis1, then op2 on axis2. */
+QLTG_API int qltg_axis_two_rank2_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* t, const qltg_tensor_desc* op1,
+                                             int32_t axis1, const qltg_tensor_desc* op2, int32_t axis2,
+                                             qltg_axis_plan** plan);
+QLTG_API int qltg_axis_plan_result(const qltg_axis_plan* plan, int32_t* rank, int64_t* nblk, int64_t* size);
+QLTG_API int qltg_axis_plan_result_blocks(const qltg_axis_plan* plan, int64_t* coords, int64_t* offsets);
+/* out_dev (the result topology) from in_dev and the operators (op2_dev: two-operator plans). */
+QLTG_API int qltg_axis_plan_exec(qltg_axis_plan* plan, const void* in_dev, const void* op1_dev, const void* op2_dev,
+                                 void* out_dev, int32_t mode, void* stream);
+QLTG_API int qltg_axis_plan_device_status(qltg_axis_plan* plan, void* stream);
+QLTG_API int qltg_axis_plan_destroy(qltg_axis_plan* plan);
+
 /* ---------------------------------------------------------------- .qlten stream I/O
  * The reference's QLTensor serialisation (qltensor/qltensor_impl.h:799-830, index.h:170-188,
  * qnsct.h:106-115, special_qn/u1qn.h / u1u1qn.h, blk_spar_data_ten.h:791-830,

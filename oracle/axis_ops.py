@@ -1,0 +1,77 @@
+"""CPU restatement of the reference's bosonic DMRG axis primitives (qlten::dmrg, reference
+tensor_manipulation/dmrg/axis_ops.h), block by block with numpy. Test infrastructure only:
+pinned against the reference's outputs in tests/golden/axis_ops.npz.
+
+  axis_diagonal        ApplyAxisDiagonal (axis_ops.h:2370-2547): out = beta out + alpha D(in),
+                       D multiplying every degeneracy slice of `axis` by its value
+  axis_sector_scalars  ApplyAxisSectorScalarsPreserveOrder (axis_ops.h:2655-2744): each block
+                       times the value of its sector on `axis`
+  axis_rank2           ApplyRank2ToAxisPreserveOrder (axis_ops.h:2862-2993): contract `axis`
+                       with the operator's index 0, index 1 takes the axis' place
+  axis_two_rank2       ApplyTwoRank2ToAxesPreserveOrder (axis_ops.h:2995-3126): op1 on axis1,
+                       then op2 on axis2
+"""
+from typing import Optional, Sequence
+
+import numpy as np
+
+from oracle import oracle
+from tensortoolkit_gb300.tensor import BSTensor, Leg
+
+
+def _sector_starts(leg: Leg) -> np.ndarray:
+    return np.concatenate([[0], np.cumsum(leg.dims)[:-1]]).astype(np.int64)
+
+
+def axis_diagonal(t: BSTensor, axis: int, values: np.ndarray, alpha=1.0, beta=0.0,
+                  out: Optional[BSTensor] = None) -> BSTensor:
+    """values: one per (sector, degeneracy) of t's `axis`, sectors in index order."""
+    starts = _sector_starts(t.legs[axis])
+    res = t.copy()
+    shapes = t.block_shapes()
+    for b in range(t.nblk):
+        s = int(t.coords[b, axis])
+        v = np.asarray(values[starts[s]:starts[s] + shapes[b, axis]])
+        shp = [1] * t.rank
+        shp[axis] = -1
+        blk = t.block(b) * v.reshape(shp) * alpha
+        if beta != 0 and out is not None:
+            blk = blk + beta * out.block(b)
+        o = int(t.offsets[b])
+        res.data[o:o + blk.size] = blk.reshape(-1)
+    return res
+
+
+def axis_sector_scalars(t: BSTensor, axis: int, values_by_sector: Sequence[float]) -> BSTensor:
+    res = t.copy()
+    for b in range(t.nblk):
+        o = int(t.offsets[b])
+        n = int(np.prod(t.block_shapes()[b]))
+        res.data[o:o + n] *= values_by_sector[int(t.coords[b, axis])]
+    return res
+
+
+def transpose(t: BSTensor, perm: Sequence[int]) -> BSTensor:
+    """Bosonic block-sparse transpose: legs and block coordinates permuted, blocks re-sorted
+    to ascending block index."""
+    legs = [t.legs[p] for p in perm]
+    coords = t.coords[:, list(perm)]
+    order = np.lexsort(coords.T[::-1]) if t.nblk else np.zeros(0, np.int64)
+    coords_s = coords[order]
+    res = BSTensor(legs, coords_s, t.dtype, np.zeros(t.size, t.dtype))
+    for nb, b in enumerate(order):
+        blk = np.transpose(t.block(int(b)), perm)
+        o = int(res.offsets[nb])
+        res.data[o:o + blk.size] = blk.reshape(-1)
+    return res
+
+
+def axis_rank2(t: BSTensor, op: BSTensor, axis: int) -> BSTensor:
+    c, _ = oracle.contract(t, op, [[axis], [0]])
+    r = t.rank
+    perm = list(range(axis)) + [r - 1] + list(range(axis, r - 1))
+    return transpose(c, perm) if axis != r - 1 else c
+
+
+def axis_two_rank2(t: BSTensor, op1: BSTensor, axis1: int, op2: BSTensor, axis2: int) -> BSTensor:
+    return axis_rank2(axis_rank2(t, op1, axis1), op2, axis2)

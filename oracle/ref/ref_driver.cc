@@ -16,6 +16,10 @@
 //   qlten_io seed dir             tensors written by the reference's QLTensor stream operator
 //                                 (dir/<tag>.qlten) and dumped to <out>: U(1) real, fermionic
 //                                 complex, a scalar, a tensor with no blocks
+//   axis_ops seed                 qlten::dmrg axis primitives on a U(1) psi: ApplyAxisDiagonal
+//                                 (out of place, accumulate), ApplyAxisSectorScalarsPreserveOrder,
+//                                 ApplyRank2ToAxisPreserveOrder (boundary and middle axes),
+//                                 ApplyTwoRank2ToAxesPreserveOrder
 //   svd_u1 qmax sigma D seed trunc Dmin Dmax   SVD of a spectrum-controlled psi (ldims 2)
 //   svd_stress nb lo hi seed trunc Dmin Dmax   SVD of a rank-2 block-diagonal tensor
 //   svd_f half D seed trunc Dmin Dmax          SVD of a fermionic complex psi
@@ -23,6 +27,7 @@
 //   qr_f half D seed                            QR of a fermionic complex psi
 //   time_matvec_u1 qmax sigma D seed threads iters   wall time of the chain (no dump)
 #include "qlten/qlten.h"
+#include "qlten/tensor_manipulation/dmrg/axis_ops.h"
 #include "synth.h"
 #include "../qtb_io.h"
 
@@ -378,6 +383,68 @@ int main(int argc, char** argv) {
       QLTensor<double, U1QN> sc2;
       Contract(&P, &Pd, {{0, 1, 2, 3}, {0, 1, 2, 3}}, &sc2);
       save("u_scalar", sc2);
+    } else if (cs == "axis_ops") {
+      using T = QLTensor<double, U1QN>;
+      sy::Normal rng(std::stoull(A(3)));
+      auto mv = sy::heisenberg_u1_random(2, 1.0, 10, std::stoull(A(3)));
+      const auto& pl = mv.psi.legs;
+      T P = to_qlten<double, U1QN>(mv.psi);
+      dump(w, "psi", P);
+      // diagonal values per (sector, degeneracy) of an axis
+      auto diag_op = [&](size_t axis) {
+        dmrg::AxisDiagonalOp<double, U1QN> op{P.GetIndex(axis), {}};
+        for (auto& sct : op.index.GetQNScts()) {
+          std::vector<double> v(sct.GetDegeneracy());
+          for (auto& x : v) x = rng.next();
+          op.values.push_back(v);
+        }
+        std::vector<double> flat;
+        for (auto& v : op.values) flat.insert(flat.end(), v.begin(), v.end());
+        return std::make_pair(op, flat);
+      };
+      for (size_t axis : {1u, 3u}) {
+        auto [op, flat] = diag_op(axis);
+        const std::string tag = "diag" + std::to_string(axis);
+        w.f64(tag + ".values", flat);
+        T out;
+        dmrg::ApplyAxisDiagonal(P, axis, op, out, 1.5, 0.0);
+        dump(w, tag + ".out", out);
+        T acc = out;                         // accumulate: acc = 0.5 acc - 2 D(P)
+        dmrg::ApplyAxisDiagonal(P, axis, op, acc, -2.0, 0.5);
+        dump(w, tag + ".acc", acc);
+      }
+      {
+        dmrg::AxisSectorScalar<double, U1QN> sc{0, {}};
+        for (size_t s2 = 0; s2 < P.GetIndex(0).GetQNSctNum(); ++s2) sc.values_by_sector.push_back(rng.next());
+        w.f64("sect.values", sc.values_by_sector);
+        T out;
+        dmrg::ApplyAxisSectorScalarsPreserveOrder(P, sc, out, dmrg::AxisApplyStorageMode::kOutOfPlace);
+        dump(w, "sect.out", out);
+      }
+      // rank-2 operators {InverseIndex(axis leg), new leg}: the new leg keeps the charges with
+      // other degeneracies
+      auto rank2 = [&](size_t axis, int64_t grow) {
+        sy::Leg in = pl[axis];
+        sy::Leg nl = in;
+        for (auto& d : nl.dims) d = std::max<int64_t>(1, d + grow);
+        return to_qlten<double, U1QN>(random_like({in.inverse(), nl}, {0}, false, rng));
+      };
+      for (size_t axis : {0u, 2u, 3u}) {
+        T op = rank2(axis, axis == 2 ? 1 : -1);
+        const std::string tag = "r2_" + std::to_string(axis);
+        dump(w, tag + ".op", op);
+        T out;
+        dmrg::ApplyRank2ToAxisPreserveOrder(P, op, axis, out);
+        dump(w, tag + ".out", out);
+      }
+      {
+        T op1 = rank2(0, 1), op2 = rank2(3, -1);
+        dump(w, "two.op1", op1);
+        dump(w, "two.op2", op2);
+        T out;
+        dmrg::ApplyTwoRank2ToAxesPreserveOrder(P, op1, 0, op2, 3, out);
+        dump(w, "two.out", out);
+      }
     } else if (cs == "svd_u1") {
       auto t = sy::svd_psi(std::stoi(A(3)), std::stod(A(4)), std::stoll(A(5)), std::stoull(A(6)));
       svd_case<double, U1QN>(w, t, 2, std::stod(A(7)), std::stoull(A(8)), std::stoull(A(9)));

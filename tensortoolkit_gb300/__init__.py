@@ -12,7 +12,9 @@ from .tensor import BSTensor, Leg, IN, OUT  # noqa: F401
 
 _API = {"Contract", "ContractionPlan", "ContractContiguousAxes", "ContiguousContractionPlan",
         "ContractTailHeadContiguous", "ContractTailHeadContiguousAccumulate",
-        "TryContractTailHeadContiguousAccumulate", "AccumulatePlan", "read_qlten", "write_qlten", "Transpose", "SVD", "QR", "Matvec", "Lanczos", "DTensor", "Context",
+        "TryContractTailHeadContiguousAccumulate", "AccumulatePlan", "read_qlten", "write_qlten", "ApplyAxisDiagonal",
+        "ApplyAxisDiagonalInPlace", "ApplyAxisSectorScalars", "AxisRank2Plan", "ApplyRank2ToAxisPreserveOrder",
+        "ApplyTwoRank2ToAxesPreserveOrder", "Transpose", "SVD", "QR", "Matvec", "Lanczos", "DTensor", "Context",
         "context"}
 
 

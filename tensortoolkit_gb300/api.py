@@ -313,6 +313,106 @@ def TryContractTailHeadContiguousAccumulate(a: DTensor, b: DTensor, a_start: int
     return True, plan.execute(a, b, c, alpha, beta, mode=mode)
 
 
+# ------------------------------------------------------------------ dmrg axis primitives
+def _ab(x) -> np.ndarray:
+    return np.array([complex(x).real, complex(x).imag])
+
+
+def _axis_values(vals, is_complex: bool) -> np.ndarray:
+    v = np.asarray(vals)
+    return np.ascontiguousarray(v.astype(np.complex128) if is_complex else v.astype(np.float64)).view(np.float64)
+
+
+def ApplyAxisDiagonal(t: DTensor, axis: int, values, alpha=1.0, beta=0.0, out: Optional[DTensor] = None) -> DTensor:
+    """out = beta out + alpha D(t): qlten::dmrg::ApplyAxisDiagonal (reference
+    tensor_manipulation/dmrg/axis_ops.h:2370-2547). `values`: one per degeneracy of `axis`,
+    sectors in index order (AxisDiagonalOp::values flattened). `out` None: a new tensor
+    (beta must then be 0); `out is t`: ApplyAxisDiagonalInPlace."""
+    if out is None:
+        if complex(beta) != 0:
+            raise ValueError("beta != 0 needs an existing output")
+        out = DTensor.empty(t.meta, t.device)
+    d = _Desc(t.meta)
+    v = _axis_values(values, t.meta.is_complex)
+    al, be = _ab(alpha), _ab(beta)   # kept alive across the call
+    check(lib().qltg_axis_diagonal(context(t.device).h, d.ref, int(axis), v.ctypes.data, C.c_void_p(t.ptr),
+                                   C.c_void_p(out.ptr), al.ctypes.data, be.ctypes.data, stream_ptr(t.device)))
+    return out
+
+
+def ApplyAxisDiagonalInPlace(t: DTensor, axis: int, values) -> DTensor:
+    """qlten::dmrg::ApplyAxisDiagonalInPlace (axis_ops.h:2549-2582)."""
+    return ApplyAxisDiagonal(t, axis, values, 1.0, 0.0, out=t)
+
+
+def ApplyAxisSectorScalars(t: DTensor, axis: int, values_by_sector, out: Optional[DTensor] = None) -> DTensor:
+    """qlten::dmrg::ApplyAxisSectorScalarsPreserveOrder (axis_ops.h:2655-2744): every block
+    times the value of its sector on `axis` (out None: a new tensor; out is t: in place)."""
+    if out is None:
+        out = DTensor.empty(t.meta, t.device)
+    d = _Desc(t.meta)
+    v = _axis_values(values_by_sector, t.meta.is_complex)
+    check(lib().qltg_axis_sector_scalars(context(t.device).h, d.ref, int(axis), v.ctypes.data, C.c_void_p(t.ptr),
+                                         C.c_void_p(out.ptr), stream_ptr(t.device)))
+    return out
+
+
+class AxisRank2Plan:
+    """Planned ApplyRank2ToAxisPreserveOrder (axis_ops.h:2862-2993) or, with a second
+    operator, ApplyTwoRank2ToAxesPreserveOrder (:2995-3126)."""
+
+    def __init__(self, t: BSTensor, op1: BSTensor, axis1: int, op2: Optional[BSTensor] = None,
+                 axis2: Optional[int] = None, device: int = 0):
+        self.h = None
+        self.ctx = context(device)
+        self.device = device
+        dt, d1 = _Desc(t), _Desc(op1)
+        h = C.c_void_p()
+        legs = list(t.legs)
+        legs[axis1] = op1.legs[1]
+        if op2 is None:
+            check(lib().qltg_axis_rank2_plan_create(self.ctx.h, dt.ref, d1.ref, int(axis1), C.byref(h)))
+        else:
+            d2 = _Desc(op2)
+            check(lib().qltg_axis_two_rank2_plan_create(self.ctx.h, dt.ref, d1.ref, int(axis1), d2.ref, int(axis2),
+                                                        C.byref(h)))
+            legs[axis2] = op2.legs[1]
+        self.h = h
+        self.two = op2 is not None
+        self.result = _result_meta(h, lib().qltg_axis_plan_result, lib().qltg_axis_plan_result_blocks, legs, t.dtype)
+
+    def execute(self, t: DTensor, op1: DTensor, op2: Optional[DTensor] = None, out: Optional[DTensor] = None,
+                mode="fp64") -> DTensor:
+        if out is None:
+            out = DTensor.empty(self.result, self.device)
+        check(lib().qltg_axis_plan_exec(self.h, C.c_void_p(t.ptr), C.c_void_p(op1.ptr),
+                                        C.c_void_p(op2.ptr) if op2 is not None else None, C.c_void_p(out.ptr),
+                                        _mode(mode), stream_ptr(self.device)))
+        return out
+
+    def device_status(self) -> None:
+        check(lib().qltg_axis_plan_device_status(self.h, stream_ptr(self.device)))
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().qltg_axis_plan_destroy(self.h)
+        except Exception:
+            pass
+
+
+def ApplyRank2ToAxisPreserveOrder(t: DTensor, op: DTensor, axis: int, mode="fp64") -> DTensor:
+    """qlten::dmrg::ApplyRank2ToAxisPreserveOrder (axis_ops.h:2862-2993)."""
+    return AxisRank2Plan(t.meta, op.meta, axis, device=t.device).execute(t, op, mode=mode)
+
+
+def ApplyTwoRank2ToAxesPreserveOrder(t: DTensor, op1: DTensor, axis1: int, op2: DTensor, axis2: int,
+                                     mode="fp64") -> DTensor:
+    """qlten::dmrg::ApplyTwoRank2ToAxesPreserveOrder (axis_ops.h:2995-3126)."""
+    plan = AxisRank2Plan(t.meta, op1.meta, axis1, op2.meta, axis2, device=t.device)
+    return plan.execute(t, op1, op2, mode=mode)
+
+
 def read_qlten(path: str, qn: str = "U1QN", dtype: str = "f64", device: int = 0) -> DTensor:
     """Read a .qlten file (the reference's QLTensor stream format) straight into device
     memory: header parsed in libqltg.so, raw buffer through a pinned staging buffer."""

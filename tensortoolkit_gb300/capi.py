@@ -47,6 +47,17 @@ _SIGS = {
     "qltg_accum_exec": ([_P, _P, _P, _P, _P, _P, _P, C.c_int32, _P], C.c_int),
     "qltg_accum_plan_device_status": ([_P, _P], C.c_int),
     "qltg_accum_plan_destroy": ([_P], C.c_int),
+    "qltg_axis_diagonal": ([_P, C.POINTER(TensorDesc), C.c_int32, _P, _P, _P, _P, _P, _P], C.c_int),
+    "qltg_axis_sector_scalars": ([_P, C.POINTER(TensorDesc), C.c_int32, _P, _P, _P, _P], C.c_int),
+    "qltg_axis_rank2_plan_create": ([_P, C.POINTER(TensorDesc), C.POINTER(TensorDesc), C.c_int32, C.POINTER(_P)],
+                                    C.c_int),
+    "qltg_axis_two_rank2_plan_create": ([_P, C.POINTER(TensorDesc), C.POINTER(TensorDesc), C.c_int32,
+                                        C.POINTER(TensorDesc), C.c_int32, C.POINTER(_P)], C.c_int),
+    "qltg_axis_plan_result": ([_P, C.POINTER(C.c_int32), _I64P, _I64P], C.c_int),
+    "qltg_axis_plan_result_blocks": ([_P, _P, _P], C.c_int),
+    "qltg_axis_plan_exec": ([_P, _P, _P, _P, _P, C.c_int32, _P], C.c_int),
+    "qltg_axis_plan_device_status": ([_P, _P], C.c_int),
+    "qltg_axis_plan_destroy": ([_P], C.c_int),
     "qltg_qlten_open": ([C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(_P)], C.c_int),
     "qltg_qlten_info": ([_P, C.POINTER(C.c_int32), _I64P, _I64P, _I64P], C.c_int),
     "qltg_qlten_meta": ([_P, _P, _P, _P, _P, _P], C.c_int),

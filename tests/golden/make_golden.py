@@ -30,6 +30,7 @@ CASES = {
     "ctrct_contig": (["ctrct_contig", "11"], None),
     # also writes tests/golden/qlten/<tag>.qlten with the reference's stream operator
     "qlten_io": (["qlten_io", "5", "{qlten_dir}"], None),
+    "axis_ops": (["axis_ops", "3"], -1),
     "svd_u1_full": (["svd_u1", "4", "2.0", "40", "3", "1e-9", "1", "1000"], -1),
     "svd_u1_trunc": (["svd_u1", "4", "2.0", "40", "3", "1e-2", "1", "1000"], -1),
     "svd_u1_dmax": (["svd_u1", "4", "2.0", "40", "3", "1e-12", "1", "12"], -1),
