@@ -242,6 +242,18 @@ QLTG_API int qltg_axis_rank2_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* 
 QLTG_API int qltg_axis_two_rank2_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* t, const qltg_tensor_desc* op1,
                                              int32_t axis1, const qltg_tensor_desc* op2, int32_t axis2,
                                              qltg_axis_plan** plan);
+/* ApplyAxisMonomial (axis_ops.h:2746-2860): `axis` of t replaced by the output index
+ * (out_nsct sectors: out_qns, out_dims; t's direction); entries[4 e .. 4 e + 3] = (in_sector,
+ * in_offset, out_sector, out_offset) with coefs[e] (complex: interleaved), each satisfying
+ * output qn = input qn + flux. Output blocks: t's blocks mapped through every matching entry.
+ * Execute with qltg_axis_monomial_exec. */
+QLTG_API int qltg_axis_monomial_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* t, int32_t axis, int32_t out_nsct,
+                                            const int32_t* out_qns, const int64_t* out_dims, const int32_t* flux,
+                                            int64_t nentries, const int64_t* entries, const double* coefs,
+                                            qltg_axis_plan** plan);
+/* out = beta out + alpha M(in) over the generated topology (beta == 0 never reads out_dev). */
+QLTG_API int qltg_axis_monomial_exec(qltg_axis_plan* plan, const void* in_dev, void* out_dev, const double* alpha,
+                                     const double* beta, void* stream);
 QLTG_API int qltg_axis_plan_result(const qltg_axis_plan* plan, int32_t* rank, int64_t* nblk, int64_t* size);
 QLTG_API int qltg_axis_plan_result_blocks(const qltg_axis_plan* plan, int64_t* coords, int64_t* offsets);
 /* out_dev (the result topology) from in_dev and the operators (op2_dev: two-operator plans). */

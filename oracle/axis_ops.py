@@ -10,6 +10,10 @@ pinned against the reference's outputs in tests/golden/axis_ops.npz.
                        with the operator's index 0, index 1 takes the axis' place
   axis_two_rank2       ApplyTwoRank2ToAxesPreserveOrder (axis_ops.h:2995-3126): op1 on axis1,
                        then op2 on axis2
+  axis_monomial        ApplyAxisMonomial (axis_ops.h:2746-2860, topology :2241-2269, slice add
+                       :2306-2332): output blocks = input blocks mapped through every entry whose
+                       input sector matches; out = beta out + sum over entries of alpha coef
+                       (input slice in_offset -> output slice out_offset)
 """
 from typing import Optional, Sequence
 
@@ -75,3 +79,42 @@ def axis_rank2(t: BSTensor, op: BSTensor, axis: int) -> BSTensor:
 
 def axis_two_rank2(t: BSTensor, op1: BSTensor, axis1: int, op2: BSTensor, axis2: int) -> BSTensor:
     return axis_rank2(axis_rank2(t, op1, axis1), op2, axis2)
+
+
+def axis_monomial(t: BSTensor, axis: int, out_leg: Leg, entries, coefs, alpha=1.0, beta=0.0,
+                  out: Optional[BSTensor] = None) -> BSTensor:
+    """entries: rows (in_sector, in_offset, out_sector, out_offset)."""
+    legs = list(t.legs)
+    legs[axis] = out_leg
+    ent = np.asarray(entries, np.int64).reshape(-1, 4)
+    seen = {}
+    for b in range(t.nblk):
+        for e in ent:
+            if e[0] != t.coords[b, axis]:
+                continue
+            c = t.coords[b].copy()
+            c[axis] = e[2]
+            seen.setdefault(tuple(int(x) for x in c), None)
+    coords = sorted(seen.keys(), key=lambda c: tuple(c))
+    res = BSTensor(legs, np.array(coords, np.int64).reshape(-1, t.rank), t.dtype,
+                   np.zeros(0, t.dtype) if not coords else None)
+    res.data = np.zeros(res.size, t.dtype)
+    pos = {tuple(int(x) for x in res.coords[q]): q for q in range(res.nblk)}
+    if beta != 0 and out is not None:
+        res.data[:] = beta * out.data
+    for b in range(t.nblk):
+        blk = t.block(b)
+        for e, cf in zip(ent, coefs):
+            if e[0] != t.coords[b, axis] or cf == 0:
+                continue
+            c = t.coords[b].copy()
+            c[axis] = e[2]
+            q = pos[tuple(int(x) for x in c)]
+            o = int(res.offsets[q])
+            shp = res.block_shapes()[q]
+            ob = res.data[o:o + int(np.prod(shp))].reshape(shp)
+            src = np.take(blk, [int(e[1])], axis=axis)
+            idx = [slice(None)] * t.rank
+            idx[axis] = slice(int(e[3]), int(e[3]) + 1)
+            ob[tuple(idx)] += alpha * cf * src
+    return res

@@ -31,6 +31,7 @@
 #include "synth.h"
 #include "../qtb_io.h"
 
+#include <array>
 #include <chrono>
 #include <complex>
 #include <cstdio>
@@ -437,6 +438,28 @@ int main(int argc, char** argv) {
         dmrg::ApplyRank2ToAxisPreserveOrder(P, op, axis, out);
         dump(w, tag + ".out", out);
       }
+      // monomial operators: a raising map on the physical leg (flux +1) and a permuting,
+      // accumulating map inside the sectors of the right bond leg (flux 0)
+      auto monomial = [&](const std::string& tag, size_t axis, int flux,
+                          const std::vector<std::array<size_t, 4>>& ent, const std::vector<double>& coefs) {
+        dmrg::AxisMonomialOp<double, U1QN> op{P.GetIndex(axis), P.GetIndex(axis), U1QN(flux), {}};
+        std::vector<int64_t> flat;
+        for (size_t i = 0; i < ent.size(); ++i) {
+          op.entries.push_back({ent[i][0], ent[i][1], ent[i][2], ent[i][3], coefs[i]});
+          flat.insert(flat.end(), {(int64_t)ent[i][0], (int64_t)ent[i][1], (int64_t)ent[i][2], (int64_t)ent[i][3]});
+        }
+        w.i64(tag + ".entries", flat);
+        w.f64(tag + ".coefs", coefs);
+        w.i64(tag + ".params", {(int64_t)axis, flux});
+        T out;
+        dmrg::ApplyAxisMonomial(P, axis, op, out, 1.25, 0.0);
+        dump(w, tag + ".out", out);
+        dmrg::ApplyAxisMonomial(P, axis, op, out, -0.5, 2.0);   // accumulate onto it
+        dump(w, tag + ".acc", out);
+      };
+      monomial("mono_p", 1, 1, {{0, 0, 1, 0}}, {1.0});
+      monomial("mono_b", 3, 0, {{2, 0, 2, 3}, {2, 3, 2, 0}, {2, 1, 2, 1}, {2, 1, 2, 3}, {1, 0, 1, 1}, {3, 1, 3, 0}},
+               {0.5, -1.0, 2.0, 0.25, 1.5, -0.75});
       {
         T op1 = rank2(0, 1), op2 = rank2(3, -1);
         dump(w, "two.op1", op1);

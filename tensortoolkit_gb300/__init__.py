@@ -14,7 +14,7 @@ _API = {"Contract", "ContractionPlan", "ContractContiguousAxes", "ContiguousCont
         "ContractTailHeadContiguous", "ContractTailHeadContiguousAccumulate",
         "TryContractTailHeadContiguousAccumulate", "AccumulatePlan", "read_qlten", "write_qlten", "ApplyAxisDiagonal",
         "ApplyAxisDiagonalInPlace", "ApplyAxisSectorScalars", "AxisRank2Plan", "ApplyRank2ToAxisPreserveOrder",
-        "ApplyTwoRank2ToAxesPreserveOrder", "Transpose", "SVD", "QR", "Matvec", "Lanczos", "DTensor", "Context",
+        "ApplyTwoRank2ToAxesPreserveOrder", "ApplyAxisMonomial", "AxisMonomialPlan", "Transpose", "SVD", "QR", "Matvec", "Lanczos", "DTensor", "Context",
         "context"}
 
 

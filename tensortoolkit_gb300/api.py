@@ -401,6 +401,56 @@ class AxisRank2Plan:
             pass
 
 
+class AxisMonomialPlan:
+    """Planned qlten::dmrg::ApplyAxisMonomial (axis_ops.h:2746-2860): `entries` rows
+    (in_sector, in_offset, out_sector, out_offset) with `coefs`; `out_leg` replaces `axis`;
+    output qn = input qn + flux for every entry."""
+
+    def __init__(self, t: BSTensor, axis: int, out_leg: Leg, flux: Sequence[int], entries, coefs,
+                 device: int = 0):
+        self.h = None
+        self.ctx = context(device)
+        self.device = device
+        dt = _Desc(t)
+        ent = np.ascontiguousarray(np.asarray(entries, np.int64).reshape(-1, 4))
+        cf = _axis_values(coefs, t.is_complex)
+        oq = np.ascontiguousarray(out_leg.qns.reshape(-1), np.int32)
+        od = np.ascontiguousarray(out_leg.dims, np.int64)
+        fl = np.ascontiguousarray(np.asarray(flux, np.int32).reshape(-1))
+        h = C.c_void_p()
+        check(lib().qltg_axis_monomial_plan_create(self.ctx.h, dt.ref, int(axis), int(out_leg.nsct), oq.ctypes.data,
+                                                   od.ctypes.data, fl.ctypes.data, len(ent),
+                                                   ent.ctypes.data if len(ent) else None,
+                                                   cf.ctypes.data if len(ent) else None, C.byref(h)))
+        self.h = h
+        legs = list(t.legs)
+        legs[axis] = Leg(t.legs[axis].dir, out_leg.qns, out_leg.dims, t.legs[axis].parity_comp)
+        self.result = _result_meta(h, lib().qltg_axis_plan_result, lib().qltg_axis_plan_result_blocks, legs, t.dtype)
+
+    def execute(self, t: DTensor, alpha=1.0, beta=0.0, out: Optional[DTensor] = None) -> DTensor:
+        if out is None:
+            if complex(beta) != 0:
+                raise ValueError("beta != 0 needs an existing output")
+            out = DTensor.empty(self.result, self.device)
+        al, be = _ab(alpha), _ab(beta)
+        check(lib().qltg_axis_monomial_exec(self.h, C.c_void_p(t.ptr), C.c_void_p(out.ptr), al.ctypes.data,
+                                            be.ctypes.data, stream_ptr(self.device)))
+        return out
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().qltg_axis_plan_destroy(self.h)
+        except Exception:
+            pass
+
+
+def ApplyAxisMonomial(t: DTensor, axis: int, out_leg: Leg, flux, entries, coefs, alpha=1.0, beta=0.0,
+                      out: Optional[DTensor] = None) -> DTensor:
+    """qlten::dmrg::ApplyAxisMonomial (axis_ops.h:2746-2860)."""
+    return AxisMonomialPlan(t.meta, axis, out_leg, flux, entries, coefs, t.device).execute(t, alpha, beta, out)
+
+
 def ApplyRank2ToAxisPreserveOrder(t: DTensor, op: DTensor, axis: int, mode="fp64") -> DTensor:
     """qlten::dmrg::ApplyRank2ToAxisPreserveOrder (axis_ops.h:2862-2993)."""
     return AxisRank2Plan(t.meta, op.meta, axis, device=t.device).execute(t, op, mode=mode)

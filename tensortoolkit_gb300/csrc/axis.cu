@@ -12,6 +12,12 @@
 //      new leg); one batched permute puts the new leg back at `axis` (none when it is the
 //      last axis).
 //  * ApplyTwoRank2ToAxesPreserveOrder (:2995-3126): op1 on axis1, then op2 on axis2.
+//  * ApplyAxisMonomial (:2746-2860; topology :2241-2269; slice add :2306-2332): entries map an
+//      input degeneracy slice (in_sector, in_offset) of `axis` to an output slice (out_sector,
+//      out_offset) with a coefficient. The plan builds the output topology and, per output
+//      slice, the list of contributing input slices in the reference's order (input blocks
+//      ascending, entries in order); one kernel writes every output slice once:
+//      out = beta out + sum alpha coef in_slice. No atomics, deterministic.
 // All are bosonic-only, as in the reference (fermionic tensors: QLTG_ERR_UNSUPPORTED).
 #include <algorithm>
 #include <memory>
@@ -52,6 +58,44 @@ __global__ void __launch_bounds__(256) k_axis_scale(const AxisItem* __restrict__
       T r = amul(alpha, amul(v, in[w.off + g]));
       if (read_out) r = aadd(r, amul(beta, out[w.off + g]));
       out[w.off + g] = r;
+    }
+  }
+}
+
+struct MonoMap {             // one contributing input slice
+  int64_t in_off;            // element offset of the input block
+  int32_t in_axis_dim, in_offset;
+  double coef_re, coef_im;
+};
+struct MonoItem {            // one output slice
+  int64_t out_off;           // element offset of the output block
+  int32_t out_axis_dim, out_offset;
+  int32_t outer, inner;      // elements before / after the axis inside the block
+  int32_t map0, map1;        // its maps
+};
+
+__device__ __forceinline__ double azero(double) { return 0.0; }
+__device__ __forceinline__ double2 azero(double2) { return make_double2(0.0, 0.0); }
+__device__ __forceinline__ double mcoef(double re, double, double) { return re; }
+__device__ __forceinline__ double2 mcoef(double re, double im, double2) { return make_double2(re, im); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_axis_monomial(const MonoItem* __restrict__ items, int nitems,
+                                                       const MonoMap* __restrict__ maps, const T* __restrict__ in,
+                                                       T* __restrict__ out, T alpha, T beta, int read_out) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const MonoItem w = items[it];
+    const int64_t n = (int64_t)w.outer * w.inner;
+    for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+      const int64_t o = e / w.inner, i = e - o * w.inner;
+      const int64_t dst = w.out_off + (o * w.out_axis_dim + w.out_offset) * w.inner + i;
+      T acc = read_out ? amul(beta, out[dst]) : azero(T());
+      for (int mi = w.map0; mi < w.map1; ++mi) {
+        const MonoMap m = maps[mi];
+        const T c = amul(alpha, mcoef(m.coef_re, m.coef_im, T()));
+        acc = aadd(acc, amul(c, in[m.in_off + (o * m.in_axis_dim + m.in_offset) * w.inner + i]));
+      }
+      out[dst] = acc;
     }
   }
 }
@@ -182,7 +226,12 @@ struct qltg_axis_plan {
   qltg::Rank2Step s1, s2;
   bool two = false;
   qltg::DevBuf mid;   // the single-axis intermediate of the two-operator form
-  const qltg::Meta& out() const { return two ? s2.out : s1.out; }
+  // monomial form
+  bool mono = false;
+  qltg::Meta mono_out;
+  int mono_items = 0;
+  qltg::DevBuf d_mono_items, d_mono_maps;
+  const qltg::Meta& out() const { return mono ? mono_out : (two ? s2.out : s1.out); }
 };
 
 using namespace qltg;
@@ -268,6 +317,136 @@ int qltg_axis_two_rank2_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* t, co
   });
 }
 
+int qltg_axis_monomial_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* t, int32_t axis, int32_t out_nsct,
+                                   const int32_t* out_qns, const int64_t* out_dims, const int32_t* flux,
+                                   int64_t nentries, const int64_t* entries, const double* coefs,
+                                   qltg_axis_plan** plan) {
+  return guarded([&] {
+    QLTG_CHECK(ctx && plan, QLTG_ERR_INVALID, "null ctx or plan out-pointer");
+    const Meta m = meta_from_desc(t);
+    require_bosonic_axis(m, axis);
+    QLTG_CHECK(out_nsct >= 1 && out_qns && out_dims && flux, QLTG_ERR_INVALID, "null or empty output index");
+    QLTG_CHECK(nentries >= 0 && (nentries == 0 || (entries && coefs)), QLTG_ERR_INVALID, "null entries");
+    QLTG_CUDA(cudaSetDevice(ctx->device));
+    const int nc = m.ncomp, per = m.dtype == QLTG_C128 ? 2 : 1;
+    auto h = std::make_unique<qltg_axis_plan>();
+    h->ctx = ctx;
+    h->mono = true;
+    // output index: the axis replaced (same direction)
+    Meta& O = h->mono_out;
+    O = m;
+    O.qns[axis].assign(out_qns, out_qns + (int64_t)out_nsct * nc);
+    O.dims[axis].assign(out_dims, out_dims + out_nsct);
+    for (auto d : O.dims[axis]) QLTG_CHECK(d >= 1, QLTG_ERR_INVALID, "output degeneracy must be >= 1");
+    // entries: range and flux checks (output qn = input qn + flux)
+    for (int64_t e = 0; e < nentries; ++e) {
+      const int64_t is = entries[4 * e], io = entries[4 * e + 1], os = entries[4 * e + 2], oo = entries[4 * e + 3];
+      QLTG_CHECK(is >= 0 && is < m.nsct(axis) && os >= 0 && os < out_nsct, QLTG_ERR_INVALID,
+                 "monomial entry sector out of range");
+      QLTG_CHECK(io >= 0 && io < m.dims[axis][is] && oo >= 0 && oo < out_dims[os], QLTG_ERR_INVALID,
+                 "monomial entry degeneracy offset out of range");
+      for (int c = 0; c < nc; ++c)
+        QLTG_CHECK(out_qns[os * nc + c] == m.qns[axis][is * nc + c] + flux[c], QLTG_ERR_INVALID,
+                   "monomial entry quantum numbers are inconsistent with the flux");
+    }
+    // output topology: input blocks mapped through every matching entry, ascending block index
+    std::vector<std::vector<int64_t>> oc;
+    std::vector<uint64_t> okey;
+    for (int64_t b = 0; b < m.nblk; ++b)
+      for (int64_t e = 0; e < nentries; ++e) {
+        if (entries[4 * e] != m.coords[b * m.rank + axis]) continue;
+        std::vector<int64_t> c(m.coords.begin() + b * m.rank, m.coords.begin() + (b + 1) * m.rank);
+        c[axis] = entries[4 * e + 2];
+        const uint64_t k = O.blk_idx(c.data());
+        if (std::find(okey.begin(), okey.end(), k) == okey.end()) {
+          okey.push_back(k);
+          oc.push_back(c);
+        }
+      }
+    std::vector<size_t> ord(oc.size());
+    std::iota(ord.begin(), ord.end(), 0);
+    std::sort(ord.begin(), ord.end(), [&](size_t x, size_t y) { return okey[x] < okey[y]; });
+    O.coords.clear();
+    for (size_t i : ord) O.coords.insert(O.coords.end(), oc[i].begin(), oc[i].end());
+    O.nblk = (int64_t)oc.size();
+    O.refresh_offsets();
+    // per output slice (block, out_offset): its maps, in the reference's order
+    std::vector<int64_t> slice_base(O.nblk + 1, 0);
+    for (int64_t q = 0; q < O.nblk; ++q) slice_base[q + 1] = slice_base[q] + O.dim(q, axis);
+    std::vector<std::vector<MonoMap>> slices(slice_base[O.nblk]);
+    auto find_block = [&](const std::vector<int64_t>& c) {
+      const uint64_t k = O.blk_idx(c.data());
+      int64_t lo = 0, hi = O.nblk - 1;
+      while (lo <= hi) {
+        const int64_t mid = (lo + hi) / 2;
+        const uint64_t km = O.blk_idx(&O.coords[mid * O.rank]);
+        if (km == k) return mid;
+        if (km < k) lo = mid + 1; else hi = mid - 1;
+      }
+      return (int64_t)-1;
+    };
+    for (int64_t b = 0; b < m.nblk; ++b)
+      for (int64_t e = 0; e < nentries; ++e) {
+        if (entries[4 * e] != m.coords[b * m.rank + axis]) continue;
+        const double cr = coefs[e * per], ci = per == 2 ? coefs[e * per + 1] : 0.0;
+        if (cr == 0.0 && ci == 0.0) continue;
+        std::vector<int64_t> c(m.coords.begin() + b * m.rank, m.coords.begin() + (b + 1) * m.rank);
+        c[axis] = entries[4 * e + 2];
+        const int64_t q = find_block(c);
+        slices[slice_base[q] + entries[4 * e + 3]].push_back(
+            MonoMap{m.offsets[b], (int32_t)m.dim(b, axis), (int32_t)entries[4 * e + 1], cr, ci});
+      }
+    std::vector<MonoItem> items;
+    std::vector<MonoMap> maps;
+    for (int64_t q = 0; q < O.nblk; ++q) {
+      int64_t outer = 1, inner = 1;
+      for (int l = 0; l < axis; ++l) outer *= O.dim(q, l);
+      for (int l = axis + 1; l < O.rank; ++l) inner *= O.dim(q, l);
+      QLTG_CHECK(outer * inner < ((int64_t)1 << 31), QLTG_ERR_UNSUPPORTED, "block slice above 2^31 elements");
+      for (int64_t o = 0; o < O.dim(q, axis); ++o) {
+        auto& v = slices[slice_base[q] + o];
+        items.push_back(MonoItem{O.offsets[q], (int32_t)O.dim(q, axis), (int32_t)o, (int32_t)outer, (int32_t)inner,
+                                 (int32_t)maps.size(), (int32_t)(maps.size() + v.size())});
+        maps.insert(maps.end(), v.begin(), v.end());
+      }
+    }
+    cudaStream_t s;
+    QLTG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    h->d_mono_items = upload(items, s);
+    h->d_mono_maps = upload(maps, s);
+    QLTG_CUDA(cudaStreamSynchronize(s));
+    QLTG_CUDA(cudaStreamDestroy(s));
+    h->mono_items = (int)items.size();
+    *plan = h.release();
+  });
+}
+
+int qltg_axis_monomial_exec(qltg_axis_plan* plan, const void* in_dev, void* out_dev, const double* alpha,
+                            const double* beta, void* stream) {
+  return guarded([&] {
+    QLTG_CHECK(plan && plan->mono, QLTG_ERR_INVALID, "not a monomial plan");
+    QLTG_CHECK(in_dev && out_dev && alpha && beta, QLTG_ERR_INVALID, "null argument");
+    QLTG_CHECK(in_dev != out_dev, QLTG_ERR_INVALID, "output aliases the input");
+    QLTG_CUDA(cudaSetDevice(plan->ctx->device));
+    if (!plan->mono_items) return;
+    const bool cplx = plan->mono_out.dtype == QLTG_C128;
+    QLTG_CHECK(cplx || (alpha[1] == 0.0 && beta[1] == 0.0), QLTG_ERR_INVALID, "complex alpha or beta for a real tensor");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int grid = std::min(plan->mono_items, std::max(1, plan->ctx->num_sms) * 8);
+    const int read_out = (beta[0] != 0.0 || beta[1] != 0.0) ? 1 : 0;
+    if (cplx)
+      k_axis_monomial<double2><<<grid, 256, 0, s>>>(
+          plan->d_mono_items.as<MonoItem>(), plan->mono_items, plan->d_mono_maps.as<MonoMap>(),
+          static_cast<const double2*>(in_dev), static_cast<double2*>(out_dev), make_double2(alpha[0], alpha[1]),
+          make_double2(beta[0], beta[1]), read_out);
+    else
+      k_axis_monomial<double><<<grid, 256, 0, s>>>(plan->d_mono_items.as<MonoItem>(), plan->mono_items,
+                                                   plan->d_mono_maps.as<MonoMap>(), static_cast<const double*>(in_dev),
+                                                   static_cast<double*>(out_dev), alpha[0], beta[0], read_out);
+    QLTG_CUDA(cudaGetLastError());
+  });
+}
+
 int qltg_axis_plan_result(const qltg_axis_plan* plan, int32_t* rank, int64_t* nblk, int64_t* size) {
   return guarded([&] {
     QLTG_CHECK(plan, QLTG_ERR_INVALID, "null plan");
@@ -288,6 +467,7 @@ int qltg_axis_plan_exec(qltg_axis_plan* plan, const void* in_dev, const void* op
                         void* out_dev, int32_t mode, void* stream) {
   return guarded([&] {
     QLTG_CHECK(plan && in_dev && op1_dev && out_dev, QLTG_ERR_INVALID, "null argument");
+    QLTG_CHECK(!plan->mono, QLTG_ERR_INVALID, "a monomial plan runs through qltg_axis_monomial_exec");
     QLTG_CHECK(!plan->two || op2_dev, QLTG_ERR_INVALID, "null second operator");
     QLTG_CHECK(out_dev != in_dev, QLTG_ERR_INVALID, "output aliases the input");
     QLTG_CUDA(cudaSetDevice(plan->ctx->device));
@@ -306,6 +486,7 @@ int qltg_axis_plan_device_status(qltg_axis_plan* plan, void* stream) {
     QLTG_CHECK(plan, QLTG_ERR_INVALID, "null plan");
     QLTG_CUDA(cudaSetDevice(plan->ctx->device));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (plan->mono) return;
     QLTG_CHECK(split_device_error(plan->s1.c, s) == 0 && (!plan->two || split_device_error(plan->s2.c, s) == 0),
                QLTG_ERR_TIMEOUT, "a bounded tensor-core wait expired in the split-precision GEMM");
   });

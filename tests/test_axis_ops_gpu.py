@@ -8,9 +8,9 @@ import pytest
 
 from oracle import axis_ops
 from tensortoolkit_gb300 import capi
-from tensortoolkit_gb300.api import (ApplyAxisDiagonal, ApplyAxisDiagonalInPlace, ApplyAxisSectorScalars,
-                                     ApplyRank2ToAxisPreserveOrder, ApplyTwoRank2ToAxesPreserveOrder, AxisRank2Plan,
-                                     DTensor)
+from tensortoolkit_gb300.api import (ApplyAxisDiagonal, ApplyAxisDiagonalInPlace, ApplyAxisMonomial,
+                                     ApplyAxisSectorScalars, ApplyRank2ToAxisPreserveOrder,
+                                     ApplyTwoRank2ToAxesPreserveOrder, AxisMonomialPlan, AxisRank2Plan, DTensor)
 from tensortoolkit_gb300.tensor import BSTensor, rel_frob, same_topology
 
 pytestmark = pytest.mark.gpu
@@ -73,6 +73,33 @@ def test_two_rank2_vs_reference(gpu, rec):
         got = ApplyTwoRank2ToAxesPreserveOrder(DTensor.from_host(psi), DTensor.from_host(op1), 0,
                                                DTensor.from_host(op2), 3, mode=mode).to_host()
         assert same_topology(got, ref) and rel_frob(got.data, ref.data) <= 1e-12
+
+
+@pytest.mark.parametrize("tag", ["mono_p", "mono_b"])
+def test_monomial_vs_reference(gpu, rec, tag):
+    """A raising map on the physical leg (flux +1) and a permuting, accumulating map inside the
+    bond sectors (flux 0): out = 1.25 M(psi), then acc = -0.5 M(psi) + 2 out."""
+    psi = _t(rec, "psi")
+    axis, flux = (int(x) for x in rec[tag + ".params"])
+    ent = rec[tag + ".entries"].reshape(-1, 4)
+    coefs = rec[tag + ".coefs"]
+    leg = psi.legs[axis]
+    dp = DTensor.from_host(psi)
+    plan = AxisMonomialPlan(psi, axis, leg, [flux], ent, coefs)
+    out = plan.execute(dp, 1.25, 0.0)
+    ref = _t(rec, tag + ".out")
+    got = out.to_host()
+    assert same_topology(got, ref) and rel_frob(got.data, ref.data) <= 1e-15
+    acc = ApplyAxisMonomial(dp, axis, leg, [flux], ent, coefs, -0.5, 2.0, out=out)
+    ref2 = _t(rec, tag + ".acc")
+    got2 = acc.to_host()
+    assert same_topology(got2, ref2) and rel_frob(got2.data, ref2.data) <= 1e-15
+
+
+def test_monomial_flux_mismatch_rejected(gpu, rec):
+    psi = _t(rec, "psi")
+    with pytest.raises(capi.QltgError):
+        AxisMonomialPlan(psi, 1, psi.legs[1], [0], [[0, 0, 1, 0]], [1.0])
 
 
 def test_rank2_large_vs_oracle(gpu):

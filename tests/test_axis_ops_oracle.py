@@ -50,3 +50,16 @@ def test_two_rank2(rec):
     out = axis_ops.axis_two_rank2(psi, _t(rec, "two.op1"), 0, _t(rec, "two.op2"), 3)
     ref = _t(rec, "two.out")
     assert same_topology(out, ref) and rel_frob(out.data, ref.data) <= 1e-13
+
+
+@pytest.mark.parametrize("tag", ["mono_p", "mono_b"])
+def test_monomial(rec, tag):
+    psi = _t(rec, "psi")
+    axis, _ = (int(x) for x in rec[tag + ".params"])
+    ent = rec[tag + ".entries"].reshape(-1, 4)
+    ref = _t(rec, tag + ".out")
+    out = axis_ops.axis_monomial(psi, axis, psi.legs[axis], ent, rec[tag + ".coefs"], 1.25, 0.0)
+    assert same_topology(out, ref) and rel_frob(out.data, ref.data) <= 1e-15
+    acc = axis_ops.axis_monomial(psi, axis, psi.legs[axis], ent, rec[tag + ".coefs"], -0.5, 2.0, out=ref)
+    ref2 = _t(rec, tag + ".acc")
+    assert same_topology(acc, ref2) and rel_frob(acc.data, ref2.data) <= 1e-15
