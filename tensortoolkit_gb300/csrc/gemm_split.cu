@@ -844,6 +844,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   QLTG_CUDA(cudaMemsetAsync(error.get(), 0, sizeof(int), s));
   // per device (the attribute belongs to the current device's copy of the kernel)
   QLTG_CUDA(cudaFuncSetAttribute(k_gemm_split, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+  df_build(df, g, p.ctx->num_sms, s);
   QLTG_CUDA(cudaStreamSynchronize(s));
   built = true;
 }
@@ -895,6 +896,7 @@ void split_prepack_static(CtrctPlan& p, const void* a_static, const void* b_stat
     if (p.b_tl.ntiles) { p.b_tl.launch(b_static, p.b_t.get(), eb, s); scr = p.b_t.get(); }
     p.split->b_static = true;
     pack_split_operand(*p.split, false, scr, b_static, s);
+    df_prep_b(p.split->df, p.sched, Operands{nullptr, nullptr, scr, b_static}, s);
   }
   QLTG_CUDA(cudaStreamSynchronize(s));
 }
@@ -911,10 +913,16 @@ void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s
     prepare_split(p, s);
   }
   SplitPlan& sp = *p.split;
-  // skinny output blocks stay on the FP64 skinny kernel (k, n <= 8: the tensor cores would
-  // pad them 8x, and exact integer emulation of these rows measured slower than the FP64
-  // pipe); everything else goes through the slices
-  launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, s);
+  // skinny output blocks (k, n <= 8: the tensor cores would pad them 8x, and exact integer
+  // emulation of these rows measured slower than the FP64 pipe) run in double-float
+  // arithmetic on the FP32 pipe; everything else goes through the slices
+  if (!p.sched.skinny.empty()) {
+    if (sp.df.nrows > 0 && !(sp.b_static && sp.df.ready)) {
+      QLTG_CHECK(pack || sp.df.ready, QLTG_ERR_INVALID, "GEMM-only stage before the operands were ever packed");
+      if (pack) df_prep_b(sp.df, p.sched, op, s);
+    }
+    launch_skinny_df(p.sched, sp.df, op, c, p.ctx->num_sms, s);
+  }
   if (sp.tiles.empty()) return;
   if (pack) {
     if (!(sp.a_static && sp.a_ready)) pack_split_operand(sp, true, op.a, op.a_src, s);
@@ -938,6 +946,7 @@ void prepare_split(CtrctPlan& p, cudaStream_t s) {
 
 int64_t split_launches(const CtrctPlan& p) {
   int64_t n = p.sched.skinny.empty() ? 0 : 1;
+  if (n && p.split && p.split->df.nrows > 0 && !(p.split->b_static && p.split->df.ready)) ++n;   // B pairs
   if (p.split) n += p.split->launches();
   return n;
 }
