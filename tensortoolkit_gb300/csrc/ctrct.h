@@ -110,32 +110,6 @@ struct SplitWork {
   uint8_t pad[10];
 };
 static_assert(sizeof(SplitWork) == 64, "SplitWork is one 64-byte record");
-
-// Double-float skinny path of split mode (gemm_f64.cu): every output block with n, k <= 8
-// whose tasks stack to K = sum of k <= kDfMaxK columns of A. Row i of the stacked K x n
-// operand is row kk of task t's B block (sign folded in); A element (row, i) sits at
-// a_off + row a_rs.
-constexpr int kDfMaxK = 8;
-struct DfADesc {
-  int64_t a_off;          // (row 0, kk) of the task's A block, | kFromSrc
-  int32_t a_rs;           // row stride
-  int32_t pad;
-};
-struct DfBDesc {
-  int64_t b_off;          // row kk of the task's B block, | kFromSrc
-  int32_t sign;           // fermion exchange sign of the task
-  int32_t pad;
-};
-struct DfCBlk {
-  int32_t desc0;          // first stacked row
-  int32_t k;              // stacked rows; 0: the block stays on the FP64 path
-};
-struct DfSkinny {
-  bool ready = false;     // B pairs prepared for the current B (static B: once)
-  int64_t nrows = 0;      // stacked rows over all blocks
-  int prep_grid = 1, grid = 1;
-  DevBuf d_cb, d_adesc, d_bdesc, d_bpair, d_fb, d_ok;
-};
 struct SplitPlan {
   bool built = false;
   bool a_static = false, b_static = false;   // operand packed once, unchanged afterwards
@@ -152,7 +126,6 @@ struct SplitPlan {
   int row_exp_grid = 1, pack_a_grid = 1, pack_b_grid = 1;   // one wave of resident CTAs of each
   int64_t n_a_chunks = 0, n_a_rows = 0;
   DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_a_row_tiles, d_a_tiles, d_b_col_tiles;
-  DfSkinny df;                    // skinny output blocks (double-float path)
   void build(const struct CtrctPlan& p, cudaStream_t s);
   int64_t launches() const;
 };
@@ -199,13 +172,6 @@ struct Operands {
 void launch_gemm_f64(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms, cudaStream_t s);
 void launch_gemm_f64_skinny(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms,
                             cudaStream_t s);
-// Double-float skinny path (real operands): stacked-row descriptors of the skinny blocks
-// (host, allocates), the B-side preparation (column scale fields and float pairs; once per
-// B), and the kernel. Blocks or rows the path cannot hold exactly enough run the FP64 rows.
-void df_build(DfSkinny& df, const GemmSchedule& g, int num_sms, cudaStream_t s);
-void df_prep_b(DfSkinny& df, const GemmSchedule& g, const Operands& op, cudaStream_t s);
-void launch_skinny_df(const GemmSchedule& g, const DfSkinny& df, const Operands& op, void* c, int num_sms,
-                      cudaStream_t s);
 
 // Block order, destination offsets and fermionic block signs of QLTensor::Transpose.
 void transpose_layout(const Meta& m, const std::vector<int>& order, std::vector<double>& signs,

@@ -182,203 +182,6 @@ __global__ void __launch_bounds__(kSkinnyRows, SkinnyMinBlocks<T>::value) k_gemm
 }
 
 
-// ------------------------------------------------------------------ double-float skinny rows
-// Split mode computes the skinny blocks in double-float arithmetic on the FP32 pipe: FP64
-// issues at about 1/64 of the FP32 rate on this GPU and these blocks do about two flops per
-// 8-byte element, so the FP64 skinny kernel is FP64-pipe bound. Each operand element becomes
-// an unevaluated sum h + l of two floats (47 significant bits) after scaling by a power of
-// two that brings the largest magnitude of its row (A) or stacked column (B) into [1, 2).
-// Products are Dekker's exact product by FMA (TwoProd) plus the two cross terms h l, sums
-// are Knuth's TwoSum, and the result goes back to FP64 by exponent arithmetic and one FP64
-// add of its two parts. Terms below 2^-126 of the row or column scale are dropped; the error
-// is about 2^-45 sum |a||b| per output (FP64's own bound is K 2^-53 sum |a||b|). Rows whose
-// scale is tiny, subnormal or not finite, and blocks whose B has such a column, run the FP64
-// rows instead, as do outputs that would leave the normal FP64 range.
-constexpr int kDfFieldMin = 200;
-
-// x (high, low words) scaled by 2^(1023 - F), F the largest exponent field of its row or
-// column (kDfFieldMin <= F <= 2046), as h + l.
-__device__ __forceinline__ float2 df_split(uint32_t hi, uint32_t lo, int F) {
-  const uint32_t mag = hi & 0x7FFFFFFFu;
-  const uint32_t thr = (uint32_t)(F - 126) << 20;   // mag >= thr: scaled value >= 2^-126
-  // fraction bits 51..29 under the low 9 bits of the exponent field; adding (127 - F) << 23
-  // makes the top bits the float exponent field - F + 127 (1..127 for kept values)
-  const uint32_t hb = (__funnelshift_l(lo, hi, 3) + ((uint32_t)(127 - F) << 23)) | (hi & 0x80000000u);
-  const float h = mag >= thr ? __uint_as_float(hb) : 0.0f;
-  // fraction bits 28..6 as the integer part of 2^23 + r, times 2^-46 of h's power of two
-  const float r = __fsub_rn(__uint_as_float(0x4B000000u | ((lo >> 6) & 0x7FFFFFu)), 8388608.0f);
-  const float unit = __fmul_rn(__uint_as_float(__float_as_uint(h) & 0xFF800000u), 0x1p-46f);
-  return make_float2(h, __fmul_rn(r, unit));
-}
-
-// The FP64 value with the sign and fraction of the normal float `bits` and exponent field
-// (its float field + D): exact; the caller keeps that field in 1..2046.
-__device__ __forceinline__ double df_to_double(uint32_t bits, int D) {
-  const uint32_t mag = bits & 0x7FFFFFFFu;
-  return __hiloint2double((int)(((mag >> 3) + ((uint32_t)D << 20)) | (bits & 0x80000000u)), (int)(bits << 29));
-}
-
-template <int K, int N>
-__device__ __forceinline__ bool df_row(const DfADesc* __restrict__ ad, const float2* __restrict__ bp,
-                                       const int* __restrict__ fb, int row, const double* __restrict__ A,
-                                       const double* __restrict__ As, double* __restrict__ out) {
-  uint32_t hi[K], lo[K];
-  uint32_t mx = 0;
-#pragma unroll
-  for (int i = 0; i < K; ++i) {
-    const DfADesc d = ad[i];
-    const double v = __ldg(operand_block(A, As, d.a_off) + (int64_t)row * d.a_rs);
-    hi[i] = (uint32_t)__double2hiint(v);
-    lo[i] = (uint32_t)__double2loint(v);
-    mx = max(mx, hi[i] & 0x7FFFFFFFu);
-  }
-  const int F = (int)(mx >> 20);
-  if (F < kDfFieldMin || F > 2046) return false;
-  float2 a[K];
-#pragma unroll
-  for (int i = 0; i < K; ++i) a[i] = df_split(hi[i], lo[i], F);
-  double res[N];
-#pragma unroll
-  for (int j = 0; j < N; ++j) {
-    float sh = 0.0f, sl = 0.0f;
-#pragma unroll
-    for (int i = 0; i < K; ++i) {
-      const float2 b = __ldg(bp + i * 8 + j);
-      const float p = __fmul_rn(a[i].x, b.x);
-      float e = __fmaf_rn(a[i].x, b.x, -p);   // TwoProd: a.h b.h = p + e exactly
-      e = __fmaf_rn(a[i].x, b.y, e);
-      e = __fmaf_rn(a[i].y, b.x, e);
-      const float s = __fadd_rn(sh, p);       // TwoSum: sh + p = s + err exactly
-      const float v = __fsub_rn(s, sh);
-      const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(p, v));
-      sh = s;
-      sl = __fadd_rn(sl, __fadd_rn(err, e));
-    }
-    const float s = __fadd_rn(sh, sl);
-    const float v = __fsub_rn(s, sh);
-    const float l = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(sl, v));
-    const uint32_t hs = __float_as_uint(s), ls = __float_as_uint(l);
-    const uint32_t hm = hs & 0x7FFFFFFFu, lm = ls & 0x7FFFFFFFu;
-    if (hm == 0) {
-      res[j] = 0.0;
-      continue;
-    }
-    // value = (s + l) 2^(F + FB - 2046): FP64 exponent field = float field + D
-    const int D = F + __ldg(fb + j) - 1150;
-    const int dh = (int)(hm >> 23) + D;
-    if (hm < 0x00800000u || dh < 64 || dh > 2046) return false;
-    const double H = df_to_double(hs, D);
-    const double L = (lm >= 0x00800000u && (int)(lm >> 23) + D >= 1) ? df_to_double(ls, D) : 0.0;
-    res[j] = __dadd_rn(H, L);
-  }
-#pragma unroll
-  for (int j = 0; j < N; ++j) out[j] = res[j];
-  return true;
-}
-
-template <int K>
-__device__ __forceinline__ bool df_row_n(int n, const DfADesc* ad, const float2* bp, const int* fb, int row,
-                                         const double* A, const double* As, double* out) {
-  switch (n) {
-    case 1: return df_row<K, 1>(ad, bp, fb, row, A, As, out);
-    case 2: return df_row<K, 2>(ad, bp, fb, row, A, As, out);
-    case 3: return df_row<K, 3>(ad, bp, fb, row, A, As, out);
-    case 4: return df_row<K, 4>(ad, bp, fb, row, A, As, out);
-    case 5: return df_row<K, 5>(ad, bp, fb, row, A, As, out);
-    case 6: return df_row<K, 6>(ad, bp, fb, row, A, As, out);
-    case 7: return df_row<K, 7>(ad, bp, fb, row, A, As, out);
-    default: return df_row<K, 8>(ad, bp, fb, row, A, As, out);
-  }
-}
-
-__device__ __forceinline__ bool df_row_kn(int k, int n, const DfADesc* ad, const float2* bp, const int* fb, int row,
-                                          const double* A, const double* As, double* out) {
-  switch (k) {
-    case 1: return df_row_n<1>(n, ad, bp, fb, row, A, As, out);
-    case 2: return df_row_n<2>(n, ad, bp, fb, row, A, As, out);
-    case 3: return df_row_n<3>(n, ad, bp, fb, row, A, As, out);
-    case 4: return df_row_n<4>(n, ad, bp, fb, row, A, As, out);
-    case 5: return df_row_n<5>(n, ad, bp, fb, row, A, As, out);
-    case 6: return df_row_n<6>(n, ad, bp, fb, row, A, As, out);
-    case 7: return df_row_n<7>(n, ad, bp, fb, row, A, As, out);
-    default: return df_row_n<8>(n, ad, bp, fb, row, A, As, out);
-  }
-}
-
-// One thread per output row, as k_gemm_skinny; rows the double-float path declines run the
-// FP64 row code.
-__global__ void __launch_bounds__(kSkinnyRows, 4) k_gemm_skinny_df(
-    const GemmCBlk* __restrict__ cblk, const GemmTask* __restrict__ task, const GemmRowChunk* __restrict__ items,
-    int nitems, const DfCBlk* __restrict__ dcb, const DfADesc* __restrict__ ad, const float2* __restrict__ bp,
-    const int* __restrict__ fb, const int* __restrict__ ok, const double* __restrict__ A,
-    const double* __restrict__ As, const double* __restrict__ B, const double* __restrict__ Bs,
-    double* __restrict__ C) {
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const GemmRowChunk item = items[it];
-    const GemmCBlk cb = cblk[item.cblk];
-    const int row = item.chunk * kSkinnyRows + threadIdx.x;
-    if (row >= cb.m) continue;
-    const DfCBlk d = dcb[item.cblk];
-    if (d.k > 0 && __ldg(ok + item.cblk) &&
-        df_row_kn(d.k, cb.n, ad + d.desc0, bp + (int64_t)d.desc0 * 8, fb + (int64_t)item.cblk * 8, row, A, As,
-                  C + cb.c_off + (int64_t)row * cb.n))
-      continue;
-    switch (cb.n) {
-      case 1: skinny_row<double, 1>(cb, task, row, A, As, B, Bs, C); break;
-      case 2: skinny_row<double, 2>(cb, task, row, A, As, B, Bs, C); break;
-      case 3: skinny_row<double, 3>(cb, task, row, A, As, B, Bs, C); break;
-      case 4: skinny_row<double, 4>(cb, task, row, A, As, B, Bs, C); break;
-      case 5: skinny_row<double, 5>(cb, task, row, A, As, B, Bs, C); break;
-      case 6: skinny_row<double, 6>(cb, task, row, A, As, B, Bs, C); break;
-      case 7: skinny_row<double, 7>(cb, task, row, A, As, B, Bs, C); break;
-      default: skinny_row<double, 8>(cb, task, row, A, As, B, Bs, C); break;
-    }
-  }
-}
-
-// B side, one warp per output block: column scale fields of the stacked K x n operand, the
-// block's eligibility (every column all zero or with a field in kDfFieldMin..2046), and the
-// float pairs of every element with the task sign folded in.
-__global__ void __launch_bounds__(256) k_df_prep_b(const GemmCBlk* __restrict__ cblk, const DfCBlk* __restrict__ dcb,
-                                                   int ncb, const DfBDesc* __restrict__ bd,
-                                                   const double* __restrict__ B, const double* __restrict__ Bs,
-                                                   float2* __restrict__ bp, int* __restrict__ fb,
-                                                   int* __restrict__ ok) {
-  const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
-  for (int q = blockIdx.x * warps + (threadIdx.x >> 5); q < ncb; q += gridDim.x * warps) {
-    const DfCBlk d = dcb[q];
-    if (d.k == 0) continue;   // uniform over the warp
-    const int n = cblk[q].n, K = d.k;
-    int f = 0;
-    bool nonzero = false;
-    if (lane < n) {
-      for (int i = 0; i < K; ++i) {
-        const uint64_t ab =
-            (uint64_t)__double_as_longlong(operand_block(B, Bs, bd[d.desc0 + i].b_off)[lane]) & 0x7FFFFFFFFFFFFFFFull;
-        nonzero |= ab != 0;
-        f = max(f, (int)(ab >> 52));
-      }
-      fb[(int64_t)q * 8 + lane] = f;
-    }
-    const bool good = __all_sync(0xffffffffu, lane >= n || !nonzero || (f >= kDfFieldMin && f <= 2046));
-    if (lane == 0) ok[q] = good ? 1 : 0;
-    for (int base = 0; base < K * n; base += 32) {
-      const int idx = base + lane;
-      const int i = idx / n, j = idx - i * n;
-      const int fj = __shfl_sync(0xffffffffu, f, j & 31);
-      if (idx < K * n) {
-        const DfBDesc e = bd[d.desc0 + i];
-        uint64_t bits = (uint64_t)__double_as_longlong(operand_block(B, Bs, e.b_off)[j]);
-        if (e.sign < 0) bits ^= 0x8000000000000000ull;
-        float2 pr = make_float2(0.0f, 0.0f);
-        if (good && fj >= kDfFieldMin) pr = df_split((uint32_t)(bits >> 32), (uint32_t)bits, fj);
-        bp[(int64_t)(d.desc0 + i) * 8 + j] = pr;
-      }
-    }
-  }
-}
-
-
 }  // namespace
 
 bool skinny_cblk(const GemmSchedule& g, int32_t q) {
@@ -432,71 +235,6 @@ void launch_gemm_f64_skinny(const GemmSchedule& g, const Operands& op, void* c, 
     launch_skinny_t<double2>(g, op, c, grid, s);
   else
     launch_skinny_t<double>(g, op, c, grid, s);
-  QLTG_CUDA(cudaGetLastError());
-}
-
-void df_build(DfSkinny& df, const GemmSchedule& g, int num_sms, cudaStream_t s) {
-  const int ncb = (int)g.cblk.size();
-  std::vector<DfCBlk> cbs(std::max(ncb, 1), DfCBlk{0, 0});
-  std::vector<DfADesc> ad;
-  std::vector<DfBDesc> bd;
-  for (int32_t q = 0; q < ncb; ++q) {
-    if (!skinny_cblk(g, q)) continue;
-    const GemmCBlk& cb = g.cblk[q];
-    int k = 0;
-    for (int32_t t = cb.t0; t < cb.t1; ++t) k += g.task[t].k;
-    if (k < 1 || k > kDfMaxK) continue;
-    cbs[q] = DfCBlk{(int32_t)ad.size(), k};
-    for (int32_t t = cb.t0; t < cb.t1; ++t) {
-      const GemmTask& tk = g.task[t];
-      for (int kk = 0; kk < tk.k; ++kk) {
-        ad.push_back(DfADesc{tk.a_off + (int64_t)kk * tk.a_cs, tk.a_rs, 0});
-        bd.push_back(DfBDesc{tk.b_off + (int64_t)kk * cb.n, tk.sign, 0});
-      }
-    }
-  }
-  QLTG_CHECK(ad.size() < ((size_t)1 << 28), QLTG_ERR_UNSUPPORTED, "too many skinny rows");
-  df.nrows = (int64_t)ad.size();
-  df.ready = false;
-  if (ad.empty()) ad.push_back(DfADesc{0, 0, 0});
-  if (bd.empty()) bd.push_back(DfBDesc{0, 1, 0});
-  df.d_cb = upload(cbs, s);
-  df.d_adesc = upload(ad, s);
-  df.d_bdesc = upload(bd, s);
-  df.d_bpair.alloc(std::max<int64_t>(df.nrows, 1) * 8 * sizeof(float2));
-  df.d_fb.alloc((int64_t)std::max(ncb, 1) * 8 * sizeof(int));
-  df.d_ok.alloc((int64_t)std::max(ncb, 1) * sizeof(int));
-  QLTG_CUDA(cudaMemsetAsync(df.d_ok.get(), 0, (int64_t)std::max(ncb, 1) * sizeof(int), s));
-  df.prep_grid = std::max(1, std::min((ncb + 7) / 8, std::max(1, num_sms) * 8));
-  int per_sm = 0;
-  QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_skinny_df, kSkinnyRows, 0));
-  df.grid = std::max(1, std::min((int)g.skinny.size(), std::max(1, num_sms) * std::max(1, per_sm)));
-}
-
-void df_prep_b(DfSkinny& df, const GemmSchedule& g, const Operands& op, cudaStream_t s) {
-  if (df.nrows > 0) {
-    k_df_prep_b<<<df.prep_grid, 256, 0, s>>>(g.d_cblk.as<GemmCBlk>(), df.d_cb.as<DfCBlk>(), (int)g.cblk.size(),
-                                             df.d_bdesc.as<DfBDesc>(), static_cast<const double*>(op.b),
-                                             static_cast<const double*>(op.b_src), df.d_bpair.as<float2>(),
-                                             df.d_fb.as<int>(), df.d_ok.as<int>());
-    QLTG_CUDA(cudaGetLastError());
-  }
-  df.ready = true;
-}
-
-void launch_skinny_df(const GemmSchedule& g, const DfSkinny& df, const Operands& op, void* c, int num_sms,
-                      cudaStream_t s) {
-  const int ns = (int)g.skinny.size();
-  if (!ns) return;
-  if (df.nrows == 0) {   // no block on the double-float path
-    launch_gemm_f64_skinny(g, op, c, false, num_sms, s);
-    return;
-  }
-  k_gemm_skinny_df<<<df.grid, kSkinnyRows, 0, s>>>(
-      g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(), g.d_skinny.as<GemmRowChunk>(), ns, df.d_cb.as<DfCBlk>(),
-      df.d_adesc.as<DfADesc>(), df.d_bpair.as<float2>(), df.d_fb.as<int>(), df.d_ok.as<int>(),
-      static_cast<const double*>(op.a), static_cast<const double*>(op.a_src), static_cast<const double*>(op.b),
-      static_cast<const double*>(op.b_src), static_cast<double*>(c));
   QLTG_CUDA(cudaGetLastError());
 }
 

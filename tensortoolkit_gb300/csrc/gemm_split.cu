@@ -624,18 +624,30 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
     const int row_in_tile = quad * 32 + lane;
     uint32_t d = 0;
     bool stop = false, written = false;
+    // outputs of the tile that a non-finite operand row or column reaches (bit c: column c);
+    // they are stored as NaN (FP64 gives NaN or an infinity there; the slices cannot carry it)
+    uint32_t poison = 0;
     const uint32_t tsum = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(kSumCol + 2 * cpart * kDrainCols);
     for (int it = beg; it < end && !stop && !aborted(&s_abort); ++it) {
       const SplitWork w = items[it];
       const int row = w.tm * kTM + row_in_tile;
       const int col0 = w.tn * kTN + cpart * kDrainCols;
       const int nst = (w.k + kKS - 1) / kKS;
-      if (w.flags & 1) written = false;
+      if (w.flags & 1) {
+        written = false;
+        poison = 0;
+      }
       // scale exponents, fetched while the first period is still on the tensor cores
-      const int ea = row < w.m ? exp_of_field(aexp[w.a_exp + row]) : 0;
+      const int fa = row < w.m ? aexp[w.a_exp + row] : 0;
+      const int ea = exp_of_field(fa);
+      if (fa == 2047) poison = (1u << kDrainCols) - 1;
       int eb[kDrainCols];
 #pragma unroll
-      for (int c = 0; c < kDrainCols; ++c) eb[c] = col0 + c < w.n ? exp_of_field(bexp[w.b_exp + col0 + c]) : 0;
+      for (int c = 0; c < kDrainCols; ++c) {
+        const int fb = col0 + c < w.n ? bexp[w.b_exp + col0 + c] : 0;
+        eb[c] = exp_of_field(fb);
+        if (fb == 2047) poison |= 1u << c;
+      }
       long long z[kDrainCols];
       // the task's periods in chunks of kFlushDrains, each folded on its own, so the int64
       // sums stay in range for any k
@@ -671,7 +683,9 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
           double* out = C + w.c_off + (int64_t)row * w.n;
 #pragma unroll
           for (int c = 0; c < kDrainCols; ++c)
-            if (col0 + c < w.n) out[col0 + c] = __hiloint2double((int)v[2 * c + 1], (int)v[2 * c]);
+            if (col0 + c < w.n)
+              out[col0 + c] = (poison >> c) & 1u ? __longlong_as_double(0x7FF8000000000000ll)
+                                                 : __hiloint2double((int)v[2 * c + 1], (int)v[2 * c]);
         }
       }
     }
@@ -844,7 +858,6 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   QLTG_CUDA(cudaMemsetAsync(error.get(), 0, sizeof(int), s));
   // per device (the attribute belongs to the current device's copy of the kernel)
   QLTG_CUDA(cudaFuncSetAttribute(k_gemm_split, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-  df_build(df, g, p.ctx->num_sms, s);
   QLTG_CUDA(cudaStreamSynchronize(s));
   built = true;
 }
@@ -896,7 +909,6 @@ void split_prepack_static(CtrctPlan& p, const void* a_static, const void* b_stat
     if (p.b_tl.ntiles) { p.b_tl.launch(b_static, p.b_t.get(), eb, s); scr = p.b_t.get(); }
     p.split->b_static = true;
     pack_split_operand(*p.split, false, scr, b_static, s);
-    df_prep_b(p.split->df, p.sched, Operands{nullptr, nullptr, scr, b_static}, s);
   }
   QLTG_CUDA(cudaStreamSynchronize(s));
 }
@@ -913,16 +925,10 @@ void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s
     prepare_split(p, s);
   }
   SplitPlan& sp = *p.split;
-  // skinny output blocks (k, n <= 8: the tensor cores would pad them 8x, and exact integer
-  // emulation of these rows measured slower than the FP64 pipe) run in double-float
-  // arithmetic on the FP32 pipe; everything else goes through the slices
-  if (!p.sched.skinny.empty()) {
-    if (sp.df.nrows > 0 && !(sp.b_static && sp.df.ready)) {
-      QLTG_CHECK(pack || sp.df.ready, QLTG_ERR_INVALID, "GEMM-only stage before the operands were ever packed");
-      if (pack) df_prep_b(sp.df, p.sched, op, s);
-    }
-    launch_skinny_df(p.sched, sp.df, op, c, p.ctx->num_sms, s);
-  }
+  // skinny output blocks stay on the FP64 skinny kernel (k, n <= 8: the tensor cores would
+  // pad them 8x, and exact integer emulation of these rows measured slower than the FP64
+  // pipe); everything else goes through the slices
+  launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, s);
   if (sp.tiles.empty()) return;
   if (pack) {
     if (!(sp.a_static && sp.a_ready)) pack_split_operand(sp, true, op.a, op.a_src, s);
@@ -946,7 +952,6 @@ void prepare_split(CtrctPlan& p, cudaStream_t s) {
 
 int64_t split_launches(const CtrctPlan& p) {
   int64_t n = p.sched.skinny.empty() ? 0 : 1;
-  if (n && p.split && p.split->df.nrows > 0 && !(p.split->b_static && p.split->df.ready)) ++n;   // B pairs
   if (p.split) n += p.split->launches();
   return n;
 }

@@ -106,3 +106,27 @@ def test_split_wide_dynamic_range(gpu):
             n = np.linalg.norm(y[i])
             if n > 0:
                 assert np.linalg.norm(x[i] - y[i]) / n <= 1e-11
+
+
+def test_split_nonfinite(gpu):
+    """NaN and infinities in A and B: every output they reach is non-finite (NaN from the
+    tensor-core path, where FP64 gives NaN or an infinity), every other output within the bar."""
+    a, b = workloads.config1(5)
+    rng = np.random.default_rng(9)
+    ad, bd = a.data.copy(), b.data.copy()
+    ad[rng.choice(ad.size, 3, replace=False)] = [np.nan, np.inf, -np.inf]
+    bd[rng.choice(bd.size, 2, replace=False)] = [np.inf, np.nan]
+    a2 = BSTensor(a.legs, a.coords, np.float64, ad)
+    b2 = BSTensor(b.legs, b.coords, np.float64, bd)
+    outs = {}
+    for mode in ("fp64", "split"):
+        plan = ContractionPlan(a2, b2, [[2], [0]])
+        with np.errstate(invalid="ignore", over="ignore"):
+            outs[mode] = plan.execute(DTensor.from_host(a2), DTensor.from_host(b2), mode=mode).to_host().data
+        plan.device_status()
+    fin = np.isfinite(outs["fp64"])
+    assert (~fin).any() and fin.any()
+    assert np.array_equal(np.isfinite(outs["split"]), fin)
+    x, y = outs["split"][~fin], outs["fp64"][~fin]
+    assert (np.isnan(x) | (x == y)).all()   # skinny blocks run FP64 rows there: exact
+    assert rel_frob(outs["split"][fin], outs["fp64"][fin]) <= TOL
