@@ -88,6 +88,7 @@ struct SplitOperand {
   int32_t ktiles;         // 64-wide k tiles
   int32_t exp_off;        // offset of its row (A) / column (B) exponent fields
   int64_t chunk_begin;    // A: prefix over operands of 8-element chunks (row-scale kernel)
+  int64_t pchunk_begin;   // A: prefix over operands of rows x ceil(cols / 8) (pack kernel)
 };
 struct SplitTask {
   int64_t a_pack, b_pack;
@@ -120,12 +121,11 @@ struct SplitPlan {
   std::vector<SplitWork> work;    // per CTA: tiles blockIdx.x, + grid, ...; each its tasks
   std::vector<int32_t> work_off;  // grid + 1 offsets into work
   int grid = 0;
-  std::vector<int2> a_row_tiles;  // (A operand, 128-row tile) items of the row-scale kernel
-  std::vector<int4> a_tiles;      // (A operand, 128-row tile, 64-wide k tile) items of the A pack
   std::vector<int2> b_col_tiles;  // (B operand, 32-column tile) items of the B packing kernel
   int row_exp_grid = 1, pack_a_grid = 1, pack_b_grid = 1;   // one wave of resident CTAs of each
-  int64_t n_a_chunks = 0, n_a_rows = 0;
-  DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_a_row_tiles, d_a_tiles, d_b_col_tiles;
+  int64_t n_a_chunks = 0, n_a_pchunks = 0, n_a_rows = 0;
+  bool row_warp = false;          // A row scales one warp per row (long rows) or by chunks
+  DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_b_col_tiles;
   void build(const struct CtrctPlan& p, cudaStream_t s);
   int64_t launches() const;
 };

@@ -185,34 +185,77 @@ __global__ void __launch_bounds__(256) k_row_field(const double* __restrict__ sc
   }
 }
 
-// Slices of A, one CTA per (operand block, 128-row tile, 64-wide k tile): one thread per
-// 16-byte chunk (8 consecutive k of one row) writes the chunk of every slice plane. Runs
-// right after k_row_exp, whose pass over A left it in L2.
-__global__ void __launch_bounds__(256) k_pack_a(const double* __restrict__ scr, const double* __restrict__ src,
-                                                const SplitOperand* __restrict__ ops, const int4* __restrict__ tiles,
-                                                int ntiles, const int32_t* __restrict__ exps,
-                                                uint8_t* __restrict__ pack) {
-  for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
-    const int4 tt = tiles[ti];   // operand, row tile, k tile
-    const SplitOperand o = ops[tt.x];
-    const double* blk = operand_block(scr, src, o.src_off);
-    for (int w = threadIdx.x; w < 1024; w += blockDim.x) {
-      // chunk order inside a (row tile, k tile): ks (4), m_core (16), k_core (2), r8 (8)
-      const int ks = w >> 8, m_core = (w >> 4) & 15, k_core = (w >> 3) & 1, r8 = w & 7;
-      const int64_t r = (int64_t)tt.y * kTM + m_core * 8 + r8;
-      const int64_t k0 = (int64_t)tt.z * kTK + ks * 16 + k_core * 8;
-      if (r >= o.rows || k0 >= o.cols) continue;   // padding: the buffer was zeroed once
-      const int e = exp_of_field(__ldg(exps + o.exp_off + r));
-      uint64_t y[8];
-      uint32_t sg[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) y[j] = scaled_y((k0 + j < o.cols) ? blk[r * o.cols + k0 + j] : 0.0, e, sg[j]);
-      // tile layout [ks][slice][m_core][k_core][8 rows x 16 B]: the 7 slices of a 16-wide k
-      // step are contiguous, so a 32-wide stage is one 56 KB copy
-      const int64_t tile = (int64_t)tt.y * o.ktiles + tt.z;
-      store_planes(y, sg, pack + o.pack_off + tile * (int64_t)(kS * kATile) + (int64_t)ks * (kS * 4096) + m_core * 256 +
-                              k_core * 128 + r8 * 16, 4096);
+// Row scales of A for long rows: one warp per row (rows of all A operands end to end, in
+// exponent-offset order), loads along the row coalesced across the warp, a warp max, one
+// store per row (no zero fill, no atomics).
+__global__ void __launch_bounds__(256) k_row_field_rows(const double* __restrict__ scr, const double* __restrict__ src,
+                                                        const SplitOperand* __restrict__ ops, int nops, int64_t nrows,
+                                                        int32_t* __restrict__ fields) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < nrows; g += nwarps) {
+    int lo = 0, hi = nops - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ops[mid].exp_off <= g) lo = mid; else hi = mid - 1;
     }
+    const SplitOperand o = ops[lo];
+    const double* row = operand_block(scr, src, o.src_off) + (g - o.exp_off) * (int64_t)o.cols;
+    uint32_t mx = 0, nz = 0;
+#pragma unroll 4
+    for (int c = lane; c < o.cols; c += 32) {
+      const uint64_t b = (uint64_t)__double_as_longlong(__ldg(row + c)) & 0x7FFFFFFFFFFFFFFFull;
+      mx = max(mx, (uint32_t)(b >> 32));
+      nz |= (uint32_t)b | (uint32_t)(b >> 32);
+    }
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    nz = __reduce_or_sync(0xffffffffu, nz);
+    if (lane == 0) fields[g] = nz ? max(1, (int)(mx >> 20)) : 0;
+  }
+}
+
+// Slices of A: one thread per 16-byte chunk (8 consecutive k of one row) that holds operand
+// data, numbered per operand in (128-row tile, 8-wide k chunk, row) order, so consecutive
+// threads take consecutive rows of one chunk column and their 16-byte plane words land side
+// by side. CTA b takes the contiguous range [b per, (b + 1) per) of all operands' chunks.
+__global__ void __launch_bounds__(256) k_pack_a(const double* __restrict__ scr, const double* __restrict__ src,
+                                                const SplitOperand* __restrict__ ops, int nops, int64_t total,
+                                                const int32_t* __restrict__ exps, uint8_t* __restrict__ pack) {
+  const int64_t per = (total + gridDim.x - 1) / gridDim.x;
+  const int64_t cbeg = (int64_t)blockIdx.x * per, cend = min(total, cbeg + per);
+  int lo = 0;
+  {
+    int hi = nops - 1;
+    const int64_t first = cbeg + threadIdx.x;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ops[mid].pchunk_begin <= first) lo = mid; else hi = mid - 1;
+    }
+  }
+  for (int64_t ch = cbeg + threadIdx.x; ch < cend; ch += blockDim.x) {
+    while (lo + 1 < nops && ops[lo + 1].pchunk_begin <= ch) ++lo;
+    const SplitOperand o = ops[lo];
+    const int nkc = (o.cols + 7) >> 3;
+    const int l = (int)(ch - o.pchunk_begin);   // below 2^31: one block has < 2^31 elements
+    const int rt = l / (kTM * nkc);
+    const int l2 = l - rt * kTM * nkc;
+    const int rows_rt = min(kTM, o.rows - rt * kTM);
+    const int kc = l2 / rows_rt;
+    const int r = l2 - kc * rows_rt;
+    const int64_t row = (int64_t)rt * kTM + r;
+    const int k0 = kc * 8;
+    const int e = exp_of_field(__ldg(exps + o.exp_off + row));
+    const double* src_row = operand_block(scr, src, o.src_off) + row * o.cols;
+    uint64_t y[8];
+    uint32_t sg[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) y[j] = scaled_y((k0 + j < o.cols) ? __ldg(src_row + k0 + j) : 0.0, e, sg[j]);
+    // tile layout [ks][slice][m_core][k_core][8 rows x 16 B]: the 7 slices of a 16-wide k
+    // step are contiguous, so a 32-wide stage is one 56 KB copy
+    const int kt = k0 / kTK, ks = (k0 % kTK) >> 4, k_core = (k0 >> 3) & 1;
+    const int64_t tile = (int64_t)rt * o.ktiles + kt;
+    store_planes(y, sg, pack + o.pack_off + tile * (int64_t)(kS * kATile) + (int64_t)ks * (kS * 4096) +
+                            (r >> 3) * 256 + k_core * 128 + (r & 7) * 16, 4096);
   }
 }
 
@@ -709,7 +752,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   b_ops.clear();
   tasks.clear();
   tiles.clear();
-  int64_t a_pack = 0, b_pack = 0, a_exp = 0, b_exp = 0, a_chunks = 0;
+  int64_t a_pack = 0, b_pack = 0, a_exp = 0, b_exp = 0, a_chunks = 0, a_pchunks = 0;
   auto a_index = [&](int64_t a_off) {   // block ordinal from its offset
     return (int64_t)(std::lower_bound(p.a.offsets.begin(), p.a.offsets.end(), a_off) - p.a.offsets.begin());
   };
@@ -734,10 +777,12 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
         o.exp_off = (int32_t)a_exp;
         o.pack_off = a_pack;
         o.chunk_begin = a_chunks;
+        o.pchunk_begin = a_pchunks;
         QLTG_CHECK((int64_t)cb.m * k < ((int64_t)1 << 31) - 8, QLTG_ERR_UNSUPPORTED, "operand block too large");
         const int64_t rtiles = (cb.m + kTM - 1) / kTM;
         a_exp += cb.m;
         a_chunks += ((int64_t)cb.m * k + 7) / 8;
+        a_pchunks += (int64_t)cb.m * ((k + 7) / 8);
         a_pack += rtiles * ktiles * kS * (int64_t)kATile;
         a_of[ia] = (int32_t)a_ops.size();
         a_ops.push_back(o);
@@ -817,27 +862,29 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
     QLTG_CHECK(work.size() < ((size_t)1 << 31), QLTG_ERR_UNSUPPORTED, "too many split work items");
   }
   work_off[grid] = (int32_t)work.size();
-  a_row_tiles.clear();
-  for (int i = 0; i < (int)a_ops.size(); ++i)
-    for (int rt = 0; rt * kTM < a_ops[i].rows; ++rt) a_row_tiles.push_back(make_int2(i, rt));
-  d_a_row_tiles = upload(a_row_tiles, s);
   b_col_tiles.clear();
   for (int i = 0; i < (int)b_ops.size(); ++i)
     for (int ct = 0; ct * kTN < b_ops[i].cols; ++ct) b_col_tiles.push_back(make_int2(i, ct));
   d_b_col_tiles = upload(b_col_tiles, s);
   n_a_chunks = a_chunks;
-  a_tiles.clear();
-  for (int i = 0; i < (int)a_ops.size(); ++i)
-    for (int rt = 0; rt * kTM < a_ops[i].rows; ++rt)
-      for (int kt = 0; kt < a_ops[i].ktiles; ++kt) a_tiles.push_back(make_int4(i, rt, kt, 0));
-  d_a_tiles = upload(a_tiles, s);
+  n_a_pchunks = a_pchunks;
+  // long rows (the matvec's t2 . renv: k up to 528) are folded one warp per row; short ones
+  // by 8-element chunks with atomics
+  row_warp = a_exp > 0 && a_chunks * 8 >= (int64_t)32 * a_exp;
   {
     int per_sm = 0;
-    QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_field, 256, 0));
-    row_exp_grid = (int)std::max<int64_t>(1, std::min<int64_t>((n_a_chunks + 255) / 256,
-                                                               (int64_t)std::max(1, per_sm) * p.ctx->num_sms));
+    if (row_warp) {
+      QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_field_rows, 256, 0));
+      row_exp_grid = (int)std::max<int64_t>(1, std::min<int64_t>((a_exp + 7) / 8,
+                                                                 (int64_t)std::max(1, per_sm) * p.ctx->num_sms));
+    } else {
+      QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_field, 256, 0));
+      row_exp_grid = (int)std::max<int64_t>(1, std::min<int64_t>((n_a_chunks + 255) / 256,
+                                                                 (int64_t)std::max(1, per_sm) * p.ctx->num_sms));
+    }
     QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pack_a, 256, 0));
-    pack_a_grid = std::max(1, std::min((int)a_tiles.size(), std::max(1, per_sm) * p.ctx->num_sms));
+    pack_a_grid = (int)std::max<int64_t>(1, std::min<int64_t>((n_a_pchunks + 255) / 256,
+                                                              (int64_t)std::max(1, per_sm) * p.ctx->num_sms));
     QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pack_b_cols, 256, 0));
     pack_b_grid = std::max(1, std::min((int)b_col_tiles.size(), std::max(1, per_sm) * p.ctx->num_sms));
   }
@@ -864,7 +911,8 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
 
 int64_t SplitPlan::launches() const {
   if (tiles.empty()) return 0;
-  return (a_static ? 0 : 3) + (b_static ? 0 : 1) + 1;   // A: memset, row scales, pack; B: pack; GEMM
+  // A: (memset,) row scales, pack; B: pack; GEMM
+  return (a_static ? 0 : (row_warp ? 2 : 3)) + (b_static ? 0 : 1) + 1;
 }
 
 // Scale exponents and slice tiles of one operand side (A: rows, B: columns), reading each
@@ -877,11 +925,16 @@ void pack_split_operand(SplitPlan& sp, bool side_a, const void* scratch, const v
       sp.a_ready = true;
       return;
     }
-    QLTG_CUDA(cudaMemsetAsync(sp.a_exps.get(), 0, sp.n_a_rows * sizeof(int32_t), s));
-    k_row_field<<<sp.row_exp_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
-                                                sp.n_a_chunks, sp.a_exps.as<int32_t>());
-    k_pack_a<<<sp.pack_a_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), sp.d_a_tiles.as<int4>(),
-                                            (int)sp.a_tiles.size(), sp.a_exps.as<int32_t>(), sp.a_packed.as<uint8_t>());
+    if (sp.row_warp) {
+      k_row_field_rows<<<sp.row_exp_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+                                                       sp.n_a_rows, sp.a_exps.as<int32_t>());
+    } else {
+      QLTG_CUDA(cudaMemsetAsync(sp.a_exps.get(), 0, sp.n_a_rows * sizeof(int32_t), s));
+      k_row_field<<<sp.row_exp_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+                                                  sp.n_a_chunks, sp.a_exps.as<int32_t>());
+    }
+    k_pack_a<<<sp.pack_a_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+                                            sp.n_a_pchunks, sp.a_exps.as<int32_t>(), sp.a_packed.as<uint8_t>());
   } else {
     if (sp.b_ops.empty()) {
       sp.b_ready = true;
