@@ -121,12 +121,11 @@ struct SplitPlan {
   std::vector<SplitWork> work;    // per CTA: tiles blockIdx.x, + grid, ...; each its tasks
   std::vector<int32_t> work_off;  // grid + 1 offsets into work
   int grid = 0;
-  std::vector<int2> a_rtiles;     // (A operand, 128-row tile) items of the fused A kernel, largest first
   std::vector<int2> b_col_tiles;  // (B operand, 32-column tile) items of the B packing kernel
   int row_exp_grid = 1, pack_a_grid = 1, pack_b_grid = 1;   // one wave of resident CTAs of each
   int64_t n_a_chunks = 0, n_a_pchunks = 0, n_a_rows = 0;
-  bool row_warp = false;          // A: fused row scales + pack per row tile (long rows) or by chunks
-  DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_a_rtiles, d_b_col_tiles;
+  bool row_warp = false;          // A row scales one warp per row (long rows) or by chunks
+  DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_b_col_tiles;
   void build(const struct CtrctPlan& p, cudaStream_t s);
   int64_t launches() const;
 };

@@ -185,57 +185,32 @@ __global__ void __launch_bounds__(256) k_row_field(const double* __restrict__ sc
   }
 }
 
-// Row scales and slices of A for long rows, one CTA per (operand block, 128-row tile), the
-// largest tiles first. Phase 1: one warp per row, loads along the row coalesced across the
-// warp, a warp max, the field to shared memory and to the plan's field array. Phase 2: one
-// thread per 16-byte chunk as in k_pack_a, the tile's rows read again from L2.
-__global__ void __launch_bounds__(256) k_pack_a_rows(const double* __restrict__ scr, const double* __restrict__ src,
-                                                     const SplitOperand* __restrict__ ops,
-                                                     const int2* __restrict__ rtiles, int ntiles,
-                                                     int32_t* __restrict__ exps, uint8_t* __restrict__ pack) {
-  __shared__ int sfield[kTM];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
-    const int2 tt = rtiles[ti];   // operand, row tile
-    const SplitOperand o = ops[tt.x];
-    const int rt = tt.y;
-    const int rows_rt = min(kTM, o.rows - rt * kTM);
-    const double* blk = operand_block(scr, src, o.src_off) + (int64_t)rt * kTM * o.cols;
-    for (int r = warp; r < rows_rt; r += nwarp) {
-      const double* row = blk + (int64_t)r * o.cols;
-      uint32_t mx = 0, nz = 0;
-#pragma unroll 8
-      for (int c = lane; c < o.cols; c += 32) {
-        const uint64_t b = (uint64_t)__double_as_longlong(__ldg(row + c)) & 0x7FFFFFFFFFFFFFFFull;
-        mx = max(mx, (uint32_t)(b >> 32));
-        nz |= (uint32_t)b | (uint32_t)(b >> 32);
-      }
-      mx = __reduce_max_sync(0xffffffffu, mx);
-      nz = __reduce_or_sync(0xffffffffu, nz);
-      if (lane == 0) {
-        const int f = nz ? max(1, (int)(mx >> 20)) : 0;
-        sfield[r] = f;
-        exps[o.exp_off + rt * kTM + r] = f;
-      }
+// Row scales of A for long rows: one warp per row (rows of all A operands end to end, in
+// exponent-offset order), loads along the row coalesced across the warp, a warp max, one
+// store per row (no zero fill, no atomics).
+__global__ void __launch_bounds__(256) k_row_field_rows(const double* __restrict__ scr, const double* __restrict__ src,
+                                                        const SplitOperand* __restrict__ ops, int nops, int64_t nrows,
+                                                        int32_t* __restrict__ fields) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < nrows; g += nwarps) {
+    int lo = 0, hi = nops - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ops[mid].exp_off <= g) lo = mid; else hi = mid - 1;
     }
-    __syncthreads();
-    const int nkc = (o.cols + 7) >> 3;
-    for (int l = threadIdx.x; l < rows_rt * nkc; l += blockDim.x) {
-      const int kc = l / rows_rt;
-      const int r = l - kc * rows_rt;
-      const int k0 = kc * 8;
-      const int e = exp_of_field(sfield[r]);
-      const double* src_row = blk + (int64_t)r * o.cols;
-      uint64_t y[8];
-      uint32_t sg[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) y[j] = scaled_y((k0 + j < o.cols) ? __ldg(src_row + k0 + j) : 0.0, e, sg[j]);
-      const int kt = k0 / kTK, ks = (k0 % kTK) >> 4, k_core = (k0 >> 3) & 1;
-      const int64_t tile = (int64_t)rt * o.ktiles + kt;
-      store_planes(y, sg, pack + o.pack_off + tile * (int64_t)(kS * kATile) + (int64_t)ks * (kS * 4096) +
-                              (r >> 3) * 256 + k_core * 128 + (r & 7) * 16, 4096);
+    const SplitOperand o = ops[lo];
+    const double* row = operand_block(scr, src, o.src_off) + (g - o.exp_off) * (int64_t)o.cols;
+    uint32_t mx = 0, nz = 0;
+#pragma unroll 4
+    for (int c = lane; c < o.cols; c += 32) {
+      const uint64_t b = (uint64_t)__double_as_longlong(__ldg(row + c)) & 0x7FFFFFFFFFFFFFFFull;
+      mx = max(mx, (uint32_t)(b >> 32));
+      nz |= (uint32_t)b | (uint32_t)(b >> 32);
     }
-    __syncthreads();   // sfield is rewritten by the next tile
+    mx = __reduce_max_sync(0xffffffffu, mx);
+    nz = __reduce_or_sync(0xffffffffu, nz);
+    if (lane == 0) fields[g] = nz ? max(1, (int)(mx >> 20)) : 0;
   }
 }
 
@@ -896,22 +871,11 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   // long rows (the matvec's t2 . renv: k up to 528) are folded one warp per row; short ones
   // by 8-element chunks with atomics
   row_warp = a_exp > 0 && a_chunks * 8 >= (int64_t)32 * a_exp;
-  a_rtiles.clear();
-  if (row_warp) {
-    for (int i = 0; i < (int)a_ops.size(); ++i)
-      for (int rt = 0; rt * kTM < a_ops[i].rows; ++rt) a_rtiles.push_back(make_int2(i, rt));
-    auto tile_elems = [&](const int2& t) {
-      return (int64_t)std::min(kTM, a_ops[t.x].rows - t.y * kTM) * a_ops[t.x].cols;
-    };
-    std::stable_sort(a_rtiles.begin(), a_rtiles.end(),
-                     [&](const int2& x, const int2& y) { return tile_elems(x) > tile_elems(y); });
-  }
-  d_a_rtiles = upload(a_rtiles, s);
   {
     int per_sm = 0;
     if (row_warp) {
-      QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pack_a_rows, 256, 0));
-      row_exp_grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)a_rtiles.size(),
+      QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_field_rows, 256, 0));
+      row_exp_grid = (int)std::max<int64_t>(1, std::min<int64_t>((a_exp + 7) / 8,
                                                                  (int64_t)std::max(1, per_sm) * p.ctx->num_sms));
     } else {
       QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_field, 256, 0));
@@ -947,8 +911,8 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
 
 int64_t SplitPlan::launches() const {
   if (tiles.empty()) return 0;
-  // A: fused row scales + pack, or memset, row scales, pack; B: pack; GEMM
-  return (a_static ? 0 : (row_warp ? 1 : 3)) + (b_static ? 0 : 1) + 1;
+  // A: (memset,) row scales, pack; B: pack; GEMM
+  return (a_static ? 0 : (row_warp ? 2 : 3)) + (b_static ? 0 : 1) + 1;
 }
 
 // Scale exponents and slice tiles of one operand side (A: rows, B: columns), reading each
@@ -962,16 +926,15 @@ void pack_split_operand(SplitPlan& sp, bool side_a, const void* scratch, const v
       return;
     }
     if (sp.row_warp) {
-      k_pack_a_rows<<<sp.row_exp_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), sp.d_a_rtiles.as<int2>(),
-                                                    (int)sp.a_rtiles.size(), sp.a_exps.as<int32_t>(),
-                                                    sp.a_packed.as<uint8_t>());
+      k_row_field_rows<<<sp.row_exp_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+                                                       sp.n_a_rows, sp.a_exps.as<int32_t>());
     } else {
       QLTG_CUDA(cudaMemsetAsync(sp.a_exps.get(), 0, sp.n_a_rows * sizeof(int32_t), s));
       k_row_field<<<sp.row_exp_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
                                                   sp.n_a_chunks, sp.a_exps.as<int32_t>());
-      k_pack_a<<<sp.pack_a_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
-                                              sp.n_a_pchunks, sp.a_exps.as<int32_t>(), sp.a_packed.as<uint8_t>());
     }
+    k_pack_a<<<sp.pack_a_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
+                                            sp.n_a_pchunks, sp.a_exps.as<int32_t>(), sp.a_packed.as<uint8_t>());
   } else {
     if (sp.b_ops.empty()) {
       sp.b_ready = true;
