@@ -251,6 +251,13 @@ QLTG_API int qltg_axis_monomial_plan_create(qltg_ctx* ctx, const qltg_tensor_des
                                             const int32_t* out_qns, const int64_t* out_dims, const int32_t* flux,
                                             int64_t nentries, const int64_t* entries, const double* coefs,
                                             qltg_axis_plan** plan);
+/* ProjectAxis (axis_ops.h:2469-2532): kept_counts[s] degeneracies kept from input sector s,
+ * their offsets concatenated in `kept` (each in range and unique within its sector; at least
+ * one kept overall). Sectors keeping none leave the output index; the others keep their
+ * quantum number and order, degeneracies in the listed order. Execute with
+ * qltg_axis_monomial_exec (alpha 1, beta 0). */
+QLTG_API int qltg_axis_project_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* t, int32_t axis,
+                                           const int64_t* kept_counts, const int64_t* kept, qltg_axis_plan** plan);
 /* out = beta out + alpha M(in) over the generated topology (beta == 0 never reads out_dev). */
 QLTG_API int qltg_axis_monomial_exec(qltg_axis_plan* plan, const void* in_dev, void* out_dev, const double* alpha,
                                      const double* beta, void* stream);
@@ -261,6 +268,24 @@ QLTG_API int qltg_axis_plan_exec(qltg_axis_plan* plan, const void* in_dev, const
                                  void* out_dev, int32_t mode, void* stream);
 QLTG_API int qltg_axis_plan_device_status(qltg_axis_plan* plan, void* stream);
 QLTG_API int qltg_axis_plan_destroy(qltg_axis_plan* plan);
+
+/* ---------------------------------------------------------------- linear combination
+ * out = sum_i coefs[i] T_i + beta res over the union of the blocks of the contributing
+ * tensors (coefs[i] != 0; res when beta != 0, or always with keep_res), ascending block
+ * index: LinearCombine (tensor_manipulation/ten_linear_combine.h:33-197); AddScaledAssign
+ * (:211-221) is ({alpha}, {x}, beta 1, res y). All tensors share the indexes of T_0
+ * (QLTG_ERR_LAYOUT otherwise); 1 to 64 tensors of rank >= 1; coefs and beta interleaved for
+ * complex tensors. beta != 0 needs res. */
+typedef struct qltg_lincomb_plan qltg_lincomb_plan;
+QLTG_API int qltg_lincomb_plan_create(qltg_ctx* ctx, int32_t n, const qltg_tensor_desc* const* tens,
+                                      const double* coefs, const qltg_tensor_desc* res, const double* beta,
+                                      int32_t keep_res, qltg_lincomb_plan** plan);
+QLTG_API int qltg_lincomb_plan_result(const qltg_lincomb_plan* plan, int32_t* rank, int64_t* nblk, int64_t* size);
+QLTG_API int qltg_lincomb_plan_result_blocks(const qltg_lincomb_plan* plan, int64_t* coords, int64_t* offsets);
+/* out_dev may be a T_i's or res's buffer only when that tensor has the output's topology. */
+QLTG_API int qltg_lincomb_exec(qltg_lincomb_plan* plan, const void* const* tens_dev, const void* res_dev,
+                               void* out_dev, void* stream);
+QLTG_API int qltg_lincomb_plan_destroy(qltg_lincomb_plan* plan);
 
 /* ---------------------------------------------------------------- .qlten stream I/O
  * The reference's QLTensor serialisation (qltensor/qltensor_impl.h:799-830, index.h:170-188,

@@ -14,6 +14,12 @@ pinned against the reference's outputs in tests/golden/axis_ops.npz.
                        :2306-2332): output blocks = input blocks mapped through every entry whose
                        input sector matches; out = beta out + sum over entries of alpha coef
                        (input slice in_offset -> output slice out_offset)
+  project_axis         ProjectAxis (axis_ops.h:2469-2532, copy :2337-2363): keep the listed
+                       degeneracies of every sector, drop sectors keeping none
+  linear_combine       LinearCombine (tensor_manipulation/ten_linear_combine.h:33-197): sum of
+                       coef T over the union of the contributing tensors' blocks, res last
+The reference's composed forms (axis_ops.h:3128-3561) are these applied in sequence; the
+tests compose them the same way.
 """
 from typing import Optional, Sequence
 
@@ -118,3 +124,42 @@ def axis_monomial(t: BSTensor, axis: int, out_leg: Leg, entries, coefs, alpha=1.
             idx[axis] = slice(int(e[3]), int(e[3]) + 1)
             ob[tuple(idx)] += alpha * cf * src
     return res
+
+
+def project_axis(t: BSTensor, axis: int, kept: Sequence[Sequence[int]]) -> BSTensor:
+    leg = t.legs[axis]
+    counts = np.asarray([len(k) for k in kept], np.int64)
+    new_sct = np.cumsum(counts > 0) - 1
+    legs = list(t.legs)
+    legs[axis] = Leg(leg.dir, leg.qns[counts > 0], counts[counts > 0], leg.parity_comp)
+    keep_blk = [b for b in range(t.nblk) if counts[t.coords[b, axis]] > 0]
+    coords = t.coords[keep_blk].copy()
+    coords[:, axis] = new_sct[coords[:, axis]]
+    res = BSTensor(legs, coords.reshape(-1, t.rank), t.dtype)
+    data = [t.block(b).take(np.asarray(kept[t.coords[b, axis]], np.int64), axis=axis).reshape(-1) for b in keep_blk]
+    res.data = np.concatenate(data) if data else np.zeros(0, t.dtype)
+    return res
+
+
+def linear_combine(coefs, tens: Sequence[BSTensor], beta=0.0, res: Optional[BSTensor] = None,
+                   keep_res: bool = False) -> BSTensor:
+    srcs = [(c, t) for c, t in zip(coefs, tens) if c != 0]
+    if res is not None and beta != 0:
+        srcs.append((beta, res))
+    topo = [t for _, t in srcs] + ([res] if res is not None and keep_res else [])
+    ref = tens[0]
+    blocks = {}
+    for t in topo:
+        for b in range(t.nblk):
+            blocks.setdefault(int(t.blk_idx()[b]), t.coords[b])
+    keys = sorted(blocks)
+    out = BSTensor(ref.legs, np.array([blocks[k] for k in keys], np.int64).reshape(-1, ref.rank), ref.dtype)
+    out.data = np.zeros(out.size, ref.dtype)
+    pos = {int(k): q for q, k in enumerate(out.blk_idx())}
+    for c, t in srcs:
+        idx = t.blk_idx()
+        for b in range(t.nblk):
+            q = pos[int(idx[b])]
+            o = int(out.offsets[q])
+            out.data[o:o + t.block(b).size] += c * t.block(b).reshape(-1)
+    return out

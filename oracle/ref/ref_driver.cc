@@ -468,6 +468,147 @@ int main(int argc, char** argv) {
         dmrg::ApplyTwoRank2ToAxesPreserveOrder(P, op1, 0, op2, 3, out);
         dump(w, "two.out", out);
       }
+      auto scalars = [&](size_t axis) {
+        dmrg::AxisSectorScalar<double, U1QN> sc{axis, {}};
+        for (size_t s2 = 0; s2 < P.GetIndex(axis).GetQNSctNum(); ++s2) sc.values_by_sector.push_back(rng.next());
+        return sc;
+      };
+      // a rank-2 operator restricted to the diagonal sector blocks listed in `keep`
+      auto partial = [&](const T& op, const std::vector<size_t>& keep) {
+        T o(op.GetIndexes());
+        const auto& i0 = op.GetIndex(0);
+        const auto& i1 = op.GetIndex(1);
+        size_t b0 = 0, b1 = 0;
+        for (size_t s2 = 0; s2 < i0.GetQNSctNum(); ++s2) {
+          const size_t d0 = i0.GetQNSct(s2).GetDegeneracy(), d1 = i1.GetQNSct(s2).GetDegeneracy();
+          if (std::find(keep.begin(), keep.end(), s2) != keep.end())
+            for (size_t a = 0; a < d0; ++a)
+              for (size_t b = 0; b < d1; ++b) o.SetElem({b0 + a, b1 + b}, op.GetElem({b0 + a, b1 + b}));
+          b0 += d0;
+          b1 += d1;
+        }
+        return o;
+      };
+      // projector on the right bond leg: sector 0 dropped, sector 1 keeps {0}, sector 2 keeps
+      // {3, 1} (reordered), the others keep everything
+      {
+        const auto& ix = P.GetIndex(3);
+        dmrg::AxisProjector<U1QN> pr{ix, {}};
+        std::vector<int64_t> counts, flat;
+        for (size_t s2 = 0; s2 < ix.GetQNSctNum(); ++s2) {
+          std::vector<size_t> k;
+          const size_t d = ix.GetQNSct(s2).GetDegeneracy();
+          if (s2 == 1) k = {0};
+          else if (s2 == 2 && d > 3) k = {3, 1};
+          else if (s2 != 0) for (size_t j = 0; j < d; ++j) k.push_back(j);
+          counts.push_back((int64_t)k.size());
+          for (auto x : k) flat.push_back((int64_t)x);
+          pr.kept_degeneracies.push_back(k);
+        }
+        w.i64("proj.counts", counts);
+        w.i64("proj.kept", flat);
+        T out;
+        dmrg::ProjectAxis(P, 3, pr, out);
+        dump(w, "proj.out", out);
+      }
+      {
+        T op = rank2(0, -1);
+        auto [dg, flat] = diag_op(3);
+        dump(w, "r2diag.op", op);
+        w.f64("r2diag.values", flat);
+        T out;
+        dmrg::ApplyRank2ThenAxisDiagonalPreserveOrder(P, op, 0, 3, dg, out);
+        dump(w, "r2diag.out", out);
+      }
+      {
+        T op = rank2(3, 1);
+        auto sc = scalars(0);
+        dump(w, "r2sect.op", op);
+        w.f64("r2sect.values", sc.values_by_sector);
+        T out;
+        dmrg::ApplyRank2ThenAxisSectorScalarsPreserveOrder(P, op, 3, sc, out);
+        dump(w, "r2sect.out", out);
+      }
+      // boundary rank-2 then sector scalars: fused (fresh output), accumulated onto it, and
+      // accumulated onto an output lacking blocks (expansion); then the last-axis form
+      {
+        T op = rank2(0, -1);
+        T opp = partial(op, {1, 2});
+        auto sc = scalars(3);
+        dump(w, "bnd.op", op);
+        dump(w, "bnd.opp", opp);
+        w.f64("bnd.values", sc.values_by_sector);
+        T fused;
+        dmrg::ApplyBoundaryRank2ThenAxisSectorScalarsFusedPreserveOrder(P, op, 0, sc, fused);
+        dump(w, "bnd.fused", fused);
+        T acc = fused;
+        dmrg::ApplyBoundaryRank2ThenAxisSectorScalarsAccumulatePreserveOrder(P, op, 0, sc, -0.5, 2.0, acc);
+        dump(w, "bnd.acc", acc);
+        T part;
+        dmrg::ApplyBoundaryRank2ThenAxisSectorScalarsFusedPreserveOrder(P, opp, 0, sc, part);
+        dump(w, "bnd.part", part);
+        dmrg::ApplyBoundaryRank2ThenAxisSectorScalarsAccumulatePreserveOrder(P, op, 0, sc, 1.25, 0.75, part);
+        dump(w, "bnd.exp", part);
+        T op3 = rank2(3, 1);
+        auto sc0 = scalars(0);
+        dump(w, "bnd.op3", op3);
+        w.f64("bnd.values0", sc0.values_by_sector);
+        T last;
+        dmrg::ApplyBoundaryRank2ThenAxisSectorScalarsFusedPreserveOrder(P, op3, 3, sc0, last);
+        dump(w, "bnd.last", last);
+      }
+      {
+        T op = rank2(0, -1);
+        dmrg::AxisMonomialOp<double, U1QN> mo{P.GetIndex(3), P.GetIndex(3), U1QN(0), {}};
+        const std::vector<std::array<size_t, 4>> ent = {{2, 0, 2, 3}, {2, 3, 2, 0}, {2, 1, 2, 1},
+                                                        {2, 1, 2, 3}, {1, 0, 1, 1}, {3, 1, 3, 0}};
+        const std::vector<double> cf = {0.5, -1.0, 2.0, 0.25, 1.5, -0.75};
+        for (size_t i = 0; i < ent.size(); ++i)
+          mo.entries.push_back({ent[i][0], ent[i][1], ent[i][2], ent[i][3], cf[i]});
+        dump(w, "r2mono.op", op);
+        T out;
+        dmrg::ApplyRank2ThenAxisMonomialFusedPreserveOrder(P, op, 0, 3, mo, out);
+        dump(w, "r2mono.out", out);
+      }
+      {
+        T op1 = rank2(0, 1), op2 = rank2(3, -1);
+        auto [dg, flat] = diag_op(1);
+        auto sc = scalars(2);
+        dump(w, "two2.op1", op1);
+        dump(w, "two2.op2", op2);
+        w.f64("two2.values", flat);
+        w.f64("two2.scalars", sc.values_by_sector);
+        T od, os;
+        dmrg::ApplyTwoRank2ThenAxisDiagonalPreserveOrder(P, op1, 0, op2, 3, 1, dg, od);
+        dump(w, "two2.diag", od);
+        dmrg::ApplyTwoRank2ThenAxisSectorScalarsPreserveOrder(P, op1, 0, op2, 3, sc, os);
+        dump(w, "two2.sect", os);
+      }
+      {
+        T out;
+        dmrg::MoveHeadAxisToTail(P, out);
+        dump(w, "move.out", out);
+      }
+      // LinearCombine over tensors with the same indexes and different block sets
+      {
+        T op = rank2(0, -1);
+        T X, Y, Z;
+        dmrg::ApplyRank2ToAxisPreserveOrder(P, partial(op, {0, 1, 2}), 0, X);
+        dmrg::ApplyRank2ToAxisPreserveOrder(P, partial(op, {2, 3, 4}), 0, Y);
+        dmrg::ApplyRank2ToAxisPreserveOrder(P, op, 0, Z);
+        dump(w, "lc.X", X);
+        dump(w, "lc.Y", Y);
+        dump(w, "lc.Z", Z);
+        T r1;
+        LinearCombine<double, U1QN>({1.5, -2.0}, {&X, &Y}, 0.0, &r1);
+        dump(w, "lc.r1", r1);
+        T r2 = Z;
+        LinearCombine<double, U1QN>({0.5, 0.0, 3.0}, {&X, &Y, &X}, 2.0, &r2);
+        dump(w, "lc.r2", r2);
+        T r3 = X;
+        AddScaledAssign(r3, 0.25, Y);
+        dump(w, "lc.r3", r3);
+      }
     } else if (cs == "svd_u1") {
       auto t = sy::svd_psi(std::stoi(A(3)), std::stod(A(4)), std::stoll(A(5)), std::stoull(A(6)));
       svd_case<double, U1QN>(w, t, 2, std::stod(A(7)), std::stoull(A(8)), std::stoull(A(9)));

@@ -14,8 +14,14 @@ _API = {"Contract", "ContractionPlan", "ContractContiguousAxes", "ContiguousCont
         "ContractTailHeadContiguous", "ContractTailHeadContiguousAccumulate",
         "TryContractTailHeadContiguousAccumulate", "AccumulatePlan", "read_qlten", "write_qlten", "ApplyAxisDiagonal",
         "ApplyAxisDiagonalInPlace", "ApplyAxisSectorScalars", "AxisRank2Plan", "ApplyRank2ToAxisPreserveOrder",
-        "ApplyTwoRank2ToAxesPreserveOrder", "ApplyAxisMonomial", "AxisMonomialPlan", "Transpose", "SVD", "QR", "Matvec", "Lanczos", "DTensor", "Context",
-        "context"}
+        "ApplyTwoRank2ToAxesPreserveOrder", "ApplyAxisMonomial", "AxisMonomialPlan", "AxisProjectPlan", "ProjectAxis",
+        "LinearCombinePlan", "LinearCombine", "AddScaledAssign", "ApplyAxisDiagonalPreserveOrder",
+        "ScaleAxisSectorsInPlace", "ApplyAxisSectorScalarsPreserveOrder", "ApplyRank2ThenAxisDiagonalPreserveOrder",
+        "ApplyRank2ThenAxisSectorScalarsPreserveOrder",
+        "ApplyBoundaryRank2ThenAxisSectorScalarsAccumulatePreserveOrder",
+        "ApplyBoundaryRank2ThenAxisSectorScalarsFusedPreserveOrder", "ApplyRank2ThenAxisMonomialFusedPreserveOrder",
+        "ApplyTwoRank2ThenAxisDiagonalPreserveOrder", "ApplyTwoRank2ThenAxisSectorScalarsPreserveOrder",
+        "MoveHeadAxisToTail", "Transpose", "SVD", "QR", "Matvec", "Lanczos", "DTensor", "Context", "context"}
 
 
 def __getattr__(name):

@@ -463,6 +463,185 @@ def ApplyTwoRank2ToAxesPreserveOrder(t: DTensor, op1: DTensor, axis1: int, op2: 
     return plan.execute(t, op1, op2, mode=mode)
 
 
+class AxisProjectPlan(AxisMonomialPlan):
+    """Planned qlten::dmrg::ProjectAxis (axis_ops.h:2469-2532): `kept[s]` lists the input
+    degeneracy offsets of sector s kept (in output order); sectors keeping none leave the
+    output index."""
+
+    def __init__(self, t: BSTensor, axis: int, kept: Sequence[Sequence[int]], device: int = 0):
+        self.h = None
+        self.ctx = context(device)
+        self.device = device
+        leg = t.legs[axis]
+        if len(kept) != leg.nsct:
+            raise ValueError("one kept list per sector of the axis")
+        counts = np.asarray([len(k) for k in kept], np.int64)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(k, np.int64) for k in kept] + [np.zeros(0, np.int64)]))
+        dt = _Desc(t)
+        h = C.c_void_p()
+        check(lib().qltg_axis_project_plan_create(self.ctx.h, dt.ref, int(axis), counts.ctypes.data,
+                                                  flat.ctypes.data if flat.size else None, C.byref(h)))
+        self.h = h
+        keep = counts > 0
+        legs = list(t.legs)
+        legs[axis] = Leg(leg.dir, leg.qns[keep], counts[keep], leg.parity_comp)
+        self.result = _result_meta(h, lib().qltg_axis_plan_result, lib().qltg_axis_plan_result_blocks, legs, t.dtype)
+
+    def execute(self, t: DTensor, out: Optional[DTensor] = None) -> DTensor:
+        return super().execute(t, 1.0, 0.0, out)
+
+
+def ProjectAxis(t: DTensor, axis: int, kept: Sequence[Sequence[int]]) -> DTensor:
+    """qlten::dmrg::ProjectAxis (axis_ops.h:2469-2532)."""
+    return AxisProjectPlan(t.meta, axis, kept, t.device).execute(t)
+
+
+class LinearCombinePlan:
+    """Planned LinearCombine (tensor_manipulation/ten_linear_combine.h:33-197):
+    out = sum_i coefs[i] T_i + beta res over the union of the contributing tensors' blocks
+    (res joins when beta != 0, or always with keep_res)."""
+
+    def __init__(self, coefs, metas: Sequence[BSTensor], beta=0.0, res: Optional[BSTensor] = None,
+                 keep_res: bool = False, device: int = 0):
+        self.h = None
+        self.device = device
+        self.n = len(metas)
+        cplx = metas[0].is_complex
+        cf = _axis_values(np.asarray(coefs), cplx)
+        be = _axis_values(np.asarray([beta]), cplx)
+        self._descs = [_Desc(m) for m in metas]
+        arr = (C.POINTER(capi.TensorDesc) * self.n)(*[C.pointer(d.s) for d in self._descs])
+        rd = _Desc(res) if res is not None else None
+        h = C.c_void_p()
+        check(lib().qltg_lincomb_plan_create(context(device).h, self.n, C.cast(arr, C.c_void_p), cf.ctypes.data,
+                                             rd.ref if rd is not None else None, be.ctypes.data, int(keep_res),
+                                             C.byref(h)))
+        self.h = h
+        self.result = _result_meta(h, lib().qltg_lincomb_plan_result, lib().qltg_lincomb_plan_result_blocks,
+                                   metas[0].legs, metas[0].dtype)
+
+    def execute(self, tens: Sequence[DTensor], res: Optional[DTensor] = None,
+                out: Optional[DTensor] = None) -> DTensor:
+        if out is None:
+            out = DTensor.empty(self.result, self.device)
+        ptrs = (C.c_void_p * self.n)(*[C.c_void_p(t.ptr) for t in tens])
+        check(lib().qltg_lincomb_exec(self.h, C.cast(ptrs, C.c_void_p), C.c_void_p(res.ptr) if res is not None else None,
+                                      C.c_void_p(out.ptr), stream_ptr(self.device)))
+        return out
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().qltg_lincomb_plan_destroy(self.h)
+        except Exception:
+            pass
+
+
+def LinearCombine(coefs, tens: Sequence[DTensor], beta=0.0, res: Optional[DTensor] = None,
+                  keep_res: bool = False) -> DTensor:
+    """LinearCombine (ten_linear_combine.h:186-197). Written into res's buffer when the result
+    has res's topology (res then is the returned tensor), else into a new tensor."""
+    plan = LinearCombinePlan(coefs, [t.meta for t in tens], beta, res.meta if res is not None else None, keep_res,
+                             tens[0].device)
+    same = res is not None and np.array_equal(plan.result.coords, res.meta.coords)
+    out = plan.execute(tens, res, res if same else None)
+    if same:
+        res.meta = plan.result
+    return out
+
+
+def AddScaledAssign(y: DTensor, alpha, x: DTensor) -> DTensor:
+    """y += alpha x (ten_linear_combine.h:211-221): in place unless x has blocks y lacks."""
+    return LinearCombine([alpha], [x], 1.0, y)
+
+
+def ApplyAxisDiagonalPreserveOrder(t: DTensor, axis: int, values, in_place: bool = False) -> DTensor:
+    """qlten::dmrg::ApplyAxisDiagonalPreserveOrder (axis_ops.h:2584-2637): out of place, or
+    in place (the reference's consume-owned storage mode)."""
+    return ApplyAxisDiagonalInPlace(t, axis, values) if in_place else ApplyAxisDiagonal(t, axis, values)
+
+
+def ScaleAxisSectorsInPlace(t: DTensor, axis: int, values_by_sector) -> DTensor:
+    """qlten::dmrg::ScaleAxisSectorsInPlace (axis_ops.h:2639-2675)."""
+    return ApplyAxisSectorScalars(t, axis, values_by_sector, out=t)
+
+
+def ApplyAxisSectorScalarsPreserveOrder(t: DTensor, axis: int, values_by_sector, in_place: bool = False) -> DTensor:
+    """qlten::dmrg::ApplyAxisSectorScalarsPreserveOrder (axis_ops.h:2677-2744)."""
+    return ApplyAxisSectorScalars(t, axis, values_by_sector, out=t if in_place else None)
+
+
+def ApplyRank2ThenAxisDiagonalPreserveOrder(t: DTensor, op: DTensor, rank2_axis: int, diagonal_axis: int, values,
+                                            mode="fp64") -> DTensor:
+    """qlten::dmrg::ApplyRank2ThenAxisDiagonalPreserveOrder (axis_ops.h:3128-3151)."""
+    return ApplyAxisDiagonalInPlace(ApplyRank2ToAxisPreserveOrder(t, op, rank2_axis, mode), diagonal_axis, values)
+
+
+def ApplyRank2ThenAxisSectorScalarsPreserveOrder(t: DTensor, op: DTensor, rank2_axis: int, scale_axis: int,
+                                                 values_by_sector, mode="fp64") -> DTensor:
+    """qlten::dmrg::ApplyRank2ThenAxisSectorScalarsPreserveOrder (axis_ops.h:3153-3180)."""
+    return ScaleAxisSectorsInPlace(ApplyRank2ToAxisPreserveOrder(t, op, rank2_axis, mode), scale_axis,
+                                   values_by_sector)
+
+
+def ApplyBoundaryRank2ThenAxisSectorScalarsAccumulatePreserveOrder(t: DTensor, op: DTensor, rank2_axis: int,
+                                                                   scale_axis: int, values_by_sector, alpha, beta,
+                                                                   out: Optional[DTensor] = None,
+                                                                   mode="fp64") -> DTensor:
+    """qlten::dmrg::ApplyBoundaryRank2ThenAxisSectorScalarsAccumulatePreserveOrder
+    (axis_ops.h:3182-3283): out = beta out + alpha S(R(t)), R on axis 0 or the last axis, S the
+    sector scalars. An existing out keeps its blocks and gains the ones R produces; a missing
+    out needs beta == 0. Returns out (updated in place when no block was added) or the
+    expanded result."""
+    if rank2_axis not in (0, t.meta.rank - 1):
+        raise ValueError("rank2_axis must be axis 0 or the last axis")
+    if out is None and complex(beta) != 0:
+        raise ValueError("beta != 0 needs an existing output")
+    r = ApplyRank2ThenAxisSectorScalarsPreserveOrder(t, op, rank2_axis, scale_axis, values_by_sector, mode)
+    if out is None:
+        return r if complex(alpha) == 1 else LinearCombine([alpha], [r])
+    return LinearCombine([alpha], [r], beta, out, keep_res=True)
+
+
+def ApplyBoundaryRank2ThenAxisSectorScalarsFusedPreserveOrder(t: DTensor, op: DTensor, rank2_axis: int,
+                                                              scale_axis: int, values_by_sector,
+                                                              mode="fp64") -> DTensor:
+    """qlten::dmrg::ApplyBoundaryRank2ThenAxisSectorScalarsFusedPreserveOrder (axis_ops.h:3285-3318)."""
+    return ApplyBoundaryRank2ThenAxisSectorScalarsAccumulatePreserveOrder(t, op, rank2_axis, scale_axis,
+                                                                          values_by_sector, 1.0, 0.0, None, mode)
+
+
+def ApplyRank2ThenAxisMonomialFusedPreserveOrder(t: DTensor, op: DTensor, rank2_axis: int, monomial_axis: int,
+                                                 out_leg: Leg, flux, entries, coefs, mode="fp64") -> DTensor:
+    """qlten::dmrg::ApplyRank2ThenAxisMonomialFusedPreserveOrder (axis_ops.h:3320-3503)."""
+    r = ApplyRank2ToAxisPreserveOrder(t, op, rank2_axis, mode)
+    return ApplyAxisMonomial(r, monomial_axis, out_leg, flux, entries, coefs)
+
+
+def ApplyTwoRank2ThenAxisDiagonalPreserveOrder(t: DTensor, op1: DTensor, axis1: int, op2: DTensor, axis2: int,
+                                               diagonal_axis: int, values, mode="fp64") -> DTensor:
+    """qlten::dmrg::ApplyTwoRank2ThenAxisDiagonalPreserveOrder (axis_ops.h:3505-3532)."""
+    r = ApplyTwoRank2ToAxesPreserveOrder(t, op1, axis1, op2, axis2, mode)
+    return ApplyAxisDiagonalInPlace(r, diagonal_axis, values)
+
+
+def ApplyTwoRank2ThenAxisSectorScalarsPreserveOrder(t: DTensor, op1: DTensor, axis1: int, op2: DTensor, axis2: int,
+                                                    scale_axis: int, values_by_sector, mode="fp64") -> DTensor:
+    """qlten::dmrg::ApplyTwoRank2ThenAxisSectorScalarsPreserveOrder (axis_ops.h:3534-3561)."""
+    r = ApplyTwoRank2ToAxesPreserveOrder(t, op1, axis1, op2, axis2, mode)
+    return ScaleAxisSectorsInPlace(r, scale_axis, values_by_sector)
+
+
+def MoveHeadAxisToTail(t: DTensor) -> DTensor:
+    """qlten::dmrg::MoveHeadAxisToTail (axis_ops.h:3563-3678): axis 0 becomes the last axis
+    (bosonic); a rank-1 tensor is copied."""
+    if t.meta.rank == 0:
+        raise ValueError("input rank must be positive")
+    if t.meta.fermionic:
+        raise ValueError("MoveHeadAxisToTail is bosonic-only")
+    return Transpose(t, list(range(1, t.meta.rank)) + [0])
+
+
 def read_qlten(path: str, qn: str = "U1QN", dtype: str = "f64", device: int = 0) -> DTensor:
     """Read a .qlten file (the reference's QLTensor stream format) straight into device
     memory: header parsed in libqltg.so, raw buffer through a pinned staging buffer."""

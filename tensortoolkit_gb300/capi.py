@@ -56,6 +56,12 @@ _SIGS = {
     "qltg_axis_monomial_plan_create": ([_P, C.POINTER(TensorDesc), C.c_int32, C.c_int32, _P, _P, _P, C.c_int64, _P,
                                         _P, C.POINTER(_P)], C.c_int),
     "qltg_axis_monomial_exec": ([_P, _P, _P, _P, _P, _P], C.c_int),
+    "qltg_axis_project_plan_create": ([_P, C.POINTER(TensorDesc), C.c_int32, _P, _P, C.POINTER(_P)], C.c_int),
+    "qltg_lincomb_plan_create": ([_P, C.c_int32, _P, _P, _P, _P, C.c_int32, C.POINTER(_P)], C.c_int),
+    "qltg_lincomb_plan_result": ([_P, C.POINTER(C.c_int32), _I64P, _I64P], C.c_int),
+    "qltg_lincomb_plan_result_blocks": ([_P, _P, _P], C.c_int),
+    "qltg_lincomb_exec": ([_P, _P, _P, _P, _P], C.c_int),
+    "qltg_lincomb_plan_destroy": ([_P], C.c_int),
     "qltg_axis_plan_result": ([_P, C.POINTER(C.c_int32), _I64P, _I64P], C.c_int),
     "qltg_axis_plan_result_blocks": ([_P, _P, _P], C.c_int),
     "qltg_axis_plan_exec": ([_P, _P, _P, _P, _P, C.c_int32, _P], C.c_int),

@@ -421,6 +421,52 @@ int qltg_axis_monomial_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* t, int
   });
 }
 
+int qltg_axis_project_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* t, int32_t axis, const int64_t* kept_counts,
+                                  const int64_t* kept, qltg_axis_plan** plan) {
+  // ProjectAxis (dmrg/axis_ops.h:2469-2532) is the monomial with one unit entry per kept
+  // degeneracy: (s, kept_s[j]) -> (s', j), s' counting the sectors that keep something
+  std::vector<int32_t> oq;
+  std::vector<int64_t> od, ent;
+  std::vector<double> cf;
+  int nc = 0, per = 1;
+  int32_t out_nsct = 0;
+  const int rc = guarded([&] {
+    QLTG_CHECK(t && kept_counts, QLTG_ERR_INVALID, "null argument");
+    const Meta m = meta_from_desc(t);
+    require_bosonic_axis(m, axis);
+    nc = m.ncomp;
+    per = m.dtype == QLTG_C128 ? 2 : 1;
+    int64_t pos = 0;
+    for (int64_t s = 0; s < m.nsct(axis); ++s) {
+      const int64_t cnt = kept_counts[s];
+      QLTG_CHECK(cnt >= 0 && cnt <= m.dims[axis][s], QLTG_ERR_INVALID, "projector keeps more degeneracies than a sector has");
+      QLTG_CHECK(cnt == 0 || kept, QLTG_ERR_INVALID, "null kept offsets");
+      std::vector<int64_t> seen;
+      for (int64_t j = 0; j < cnt; ++j) {
+        const int64_t d = kept[pos + j];
+        QLTG_CHECK(d >= 0 && d < m.dims[axis][s], QLTG_ERR_INVALID, "projector offset out of range");
+        QLTG_CHECK(std::find(seen.begin(), seen.end(), d) == seen.end(), QLTG_ERR_INVALID,
+                   "projector offset repeated within a sector");
+        seen.push_back(d);
+        ent.insert(ent.end(), {s, d, (int64_t)out_nsct, j});
+        cf.push_back(1.0);
+        if (per == 2) cf.push_back(0.0);
+      }
+      if (cnt > 0) {
+        oq.insert(oq.end(), m.qns[axis].begin() + s * nc, m.qns[axis].begin() + (s + 1) * nc);
+        od.push_back(cnt);
+        ++out_nsct;
+      }
+      pos += cnt;
+    }
+    QLTG_CHECK(out_nsct > 0, QLTG_ERR_INVALID, "projector keeps no degeneracy");
+  });
+  if (rc != QLTG_OK) return rc;
+  const std::vector<int32_t> flux(nc, 0);
+  return qltg_axis_monomial_plan_create(ctx, t, axis, out_nsct, oq.data(), od.data(), flux.data(),
+                                        (int64_t)ent.size() / 4, ent.data(), cf.data(), plan);
+}
+
 int qltg_axis_monomial_exec(qltg_axis_plan* plan, const void* in_dev, void* out_dev, const double* alpha,
                             const double* beta, void* stream) {
   return guarded([&] {

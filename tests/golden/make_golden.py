@@ -51,7 +51,10 @@ def parity_for(name, key, default):
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build the reference driver first: make -C oracle/ref")
+    only = set(sys.argv[1:])   # optional: regenerate only the named fixtures
     for name, (args, pc) in CASES.items():
+        if only and name not in only:
+            continue
         with tempfile.TemporaryDirectory() as td:
             path = os.path.join(td, "out.qtb")
             qdir = os.path.join(HERE, "qlten")
