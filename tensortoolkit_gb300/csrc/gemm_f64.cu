@@ -122,9 +122,13 @@ __global__ void __launch_bounds__(NT) k_gemm_dfma(const GemmCBlk* __restrict__ c
   }
 }
 
-// Skinny output blocks (n <= 8, every task k <= 8): thread per output row, the row's n
-// outputs in registers, instantiated per n so no FP64 slot is spent on absent columns.
+// Skinny output blocks (n <= 8, every task k <= 8): the rows' n outputs in registers,
+// instantiated per n so no FP64 slot is spent on absent columns. A work item is 256 rows of
+// one block; each of the 128 threads takes rows r and r + 128, both in one pass over the
+// tasks when n <= 4 (real): the task records and B values are loaded once for two rows and
+// two independent FMA chains hide each other's load latency.
 constexpr int kSkinnyRows = 256;
+constexpr int kSkinnyThreads = 128;
 constexpr int kSkinnyMax = 8;
 
 template <typename T, int NN>
@@ -151,32 +155,82 @@ __device__ __forceinline__ void skinny_row(const GemmCBlk& cb, const GemmTask* _
   for (int j = 0; j < NN; ++j) out[j] = acc[j];
 }
 
-// Resident CTAs per SM the kernel is compiled for: 6 for real operands (40 registers, no
-// spills); complex ones need their registers (1).
-template <typename T> struct SkinnyMinBlocks { static constexpr int value = 1; };
-template <> struct SkinnyMinBlocks<double> { static constexpr int value = 6; };
+// Rows row0 and row0 + kSkinnyThreads (both inside the block) in one pass.
+template <typename T, int NN>
+__device__ __forceinline__ void skinny_row_pair(const GemmCBlk& cb, const GemmTask* __restrict__ task, int row0,
+                                                const T* __restrict__ A, const T* __restrict__ As,
+                                                const T* __restrict__ B, const T* __restrict__ Bs,
+                                                T* __restrict__ C) {
+  T acc0[NN], acc1[NN];
+#pragma unroll
+  for (int j = 0; j < NN; ++j) acc0[j] = acc1[j] = zero_of(T());
+  for (int t = cb.t0; t < cb.t1; ++t) {
+    const GemmTask tk = task[t];
+    const int k = tk.k;
+    const T* a0 = operand_block(A, As, tk.a_off) + (int64_t)row0 * tk.a_rs;
+    const T* a1 = a0 + (int64_t)kSkinnyThreads * tk.a_rs;
+    const T* b = operand_block(B, Bs, tk.b_off);
+    const unsigned long long sg = sign_mask(tk.sign);
+    for (int kk = 0; kk < k; ++kk) {
+      const T x0 = flip(__ldg(a0 + (int64_t)kk * tk.a_cs), sg);
+      const T x1 = flip(__ldg(a1 + (int64_t)kk * tk.a_cs), sg);
+#pragma unroll
+      for (int j = 0; j < NN; ++j) {
+        const T bj = __ldg(b + kk * NN + j);
+        fma_acc(acc0[j], x0, bj);
+        fma_acc(acc1[j], x1, bj);
+      }
+    }
+  }
+  T* out0 = C + cb.c_off + (int64_t)row0 * NN;
+  T* out1 = out0 + (int64_t)kSkinnyThreads * NN;
+#pragma unroll
+  for (int j = 0; j < NN; ++j) {
+    out0[j] = acc0[j];
+    out1[j] = acc1[j];
+  }
+}
+
+// Row row0 of an item and, if inside the block, row0 + kSkinnyThreads.
+template <typename T, int NN>
+__device__ __forceinline__ void skinny_rows(const GemmCBlk& cb, const GemmTask* __restrict__ task, int row0,
+                                            const T* __restrict__ A, const T* __restrict__ As, const T* __restrict__ B,
+                                            const T* __restrict__ Bs, T* __restrict__ C) {
+  const int row1 = row0 + kSkinnyThreads;
+  if constexpr (sizeof(T) == 8 && NN <= 4) {
+    if (row1 < cb.m) {
+      skinny_row_pair<T, NN>(cb, task, row0, A, As, B, Bs, C);
+      return;
+    }
+  }
+  skinny_row<T, NN>(cb, task, row0, A, As, B, Bs, C);
+  if (row1 < cb.m) skinny_row<T, NN>(cb, task, row1, A, As, B, Bs, C);
+}
+
+// Resident CTAs per SM the kernel is compiled for: 8 for real operands (64 registers, no
+// spills at two rows per thread); complex ones need their registers (2).
+template <typename T> struct SkinnyMinBlocks { static constexpr int value = 2; };
+template <> struct SkinnyMinBlocks<double> { static constexpr int value = 8; };
 
 template <typename T>
-__global__ void __launch_bounds__(kSkinnyRows, SkinnyMinBlocks<T>::value) k_gemm_skinny(const GemmCBlk* __restrict__ cblk,
-                                                             const GemmTask* __restrict__ task,
-                                                             const GemmRowChunk* __restrict__ items, int nitems,
-                                                             const T* __restrict__ A, const T* __restrict__ As,
-                                                             const T* __restrict__ B, const T* __restrict__ Bs,
-                                                             T* __restrict__ C) {
+__global__ void __launch_bounds__(kSkinnyThreads, SkinnyMinBlocks<T>::value) k_gemm_skinny(
+    const GemmCBlk* __restrict__ cblk, const GemmTask* __restrict__ task, const GemmRowChunk* __restrict__ items,
+    int nitems, const T* __restrict__ A, const T* __restrict__ As, const T* __restrict__ B, const T* __restrict__ Bs,
+    T* __restrict__ C) {
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const GemmRowChunk item = items[it];
     const GemmCBlk cb = cblk[item.cblk];
     const int row = item.chunk * kSkinnyRows + threadIdx.x;
     if (row >= cb.m) continue;
     switch (cb.n) {
-      case 1: skinny_row<T, 1>(cb, task, row, A, As, B, Bs, C); break;
-      case 2: skinny_row<T, 2>(cb, task, row, A, As, B, Bs, C); break;
-      case 3: skinny_row<T, 3>(cb, task, row, A, As, B, Bs, C); break;
-      case 4: skinny_row<T, 4>(cb, task, row, A, As, B, Bs, C); break;
-      case 5: skinny_row<T, 5>(cb, task, row, A, As, B, Bs, C); break;
-      case 6: skinny_row<T, 6>(cb, task, row, A, As, B, Bs, C); break;
-      case 7: skinny_row<T, 7>(cb, task, row, A, As, B, Bs, C); break;
-      default: skinny_row<T, 8>(cb, task, row, A, As, B, Bs, C); break;
+      case 1: skinny_rows<T, 1>(cb, task, row, A, As, B, Bs, C); break;
+      case 2: skinny_rows<T, 2>(cb, task, row, A, As, B, Bs, C); break;
+      case 3: skinny_rows<T, 3>(cb, task, row, A, As, B, Bs, C); break;
+      case 4: skinny_rows<T, 4>(cb, task, row, A, As, B, Bs, C); break;
+      case 5: skinny_rows<T, 5>(cb, task, row, A, As, B, Bs, C); break;
+      case 6: skinny_rows<T, 6>(cb, task, row, A, As, B, Bs, C); break;
+      case 7: skinny_rows<T, 7>(cb, task, row, A, As, B, Bs, C); break;
+      default: skinny_rows<T, 8>(cb, task, row, A, As, B, Bs, C); break;
     }
   }
 }
@@ -196,7 +250,7 @@ int skinny_rows_per_item() { return kSkinnyRows; }
 
 template <typename T>
 void launch_skinny_t(const GemmSchedule& g, const Operands& op, void* c, int grid, cudaStream_t s) {
-  k_gemm_skinny<T><<<grid, kSkinnyRows, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
+  k_gemm_skinny<T><<<grid, kSkinnyThreads, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
                                                 g.d_skinny.as<GemmRowChunk>(), (int)g.skinny.size(),
                                                 static_cast<const T*>(op.a), static_cast<const T*>(op.a_src),
                                                 static_cast<const T*>(op.b), static_cast<const T*>(op.b_src),
@@ -216,7 +270,7 @@ template <typename T>
 int skinny_wave(int num_sms) {
   static int per_sm = [] {
     int n = 0;
-    QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_gemm_skinny<T>, kSkinnyRows, 0));
+    QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_gemm_skinny<T>, kSkinnyThreads, 0));
     return std::max(1, n);
   }();
   return std::max(1, num_sms) * per_sm;

@@ -59,20 +59,25 @@ constexpr int kDrainK = 128;               // k between drains (exactness bound)
 // max(1, largest biased exponent field of |x|), so that atomicMax can fold them. The scale
 // exponent is e = F - 1022 (max |x| < 2^e; subnormal-only rows use 2^-1021), 0 for F = 0.
 __device__ __forceinline__ int field_of_bits(uint64_t absbits) {
-  return absbits == 0 ? 0 : max(1, (int)(absbits >> 52));
+  // 32-bit halves only: 64-bit compares and shifts cost extra issue slots
+  const uint32_t hi = (uint32_t)(absbits >> 32), lo = (uint32_t)absbits;
+  return (hi | lo) ? max(1, (int)(hi >> 20)) : 0;
 }
 __device__ __forceinline__ int exp_of_field(int f) { return f ? f - 1022 : 0; }
 
-// |x| / 2^e as the 49-bit integer Y = floor(|x| 2^(49 - e)) and the sign as a BF16 sign bit.
+// |x| / 2^e as the 49-bit integer Y = floor(|x| 2^(49 - e)) and the sign as a BF16 sign bit,
+// in 32-bit halves: Y = (hidden bit : fraction) >> sh with sh = 1026 + e - max(ex, 1) >= 4
+// (|x| < 2^e); zero has no hidden bit and a zero fraction, so it gives Y = 0.
 __device__ __forceinline__ uint64_t scaled_y(double x, int e, uint32_t& sgn) {
-  const uint64_t bits = (uint64_t)__double_as_longlong(x);
-  const uint64_t ab = bits & 0x7FFFFFFFFFFFFFFFull;
-  sgn = (uint32_t)(bits >> 48) & 0x8000u;
-  if (ab == 0) return 0;
-  const int ex = (int)(ab >> 52);
-  const uint64_t mant = (ab & 0xFFFFFFFFFFFFFull) | (ex ? (1ull << 52) : 0ull);
-  const int sh = 1026 + e - (ex ? ex : 1);
-  return sh >= 64 ? 0 : (mant >> sh);
+  const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+  sgn = (hi >> 16) & 0x8000u;
+  const uint32_t ex = (hi >> 20) & 0x7FFu;
+  const uint32_t mhi = (hi & 0xFFFFFu) | (ex ? 0x100000u : 0u);
+  const int sh = 1026 + e - (int)max(ex, 1u);
+  const bool small = sh < 32;
+  const uint32_t yl = small ? __funnelshift_r(lo, mhi, sh) : (mhi >> min(sh - 32, 31));
+  const uint32_t yh = small ? (mhi >> sh) : 0u;
+  return ((uint64_t)yh << 32) | yl;
 }
 // Slice p of two elements as one word of two BF16 values: digit d = bits 7 (kS - 1 - p) ..
 // + 6 of Y, value d 2^(-7(p+1)) with the element's sign. The digit is or-ed into the
@@ -268,7 +273,7 @@ __global__ void __launch_bounds__(256) k_pack_b_cols(const double* __restrict__ 
                                                      const SplitOperand* __restrict__ ops,
                                                      const int2* __restrict__ col_tiles, int ntiles,
                                                      int32_t* __restrict__ exps, uint8_t* __restrict__ pack) {
-  __shared__ uint64_t smx[8][kTN];
+  __shared__ uint32_t smx[8][kTN], snz[8][kTN];
   __shared__ int se[kTN];
   const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
@@ -277,28 +282,32 @@ __global__ void __launch_bounds__(256) k_pack_b_cols(const double* __restrict__ 
     const double* blk = operand_block(scr, src, o.src_off);
     const int c0 = tt.y * kTN;
     const int nc = min(kTN, o.cols - c0);
-    uint64_t mx = 0;
+    uint32_t mx = 0, nz = 0;   // largest high word of |x|, any nonzero bit
     if (lane < nc) {
       const double* col = blk + c0 + lane;
       for (int r = g; r < o.rows; r += 32) {
-        uint64_t v[4];
+        double v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-          v[u] = r + 8 * u < o.rows ? (uint64_t)__double_as_longlong(__ldg(col + (int64_t)(r + 8 * u) * o.cols)) : 0ull;
+        for (int u = 0; u < 4; ++u) v[u] = r + 8 * u < o.rows ? __ldg(col + (int64_t)(r + 8 * u) * o.cols) : 0.0;
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          const uint64_t b1 = v[u] & 0x7FFFFFFFFFFFFFFFull;
-          mx = b1 > mx ? b1 : mx;
+          const uint32_t h = (uint32_t)__double2hiint(v[u]) & 0x7FFFFFFFu;
+          mx = max(mx, h);
+          nz |= h | (uint32_t)__double2loint(v[u]);
         }
       }
     }
     smx[g][lane] = mx;
+    snz[g][lane] = nz;
     __syncthreads();
     if (threadIdx.x < kTN) {
-      uint64_t m = 0;
+      uint32_t m = 0, z = 0;
 #pragma unroll
-      for (int q = 0; q < 8; ++q) m = smx[q][threadIdx.x] > m ? smx[q][threadIdx.x] : m;
-      const int f = field_of_bits(m);
+      for (int q = 0; q < 8; ++q) {
+        m = max(m, smx[q][threadIdx.x]);
+        z |= snz[q][threadIdx.x];
+      }
+      const int f = z ? max(1, (int)(m >> 20)) : 0;
       se[threadIdx.x] = exp_of_field(f);
       if ((int)threadIdx.x < nc) exps[o.exp_off + c0 + threadIdx.x] = f;
     }
