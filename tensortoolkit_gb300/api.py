@@ -751,6 +751,20 @@ class Matvec:
                                       stream_ptr(self.device)))
         return out
 
+    def apply_host(self, psi_host: torch.Tensor, out_host: torch.Tensor) -> torch.Tensor:
+        """H_eff psi with page-locked host buffers (torch `pin_memory()` tensors of float64 raw
+        data): psi copied in, the result written by the last step's kernels straight into
+        out_host. Asynchronous on the device's current stream."""
+        for t in (psi_host, out_host):
+            if t.is_cuda or not t.is_pinned() or t.dtype != torch.float64:
+                raise ValueError("host buffers must be pinned float64 CPU tensors")
+        n = self.result.size * (2 if self.result.is_complex else 1)
+        if out_host.numel() < n:
+            raise ValueError("output buffer smaller than the result")
+        check(lib().qltg_matvec_apply_host(self.h, C.c_void_p(psi_host.data_ptr()), C.c_void_p(out_host.data_ptr()),
+                                           stream_ptr(self.device)))
+        return out_host
+
     def apply_raw(self, psi_ptr: int, out_ptr: int, stream: Optional[int] = None) -> None:
         s = stream_ptr(self.device) if stream is None else C.c_void_p(stream)
         check(lib().qltg_matvec_apply(self.h, C.c_void_p(psi_ptr), C.c_void_p(out_ptr), s))

@@ -101,6 +101,28 @@ int qltg_matvec_apply(qltg_matvec* mv, const void* psi_dev, void* out_dev, void*
   });
 }
 
+int qltg_matvec_apply_host(qltg_matvec* mv, const void* psi_host, void* out_host, void* stream) {
+  return guarded([&] {
+    QLTG_CHECK(mv && psi_host && out_host, QLTG_ERR_INVALID, "null matvec or buffer");
+    QLTG_CUDA(cudaSetDevice(mv->ctx->device));
+    for (const void* p : {psi_host, static_cast<const void*>(out_host)}) {
+      cudaPointerAttributes at{};
+      QLTG_CUDA(cudaPointerGetAttributes(&at, p));
+      QLTG_CHECK(at.type == cudaMemoryTypeHost && at.devicePointer == p, QLTG_ERR_INVALID,
+                 "host buffers must be page-locked and mapped at their host address (cudaMallocHost, cudaHostAlloc)");
+    }
+    const Meta& pm = mv->step[0].b;
+    const int64_t bytes = pm.size * (int64_t)pm.elem_bytes();
+    if (!mv->psi_stage.get()) mv->psi_stage.alloc(std::max<int64_t>(bytes, 16));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (bytes) QLTG_CUDA(cudaMemcpyAsync(mv->psi_stage.get(), psi_host, bytes, cudaMemcpyHostToDevice, s));
+    // the last step's kernels store the result straight into the mapped host buffer, so the
+    // device-to-host transfer overlaps that step instead of following it
+    cudaGraphExec_t g = mv->graph_for(mv->psi_stage.get(), out_host);
+    QLTG_CUDA(cudaGraphLaunch(g, s));
+  });
+}
+
 int qltg_matvec_device_status(qltg_matvec* mv, void* stream) {
   return guarded([&] {
     QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");

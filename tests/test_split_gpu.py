@@ -130,3 +130,23 @@ def test_split_nonfinite(gpu):
     x, y = outs["split"][~fin], outs["fp64"][~fin]
     assert (np.isnan(x) | (x == y)).all()   # skinny blocks run FP64 rows there: exact
     assert rel_frob(outs["split"][fin], outs["fp64"][fin]) <= TOL
+
+
+@pytest.mark.parametrize("mode", ["fp64", "split"])
+def test_matvec_apply_host(gpu, mode):
+    """Host-buffer matvec (psi copied in, the result written straight into page-locked host
+    memory) gives exactly the device-buffer result; an unpinned buffer is refused."""
+    import torch
+    from tensortoolkit_gb300 import capi
+    lenv, psi, mpo1, mpo2, renv = workloads.heisenberg(800, 10, 3.0, 3)
+    dl, d1, d2, dr = (DTensor.from_host(x) for x in (lenv, mpo1, mpo2, renv))
+    mv = Matvec(dl, psi, d1, d2, dr, mode=mode)
+    ref = mv.apply(DTensor.from_host(psi)).to_host()
+    h_in = torch.from_numpy(psi.raw_f64()).pin_memory()
+    h_out = torch.full((mv.result.size,), float("nan"), dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        mv.apply_host(h_in, h_out)
+    torch.cuda.synchronize()
+    assert np.array_equal(h_out.numpy(), ref.data)
+    with pytest.raises((capi.QltgError, ValueError)):
+        mv.apply_host(h_in, torch.empty(mv.result.size, dtype=torch.float64))
