@@ -11,8 +11,7 @@ tensortoolkit_gb300/csrc/synth.h; no dataset is involved.
 
 value  : device-resident time per matvec (graph launch only), L2 flushed between steps.
 e2e    : the same through the public API with host buffers (qltg_matvec_apply_host) - pinned
-         host psi copied in, H_eff psi computed, the result written to the pinned host buffer
-         by the last step's kernels - every step.
+         host psi copied in, H_eff psi computed, result copied back - every step.
 roofline: the dominant kernel (grouped GEMM) timed with CUDA events on its own stream.
 cpu_baseline: the CPU restatement of the reference's algorithm (OpenBLAS dgemm per block
          pair, as the reference's CPU build) on a bounded sample of the same workload.
@@ -483,8 +482,7 @@ def main():
         if clk_summary is None:
             clk_summary = clk.summary()
         # end to end through the public API with pinned host buffers
-        # (qltg_matvec_apply_host: psi copied in, the last step writing the result straight
-        # into the page-locked output)
+        # (qltg_matvec_apply_host: psi copied in, the product, the result copied out)
         h_in = torch.from_numpy(psi.raw_f64()).pin_memory()
         h_out = torch.empty(mv.result.size, dtype=torch.float64).pin_memory()
         for _ in range(2):

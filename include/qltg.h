@@ -337,10 +337,9 @@ QLTG_API int qltg_matvec_stats(const qltg_matvec* mv, double* flops, int64_t* la
 
 /* out_dev = H_eff . psi_dev (one graph launch on `stream`). */
 QLTG_API int qltg_matvec_apply(qltg_matvec* mv, const void* psi_dev, void* out_dev, void* stream);
-/* The same with host buffers, both page-locked and mapped (cudaMallocHost / cudaHostAlloc):
- * psi is copied in on `stream`; the last contraction's kernels write the result straight into
- * out_host, overlapping the device-to-host transfer with that step. Asynchronous: the result
- * is in out_host once `stream` has completed. */
+/* The same with host buffers, both page-locked (cudaMallocHost / cudaHostAlloc): psi copied
+ * in, the product, the result copied out, all on `stream`. Asynchronous: the result is in
+ * out_host once `stream` has completed. */
 QLTG_API int qltg_matvec_apply_host(qltg_matvec* mv, const void* psi_host, void* out_host, void* stream);
 
 /* Device-side status of the four captured contractions (see qltg_ctrct_plan_device_status). */

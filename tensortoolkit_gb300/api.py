@@ -753,8 +753,8 @@ class Matvec:
 
     def apply_host(self, psi_host: torch.Tensor, out_host: torch.Tensor) -> torch.Tensor:
         """H_eff psi with page-locked host buffers (torch `pin_memory()` tensors of float64 raw
-        data): psi copied in, the result written by the last step's kernels straight into
-        out_host. Asynchronous on the device's current stream."""
+        data): psi copied in, the product, the result copied out. Asynchronous on the device's
+        current stream."""
         for t in (psi_host, out_host):
             if t.is_cuda or not t.is_pinned() or t.dtype != torch.float64:
                 raise ValueError("host buffers must be pinned float64 CPU tensors")

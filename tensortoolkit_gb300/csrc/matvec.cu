@@ -112,14 +112,16 @@ int qltg_matvec_apply_host(qltg_matvec* mv, const void* psi_host, void* out_host
                  "host buffers must be page-locked and mapped at their host address (cudaMallocHost, cudaHostAlloc)");
     }
     const Meta& pm = mv->step[0].b;
-    const int64_t bytes = pm.size * (int64_t)pm.elem_bytes();
-    if (!mv->psi_stage.get()) mv->psi_stage.alloc(std::max<int64_t>(bytes, 16));
+    const Meta& om = mv->step[3].c;
+    const int64_t in_bytes = pm.size * (int64_t)pm.elem_bytes(), out_bytes = om.size * (int64_t)om.elem_bytes();
+    if (!mv->psi_stage.get()) mv->psi_stage.alloc(std::max<int64_t>(in_bytes, 16));
+    if (!mv->out_stage.get()) mv->out_stage.alloc(std::max<int64_t>(out_bytes, 16));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (bytes) QLTG_CUDA(cudaMemcpyAsync(mv->psi_stage.get(), psi_host, bytes, cudaMemcpyHostToDevice, s));
-    // the last step's kernels store the result straight into the mapped host buffer, so the
-    // device-to-host transfer overlaps that step instead of following it
-    cudaGraphExec_t g = mv->graph_for(mv->psi_stage.get(), out_host);
-    QLTG_CUDA(cudaGraphLaunch(g, s));
+    // copy engine both ways: the last step storing straight into host memory measured slower
+    // (its scattered 64-byte row stores over the host link stall the epilogue)
+    if (in_bytes) QLTG_CUDA(cudaMemcpyAsync(mv->psi_stage.get(), psi_host, in_bytes, cudaMemcpyHostToDevice, s));
+    QLTG_CUDA(cudaGraphLaunch(mv->graph_for(mv->psi_stage.get(), mv->out_stage.get()), s));
+    if (out_bytes) QLTG_CUDA(cudaMemcpyAsync(out_host, mv->out_stage.get(), out_bytes, cudaMemcpyDeviceToHost, s));
   });
 }
 

@@ -22,7 +22,7 @@ struct qltg_matvec {
   const void* mpo2 = nullptr;
   const void* renv = nullptr;
   int64_t psi_size = 0;
-  DevBuf psi_stage;   // device copy of a host psi (qltg_matvec_apply_host)
+  DevBuf psi_stage, out_stage;   // device copies of host psi / result (qltg_matvec_apply_host)
   struct Graph {
     const void* in;
     void* out;

@@ -134,8 +134,8 @@ def test_split_nonfinite(gpu):
 
 @pytest.mark.parametrize("mode", ["fp64", "split"])
 def test_matvec_apply_host(gpu, mode):
-    """Host-buffer matvec (psi copied in, the result written straight into page-locked host
-    memory) gives exactly the device-buffer result; an unpinned buffer is refused."""
+    """Host-buffer matvec (page-locked psi copied in, the result copied out) gives exactly the
+    device-buffer result; an unpinned buffer is refused."""
     import torch
     from tensortoolkit_gb300 import capi
     lenv, psi, mpo1, mpo2, renv = workloads.heisenberg(800, 10, 3.0, 3)
