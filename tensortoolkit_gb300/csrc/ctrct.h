@@ -126,7 +126,6 @@ struct SplitPlan {
   int64_t n_a_chunks = 0, n_a_pchunks = 0, n_a_rows = 0;
   bool row_warp = false;          // A row scales one warp per row (long rows) or by chunks
   DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_b_col_tiles;
-  DevBuf d_row_op;                // row_warp: operand ordinal of every A row
   void build(const struct CtrctPlan& p, cudaStream_t s);
   int64_t launches() const;
 };

@@ -194,16 +194,20 @@ __global__ void __launch_bounds__(256) k_row_field(const double* __restrict__ sc
 // exponent-offset order), loads along the row coalesced across the warp, a warp max, one
 // store per row (no zero fill, no atomics).
 __global__ void __launch_bounds__(256) k_row_field_rows(const double* __restrict__ scr, const double* __restrict__ src,
-                                                        const SplitOperand* __restrict__ ops,
-                                                        const int32_t* __restrict__ row_op, int64_t nrows,
+                                                        const SplitOperand* __restrict__ ops, int nops, int64_t nrows,
                                                         int32_t* __restrict__ fields) {
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t g = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < nrows; g += nwarps) {
-    const SplitOperand o = ops[__ldg(row_op + g)];   // operand owning row g (built on the host)
+    int lo = 0, hi = nops - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ops[mid].exp_off <= g) lo = mid; else hi = mid - 1;
+    }
+    const SplitOperand o = ops[lo];
     const double* row = operand_block(scr, src, o.src_off) + (g - o.exp_off) * (int64_t)o.cols;
     uint32_t mx = 0, nz = 0;
-#pragma unroll 8
+#pragma unroll 4
     for (int c = lane; c < o.cols; c += 32) {
       const uint64_t b = (uint64_t)__double_as_longlong(__ldg(row + c)) & 0x7FFFFFFFFFFFFFFFull;
       mx = max(mx, (uint32_t)(b >> 32));
@@ -233,16 +237,10 @@ __global__ void __launch_bounds__(256) k_pack_a(const double* __restrict__ scr, 
       if (ops[mid].pchunk_begin <= first) lo = mid; else hi = mid - 1;
     }
   }
-  int cur = -1;
-  SplitOperand o{};
-  int nkc = 1;
   for (int64_t ch = cbeg + threadIdx.x; ch < cend; ch += blockDim.x) {
     while (lo + 1 < nops && ops[lo + 1].pchunk_begin <= ch) ++lo;
-    if (lo != cur) {   // the operand record is read again only when the thread moves on
-      cur = lo;
-      o = ops[lo];
-      nkc = (o.cols + 7) >> 3;
-    }
+    const SplitOperand o = ops[lo];
+    const int nkc = (o.cols + 7) >> 3;
     const int l = (int)(ch - o.pchunk_begin);   // below 2^31: one block has < 2^31 elements
     const int rt = l / (kTM * nkc);
     const int l2 = l - rt * kTM * nkc;
@@ -882,12 +880,6 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   // long rows (the matvec's t2 . renv: k up to 528) are folded one warp per row; short ones
   // by 8-element chunks with atomics
   row_warp = a_exp > 0 && a_chunks * 8 >= (int64_t)32 * a_exp;
-  if (row_warp) {
-    std::vector<int32_t> row_op(a_exp);
-    for (int i = 0; i < (int)a_ops.size(); ++i)
-      std::fill(row_op.begin() + a_ops[i].exp_off, row_op.begin() + a_ops[i].exp_off + a_ops[i].rows, i);
-    d_row_op = upload(row_op, s);
-  }
   {
     int per_sm = 0;
     if (row_warp) {
@@ -943,7 +935,7 @@ void pack_split_operand(SplitPlan& sp, bool side_a, const void* scratch, const v
       return;
     }
     if (sp.row_warp) {
-      k_row_field_rows<<<sp.row_exp_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), sp.d_row_op.as<int32_t>(),
+      k_row_field_rows<<<sp.row_exp_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
                                                        sp.n_a_rows, sp.a_exps.as<int32_t>());
     } else {
       QLTG_CUDA(cudaMemsetAsync(sp.a_exps.get(), 0, sp.n_a_rows * sizeof(int32_t), s));
