@@ -126,6 +126,18 @@ struct SplitPlan {
   int64_t n_a_chunks = 0, n_a_pchunks = 0, n_a_rows = 0;
   bool row_warp = false;          // A row scales one warp per row (long rows) or by chunks
   DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_b_col_tiles;
+  // a plan with skinny blocks and tiles runs the skinny kernel on a side stream (forked and
+  // joined with events, capturable), beside the slicing kernels and the split GEMM
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  SplitPlan() = default;
+  SplitPlan(const SplitPlan&) = delete;
+  SplitPlan& operator=(const SplitPlan&) = delete;
+  ~SplitPlan() {
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (side) cudaStreamDestroy(side);
+  }
   void build(const struct CtrctPlan& p, cudaStream_t s);
   int64_t launches() const;
 };

@@ -914,6 +914,11 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   QLTG_CUDA(cudaMemsetAsync(error.get(), 0, sizeof(int), s));
   // per device (the attribute belongs to the current device's copy of the kernel)
   QLTG_CUDA(cudaFuncSetAttribute(k_gemm_split, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+  if (!g.skinny.empty() && !tiles.empty() && !side) {
+    QLTG_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    QLTG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    QLTG_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+  }
   QLTG_CUDA(cudaStreamSynchronize(s));
   built = true;
 }
@@ -989,9 +994,26 @@ void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s
   SplitPlan& sp = *p.split;
   // skinny output blocks stay on the FP64 skinny kernel (k, n <= 8: the tensor cores would
   // pad them 8x, and exact integer emulation of these rows measured slower than the FP64
-  // pipe); everything else goes through the slices
-  launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, s);
+  // pipe); everything else goes through the slices. With both present the skinny kernel
+  // runs on the side stream (it writes other output blocks) and joins after the split GEMM.
+  const bool fork = !p.sched.skinny.empty() && !sp.tiles.empty() && sp.side;
+  if (fork) {
+    QLTG_CUDA(cudaEventRecord(sp.fork, s));
+    QLTG_CUDA(cudaStreamWaitEvent(sp.side, sp.fork, 0));
+    launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, sp.side);
+    QLTG_CUDA(cudaEventRecord(sp.join, sp.side));
+  } else {
+    launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, s);
+  }
   if (sp.tiles.empty()) return;
+  struct Join {   // the main stream waits for the side stream on every way out
+    bool on;
+    SplitPlan& sp;
+    cudaStream_t s;
+    ~Join() {
+      if (on) cudaStreamWaitEvent(s, sp.join, 0);
+    }
+  } join{fork, sp, s};
   if (pack) {
     if (!(sp.a_static && sp.a_ready)) pack_split_operand(sp, true, op.a, op.a_src, s);
     if (!(sp.b_static && sp.b_ready)) pack_split_operand(sp, false, op.b, op.b_src, s);
