@@ -70,6 +70,15 @@ struct GemmRowChunk {          // skinny output blocks: 256 consecutive rows of 
   int32_t chunk;
 };
 
+// Row-scale fields of a later split-mode contraction's A operand, folded by the skinny kernel
+// that writes that operand (the matvec's second MPO step writing the last step's A): per
+// skinny output block, the first field of its rows in that operand and the operand's row
+// length k3 (a multiple of the block's n); exp_base < 0: not folded.
+struct SkinnyFuse {
+  int32_t exp_base;
+  int32_t k3;
+};
+
 struct GemmSchedule {
   std::vector<GemmCBlk> cblk;
   std::vector<GemmTask> task;
@@ -125,6 +134,7 @@ struct SplitPlan {
   int row_exp_grid = 1, pack_a_grid = 1, pack_b_grid = 1;   // one wave of resident CTAs of each
   int64_t n_a_chunks = 0, n_a_pchunks = 0, n_a_rows = 0;
   bool row_warp = false;          // A row scales one warp per row (long rows) or by chunks
+  bool a_fields_external = false; // A row scales written by the kernel producing A (matvec)
   DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_b_col_tiles;
   // a plan with skinny blocks and tiles runs the skinny kernel on a side stream (forked and
   // joined with events, capturable), beside the slicing kernels and the split GEMM
@@ -158,6 +168,8 @@ struct CtrctPlan {
   DevBuf a_t, b_t;             // transposed operand scratch
   GemmSchedule sched;
   std::unique_ptr<SplitPlan> split;   // built on first use of QLTG_MODE_SPLIT
+  DevBuf d_fuse;                      // split mode: SkinnyFuse per output block, or empty
+  int32_t* fuse_fields = nullptr;     // the field array those blocks fold into
   int64_t launches_per_exec = 0;
 };
 
@@ -183,7 +195,7 @@ struct Operands {
 };
 void launch_gemm_f64(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms, cudaStream_t s);
 void launch_gemm_f64_skinny(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms,
-                            cudaStream_t s);
+                            cudaStream_t s, const SkinnyFuse* fuse = nullptr, int32_t* fields = nullptr);
 
 // Block order, destination offsets and fermionic block signs of QLTensor::Transpose.
 void transpose_layout(const Meta& m, const std::vector<int>& order, std::vector<double>& signs,

@@ -131,10 +131,18 @@ constexpr int kSkinnyRows = 256;
 constexpr int kSkinnyThreads = 128;
 constexpr int kSkinnyMax = 8;
 
+// Scale field of an output value as the split path defines it (0 for zero, else
+// max(1, biased exponent)); complex outputs are never folded.
+__device__ __forceinline__ int out_field(double v) {
+  const uint32_t hi = (uint32_t)__double2hiint(v) & 0x7FFFFFFFu, lo = (uint32_t)__double2loint(v);
+  return (hi | lo) ? max(1, (int)(hi >> 20)) : 0;
+}
+__device__ __forceinline__ int out_field(double2) { return 0; }
+
 template <typename T, int NN>
 __device__ __forceinline__ void skinny_row(const GemmCBlk& cb, const GemmTask* __restrict__ task, int row,
                                            const T* __restrict__ A, const T* __restrict__ As, const T* __restrict__ B,
-                                           const T* __restrict__ Bs, T* __restrict__ C) {
+                                           const T* __restrict__ Bs, T* __restrict__ C, bool want, int& f) {
   T acc[NN];
 #pragma unroll
   for (int j = 0; j < NN; ++j) acc[j] = zero_of(T());
@@ -153,6 +161,11 @@ __device__ __forceinline__ void skinny_row(const GemmCBlk& cb, const GemmTask* _
   T* out = C + cb.c_off + (int64_t)row * NN;
 #pragma unroll
   for (int j = 0; j < NN; ++j) out[j] = acc[j];
+  if (want) {
+    f = 0;
+#pragma unroll
+    for (int j = 0; j < NN; ++j) f = max(f, out_field(acc[j]));
+  }
 }
 
 // Rows row0 and row0 + kSkinnyThreads (both inside the block) in one pass.
@@ -160,7 +173,7 @@ template <typename T, int NN>
 __device__ __forceinline__ void skinny_row_pair(const GemmCBlk& cb, const GemmTask* __restrict__ task, int row0,
                                                 const T* __restrict__ A, const T* __restrict__ As,
                                                 const T* __restrict__ B, const T* __restrict__ Bs,
-                                                T* __restrict__ C) {
+                                                T* __restrict__ C, bool want, int& f0, int& f1) {
   T acc0[NN], acc1[NN];
 #pragma unroll
   for (int j = 0; j < NN; ++j) acc0[j] = acc1[j] = zero_of(T());
@@ -189,22 +202,39 @@ __device__ __forceinline__ void skinny_row_pair(const GemmCBlk& cb, const GemmTa
     out0[j] = acc0[j];
     out1[j] = acc1[j];
   }
+  if (want) {
+    f0 = f1 = 0;
+#pragma unroll
+    for (int j = 0; j < NN; ++j) {
+      f0 = max(f0, out_field(acc0[j]));
+      f1 = max(f1, out_field(acc1[j]));
+    }
+  }
 }
 
 // Row row0 of an item and, if inside the block, row0 + kSkinnyThreads.
+// f0, f1: the rows' output fields when `want` (f1 stays -1 when row1 is outside the block).
 template <typename T, int NN>
 __device__ __forceinline__ void skinny_rows(const GemmCBlk& cb, const GemmTask* __restrict__ task, int row0,
                                             const T* __restrict__ A, const T* __restrict__ As, const T* __restrict__ B,
-                                            const T* __restrict__ Bs, T* __restrict__ C) {
+                                            const T* __restrict__ Bs, T* __restrict__ C, bool want, int& f0,
+                                            int& f1) {
   const int row1 = row0 + kSkinnyThreads;
   if constexpr (sizeof(T) == 8 && NN <= 4) {
     if (row1 < cb.m) {
-      skinny_row_pair<T, NN>(cb, task, row0, A, As, B, Bs, C);
+      skinny_row_pair<T, NN>(cb, task, row0, A, As, B, Bs, C, want, f0, f1);
       return;
     }
   }
-  skinny_row<T, NN>(cb, task, row0, A, As, B, Bs, C);
-  if (row1 < cb.m) skinny_row<T, NN>(cb, task, row1, A, As, B, Bs, C);
+  skinny_row<T, NN>(cb, task, row0, A, As, B, Bs, C, want, f0);
+  if (row1 < cb.m) skinny_row<T, NN>(cb, task, row1, A, As, B, Bs, C, want, f1);
+}
+
+// atomicMax of v into fields[key] once per group of lanes with the same key.
+__device__ __forceinline__ void fold_field(unsigned mask, int key, int v, int32_t* __restrict__ fields) {
+  const unsigned m = __match_any_sync(mask, key);
+  const int x = (int)__reduce_max_sync(m, (unsigned)max(v, 0));
+  if (key >= 0 && x > 0 && (int)(threadIdx.x & 31) == __ffs(m) - 1) atomicMax(fields + key, x);
 }
 
 // Resident CTAs per SM the kernel is compiled for: 8 for real operands (64 registers, no
@@ -216,21 +246,30 @@ template <typename T>
 __global__ void __launch_bounds__(kSkinnyThreads, SkinnyMinBlocks<T>::value) k_gemm_skinny(
     const GemmCBlk* __restrict__ cblk, const GemmTask* __restrict__ task, const GemmRowChunk* __restrict__ items,
     int nitems, const T* __restrict__ A, const T* __restrict__ As, const T* __restrict__ B, const T* __restrict__ Bs,
-    T* __restrict__ C) {
+    T* __restrict__ C, const SkinnyFuse* __restrict__ fuse, int32_t* __restrict__ fields) {
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const GemmRowChunk item = items[it];
     const GemmCBlk cb = cblk[item.cblk];
     const int row = item.chunk * kSkinnyRows + threadIdx.x;
     if (row >= cb.m) continue;
+    const SkinnyFuse fz = fuse ? fuse[item.cblk] : SkinnyFuse{-1, 1};
+    const bool want = fz.exp_base >= 0;   // uniform over the item
+    int f0 = 0, f1 = -1;
     switch (cb.n) {
-      case 1: skinny_rows<T, 1>(cb, task, row, A, As, B, Bs, C); break;
-      case 2: skinny_rows<T, 2>(cb, task, row, A, As, B, Bs, C); break;
-      case 3: skinny_rows<T, 3>(cb, task, row, A, As, B, Bs, C); break;
-      case 4: skinny_rows<T, 4>(cb, task, row, A, As, B, Bs, C); break;
-      case 5: skinny_rows<T, 5>(cb, task, row, A, As, B, Bs, C); break;
-      case 6: skinny_rows<T, 6>(cb, task, row, A, As, B, Bs, C); break;
-      case 7: skinny_rows<T, 7>(cb, task, row, A, As, B, Bs, C); break;
-      default: skinny_rows<T, 8>(cb, task, row, A, As, B, Bs, C); break;
+      case 1: skinny_rows<T, 1>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+      case 2: skinny_rows<T, 2>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+      case 3: skinny_rows<T, 3>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+      case 4: skinny_rows<T, 4>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+      case 5: skinny_rows<T, 5>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+      case 6: skinny_rows<T, 6>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+      case 7: skinny_rows<T, 7>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+      default: skinny_rows<T, 8>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+    }
+    if (want) {
+      // a row's n outputs lie in one row of the later operand (k3 is a multiple of n)
+      const unsigned mask = __activemask();
+      fold_field(mask, fz.exp_base + row * cb.n / fz.k3, f0, fields);
+      fold_field(mask, f1 >= 0 ? fz.exp_base + (row + kSkinnyThreads) * cb.n / fz.k3 : -1, f1, fields);
     }
   }
 }
@@ -249,12 +288,13 @@ bool skinny_cblk(const GemmSchedule& g, int32_t q) {
 int skinny_rows_per_item() { return kSkinnyRows; }
 
 template <typename T>
-void launch_skinny_t(const GemmSchedule& g, const Operands& op, void* c, int grid, cudaStream_t s) {
+void launch_skinny_t(const GemmSchedule& g, const Operands& op, void* c, int grid, cudaStream_t s,
+                     const SkinnyFuse* fuse, int32_t* fields) {
   k_gemm_skinny<T><<<grid, kSkinnyThreads, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
-                                                g.d_skinny.as<GemmRowChunk>(), (int)g.skinny.size(),
-                                                static_cast<const T*>(op.a), static_cast<const T*>(op.a_src),
-                                                static_cast<const T*>(op.b), static_cast<const T*>(op.b_src),
-                                                static_cast<T*>(c));
+                                                   g.d_skinny.as<GemmRowChunk>(), (int)g.skinny.size(),
+                                                   static_cast<const T*>(op.a), static_cast<const T*>(op.a_src),
+                                                   static_cast<const T*>(op.b), static_cast<const T*>(op.b_src),
+                                                   static_cast<T*>(c), fuse, fields);
 }
 
 template <typename T>
@@ -281,14 +321,14 @@ int skinny_grid(int items, bool cplx, int num_sms) {
 }
 
 void launch_gemm_f64_skinny(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms,
-                            cudaStream_t s) {
+                            cudaStream_t s, const SkinnyFuse* fuse, int32_t* fields) {
   const int ns = (int)g.skinny.size();
   if (!ns) return;
   const int grid = skinny_grid(ns, cplx, num_sms);
   if (cplx)
-    launch_skinny_t<double2>(g, op, c, grid, s);
+    launch_skinny_t<double2>(g, op, c, grid, s, nullptr, nullptr);
   else
-    launch_skinny_t<double>(g, op, c, grid, s);
+    launch_skinny_t<double>(g, op, c, grid, s, fuse, fields);
   QLTG_CUDA(cudaGetLastError());
 }
 

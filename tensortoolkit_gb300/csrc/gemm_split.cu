@@ -926,7 +926,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
 int64_t SplitPlan::launches() const {
   if (tiles.empty()) return 0;
   // A: (memset,) row scales, pack; B: pack; GEMM
-  return (a_static ? 0 : (row_warp ? 2 : 3)) + (b_static ? 0 : 1) + 1;
+  return (a_static ? 0 : (a_fields_external ? 1 : (row_warp ? 2 : 3))) + (b_static ? 0 : 1) + 1;
 }
 
 // Scale exponents and slice tiles of one operand side (A: rows, B: columns), reading each
@@ -939,7 +939,9 @@ void pack_split_operand(SplitPlan& sp, bool side_a, const void* scratch, const v
       sp.a_ready = true;
       return;
     }
-    if (sp.row_warp) {
+    if (sp.a_fields_external) {
+      // the row scales were folded by the kernel that wrote this operand
+    } else if (sp.row_warp) {
       k_row_field_rows<<<sp.row_exp_grid, 256, 0, s>>>(X, Xs, sp.d_a_ops.as<SplitOperand>(), (int)sp.a_ops.size(),
                                                        sp.n_a_rows, sp.a_exps.as<int32_t>());
     } else {
@@ -997,13 +999,14 @@ void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s
   // pipe); everything else goes through the slices. With both present the skinny kernel
   // runs on the side stream (it writes other output blocks) and joins after the split GEMM.
   const bool fork = !p.sched.skinny.empty() && !sp.tiles.empty() && sp.side;
+  const SkinnyFuse* fuse = p.fuse_fields ? p.d_fuse.as<SkinnyFuse>() : nullptr;
   if (fork) {
     QLTG_CUDA(cudaEventRecord(sp.fork, s));
     QLTG_CUDA(cudaStreamWaitEvent(sp.side, sp.fork, 0));
-    launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, sp.side);
+    launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, sp.side, fuse, p.fuse_fields);
     QLTG_CUDA(cudaEventRecord(sp.join, sp.side));
   } else {
-    launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, s);
+    launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, s, fuse, p.fuse_fields);
   }
   if (sp.tiles.empty()) return;
   struct Join {   // the main stream waits for the side stream on every way out

@@ -7,6 +7,7 @@
 // topology of a Lanczos matvec never changes, so here the four plans (device pairing,
 // schedules, operand scratch) are built once, the intermediates t1..t3 live in HBM for
 // the life of the object, and the whole chain replays as one graph launch.
+#include <map>
 #include <memory>
 
 #include "matvec.h"
@@ -15,6 +16,43 @@
 using namespace qltg;
 
 extern "C" {
+
+namespace {
+
+// Split mode: when every A block of the last step's slices is written by the second MPO
+// step's skinny kernel in the layout the slices read (no transpose; each block's row length
+// a multiple of the skinny block's n), that kernel folds the row scales while it writes them
+// and the last step skips its row-scale pass.
+void link_row_fields(qltg_matvec& mv, cudaStream_t s) {
+  CtrctPlan& p2 = mv.step[2];
+  CtrctPlan& p3 = mv.step[3];
+  if (!p2.split || !p3.split || p3.split->a_ops.empty() || p3.split->a_static) return;
+  if (p3.a_tl.ntiles || !p2.split->tiles.empty()) return;
+  const auto& ops = p3.split->a_ops;
+  std::map<int64_t, int> op_of;
+  for (int i = 0; i < (int)ops.size(); ++i) op_of[ops[i].src_off & ~qltg::kFromSrc] = i;
+  const qltg::GemmSchedule& g = p2.sched;
+  std::vector<qltg::SkinnyFuse> fz(std::max<size_t>(g.cblk.size(), 1), qltg::SkinnyFuse{-1, 1});
+  size_t covered = 0;
+  for (size_t q = 0; q < g.cblk.size(); ++q) {
+    auto it = op_of.find(g.cblk[q].c_off);
+    if (it == op_of.end()) continue;
+    const qltg::SplitOperand& o = ops[it->second];
+    if (!qltg::skinny_cblk(g, (int32_t)q) || o.cols % g.cblk[q].n != 0 ||
+        (int64_t)o.rows * o.cols != (int64_t)g.cblk[q].m * g.cblk[q].n)
+      return;
+    fz[q] = qltg::SkinnyFuse{o.exp_off, o.cols};
+    ++covered;
+  }
+  if (covered != ops.size()) return;
+  p2.d_fuse = qltg::upload(fz, s);
+  QLTG_CUDA(cudaStreamSynchronize(s));
+  p2.fuse_fields = p3.split->a_exps.as<int32_t>();
+  p3.split->a_fields_external = true;
+  mv.fused_fields = true;
+}
+
+}  // namespace
 
 int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* lenv_dev,
                        const qltg_tensor_desc* psi, const qltg_tensor_desc* mpo1, const void* mpo1_dev,
@@ -59,6 +97,7 @@ int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* 
       }
       if (i < 3) h->t[i].alloc(std::max<int64_t>(1, p.c.size) * p.c.elem_bytes());
     }
+    if (mode == QLTG_MODE_SPLIT) link_row_fields(*h, s);
     *mv = h.release();
   });
 }
@@ -87,6 +126,7 @@ int qltg_matvec_stats(const qltg_matvec* mv, double* flops, int64_t* launches) {
       f += p.flops;
       l += mv->mode == QLTG_MODE_SPLIT && p.split ? exec_launches_split(p) : p.launches_per_exec;
     }
+    if (mv->fused_fields) ++l;   // the zero fill of the folded row scales
     if (flops) *flops = f;
     if (launches) *launches = l;
   });

@@ -40,9 +40,13 @@ struct qltg_matvec {
     if (capture_stream) cudaStreamDestroy(capture_stream);
   }
 
+  bool fused_fields = false;   // split mode: step 2 folds the row scales of step 3's A
+
   void enqueue(const void* psi, void* out, cudaStream_t s) {
     qltg::exec_contraction(step[0], lenv, psi, t[0].get(), mode, s);
     qltg::exec_contraction(step[1], t[0].get(), mpo1, t[1].get(), mode, s);
+    if (fused_fields)
+      QLTG_CUDA(cudaMemsetAsync(step[3].split->a_exps.get(), 0, step[3].split->n_a_rows * sizeof(int32_t), s));
     qltg::exec_contraction(step[2], t[1].get(), mpo2, t[2].get(), mode, s);
     qltg::exec_contraction(step[3], t[2].get(), renv, out, mode, s);
   }
