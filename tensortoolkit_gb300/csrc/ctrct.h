@@ -97,7 +97,7 @@ struct SplitOperand {
   int32_t ktiles;         // 64-wide k tiles
   int32_t exp_off;        // offset of its row (A) / column (B) exponent fields
   int64_t chunk_begin;    // A: prefix over operands of 8-element chunks (row-scale kernel)
-  int64_t pchunk_begin;   // A: prefix over operands of rows x ceil(cols / 8) (pack kernel)
+  int64_t pchunk_begin;   // A: prefix over operands of rows x ceil(cols / 16) (pack kernel)
 };
 struct SplitTask {
   int64_t a_pack, b_pack;

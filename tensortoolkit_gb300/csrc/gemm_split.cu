@@ -219,10 +219,10 @@ __global__ void __launch_bounds__(256) k_row_field_rows(const double* __restrict
   }
 }
 
-// Slices of A: one thread per 16-byte chunk (8 consecutive k of one row) that holds operand
-// data, numbered per operand in (128-row tile, 8-wide k chunk, row) order, so consecutive
-// threads take consecutive rows of one chunk column and their 16-byte plane words land side
-// by side. CTA b takes the contiguous range [b per, (b + 1) per) of all operands' chunks.
+// Slices of A: one thread per 16-wide k step of one row that holds operand data (its two
+// 16-byte chunks, 8 consecutive k each), numbered per operand in (128-row tile, k step, row)
+// order, so consecutive threads take consecutive rows and their 16-byte plane words land
+// side by side. CTA b takes the contiguous range [b per, (b + 1) per) of all operands' items.
 __global__ void __launch_bounds__(256) k_pack_a(const double* __restrict__ scr, const double* __restrict__ src,
                                                 const SplitOperand* __restrict__ ops, int nops, int64_t total,
                                                 const int32_t* __restrict__ exps, uint8_t* __restrict__ pack) {
@@ -240,27 +240,33 @@ __global__ void __launch_bounds__(256) k_pack_a(const double* __restrict__ scr, 
   for (int64_t ch = cbeg + threadIdx.x; ch < cend; ch += blockDim.x) {
     while (lo + 1 < nops && ops[lo + 1].pchunk_begin <= ch) ++lo;
     const SplitOperand o = ops[lo];
-    const int nkc = (o.cols + 7) >> 3;
+    const int npair = (o.cols + 15) >> 4;        // 16-wide k steps of a row
     const int l = (int)(ch - o.pchunk_begin);   // below 2^31: one block has < 2^31 elements
-    const int rt = l / (kTM * nkc);
-    const int l2 = l - rt * kTM * nkc;
+    const int rt = l / (kTM * npair);
+    const int l2 = l - rt * kTM * npair;
     const int rows_rt = min(kTM, o.rows - rt * kTM);
-    const int kc = l2 / rows_rt;
-    const int r = l2 - kc * rows_rt;
+    const int kp = l2 / rows_rt;
+    const int r = l2 - kp * rows_rt;
     const int64_t row = (int64_t)rt * kTM + r;
-    const int k0 = kc * 8;
+    const int k0 = kp * 16;
     const int e = exp_of_field(__ldg(exps + o.exp_off + row));
     const double* src_row = operand_block(scr, src, o.src_off) + row * o.cols;
-    uint64_t y[8];
-    uint32_t sg[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) y[j] = scaled_y((k0 + j < o.cols) ? __ldg(src_row + k0 + j) : 0.0, e, sg[j]);
     // tile layout [ks][slice][m_core][k_core][8 rows x 16 B]: the 7 slices of a 16-wide k
     // step are contiguous, so a 32-wide stage is one 56 KB copy
-    const int kt = k0 / kTK, ks = (k0 % kTK) >> 4, k_core = (k0 >> 3) & 1;
+    const int kt = k0 / kTK, ks = (k0 % kTK) >> 4;
     const int64_t tile = (int64_t)rt * o.ktiles + kt;
-    store_planes(y, sg, pack + o.pack_off + tile * (int64_t)(kS * kATile) + (int64_t)ks * (kS * 4096) +
-                            (r >> 3) * 256 + k_core * 128 + (r & 7) * 16, 4096);
+    uint8_t* dst = pack + o.pack_off + tile * (int64_t)(kS * kATile) + (int64_t)ks * (kS * 4096) + (r >> 3) * 256 +
+                   (r & 7) * 16;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {   // k_core 0 and 1: the two 8-wide chunks of the step
+      const int kb = k0 + 8 * half;
+      if (kb >= o.cols) break;
+      uint64_t y[8];
+      uint32_t sg[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) y[j] = scaled_y((kb + j < o.cols) ? __ldg(src_row + kb + j) : 0.0, e, sg[j]);
+      store_planes(y, sg, dst + half * 128, 4096);
+    }
   }
 }
 
@@ -791,7 +797,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
         const int64_t rtiles = (cb.m + kTM - 1) / kTM;
         a_exp += cb.m;
         a_chunks += ((int64_t)cb.m * k + 7) / 8;
-        a_pchunks += (int64_t)cb.m * ((k + 7) / 8);
+        a_pchunks += (int64_t)cb.m * ((k + 15) / 16);
         a_pack += rtiles * ktiles * kS * (int64_t)kATile;
         a_of[ia] = (int32_t)a_ops.size();
         a_ops.push_back(o);
