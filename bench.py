@@ -37,6 +37,19 @@ METRIC = "two-site H*psi matvec s/iter at D=4000"
 L2_FLUSH_BYTES = 512 << 20
 
 
+def replica_time(t_step: float, world: int, device=None) -> float:
+    """The job's time per step with one replica per rank: the max over ranks of each rank's
+    time (collective on the default process group; device: where the reduced tensor lives -
+    the rank's GPU under NCCL, the CPU under gloo)."""
+    if world <= 1:
+        return t_step
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([t_step], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def peaks():
     p = {}
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -504,11 +517,7 @@ def main():
     head = results[modes[0]]
     t_step = head["s_per_iter"]
     # max over ranks
-    t_max = t_step
-    if world > 1:
-        tt = torch.tensor([t_step], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = replica_time(t_step, world, f"cuda:{local}")
 
     if rank == 0:
         cpu = None
