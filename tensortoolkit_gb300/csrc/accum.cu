@@ -65,12 +65,6 @@ __global__ void __launch_bounds__(256) k_accum_combine(const AccumItem* __restri
   }
 }
 
-bool same_legs(const Meta& x, const Meta& y) {
-  if (x.rank != y.rank || x.dtype != y.dtype || x.ncomp != y.ncomp || x.parity_comp != y.parity_comp) return false;
-  for (int l = 0; l < x.rank; ++l)
-    if (x.dirs[l] != y.dirs[l] || x.qns[l] != y.qns[l] || x.dims[l] != y.dims[l]) return false;
-  return true;
-}
 
 // Contracted axes and cyclic saved orders of a contiguous-axes contraction.
 void contiguous_plan_axes(CtrctPlan& p, int64_t a0, int64_t b0, int32_t n) {
@@ -152,7 +146,7 @@ int qltg_accum_plan_create(qltg_ctx* ctx, const qltg_tensor_desc* a, const qltg_
     std::map<uint64_t, std::pair<int64_t, int64_t>> blocks;   // blk_idx -> (ordinal in C_in, in T)
     if (c_in) {
       cm = meta_from_desc(c_in);
-      QLTG_CHECK(same_legs(cm, T), QLTG_ERR_LAYOUT, "output indexes are not those of the contraction result");
+      QLTG_CHECK(same_indexes(cm, T), QLTG_ERR_LAYOUT, "output indexes are not those of the contraction result");
       h->has_c_in = true;
       for (int64_t q = 0; q < cm.nblk; ++q) blocks[cm.rank ? cm.blk_idx(&cm.coords[q * cm.rank]) : 0] = {q, -1};
     }

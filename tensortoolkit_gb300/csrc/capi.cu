@@ -85,6 +85,13 @@ bool inverse_leg(const Meta& a, int la, const Meta& b, int lb) {
   return a.dirs[la] != b.dirs[lb] && a.qns[la] == b.qns[lb] && a.dims[la] == b.dims[lb];
 }
 
+bool same_indexes(const Meta& x, const Meta& y) {
+  if (x.rank != y.rank || x.dtype != y.dtype || x.ncomp != y.ncomp || x.parity_comp != y.parity_comp) return false;
+  for (int l = 0; l < x.rank; ++l)
+    if (!same_leg(x, l, y, l)) return false;
+  return true;
+}
+
 
 // FermionicInplaceReorder (reference utility/utils_inl.h:52-75): sign of moving the legs
 // into `order` by the cycle-following in-place reorder, counting odd legs passed over.

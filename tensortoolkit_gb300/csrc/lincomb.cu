@@ -70,13 +70,6 @@ __global__ void __launch_bounds__(256) k_lincomb(const LincombItem* __restrict__
   }
 }
 
-bool same_indexes(const Meta& x, const Meta& y) {
-  if (x.rank != y.rank || x.dtype != y.dtype || x.ncomp != y.ncomp || x.parity_comp != y.parity_comp) return false;
-  for (int l = 0; l < x.rank; ++l)
-    if (x.dirs[l] != y.dirs[l] || x.qns[l] != y.qns[l] || x.dims[l] != y.dims[l]) return false;
-  return true;
-}
-
 }  // namespace
 }  // namespace qltg
 

@@ -135,6 +135,7 @@ struct Meta {
 Meta meta_from_desc(const qltg_tensor_desc* d);
 bool same_leg(const Meta& a, int la, const Meta& b, int lb);        // identical space
 bool inverse_leg(const Meta& a, int la, const Meta& b, int lb);     // same sectors, opposite dir
+bool same_indexes(const Meta& x, const Meta& y);                    // element type and every leg
 
 }  // namespace qltg
 
