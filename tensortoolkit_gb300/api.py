@@ -507,8 +507,13 @@ class LinearCombinePlan:
         self.device = device
         self.n = len(metas)
         cplx = metas[0].is_complex
-        cf = _axis_values(np.asarray(coefs), cplx)
-        be = _axis_values(np.asarray([beta]), cplx)
+        if len(coefs) != len(metas):
+            raise ValueError("one coefficient per tensor")
+        if not cplx and (np.iscomplexobj(np.asarray(coefs)) and np.any(np.imag(coefs) != 0)
+                         or np.imag(complex(beta)) != 0):
+            raise ValueError("complex coefficients for real tensors")
+        cf = _axis_values(np.real_if_close(np.asarray(coefs)) if not cplx else np.asarray(coefs), cplx)
+        be = _axis_values(np.asarray([beta if cplx else complex(beta).real]), cplx)
         self._descs = [_Desc(m) for m in metas]
         arr = (C.POINTER(capi.TensorDesc) * self.n)(*[C.pointer(d.s) for d in self._descs])
         rd = _Desc(res) if res is not None else None
