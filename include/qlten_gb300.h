@@ -11,6 +11,12 @@
  *     -> qlten_gb300::SVD(..., ctx)
  *   qlten::QR(&T, ldims, lqndiv, &Q, &R)      (ten_decomp/ten_qr.h:152-162)
  *     -> qlten_gb300::QR(..., ctx)
+ *   qlten::ContractContiguousAxes<..., ASide, BSide>(A, B, a0, b0, n, C)
+ *     -> qlten_gb300::ContractContiguousAxes(A, B, a0, b0, n, C, ctx [, mode, a_side, b_side])
+ *   qlten::ContractTailHeadContiguousAccumulate / TryContract...(A, B, a0, b0, n, alpha, beta, C)
+ *     -> the same names with (..., C, ctx [, mode])  (contract_contiguous_axes.h:953-1040)
+ *   qlten::LinearCombine(coefs, tens, beta, &res)   (ten_linear_combine.h:186-197)
+ *     -> qlten_gb300::LinearCombine(coefs, tens, beta, &res, ctx)
  *
  * With the reference built for the GPU (USE_GPU) the QLTensor raw buffers already live in
  * device memory and are passed straight through. With the CPU build they are staged
@@ -24,6 +30,7 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -124,6 +131,8 @@ class DeviceView {
     if (ptr_) cudaFree(ptr_);
 #endif
   }
+  DeviceView(const DeviceView&) = delete;
+  DeviceView& operator=(const DeviceView&) = delete;
   void* get() const { return ptr_; }
   void sync_back() {
 #ifndef USE_GPU
@@ -266,6 +275,200 @@ void QR(const qlten::QLTensor<ElemT, QNT>* pt, size_t ldims, const QNT& lqndiv, 
     throw;
   }
   qltg_decomp_destroy(d);
+}
+
+// ------------------------------------------------------------------ contiguous axes
+namespace detail {
+
+inline void scalar_pair(double v, double* o) {
+  o[0] = v;
+  o[1] = 0.0;
+}
+inline void scalar_pair(const qlten::QLTEN_Complex& v, double* o) {
+  o[0] = v.real();
+  o[1] = v.imag();
+}
+
+// *out = a tensor with `idxs` holding the blocks listed by a plan's result query.
+template <typename ElemT, typename QNT, typename ResultFn, typename BlocksFn, typename Plan>
+void init_from_plan(qlten::QLTensor<ElemT, QNT>* out, const qlten::IndexVec<QNT>& idxs, Plan* plan, ResultFn result,
+                    BlocksFn blocks) {
+  int32_t rank = 0;
+  int64_t nblk = 0, size = 0;
+  check(result(plan, &rank, &nblk, &size));
+  if (rank == 0) throw std::invalid_argument("qlten_gb300: scalar results go through Contract");
+  std::vector<int64_t> coords((size_t)nblk * rank);
+  check(blocks(plan, coords.data(), nullptr));
+  *out = qlten::QLTensor<ElemT, QNT>(idxs);
+  std::vector<qlten::CoorsT> blk_coors(nblk);
+  for (int64_t b = 0; b < nblk; ++b) blk_coors[b].assign(coords.begin() + b * rank, coords.begin() + (b + 1) * rank);
+  if (nblk) out->GetBlkSparDataTen().DataBlksInsert(blk_coors, true, false);
+}
+
+// Result indexes of ContractContiguousAxes: A's saved legs, then B's, each in cyclic order from
+// the end of its contracted range (contract_contiguous_axes.h:849-868).
+template <typename ElemT, typename QNT>
+qlten::IndexVec<QNT> contiguous_result_indexes(const qlten::QLTensor<ElemT, QNT>& a, const qlten::QLTensor<ElemT, QNT>& b,
+                                               size_t a0, size_t b0, size_t n) {
+  qlten::IndexVec<QNT> idxs;
+  const size_t ra = a.Rank(), rb = b.Rank();
+  for (size_t i = 0; i + n < ra; ++i) idxs.push_back(a.GetIndex((a0 + n + i) % ra));
+  for (size_t i = 0; i + n < rb; ++i) idxs.push_back(b.GetIndex((b0 + n + i) % rb));
+  return idxs;
+}
+
+template <typename ElemT, typename QNT>
+bool accumulate(const qlten::QLTensor<ElemT, QNT>& a, const qlten::QLTensor<ElemT, QNT>& b, size_t a0, size_t b0,
+                size_t n, ElemT alpha, ElemT beta, qlten::QLTensor<ElemT, QNT>& c, const Context& ctx, int mode,
+                bool allow_expand) {
+  Desc<ElemT, QNT> da(a), db(b);
+  const bool has_c = !c.IsDefault();
+  std::vector<Desc<ElemT, QNT>> dc;
+  if (has_c) dc.emplace_back(c);
+  qltg_accum_plan* acc = nullptr;
+  int32_t expanded = 0;
+  const int rc = qltg_accum_plan_create(ctx.get(), &da.d, &db.d, (int64_t)a0, (int64_t)b0, (int32_t)n,
+                                        has_c ? &dc[0].d : nullptr, allow_expand ? 1 : 0, &acc, &expanded);
+  if (rc == QLTG_ERR_LAYOUT && !allow_expand) return false;   // the Try form: C untouched
+  check(rc);
+  try {
+    double al[2], be[2];
+    scalar_pair(alpha, al);
+    scalar_pair(beta, be);
+    auto& ma = const_cast<qlten::QLTensor<ElemT, QNT>&>(a);
+    auto& mb = const_cast<qlten::QLTensor<ElemT, QNT>&>(b);
+    DeviceView<ElemT, QNT> va(ma, true), vb(mb, true);
+    if (!has_c || expanded) {   // a new output topology
+      qlten::QLTensor<ElemT, QNT> out;
+      init_from_plan(&out, has_c ? c.GetIndexes() : contiguous_result_indexes(a, b, a0, b0, n), acc,
+                     qltg_accum_plan_result, qltg_accum_plan_result_blocks);
+      DeviceView<ElemT, QNT> vo(out, false);
+      if (has_c) {
+        DeviceView<ElemT, QNT> vc(c, true);
+        check(qltg_accum_exec(acc, va.get(), vb.get(), vc.get(), vo.get(), al, be, mode, nullptr));
+      } else {
+        check(qltg_accum_exec(acc, va.get(), vb.get(), nullptr, vo.get(), al, be, mode, nullptr));
+      }
+      if (cudaStreamSynchronize(nullptr) != cudaSuccess) throw std::runtime_error("qlten_gb300: accumulate failed");
+      vo.sync_back();
+      c = std::move(out);
+    } else {                    // in place
+      DeviceView<ElemT, QNT> vc(c, true);
+      check(qltg_accum_exec(acc, va.get(), vb.get(), vc.get(), vc.get(), al, be, mode, nullptr));
+      if (cudaStreamSynchronize(nullptr) != cudaSuccess) throw std::runtime_error("qlten_gb300: accumulate failed");
+      vc.sync_back();
+    }
+  } catch (...) {
+    qltg_accum_plan_destroy(acc);
+    throw;
+  }
+  qltg_accum_plan_destroy(acc);
+  return true;
+}
+
+}  // namespace detail
+
+// qlten::ContractContiguousAxes<ElemT, QNT, ASide, BSide>(A, B, a0, b0, n, C)
+// (contract_contiguous_axes.h:849-868); the sides only tell which view needs no transpose.
+template <typename ElemT, typename QNT>
+void ContractContiguousAxes(const qlten::QLTensor<ElemT, QNT>& a, const qlten::QLTensor<ElemT, QNT>& b, size_t a0,
+                            size_t b0, size_t n, qlten::QLTensor<ElemT, QNT>& c, const Context& ctx,
+                            int mode = QLTG_MODE_FP64, int a_side = QLTG_SIDE_TAIL, int b_side = QLTG_SIDE_HEAD) {
+  Desc<ElemT, QNT> da(a), db(b);
+  qltg_ctrct_plan* plan = nullptr;
+  check(qltg_ctrct_plan_create_contiguous(ctx.get(), &da.d, &db.d, (int64_t)a0, (int64_t)b0, (int32_t)n, a_side,
+                                          b_side, &plan));
+  try {
+    detail::init_from_plan(&c, detail::contiguous_result_indexes(a, b, a0, b0, n), plan, qltg_ctrct_plan_result,
+                           qltg_ctrct_plan_result_blocks);
+    auto& ma = const_cast<qlten::QLTensor<ElemT, QNT>&>(a);
+    auto& mb = const_cast<qlten::QLTensor<ElemT, QNT>&>(b);
+    DeviceView<ElemT, QNT> va(ma, true), vb(mb, true), vc(c, false);
+    check(qltg_ctrct_exec(plan, va.get(), vb.get(), vc.get(), mode, nullptr));
+    if (cudaStreamSynchronize(nullptr) != cudaSuccess) throw std::runtime_error("qlten_gb300: contraction failed");
+    vc.sync_back();
+  } catch (...) {
+    qltg_ctrct_plan_destroy(plan);
+    throw;
+  }
+  qltg_ctrct_plan_destroy(plan);
+}
+
+// C = beta C + alpha A.B over the union topology (ContractTailHeadContiguousAccumulate,
+// contract_contiguous_axes.h:953-1000); a default C needs beta == 0.
+template <typename ElemT, typename QNT>
+void ContractTailHeadContiguousAccumulate(const qlten::QLTensor<ElemT, QNT>& a, const qlten::QLTensor<ElemT, QNT>& b,
+                                          size_t a0, size_t b0, size_t n, ElemT alpha, ElemT beta,
+                                          qlten::QLTensor<ElemT, QNT>& c, const Context& ctx,
+                                          int mode = QLTG_MODE_FP64) {
+  detail::accumulate(a, b, a0, b0, n, alpha, beta, c, ctx, mode, true);
+}
+
+// The no-expansion form (contract_contiguous_axes.h:1002-1040): false, C untouched, when C
+// lacks blocks the product needs or has other indexes.
+template <typename ElemT, typename QNT>
+bool TryContractTailHeadContiguousAccumulate(const qlten::QLTensor<ElemT, QNT>& a,
+                                             const qlten::QLTensor<ElemT, QNT>& b, size_t a0, size_t b0, size_t n,
+                                             ElemT alpha, ElemT beta, qlten::QLTensor<ElemT, QNT>& c,
+                                             const Context& ctx, int mode = QLTG_MODE_FP64) {
+  return detail::accumulate(a, b, a0, b0, n, alpha, beta, c, ctx, mode, false);
+}
+
+// ------------------------------------------------------------------ LinearCombine
+// *pres = sum_i coefs[i] *tens[i] + beta *pres over the union of the contributing blocks
+// (LinearCombine, tensor_manipulation/ten_linear_combine.h:186-197).
+template <typename ElemT, typename QNT>
+void LinearCombine(const std::vector<ElemT>& coefs, const std::vector<qlten::QLTensor<ElemT, QNT>*>& tens, ElemT beta,
+                   qlten::QLTensor<ElemT, QNT>* pres, const Context& ctx) {
+  const size_t n = tens.size();
+  if (n == 0 || coefs.size() != n) throw std::invalid_argument("qlten_gb300: one coefficient per tensor");
+  std::vector<Desc<ElemT, QNT>> descs;
+  descs.reserve(n + 1);
+  std::vector<const qltg_tensor_desc*> dptr;
+  for (auto* t : tens) {
+    descs.emplace_back(*t);
+    dptr.push_back(&descs.back().d);
+  }
+  const bool has_res = !pres->IsDefault();
+  if (has_res) descs.emplace_back(*pres);
+  std::vector<double> cf;
+  for (const auto& x : coefs) {
+    double v[2];
+    detail::scalar_pair(x, v);
+    cf.push_back(v[0]);
+    if (dtype_of<ElemT>() == QLTG_C128) cf.push_back(v[1]);
+  }
+  double be[2];
+  detail::scalar_pair(beta, be);
+  qltg_lincomb_plan* lc = nullptr;
+  check(qltg_lincomb_plan_create(ctx.get(), (int32_t)n, dptr.data(), cf.data(), has_res ? &descs[n].d : nullptr, be,
+                                 0, &lc));
+  try {
+    qlten::QLTensor<ElemT, QNT> out;
+    detail::init_from_plan(&out, tens[0]->GetIndexes(), lc, qltg_lincomb_plan_result,
+                           qltg_lincomb_plan_result_blocks);
+    std::vector<std::unique_ptr<DeviceView<ElemT, QNT>>> views;
+    std::vector<const void*> devs;
+    for (auto* t : tens) {
+      views.push_back(std::make_unique<DeviceView<ElemT, QNT>>(*t, true));
+      devs.push_back(views.back()->get());
+    }
+    DeviceView<ElemT, QNT> vo(out, false);
+    if (has_res) {
+      DeviceView<ElemT, QNT> vr(*pres, true);
+      check(qltg_lincomb_exec(lc, devs.data(), vr.get(), vo.get(), nullptr));
+      if (cudaStreamSynchronize(nullptr) != cudaSuccess) throw std::runtime_error("qlten_gb300: combination failed");
+    } else {
+      check(qltg_lincomb_exec(lc, devs.data(), nullptr, vo.get(), nullptr));
+      if (cudaStreamSynchronize(nullptr) != cudaSuccess) throw std::runtime_error("qlten_gb300: combination failed");
+    }
+    vo.sync_back();
+    *pres = std::move(out);
+  } catch (...) {
+    qltg_lincomb_plan_destroy(lc);
+    throw;
+  }
+  qltg_lincomb_plan_destroy(lc);
 }
 
 }  // namespace qlten_gb300

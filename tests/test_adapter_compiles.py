@@ -1,5 +1,6 @@
 """The drop-in adapter include/qlten_gb300.h compiles against the reference's own headers
-(U1QN / FP64 and fU1U1QN / complex128 instantiations of Contract, SVD and QR). Runs where
+(U1QN / FP64 and fU1U1QN / complex128 instantiations of Contract, SVD, QR,
+ContractContiguousAxes, the contiguous accumulate forms and LinearCombine). Runs where
 the reference tree is available (the development container); skipped elsewhere."""
 import os
 import shutil
