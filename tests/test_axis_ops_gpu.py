@@ -239,3 +239,28 @@ def test_linear_combine_complex_vs_oracle(gpu):
     ref = axis_ops.linear_combine(coefs, ts, 0.5 + 0.25j, res)
     got = api.LinearCombine(coefs, [DTensor.from_host(t) for t in ts], 0.5 + 0.25j, DTensor.from_host(res))
     _close(got, ref, 1e-15)
+
+
+def test_linear_combine_limits_and_aliasing(gpu, rec):
+    X = _d(rec, "lc.X")
+    ref = _t(rec, "lc.X")
+    # 64 tensors (the most one plan takes), then 65
+    got = api.LinearCombine([1.0] * 64, [X] * 64).to_host()
+    assert same_topology(got, ref) and rel_frob(got.data, 64.0 * ref.data) <= 1e-15
+    with pytest.raises(capi.QltgError):
+        api.LinearCombine([1.0] * 65, [X] * 65)
+    # y += 0.5 y in place
+    y = _d(rec, "lc.X")
+    out = api.AddScaledAssign(y, 0.5, y)
+    assert out is y and rel_frob(y.to_host().data, 1.5 * ref.data) <= 1e-15
+    with pytest.raises(ValueError):   # complex coefficient for a real tensor
+        api.LinearCombine([1.0 + 1.0j], [X])
+
+
+def test_project_errors(gpu, rec):
+    psi = _d(rec, "psi")
+    nsct = _t(rec, "psi").legs[3].nsct
+    with pytest.raises(capi.QltgError):   # nothing kept
+        api.ProjectAxis(psi, 3, [[] for _ in range(nsct)])
+    with pytest.raises(capi.QltgError):   # offset outside its sector
+        api.ProjectAxis(psi, 3, [[5]] + [[] for _ in range(nsct - 1)])
