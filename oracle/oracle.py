@@ -1,6 +1,6 @@
 """ctypes front of the CPU restatement in oracle/oracle.cc.
 
-Test infrastructure only: imported by tests/, by `__graft_entry__.smoke()` as the checker
+Test infrastructure only: imported by tests/, by `__graft_entry__.smoke()` to check its result
 and by bench.py's CPU-baseline / reference arm. The GPU library never imports it.
 The restatement's parity with the reference is pinned by the committed fixtures in
 tests/golden/ (produced by the reference itself, see oracle/ref/ref_driver.cc).

@@ -1,5 +1,5 @@
-"""Lanczos with full reorthogonalisation on the CPU oracle's matvec: the checker for the
-device Lanczos (same recurrence: two passes of classical Gram-Schmidt per step,
+"""Lanczos with full reorthogonalisation on the CPU oracle's matvec: the reference computation
+for the device Lanczos (same recurrence: two passes of classical Gram-Schmidt per step,
 alpha_j = <v_j, H v_j> including both corrections, beta_{j+1} = ||w||)."""
 import numpy as np
 

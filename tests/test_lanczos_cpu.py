@@ -1,4 +1,4 @@
-"""The Lanczos checker itself, on the CPU: on a symmetric two-site H_eff small enough to
+"""The CPU Lanczos itself: on a symmetric two-site H_eff small enough to
 build densely, the Ritz values decrease monotonically to the lowest eigenvalue of the dense
 matrix, the Krylov basis stays orthonormal, and the synthetic symmetric workload really is
 symmetric."""

@@ -1,6 +1,6 @@
-"""Device Lanczos (row f1) against the CPU checker on a symmetric two-site H_eff.
+"""Device Lanczos against the CPU Lanczos on a symmetric two-site H_eff.
 
-Bar: alpha, beta and the lowest Ritz values of 20 FP64 steps agree with the checker (same
+Bar: alpha, beta and the lowest Ritz values of 20 FP64 steps agree with the CPU Lanczos (same
 recurrence on the oracle's matvec) to 1e-10 relative; the device Krylov basis is orthonormal
 to 1e-12; two runs are bit-identical; the split-precision matvec's Ritz values stay within
 1e-10 relative of the FP64 ones (the energy drift the precision study reports)."""
@@ -39,7 +39,7 @@ def run_device(tensors, x0, mode, n=NSTEP):
     return mv, lz, a, b
 
 
-def test_lanczos_matches_checker(gpu, case):
+def test_lanczos_matches_cpu_lanczos(gpu, case):
     tensors, x0 = case
     lenv, psi, mpo1, mpo2, renv = tensors
     _, _, a, b = run_device(tensors, x0, "fp64")

@@ -80,7 +80,7 @@ def test_svd_matches_reference(golden, case):
         assert same_topology(mine, ref), f"{case}: {name} topology differs"
         # same LAPACK routine on the same dense block-matrices: equal to rounding
         assert rel_frob(mine.data, ref.data) <= 1e-12, f"{case}: {name} values differ"
-    # the gauge-invariant checker used for the GPU Jacobi SVD accepts the oracle's result
+    # the gauge-invariant SVD check used for the GPU Jacobi SVD accepts the oracle's result
     check_svd(t, u, s, vt, err, D, BSTensor.from_record(rec, "U"), BSTensor.from_record(rec, "S"),
               BSTensor.from_record(rec, "Vt"), float(rec["err"][0]), int(rec["D"][0]), ldims)
 
