@@ -39,7 +39,7 @@ enum {
   QLTG_ERR_TIMEOUT = 4,      /* a bounded device-side wait expired */
   QLTG_ERR_NOCONV = 5,       /* an iterative decomposition did not converge */
   QLTG_ERR_EMPTY_SVD = 6,    /* no block fits lqndiv: reference EmptySVDResultError */
-  QLTG_ERR_UNSUPPORTED = 7,  /* valid input outside what this build implements */
+  QLTG_ERR_UNSUPPORTED = 7,  /* valid input outside what the library implements */
   QLTG_ERR_LAYOUT = 8        /* accumulate: the output's indexes differ from the contraction
                                 result, or it lacks result blocks and expansion is off
                                 (reference ContractAccumulateLayoutMismatch) */
