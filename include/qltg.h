@@ -90,6 +90,12 @@ QLTG_API int qltg_destroy(qltg_ctx* ctx);
 /* Message of the last failing call on this thread (never NULL). */
 QLTG_API const char* qltg_last_error(void);
 
+/* Failure-path self-test of the device-side bounded waits the tensor-core kernels use: one
+ * warp waits on an mbarrier nothing arrives on, with a limit of limit_cycles (1 .. 2^31 SM
+ * cycles). Returns QLTG_ERR_TIMEOUT when the wait gave up as designed (the expected result;
+ * the context stays usable), QLTG_OK if it had completed. Synchronises `stream`. */
+QLTG_API int qltg_selftest_bounded_wait(qltg_ctx* ctx, int64_t limit_cycles, void* stream);
+
 /* ---------------------------------------------------------------- contraction */
 typedef struct qltg_ctrct_plan qltg_ctrct_plan;
 

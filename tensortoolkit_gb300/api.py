@@ -647,6 +647,12 @@ def MoveHeadAxisToTail(t: DTensor) -> DTensor:
     return Transpose(t, list(range(1, t.meta.rank)) + [0])
 
 
+def selftest_bounded_wait(limit_cycles: int = 1 << 21, device: int = 0) -> None:
+    """Run the device-side bounded-wait self-test (qltg_selftest_bounded_wait): raises
+    QltgError with code QLTG_ERR_TIMEOUT when the wait gave up as designed."""
+    check(lib().qltg_selftest_bounded_wait(context(device).h, int(limit_cycles), stream_ptr(device)))
+
+
 def read_qlten(path: str, qn: str = "U1QN", dtype: str = "f64", device: int = 0) -> DTensor:
     """Read a .qlten file (the reference's QLTensor stream format) straight into device
     memory: header parsed in libqltg.so, raw buffer through a pinned staging buffer."""

@@ -355,3 +355,15 @@ int qltg_transpose_noalloc(qltg_ctx* ctx, const qltg_tensor_desc* a, const void*
 }
 
 }  // extern "C"
+
+extern "C" int qltg_selftest_bounded_wait(qltg_ctx* ctx, int64_t limit_cycles, void* stream) {
+  return qltg::guarded([&] {
+    QLTG_CHECK(ctx, QLTG_ERR_INVALID, "null ctx");
+    QLTG_CHECK(limit_cycles >= 1 && limit_cycles <= ((int64_t)1 << 31), QLTG_ERR_INVALID,
+               "wait limit must be 1 .. 2^31 cycles");
+    QLTG_CUDA(cudaSetDevice(ctx->device));
+    const int expired = qltg::wait_selftest(limit_cycles, static_cast<cudaStream_t>(stream));
+    QLTG_CHECK(expired == 0 || expired == 1, QLTG_ERR_CUDA, "self-test kernel did not report");
+    QLTG_CHECK(!expired, QLTG_ERR_TIMEOUT, "the bounded wait expired after its limit, as intended");
+  });
+}

@@ -440,7 +440,8 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
 }
 
 // Bounded wait that also gives up as soon as another role has aborted.
-__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t phase, const volatile int* abort_flag) {
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t phase, const volatile int* abort_flag,
+                                                   long long limit = kWaitCycles) {
   uint32_t done = 0;
   const long long t0 = clock64();
   while (true) {
@@ -451,7 +452,7 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t phase
           : "r"(mbar), "r"(phase));
       if (done) return true;
     }
-    if (*abort_flag || clock64() - t0 > kWaitCycles) return false;
+    if (*abort_flag || clock64() - t0 > limit) return false;
   }
 }
 
@@ -468,6 +469,21 @@ __device__ __forceinline__ bool wait_warp(uint32_t mbar, uint32_t phase, volatil
 __device__ __forceinline__ bool wait_warp_own(uint32_t mbar, uint32_t phase) {
   const int never = 0;
   return __all_sync(0xffffffffu, mbar_wait_or_abort(mbar, phase, &never));
+}
+
+// The bounded wait itself, checked on the device: one warp waits on an mbarrier nothing
+// arrives on, with a limit of `limit` cycles, and reports 1 when the wait gave up (the
+// expected outcome) or 0 had it completed. Nothing else runs; the context stays usable.
+__global__ void __launch_bounds__(32) k_wait_selftest(long long limit, int* __restrict__ status) {
+  __shared__ alignas(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&bar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  __syncwarp();
+  const int never = 0;
+  const bool ok = __all_sync(0xffffffffu, mbar_wait_or_abort(smem_u32(&bar), 0, &never, limit));
+  if (threadIdx.x == 0) *status = ok ? 0 : 1;
 }
 
 // Fold one drained accumulator set into the int64 sums z (units 2^-49) of this thread's
@@ -1047,6 +1063,18 @@ int64_t split_launches(const CtrctPlan& p) {
   int64_t n = p.sched.skinny.empty() ? 0 : 1;
   if (p.split) n += p.split->launches();
   return n;
+}
+
+int wait_selftest(int64_t limit_cycles, cudaStream_t s) {
+  DevBuf st;
+  st.alloc(sizeof(int));
+  QLTG_CUDA(cudaMemsetAsync(st.get(), 0xFF, sizeof(int), s));
+  k_wait_selftest<<<1, 32, 0, s>>>((long long)limit_cycles, st.as<int>());
+  QLTG_CUDA(cudaGetLastError());
+  int v = -1;
+  QLTG_CUDA(cudaMemcpyAsync(&v, st.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+  QLTG_CUDA(cudaStreamSynchronize(s));
+  return v;
 }
 
 int split_device_error(const CtrctPlan& p, cudaStream_t s) {

@@ -15,5 +15,8 @@ void split_prepack_static(CtrctPlan& p, const void* a_static, const void* b_stat
 int64_t split_launches(const CtrctPlan& p);
 // Device error word of the split GEMM (1 = a bounded tensor-core wait expired).
 int split_device_error(const CtrctPlan& p, cudaStream_t s);
+// One warp's bounded wait on an mbarrier nothing arrives on: 1 when it gave up after
+// limit_cycles (expected), 0 if it completed.
+int wait_selftest(int64_t limit_cycles, cudaStream_t s);
 
 }  // namespace qltg
