@@ -470,11 +470,11 @@ class AxisProjectPlan(AxisMonomialPlan):
 
     def __init__(self, t: BSTensor, axis: int, kept: Sequence[Sequence[int]], device: int = 0):
         self.h = None
-        self.ctx = context(device)
-        self.device = device
         leg = t.legs[axis]
         if len(kept) != leg.nsct:
             raise ValueError("one kept list per sector of the axis")
+        self.ctx = context(device)
+        self.device = device
         counts = np.asarray([len(k) for k in kept], np.int64)
         flat = np.ascontiguousarray(np.concatenate([np.asarray(k, np.int64) for k in kept] + [np.zeros(0, np.int64)]))
         dt = _Desc(t)
