@@ -98,6 +98,8 @@ struct SplitOperand {
   int32_t exp_off;        // offset of its row (A) / column (B) exponent fields
   int64_t chunk_begin;    // A: prefix over operands of 8-element chunks (row-scale kernel)
   int64_t pchunk_begin;   // A: prefix over operands of rows x ceil(cols / 16) (pack kernel)
+  int32_t cplx;           // B: complex block read as its real 2k x 2n form
+  int32_t pad;
 };
 struct SplitTask {
   int64_t a_pack, b_pack;

@@ -270,6 +270,14 @@ __global__ void __launch_bounds__(256) k_pack_a(const double* __restrict__ scr, 
   }
 }
 
+// Element (r, c) of a B operand block: the block itself (k x n row-major), or for a complex
+// block (k x n complex, interleaved) its real 2k x 2n form of 2 x 2 blocks [[Re, Im], [-Im, Re]].
+__device__ __forceinline__ double b_elem(const double* __restrict__ blk, int64_t r, int c, int cols, int cplx) {
+  if (!cplx) return __ldg(blk + r * cols + c);
+  const double v = __ldg(blk + (r >> 1) * cols + (c & ~1) + ((r ^ c) & 1));
+  return ((r & 1) && !(c & 1)) ? -v : v;
+}
+
 // Column scales and slices of B (k x n row-major), one CTA per (operand block, 32-column
 // tile). Phase 1: thread (row group g, column c) folds rows g, g + 8, ... of its column (a
 // warp reads 32 consecutive columns of one row); the 8 partial maxima per column meet in
@@ -290,11 +298,10 @@ __global__ void __launch_bounds__(256) k_pack_b_cols(const double* __restrict__ 
     const int nc = min(kTN, o.cols - c0);
     uint32_t mx = 0, nz = 0;   // largest high word of |x|, any nonzero bit
     if (lane < nc) {
-      const double* col = blk + c0 + lane;
       for (int r = g; r < o.rows; r += 32) {
         double v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = r + 8 * u < o.rows ? __ldg(col + (int64_t)(r + 8 * u) * o.cols) : 0.0;
+        for (int u = 0; u < 4; ++u) v[u] = r + 8 * u < o.rows ? b_elem(blk, r + 8 * u, c0 + lane, o.cols, o.cplx) : 0.0;
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const uint32_t h = (uint32_t)__double2hiint(v[u]) & 0x7FFFFFFFu;
@@ -327,11 +334,11 @@ __global__ void __launch_bounds__(256) k_pack_b_cols(const double* __restrict__ 
       const int64_t k0 = (int64_t)kt * kTK + ks * 16 + k_core * 8;
       if (cc >= nc || k0 >= o.rows) continue;   // padding: the buffer was zeroed once
       const int e = se[cc];
-      const double* col = blk + c0 + cc;
       uint64_t y[8];
       uint32_t sg[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) y[j] = scaled_y((k0 + j < o.rows) ? col[(k0 + j) * o.cols] : 0.0, e, sg[j]);
+      for (int j = 0; j < 8; ++j)
+        y[j] = scaled_y((k0 + j < o.rows) ? b_elem(blk, k0 + j, c0 + cc, o.cols, o.cplx) : 0.0, e, sg[j]);
       // tile layout [ks][slice][n_core][k_core][8 columns x 16 B]: the 7 slices of a 16-wide k
       // step form one 224-row K-major operand (slice q = rows 32 (q-1) .. 32 q - 1)
       const int64_t tile = (int64_t)tt.y * o.ktiles + kt;
@@ -791,17 +798,23 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
     return (int64_t)(std::lower_bound(p.b.offsets.begin(), p.b.offsets.end(), b_off) - p.b.offsets.begin());
   };
   tasks.resize(g.task.size());
+  // complex operands as real ones: A (m x k complex) is the real m x 2k matrix of its
+  // interleaved parts, C likewise m x 2n, and B becomes the real 2k x 2n matrix of 2 x 2
+  // blocks [[Re, Im], [-Im, Re]] (built by the B slicing kernel), so C' = A' B'
+  const int cw = p.a.dtype == QLTG_C128 ? 2 : 1;
+  auto real_off = [cw](int64_t off) { return ((off & ~kFromSrc) * cw) | (off & kFromSrc); };
   for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q) {
     const GemmCBlk& cb = g.cblk[q];
     if (skinny_cblk(g, q)) continue;
+    const int cn = cw * cb.n;
     for (int32_t t = cb.t0; t < cb.t1; ++t) {
       const GemmTask& gt = g.task[t];
       const int64_t ia = a_index(gt.a_off & ~kFromSrc), ib = b_index(gt.b_off & ~kFromSrc);
-      const int k = gt.k;
+      const int k = cw * gt.k;
       const int ktiles = (k + kTK - 1) / kTK;
       if (a_of[ia] < 0) {
         SplitOperand o{};
-        o.src_off = gt.a_off;
+        o.src_off = real_off(gt.a_off);
         o.rows = cb.m;
         o.cols = k;
         o.ktiles = ktiles;
@@ -820,25 +833,26 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
       }
       if (b_of[ib] < 0) {
         SplitOperand o{};
-        o.src_off = gt.b_off;
+        o.src_off = real_off(gt.b_off);
         o.rows = k;
-        o.cols = cb.n;
+        o.cols = cn;
         o.ktiles = ktiles;
         o.exp_off = (int32_t)b_exp;
         o.pack_off = b_pack;
-        const int64_t ctiles = (cb.n + kTN - 1) / kTN;
-        b_exp += cb.n;
+        o.cplx = cw == 2 ? 1 : 0;
+        const int64_t ctiles = (cn + kTN - 1) / kTN;
+        b_exp += cn;
         b_pack += ctiles * ktiles * kS * (int64_t)kBTile;
         b_of[ib] = (int32_t)b_ops.size();
         b_ops.push_back(o);
       }
       const SplitOperand& oa = a_ops[a_of[ia]];
       const SplitOperand& ob = b_ops[b_of[ib]];
-      QLTG_CHECK(oa.rows == cb.m && oa.cols == k && ob.rows == k && ob.cols == cb.n, QLTG_ERR_INVALID,
+      QLTG_CHECK(oa.rows == cb.m && oa.cols == k && ob.rows == k && ob.cols == cn, QLTG_ERR_INVALID,
                  "internal: inconsistent operand shapes in the split schedule");
       tasks[t] = SplitTask{oa.pack_off, ob.pack_off, oa.exp_off, ob.exp_off, ktiles, gt.sign};
     }
-    const int rtiles = (cb.m + kTM - 1) / kTM, ctiles = (cb.n + kTN - 1) / kTN;
+    const int rtiles = (cb.m + kTM - 1) / kTM, ctiles = (cn + kTN - 1) / kTN;
     for (int i = 0; i < rtiles; ++i)
       for (int j = 0; j < ctiles; ++j) tiles.push_back(GemmTile{q, (int16_t)i, (int16_t)j});
   }
@@ -848,7 +862,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   // task (the drain and rounding that end a task).
   std::vector<int64_t> cost(g.cblk.size(), 0);
   for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q)
-    for (int32_t t = g.cblk[q].t0; t < g.cblk[q].t1; ++t) cost[q] += 2 * ((g.task[t].k + 31) / 32) + 1;
+    for (int32_t t = g.cblk[q].t0; t < g.cblk[q].t1; ++t) cost[q] += 2 * ((cw * g.task[t].k + 31) / 32) + 1;
   std::stable_sort(tiles.begin(), tiles.end(), [&](const GemmTile& x, const GemmTile& y) { return cost[x.cblk] > cost[y.cblk]; });
   grid = (int)std::min<int64_t>((int64_t)tiles.size(), std::max(1, p.ctx->num_sms));
   std::vector<std::vector<int32_t>> owned(grid);
@@ -874,15 +888,15 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
       for (int32_t t = cb.t0; t < cb.t1; ++t) {
         const SplitTask& tk = tasks[t];
         SplitWork w{};
-        w.c_off = cb.c_off;
+        w.c_off = cw * cb.c_off;
         w.a_pack = tk.a_pack;
         w.b_pack = tk.b_pack;
         w.m = cb.m;
-        w.n = cb.n;
+        w.n = cw * cb.n;
         w.a_exp = tk.a_exp;
         w.b_exp = tk.b_exp;
         w.ktiles = tk.ktiles;
-        w.k = g.task[t].k;
+        w.k = cw * g.task[t].k;
         w.tm = tl.tm;
         w.tn = tl.tn;
         w.sign = (int8_t)(tk.sign < 0 ? -1 : 1);
@@ -1005,7 +1019,7 @@ void split_prepack_static(CtrctPlan& p, const void* a_static, const void* b_stat
 }
 
 void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s, bool pack) {
-  QLTG_CHECK(p.a.dtype == QLTG_F64, QLTG_ERR_UNSUPPORTED, "split-precision mode supports FP64 tensors");
+  const bool cplx = p.a.dtype == QLTG_C128;
   if (!p.split) {
     // first split-mode execution of this plan: build the slice schedule (allocates; not
     // allowed inside a stream capture - the matvec builds it before capturing)
@@ -1021,14 +1035,14 @@ void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s
   // pipe); everything else goes through the slices. With both present the skinny kernel
   // runs on the side stream (it writes other output blocks) and joins after the split GEMM.
   const bool fork = !p.sched.skinny.empty() && !sp.tiles.empty() && sp.side;
-  const SkinnyFuse* fuse = p.fuse_fields ? p.d_fuse.as<SkinnyFuse>() : nullptr;
+  const SkinnyFuse* fuse = p.fuse_fields && !cplx ? p.d_fuse.as<SkinnyFuse>() : nullptr;
   if (fork) {
     QLTG_CUDA(cudaEventRecord(sp.fork, s));
     QLTG_CUDA(cudaStreamWaitEvent(sp.side, sp.fork, 0));
-    launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, sp.side, fuse, p.fuse_fields);
+    launch_gemm_f64_skinny(p.sched, op, c, cplx, p.ctx->num_sms, sp.side, fuse, p.fuse_fields);
     QLTG_CUDA(cudaEventRecord(sp.join, sp.side));
   } else {
-    launch_gemm_f64_skinny(p.sched, op, c, false, p.ctx->num_sms, s, fuse, p.fuse_fields);
+    launch_gemm_f64_skinny(p.sched, op, c, cplx, p.ctx->num_sms, s, fuse, p.fuse_fields);
   }
   if (sp.tiles.empty()) return;
   struct Join {   // the main stream waits for the side stream on every way out
@@ -1054,7 +1068,6 @@ void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s
 
 void prepare_split(CtrctPlan& p, cudaStream_t s) {
   if (p.split && p.split->built) return;
-  if (p.a.dtype != QLTG_F64) return;   // complex operands stay on the FP64 path
   p.split = std::make_unique<SplitPlan>();
   p.split->build(p, s);
 }

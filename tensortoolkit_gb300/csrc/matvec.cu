@@ -27,6 +27,7 @@ void link_row_fields(qltg_matvec& mv, cudaStream_t s) {
   CtrctPlan& p2 = mv.step[2];
   CtrctPlan& p3 = mv.step[3];
   if (!p2.split || !p3.split || p3.split->a_ops.empty() || p3.split->a_static) return;
+  if (p3.a.dtype != QLTG_F64) return;   // the skinny kernel folds real outputs only
   if (p3.a_tl.ntiles || !p2.split->tiles.empty()) return;
   const auto& ops = p3.split->a_ops;
   std::map<int64_t, int> op_of;

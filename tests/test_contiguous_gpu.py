@@ -2,7 +2,7 @@
 reference's own outputs (tests/golden/ctrct_contig.npz) and the oracle.
 
 Bar: block topology identical to the reference's; values within 1e-12 relative Frobenius
-(FP64 and, for real tensors, split precision); the no-expansion form refuses exactly when
+(FP64 and split precision, real and complex); the no-expansion form refuses exactly when
 the reference's does and then leaves C untouched."""
 import numpy as np
 import pytest
@@ -33,7 +33,7 @@ def _scalars(rec, tag, t):
 
 
 def _modes(t):
-    return ["fp64"] if t.is_complex else ["fp64", "split"]
+    return ["fp64", "split"]
 
 
 @pytest.mark.parametrize("pre", ["u_", "f_"])

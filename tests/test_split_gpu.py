@@ -28,7 +28,10 @@ def block_errors(c: BSTensor, ref: BSTensor) -> np.ndarray:
 
 
 CASES = [("cfg1", ["c"]), ("matvec_u1_small", ["s1", "s2", "s3", "s4"]),
-         ("ctrct_misc_u1", ["u_scalar", "u_perm", "u_mid"])]
+         ("ctrct_misc_u1", ["u_scalar", "u_perm", "u_mid"]),
+         # fermionic complex128: the real 2k x 2n embedding of complex B
+         ("matvec_f_small", ["s1", "s2", "s3", "s4"]),
+         ("ctrct_misc_u1", ["f_env", "f_in", "f_mpo", "f_rev", "f_scalar"])]
 
 
 @pytest.mark.parametrize("case,tags", CASES)
@@ -150,3 +153,20 @@ def test_matvec_apply_host(gpu, mode):
     assert np.array_equal(h_out.numpy(), ref.data)
     with pytest.raises((capi.QltgError, ValueError)):
         mv.apply_host(h_in, torch.empty(mv.result.size, dtype=torch.float64))
+
+
+@pytest.mark.parametrize("D", [1500, 6000])
+def test_split_complex_fermionic_matvec_vs_oracle(gpu, D):
+    """Split precision on complex operands (fU(1)xU(1) Hubbard-like chain, complex128): each
+    complex GEMM runs as the real product of A's interleaved parts with B's 2 x 2 real form."""
+    lenv, psi, mpo1, mpo2, renv = workloads.hubbard(D)
+    ref, _ = oracle.matvec(lenv, psi, mpo1, mpo2, renv)
+    dl, d1, d2, dr = (DTensor.from_host(x) for x in (lenv, mpo1, mpo2, renv))
+    mv = Matvec(dl, psi, d1, d2, dr, mode="split")
+    out = mv.apply(DTensor.from_host(psi))
+    mv.device_status()
+    out = out.to_host()
+    assert same_topology(out, ref)
+    err = rel_frob(out.data, ref.data)
+    print(f"complex D={D}: split vs FP64 oracle rel Frobenius {err:.3e}")
+    assert err <= TOL
