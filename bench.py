@@ -346,8 +346,8 @@ def run_aux(local: int, part: str = "all"):
                      "or Q/R tensors); per-block = torch.linalg.svd / qr (cuSOLVER) on dense matrices of "
                      "the same shapes, kernels only"})
         del dt, mats
-    # 3. matvec of Config 2 (U(1), D=2000) in both forms, and Config 5 (fermionic complex128,
-    #    D=6000, plain FP64: complex operands have no split form)
+    # 3. matvec of Config 2 (U(1), D=2000) and Config 5 (fermionic complex128, D=6000), each in
+    #    plain FP64 and split precision
     def mv_time(tensors, mode):
         lenv_, psi_, mpo1_, mpo2_, renv_ = tensors
         dl_, dp_, d1_, d2_, dr_ = (DTensor.from_host(x, local) for x in tensors)
@@ -364,7 +364,7 @@ def run_aux(local: int, part: str = "all"):
         c2 = workloads.heisenberg(2000, 20, 6.0, 1)
         out["config2_matvec_d2000"] = [mv_time(c2, "fp64"), mv_time(c2, "split")]
         c5 = workloads.hubbard(6000, 10, 4)
-        out["config5_matvec_d6000_complex"] = [mv_time(c5, "fp64")]
+        out["config5_matvec_d6000_complex"] = [mv_time(c5, "fp64"), mv_time(c5, "split")]
     print(json.dumps(out))
 
 
