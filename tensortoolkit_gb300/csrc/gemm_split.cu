@@ -272,8 +272,9 @@ __global__ void __launch_bounds__(256) k_pack_a(const double* __restrict__ scr, 
 
 // Element (r, c) of a B operand block: the block itself (k x n row-major), or for a complex
 // block (k x n complex, interleaved) its real 2k x 2n form of 2 x 2 blocks [[Re, Im], [-Im, Re]].
-__device__ __forceinline__ double b_elem(const double* __restrict__ blk, int64_t r, int c, int cols, int cplx) {
-  if (!cplx) return __ldg(blk + r * cols + c);
+template <bool CPLX>
+__device__ __forceinline__ double b_elem(const double* __restrict__ blk, int64_t r, int c, int cols) {
+  if constexpr (!CPLX) return __ldg(blk + r * cols + c);
   const double v = __ldg(blk + (r >> 1) * cols + (c & ~1) + ((r ^ c) & 1));
   return ((r & 1) && !(c & 1)) ? -v : v;
 }
@@ -283,6 +284,7 @@ __device__ __forceinline__ double b_elem(const double* __restrict__ blk, int64_t
 // warp reads 32 consecutive columns of one row); the 8 partial maxima per column meet in
 // shared memory. Phase 2: one thread per 16-byte chunk (8 consecutive k of one column) of
 // every 64-wide k tile writes the chunk of every slice plane.
+template <bool CPLX>
 __global__ void __launch_bounds__(256) k_pack_b_cols(const double* __restrict__ scr, const double* __restrict__ src,
                                                      const SplitOperand* __restrict__ ops,
                                                      const int2* __restrict__ col_tiles, int ntiles,
@@ -298,10 +300,16 @@ __global__ void __launch_bounds__(256) k_pack_b_cols(const double* __restrict__ 
     const int nc = min(kTN, o.cols - c0);
     uint32_t mx = 0, nz = 0;   // largest high word of |x|, any nonzero bit
     if (lane < nc) {
+      const double* col = blk + c0 + lane;
       for (int r = g; r < o.rows; r += 32) {
         double v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = r + 8 * u < o.rows ? b_elem(blk, r + 8 * u, c0 + lane, o.cols, o.cplx) : 0.0;
+        for (int u = 0; u < 4; ++u) {
+          if constexpr (CPLX)
+            v[u] = r + 8 * u < o.rows ? b_elem<true>(blk, r + 8 * u, c0 + lane, o.cols) : 0.0;
+          else
+            v[u] = r + 8 * u < o.rows ? __ldg(col + (int64_t)(r + 8 * u) * o.cols) : 0.0;
+        }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const uint32_t h = (uint32_t)__double2hiint(v[u]) & 0x7FFFFFFFu;
@@ -334,11 +342,18 @@ __global__ void __launch_bounds__(256) k_pack_b_cols(const double* __restrict__ 
       const int64_t k0 = (int64_t)kt * kTK + ks * 16 + k_core * 8;
       if (cc >= nc || k0 >= o.rows) continue;   // padding: the buffer was zeroed once
       const int e = se[cc];
+      const double* col = blk + c0 + cc;
       uint64_t y[8];
       uint32_t sg[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j)
-        y[j] = scaled_y((k0 + j < o.rows) ? b_elem(blk, k0 + j, c0 + cc, o.cols, o.cplx) : 0.0, e, sg[j]);
+      for (int j = 0; j < 8; ++j) {
+        double x = 0.0;
+        if (k0 + j < o.rows) {
+          if constexpr (CPLX) x = b_elem<true>(blk, k0 + j, c0 + cc, o.cols);
+          else x = col[(k0 + j) * o.cols];
+        }
+        y[j] = scaled_y(x, e, sg[j]);
+      }
       // tile layout [ks][slice][n_core][k_core][8 columns x 16 B]: the 7 slices of a 16-wide k
       // step form one 224-row K-major operand (slice q = rows 32 (q-1) .. 32 q - 1)
       const int64_t tile = (int64_t)tt.y * o.ktiles + kt;
@@ -930,7 +945,10 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
     QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pack_a, 256, 0));
     pack_a_grid = (int)std::max<int64_t>(1, std::min<int64_t>((n_a_pchunks + 255) / 256,
                                                               (int64_t)std::max(1, per_sm) * p.ctx->num_sms));
-    QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pack_b_cols, 256, 0));
+    if (p.a.dtype == QLTG_C128)
+      QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pack_b_cols<true>, 256, 0));
+    else
+      QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pack_b_cols<false>, 256, 0));
     pack_b_grid = std::max(1, std::min((int)b_col_tiles.size(), std::max(1, per_sm) * p.ctx->num_sms));
   }
   d_a_ops = upload(a_ops, s);
@@ -993,8 +1011,14 @@ void pack_split_operand(SplitPlan& sp, bool side_a, const void* scratch, const v
       return;
     }
     const int nt = (int)sp.b_col_tiles.size();
-    k_pack_b_cols<<<sp.pack_b_grid, 256, 0, s>>>(X, Xs, sp.d_b_ops.as<SplitOperand>(), sp.d_b_col_tiles.as<int2>(), nt,
-                                                 sp.b_exps.as<int32_t>(), sp.b_packed.as<uint8_t>());
+    if (sp.b_ops[0].cplx)
+      k_pack_b_cols<true><<<sp.pack_b_grid, 256, 0, s>>>(X, Xs, sp.d_b_ops.as<SplitOperand>(),
+                                                         sp.d_b_col_tiles.as<int2>(), nt, sp.b_exps.as<int32_t>(),
+                                                         sp.b_packed.as<uint8_t>());
+    else
+      k_pack_b_cols<false><<<sp.pack_b_grid, 256, 0, s>>>(X, Xs, sp.d_b_ops.as<SplitOperand>(),
+                                                          sp.d_b_col_tiles.as<int2>(), nt, sp.b_exps.as<int32_t>(),
+                                                          sp.b_packed.as<uint8_t>());
   }
   QLTG_CUDA(cudaGetLastError());
   (side_a ? sp.a_ready : sp.b_ready) = true;
