@@ -211,14 +211,18 @@ QLTG_API int qltg_transpose_plan_exec(qltg_transpose_plan* plan, const void* src
 QLTG_API int qltg_transpose_plan_destroy(qltg_transpose_plan* plan);
 
 /* Same result as qltg_transpose, but allocates nothing: no cudaMalloc / cudaFree and no
- * allocating library call. No counterpart in the reference; it is for callers that cannot
- * allocate device memory while they run (for example code executing under another
- * library's stream capture or inside a fixed memory-pool budget). The per-block work list
- * goes to a fixed table of at most 4096 blocks compiled into the library; larger tensors
- * are rejected with QLTG_ERR_INVALID. The first call on a device looks up that table's
- * device address, so make the first call on each device before any stream capture. All
- * calls share the table: calls that overlap on the GPU race. Returns after its kernel has
- * finished. */
+ * allocating library call. No counterpart in the reference. It is for callers that cannot
+ * allocate device memory while they run: a host whose device memory is all handed out up
+ * front to another framework's pool (a cudaMalloc there fails or evicts that pool's cache),
+ * or a latency-critical loop that cannot afford cudaMalloc / cudaFree, which synchronise the
+ * device. The per-block work list goes to a fixed table of at most 4096 blocks compiled into
+ * the library (about 600 KB, held by every GPU that loads the library until the process
+ * exits); larger tensors are rejected with QLTG_ERR_INVALID. The first call on a device looks
+ * up that table's device address (once per device, with the device current) and keeps it for
+ * the life of the process, so the library must not outlive a cudaDeviceReset; make that first
+ * call before any stream capture. All calls share the table and it keeps the last call's
+ * descriptors: calls that overlap on the GPU race. The call copies its descriptors from host
+ * memory and synchronises `stream` before it returns. */
 QLTG_API int qltg_transpose_noalloc(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev,
                                     const int32_t* perm, void* dst_dev, void* stream);
 

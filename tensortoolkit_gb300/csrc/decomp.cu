@@ -598,7 +598,7 @@ int64_t block_of(const Meta& t, const std::vector<int64_t>& c) {
   return lo;
 }
 
-unsigned grid_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+unsigned grid_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)current_sm_count() * 16)); }
 
 template <typename T>
 void launch_gather(const std::vector<CopyDesc>& d, int64_t total, const void* src, void* dst, cudaStream_t s,
@@ -855,7 +855,7 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   // singular values and the right vectors from X; the left vectors W = Q J
   DevBuf d_jobs = upload(xjobs, s);
   if (ng) {
-    k_qj<T><<<(unsigned)std::min<size_t>(std::max<size_t>(1, qtiles.size()), 152 * 8), 256, 0, s>>>(
+    k_qj<T><<<(unsigned)std::min<size_t>(std::max<size_t>(1, qtiles.size()), (size_t)current_sm_count() * 8), 256, 0, s>>>(
         d_pre.as<PrecondJob>(), d_qtiles.as<QjTile>(), (int)qtiles.size(), qbuf.as<T>(), jbuf.as<T>(), ws.as<T>());
     QLTG_CUDA(cudaGetLastError());
     k_svd_finish<T><<<ng, kThreads, 0, s>>>(d_jobs.as<JacobiJob>(), ws.as<T>(), sv.as<double>(),

@@ -51,11 +51,14 @@ __device__ __forceinline__ double2 lc_add(double2 a, double2 b) { return make_do
 __device__ __forceinline__ double lc_zero(double) { return 0.0; }
 __device__ __forceinline__ double2 lc_zero(double2) { return make_double2(0.0, 0.0); }
 
+// `out` may be one of the source buffers (in-place LinearCombine / AddScaledAssign: the same
+// layout, so each element is read and written by one thread at the same position); it is
+// therefore not declared __restrict__.
 template <typename T>
 __global__ void __launch_bounds__(256) k_lincomb(const LincombItem* __restrict__ items, int nitems,
                                                  const LincombSrc* __restrict__ srcs,
                                                  const __grid_constant__ LincombArgs<T> args,
-                                                 T* __restrict__ out) {
+                                                 T* out) {
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const LincombItem w = items[it];
     for (int e = threadIdx.x; e < w.n; e += blockDim.x) {

@@ -88,6 +88,17 @@ class DevBuf {
   size_t n_ = 0;
 };
 
+// Streaming multiprocessors of the current device (grid sizing for kernels launched without
+// a context at hand).
+inline int current_sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 1;
+  }
+  return n > 0 ? n : 1;
+}
+
 template <typename T>
 DevBuf upload(const std::vector<T>& v, cudaStream_t s) {
   DevBuf b(v.size() * sizeof(T));

@@ -396,7 +396,7 @@ void TransposeList::build(const Meta& t, const std::vector<int>& order, const st
 void TransposeList::launch(const void* src, void* dst, int elem_bytes, cudaStream_t s) const {
   if (ntiles == 0) return;
   perm_set_smem_attr();
-  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, 152 * 8);
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)current_sm_count() * 8);
   if (elem_bytes == 8)
     k_permute<double><<<grid, kPermThreads, perm_smem_bytes(8), s>>>(dev.as<PermDesc>(), (int)nblocks, ntiles, static_cast<const double*>(src),
                                            static_cast<double*>(dst));
@@ -408,13 +408,15 @@ void TransposeList::launch(const void* src, void* dst, int elem_bytes, cudaStrea
 
 // ---------------------------------------------------------------------------
 // Allocation-free variant (qltg_transpose_noalloc). Some callers cannot allocate device
-// memory while they run - a DMRG sweep driven from inside another library's CUDA-graph
-// capture or memory-pool budget, or a host thread that must not take the allocator's
-// locks - so the per-call permutation work list lives in this fixed device table instead
-// of a fresh cudaMalloc. Every GPU that loads the library holds the table (about 600 KB)
-// until the process exits. All calls share it and it keeps the last call's descriptors, so
-// calls that overlap on the GPU (on different streams or devices' queues at once) race;
-// each call waits for its own kernel before returning.
+// memory while they run - a DMRG sweep whose device memory was handed up front to another
+// framework's pool (a cudaMalloc then fails or evicts that pool's cache), or a loop that
+// cannot pay for the device-wide synchronisation of cudaMalloc / cudaFree - so the per-call
+// permutation work list lives in this fixed device table instead of a fresh cudaMalloc.
+// Every GPU that loads the library holds the table (about 600 KB) until the process exits.
+// All calls share it and it keeps the last call's descriptors, so calls that overlap on the
+// GPU (on different streams at once) race; each call waits for its own kernel before
+// returning. The table's device address is looked up once per device and kept for the life
+// of the process: the library must not outlive a cudaDeviceReset.
 namespace {
 
 __device__ __align__(256) PermDesc g_noalloc_perm[kNoAllocPermBlocks];
@@ -447,7 +449,7 @@ void launch_permute_noalloc(int device, const TransposeList& tl, const void* src
   perm_set_smem_attr();
   if (tl.ntiles == 0) return;
   QLTG_CUDA(cudaMemcpyAsync(table, tl.host.data(), tl.host.size() * sizeof(PermDesc), cudaMemcpyHostToDevice, s));
-  const unsigned grid = (unsigned)std::min<int64_t>(tl.ntiles, 152 * 8);
+  const unsigned grid = (unsigned)std::min<int64_t>(tl.ntiles, (int64_t)current_sm_count() * 8);
   if (elem_bytes == 8)
     k_permute<double><<<grid, kPermThreads, perm_smem_bytes(8), s>>>(table, (int)tl.nblocks, tl.ntiles, static_cast<const double*>(src),
                                            static_cast<double*>(dst));
