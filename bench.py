@@ -12,7 +12,10 @@ tensortoolkit_gb300/csrc/synth.h; no dataset is involved.
 value  : device-resident time per matvec (graph launch only), L2 flushed between steps.
 e2e    : the same through the public API with host buffers (qltg_matvec_apply_host) - pinned
          host psi copied in, H_eff psi computed, result copied back - every step.
-roofline: the dominant kernel (grouped GEMM) timed with CUDA events on its own stream.
+roofline: the dominant kernel (grouped GEMM) timed with CUDA events on its own stream:
+         algorithmic FP64 flops sum(2mkn) / launch time against the FP64-equivalent peak
+         (split: the BF16 peak / 28 slice products; FP64: cuBLAS DGEMM measured in the run);
+         sum_T_over_t = sum over the four steps of max(F/P, B/BW) / the matvec time.
 cpu_baseline: the CPU restatement of the reference's algorithm (OpenBLAS dgemm per block
          pair, as the reference's CPU build) on a bounded sample of the same workload.
 --impl reference: that CPU path alone, timed over the same steps.
@@ -35,6 +38,33 @@ WORKLOAD = dict(D=4000, qmax=30, sigma=9.0, seed=1)
 WORKLOAD_NAME = "two-site H*psi matvec, U(1) Heisenberg chain, D=4000 (Sz -30..30, sigma 9), d=2, w=5"
 METRIC = "two-site H*psi matvec s/iter at D=4000"
 L2_FLUSH_BYTES = 512 << 20
+
+
+def bench_config(world: int) -> dict:
+    """The workload description both arms print (identical dicts, so the two lines compare)."""
+    return {"workload": WORKLOAD_NAME, **WORKLOAD,
+            "l2": "GPU arm: 512 MiB buffer written between timed steps",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for line in r.stdout.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
 
 
 def replica_time(t_step: float, world: int, device=None) -> float:
@@ -156,8 +186,12 @@ def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
     sp = C.c_void_p(stream.cuda_stream)
     per, stage_ms, kern_ms, alg_flops, tc_flops = [], 0.0, 0.0, 0.0, 0.0
     best = None
+    step_fb = []                       # per step: (algorithmic flops, operand + result bytes)
     for i in range(4):
-        p = ContractionPlan(a_meta, bs[i].meta if i else psi, axes[i], local)
+        b_meta = bs[i].meta if i else psi
+        p = ContractionPlan(a_meta, b_meta, axes[i], local)
+        eb = 16 if a_meta.is_complex else 8
+        step_fb.append((p.stats()[0], (a_meta.size + b_meta.size + p.result.size) * eb))
         c = DTensor.empty(p.result, local)
         p.execute(cur_a, bs[i], c, mode=mode)
         args = (p.h, C.c_void_p(cur_a.ptr), C.c_void_p(bs[i].ptr), C.c_void_p(c.ptr), mode_i)
@@ -190,11 +224,17 @@ def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
             best = (i, ms3, work, f)
         cur_a, a_meta = c, p.result
     i, ms, work, f = best
+    exec_tflops = exec_frac = None
     if mode == "split":
-        peak = pk["bf16_tflops"]
-        src = f"bf16 dense burst, {pk['source']} (MEASURED_PEAKS.json)"
-        what = (f"k_gemm_split, one launch (matvec step {i}): executed BF16 tensor flops "
-                "(28 slice pairs on 128x32x32 padded tiles) / launch time")
+        # the slice-pipe peak divided by the 28 slice products each FP64 product needs
+        bf16 = pk["bf16_tflops"]
+        peak = bf16 / 28.0
+        src = (f"bf16 dense burst {bf16:.1f} TFLOP/s ({pk['source']}, MEASURED_PEAKS.json) / 28 slice "
+               "products = the FP64-equivalent peak of the split form")
+        what = (f"k_gemm_split, one launch (matvec step {i}): algorithmic FP64 flops sum(2mkn) / launch time, "
+                "against the BF16 peak / 28")
+        exec_tflops = work / (ms / 1e3) / 1e12
+        exec_frac = exec_tflops / bf16
     else:
         n = 8192
         x = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
@@ -213,12 +253,24 @@ def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
         del x, y
         src = "cuBLAS DGEMM 8192^3 measured in this run (the FP64 pipe)"
         what = f"k_gemm_dfma (+ k_gemm_skinny), one launch (matvec step {i}): algorithmic flops sum(2mkn) / launch time"
-    achieved = work / (ms / 1e3) / 1e12
-    return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak if peak else None, "traffic": NCU_TRAFFIC.get(mode, {}).get(i),
-            "kernel": what, "peak_source": src, "launch_ms": round(ms, 4),
-            "fp64_equiv_tflops": f / (ms / 1e3) / 1e12,
-            "per_step": per, "gemm_stage_ms": round(stage_ms, 4), "gemm_kernels_ms": round(kern_ms, 4)}
+    achieved = f / (ms / 1e3) / 1e12
+    # whole-matvec bound: per step T_s = max(F_s / P, B_s / BW)
+    bw = pk["hbm_gbs"] * 1e9
+    t_bound = sum(max(fs / (peak * 1e12), bs_ / bw) for fs, bs_ in step_fb)
+    out = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+           "frac": achieved / peak if peak else None, "traffic": NCU_TRAFFIC.get(mode, {}).get(i),
+           "kernel": what, "peak_source": src, "launch_ms": round(ms, 4),
+           "fp64_equiv_tflops": achieved,
+           "sum_T_bound_ms": round(t_bound * 1e3, 4),
+           "step_bounds": [{"gflop": round(fs / 1e9, 4), "mbytes": round(bs_ / 1e6, 2),
+                            "T_flops_ms": round(fs / (peak * 1e12) * 1e3, 4),
+                            "T_bytes_ms": round(bs_ / bw * 1e3, 4)} for fs, bs_ in step_fb],
+           "per_step": per, "gemm_stage_ms": round(stage_ms, 4), "gemm_kernels_ms": round(kern_ms, 4)}
+    if exec_tflops is not None:
+        out["executed_tensor_tflops"] = exec_tflops
+        out["executed_tensor_frac"] = exec_frac
+        out["executed_note"] = "executed BF16 tensor flops (28 slice pairs on 128x32x32 padded tiles) / launch time / BF16 peak"
+    return out
 
 
 def precision_study(local: int, steps: int = 20):
@@ -369,7 +421,7 @@ def run_aux(local: int, part: str = "all"):
 
 
 def cpu_matvec_time(tensors, iters: int, threads: int) -> float:
-    """Seconds per matvec of the CPU restatement (median of `iters`)."""
+    """Seconds per matvec of the CPU restatement (median of `iters` after one warm-up)."""
     from oracle import oracle
     oracle.set_threads(threads)
     lenv, psi, mpo1, mpo2, renv = tensors
@@ -382,14 +434,28 @@ def cpu_matvec_time(tensors, iters: int, threads: int) -> float:
     return statistics.median(ts)
 
 
+def cpu_thread_sweep(tensors, iters: int = 3):
+    """The CPU restatement at 1, 2, 4 and all host threads (the reference's default is 4:
+    framework/consts.h:24, framework/hp_numeric/omp_set.h:27-83). Returns ({threads: s/iter},
+    best thread count)."""
+    n = os.cpu_count() or 1
+    counts = sorted({1, 2, 4, n} & set(range(1, n + 1)))
+    sweep = {t: cpu_matvec_time(tensors, iters, t) for t in counts}
+    return sweep, min(sweep, key=sweep.get)
+
+
 def run_reference(args):
+    """The reference's algorithm on the host cores: the CPU restatement (oracle/oracle.cc,
+    OpenBLAS dgemm per block pair as the reference's CPU build) on the same synthetic D=4000
+    inputs, made by the generator compiled into the oracle's own library. A short thread
+    sweep picks the thread count; the timed steps run at the best one."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
-    from tensortoolkit_gb300 import workloads
-    tensors = workloads.heisenberg(WORKLOAD["D"], WORKLOAD["qmax"], WORKLOAD["sigma"], WORKLOAD["seed"])
-    threads = os.cpu_count() or 1
     from oracle import oracle
+    tensors = oracle.workload("matvec_u1", WORKLOAD["qmax"], WORKLOAD["sigma"], WORKLOAD["D"], WORKLOAD["seed"])
+    sweep, threads = cpu_thread_sweep(tensors)
     oracle.set_threads(threads)
     for _ in range(args.warmup):
         oracle.matvec(*tensors)
@@ -401,10 +467,15 @@ def run_reference(args):
     v = sum(ts) / len(ts)
     out = {"metric": METRIC, "value": v, "unit": "s/iter", "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1), reference shapes)",
-           "config": {"workload": WORKLOAD_NAME, **WORKLOAD}, "impl": "reference",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1) operands with the reference case's shapes)",
+           "config": bench_config(world), "impl": "reference",
            "cpu_baseline": {"value": v, "unit": "s/iter", "cores": threads, "kind": "port",
-                            "sample": f"{args.steps} full matvecs after {args.warmup} warm-up"},
+                            "sample": f"{args.steps} full D=4000 matvecs after {args.warmup} warm-up, at the best "
+                                      f"thread count of the sweep",
+                            "cpu_model": cpu_model(), "nproc": os.cpu_count(),
+                            "thread_sweep_s_per_iter": {str(k): round(x, 4) for k, x in sweep.items()},
+                            "reference_default_threads": 4,
+                            "at_default_threads_s_per_iter": round(sweep.get(4, float("nan")), 4)},
            "e2e": {"value": v, "unit": "s/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -509,6 +580,7 @@ def main():
         torch.cuda.synchronize()
         e2e_step = e0.elapsed_time(e1) / 1e3 / args.steps
         roof = gemm_roofline(m, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
+        roof["sum_T_over_t"] = roof["sum_T_bound_ms"] / (t_step * 1e3)
         results[m] = {"s_per_iter": t_step, "e2e_s_per_iter": e2e_step, "flops": flops,
                       "launches_per_step": launches_per_step, "roofline": roof,
                       "h2d": int(h_in.numel() * 8), "d2h": int(h_out.numel() * 8)}
@@ -523,10 +595,14 @@ def main():
         cpu = None
         try:
             cpu_iters = 10 if args.cpu_iters is None else args.cpu_iters
-            threads = os.cpu_count() or 1
+            sweep, threads = cpu_thread_sweep(tensors)
             v = cpu_matvec_time(tensors, cpu_iters, threads)
             cpu = {"value": v, "unit": "s/iter", "cores": threads, "kind": "port",
-                   "sample": f"median of {cpu_iters} full D=4000 matvecs (OpenBLAS dgemm per block pair)"}
+                   "sample": f"median of {cpu_iters} full D=4000 matvecs (OpenBLAS dgemm per block pair) at the "
+                             f"best thread count of the sweep",
+                   "cpu_model": cpu_model(), "nproc": os.cpu_count(),
+                   "thread_sweep_s_per_iter": {str(k): round(x, 4) for k, x in sweep.items()},
+                   "at_default_threads_s_per_iter": round(sweep.get(4, float("nan")), 4)}
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "s/iter", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"unavailable: {e}"}
@@ -537,9 +613,8 @@ def main():
             "precision": ("split: FP64 emulated with BF16 slices on tcgen05, <=1e-12 rel. err vs FP64"
                           if modes[0] == "split" else "plain FP64"),
             "data": "synthetic (seeded N(0,1) operands with the reference case's shapes)",
-            "config": {"workload": WORKLOAD_NAME, **WORKLOAD, "mode": modes[0],
-                       "l2": "512 MiB buffer written between timed steps",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": bench_config(world),
+            "mode": modes[0],
             "gflops_fp64_equiv": head["flops"] / t_step / 1e9,
             "algorithmic_gflop_per_step": head["flops"] / 1e9,
             "e2e": {"value": head["e2e_s_per_iter"], "unit": "s/iter", "h2d_bytes_per_step": head["h2d"],

@@ -28,13 +28,26 @@ class _TensorIn(C.Structure):
                 ("coords", C.c_void_p), ("data", C.c_void_p)]
 
 
+_SYNTH = os.path.join(os.path.dirname(_HERE), "tensortoolkit_gb300", "csrc")
+
+
 def build(force: bool = False) -> str:
-    """Compile liboracle.so with g++ (OpenMP, position independent)."""
-    src = os.path.join(_HERE, "oracle.cc")
-    if force or not os.path.exists(_SO) or os.path.getmtime(_SO) < os.path.getmtime(src):
-        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", src,
+    """Compile liboracle.so with g++ (OpenMP, position independent): the restatement plus the
+    deterministic workload generator (csrc/synth_capi.cc), so a CPU-only run (the reference
+    arm of bench.py) maps no library of the GPU package."""
+    srcs = [os.path.join(_HERE, "oracle.cc"), os.path.join(_SYNTH, "synth_capi.cc")]
+    deps = srcs + [os.path.join(_SYNTH, "synth.h")]
+    if force or not os.path.exists(_SO) or any(os.path.getmtime(_SO) < os.path.getmtime(d) for d in deps):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", *srcs,
                                "-o", _SO, "-ldl"])
     return _SO
+
+
+def workload(kind: str, *params: float) -> List[BSTensor]:
+    """A named synthetic workload (tensortoolkit_gb300.workloads.generate) made by the copy of
+    the generator compiled into liboracle.so: the same bytes as the GPU package's generator."""
+    from tensortoolkit_gb300 import workloads
+    return workloads.generate(kind, *params, lib=lib())
 
 
 def find_openblas() -> Optional[str]:

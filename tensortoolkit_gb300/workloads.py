@@ -17,8 +17,12 @@ from . import _native
 from .tensor import BSTensor
 
 
-def _lib():
-    L = _native.load_synth()
+def _lib(L=None):
+    """The generator library: libqltg_synth.so, or another library that exports the same
+    qltg_synth_* entry points (the CPU oracle compiles the generator into its own library,
+    so a CPU-only process never maps this package's shared objects)."""
+    if L is None:
+        L = _native.load_synth()
     if not getattr(L, "_qltg_synth_typed", False):
         L.qltg_synth_create.restype = C.c_void_p
         L.qltg_synth_create.argtypes = [C.c_char_p, C.c_void_p, C.c_int]
@@ -31,8 +35,8 @@ def _lib():
     return L
 
 
-def generate(kind: str, *params: float) -> List[BSTensor]:
-    L = _lib()
+def generate(kind: str, *params: float, lib=None) -> List[BSTensor]:
+    L = _lib(lib)
     p = np.asarray(params, np.float64)
     h = L.qltg_synth_create(kind.encode(), p.ctypes.data if p.size else None, len(p))
     if not h:
@@ -64,9 +68,9 @@ def config1(seed: int = 0):
     return generate("cfg1", seed)
 
 
-def heisenberg(D: int, qmax: int, sigma: float, seed: int = 1, hermitian: bool = False):
+def heisenberg(D: int, qmax: int, sigma: float, seed: int = 1, hermitian: bool = False, lib=None):
     """(lenv, psi, mpo1, mpo2, renv) of the U(1) two-site matvec at bond dimension D."""
-    return generate("matvec_u1h" if hermitian else "matvec_u1", qmax, sigma, D, seed)
+    return generate("matvec_u1h" if hermitian else "matvec_u1", qmax, sigma, D, seed, lib=lib)
 
 
 def hubbard(D: int, half: int = 10, seed: int = 4):
