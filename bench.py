@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -169,6 +170,47 @@ def _time_events(fn, stream, flush, reps=5):
     return statistics.median(x.elapsed_time(y) for x, y in ts)
 
 
+_FP64_PEAK = {}
+
+
+def fp64_peak_tflops(local, stream) -> float:
+    """The FP64 pipe's rate on this GPU: cuBLAS DGEMM 8192^3, best of 3, measured once per run."""
+    import torch
+    if local not in _FP64_PEAK:
+        n = 8192
+        x = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
+        y = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
+        torch.matmul(x, y)
+        torch.cuda.synchronize()
+        best_ms = 1e9
+        for _ in range(3):
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            torch.matmul(x, y)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            best_ms = min(best_ms, s0.elapsed_time(s1))
+        _FP64_PEAK[local] = 2 * n ** 3 / (best_ms / 1e3) / 1e12
+    return _FP64_PEAK[local]
+
+
+def matvec_step_bounds(tensors, local, peak_tflops, hbm_gbs):
+    """Per step of the matvec chain (F_s algorithmic flops, B_s = operand + result bytes) and
+    the sum over steps of max(F_s / P, B_s / BW) in ms."""
+    from tensortoolkit_gb300.api import ContractionPlan
+    lenv, psi, mpo1, mpo2, renv = tensors
+    axes = [[[0], [0]], [[0, 2], [0, 1]], [[4, 1], [0, 1]], [[4, 1], [1, 0]]]
+    a_meta, out = lenv, []
+    for i, b in enumerate((psi, mpo1, mpo2, renv)):
+        p = ContractionPlan(a_meta, b, axes[i], local)
+        f, nbytes = p.stats()
+        out.append((f, nbytes))
+        a_meta = p.result
+        del p
+    t = sum(max(f / (peak_tflops * 1e12), nb / (hbm_gbs * 1e9)) for f, nb in out)
+    return out, t * 1e3
+
+
 def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk):
     """Per matvec step: the operand transposes, the GEMM stage (incl. operand slicing) and the
     GEMM kernels alone, each timed with CUDA events on the launching stream with L2 flushed
@@ -236,21 +278,7 @@ def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
         exec_tflops = work / (ms / 1e3) / 1e12
         exec_frac = exec_tflops / bf16
     else:
-        n = 8192
-        x = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
-        y = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{local}")
-        torch.matmul(x, y)
-        torch.cuda.synchronize()
-        best_ms = 1e9
-        for _ in range(3):
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            torch.matmul(x, y)
-            s1.record(stream)
-            torch.cuda.synchronize()
-            best_ms = min(best_ms, s0.elapsed_time(s1))
-        peak = 2 * n ** 3 / (best_ms / 1e3) / 1e12
-        del x, y
+        peak = fp64_peak_tflops(local, stream)
         src = "cuBLAS DGEMM 8192^3 measured in this run (the FP64 pipe)"
         what = f"k_gemm_dfma (+ k_gemm_skinny), one launch (matvec step {i}): algorithmic flops sum(2mkn) / launch time"
     achieved = f / (ms / 1e3) / 1e12
@@ -343,6 +371,95 @@ def time_call(fn, reps: int = 5) -> float:
     return statistics.median(ts)
 
 
+class ProxyStep:
+    """One contraction in the reference GPU build's call pattern (a labelled proxy, not the
+    reference itself): BlockSparseDataTensor::CtrctTwoBSDTAndAssignIn
+    (qltensor/blk_spar_data_ten/global_operations.h:895-992) transposes every operand block it
+    uses once - cutensorPermute per block (framework/hp_numeric/ten_trans.h:245-349), here a
+    plain strided copy (torch permute + contiguous) - then issues one cublasDgemm per task on
+    the default stream in task order (framework/hp_numeric/blas_level3.h:797-856): beta 0 for
+    the task that creates its output block, 1 after, alpha the task's sign. cuBLAS is reached
+    through torch (addmm with out=). Bosonic real FP64 tensors only."""
+
+    def __init__(self, a_meta, b_meta, axes, plan):
+        sa = [i for i in range(a_meta.rank) if i not in axes[0]]
+        sb = [i for i in range(b_meta.rank) if i not in axes[1]]
+        self.perm_a, self.perm_b = sa + list(axes[0]), list(axes[1]) + sb
+        self.tasks = [tuple(int(x) for x in t) for t in plan.tasks()]
+        self.a_pos = {int(x): i for i, x in enumerate(a_meta.blk_idx())}
+        self.b_pos = {int(x): i for i, x in enumerate(b_meta.blk_idx())}
+        self.c_pos = {int(x): i for i, x in enumerate(plan.result.blk_idx())}
+        self.a_meta, self.b_meta, self.c_meta = a_meta, b_meta, plan.result
+        self.a_shapes, self.b_shapes = a_meta.block_shapes(), b_meta.block_shapes()
+        self.a_used = sorted({self.a_pos[t[0]] for t in self.tasks})
+        self.b_used = sorted({self.b_pos[t[1]] for t in self.tasks})
+
+    def run(self, a_buf, b_buf, c_buf):
+        import torch
+        at, bt = {}, {}
+        for i in self.a_used:
+            shp = [int(x) for x in self.a_shapes[i]]
+            o = int(self.a_meta.offsets[i])
+            at[i] = a_buf[o:o + math.prod(shp)].view(shp).permute(self.perm_a).contiguous()
+        for i in self.b_used:
+            shp = [int(x) for x in self.b_shapes[i]]
+            o = int(self.b_meta.offsets[i])
+            bt[i] = b_buf[o:o + math.prod(shp)].view(shp).permute(self.perm_b).contiguous()
+        for a_idx, b_idx, c_idx, m, k, n, sign, beta in self.tasks:
+            A = at[self.a_pos[a_idx]].view(m, k)
+            B = bt[self.b_pos[b_idx]].view(k, n)
+            o = int(self.c_meta.offsets[self.c_pos[c_idx]])
+            Cb = c_buf[o:o + m * n].view(m, n)
+            torch.addmm(Cb, A, B, beta=float(beta), alpha=float(sign), out=Cb)
+
+
+def run_proxy(local: int, stream, flush, reps: int = 5) -> dict:
+    """The plain FP64 matvec at D=4000 in the reference GPU build's call pattern (ProxyStep)
+    against this library's FP64 matvec on the same inputs: result agreement, time per matvec
+    and per step."""
+    import numpy as np
+    import torch
+    from tensortoolkit_gb300 import workloads
+    from tensortoolkit_gb300.api import ContractionPlan, DTensor, Matvec
+    tensors = workloads.heisenberg(WORKLOAD["D"], WORKLOAD["qmax"], WORKLOAD["sigma"], WORKLOAD["seed"])
+    lenv, psi, mpo1, mpo2, renv = tensors
+    dl, dp, d1, d2, dr = (DTensor.from_host(x, local) for x in tensors)
+    axes = [[[0], [0]], [[0, 2], [0, 1]], [[4, 1], [0, 1]], [[4, 1], [1, 0]]]
+    steps, bufs, a_meta, a_buf = [], [], lenv, dl.buf
+    for i, b in enumerate((dp, d1, d2, dr)):
+        plan = ContractionPlan(a_meta, b.meta, axes[i], local)
+        steps.append(ProxyStep(a_meta, b.meta, axes[i], plan))
+        c = torch.zeros(max(plan.result.size, 1), dtype=torch.float64, device=f"cuda:{local}")
+        bufs.append((a_buf, b.buf, c))
+        a_meta, a_buf = plan.result, c
+        del plan
+
+    def proxy_matvec():
+        for st, (a, b, c) in zip(steps, bufs):
+            st.run(a, b, c)
+    proxy_matvec()
+    torch.cuda.synchronize()
+    mv = Matvec(dl, psi, d1, d2, dr, mode="fp64")
+    ours = mv.apply(dp).to_host()
+    got = bufs[-1][2][: ours.size].cpu().numpy()
+    err = float(np.linalg.norm(got - ours.data) / np.linalg.norm(ours.data))
+    t_proxy = _time_events(proxy_matvec, stream, flush, reps=reps)
+    per_step = []
+    for st, (a, b, c) in zip(steps, bufs):
+        per_step.append(round(_time_events(lambda: st.run(a, b, c), stream, flush, reps=reps), 3))
+    o = DTensor.empty(mv.result, local)
+    t_ours = _time_events(lambda: mv.apply(dp, o), stream, flush, reps=10)
+    ntasks = sum(len(st.tasks) for st in steps)
+    return {"proxy_fp64_ms_per_matvec": round(t_proxy, 3), "proxy_ms_per_step": per_step,
+            "ours_fp64_ms_per_matvec": round(t_ours, 4), "ours_vs_proxy_speedup": round(t_proxy / t_ours, 2),
+            "proxy_vs_ours_rel_err": err, "gemm_calls_per_matvec": ntasks,
+            "note": "labelled proxy of the reference CUDA build's pattern (the build itself needs cuTENSOR, "
+                    "absent on this host): per operand block one strided-copy permute, then one cuBLAS "
+                    "DGEMM per task in task order on one stream, with torch's caching allocator in place "
+                    "of the reference's cudaMalloc / cudaFree per transposed block (so the proxy is, if "
+                    "anything, faster than the reference build)"}
+
+
 def run_aux(local: int, part: str = "all"):
     """Measurements beside the headline: the batched permute's achieved HBM bandwidth, the
     batched block SVD / QR (Config 3) against a per-block cuSOLVER loop on the same shapes
@@ -350,7 +467,7 @@ def run_aux(local: int, part: str = "all"):
     import numpy as np
     import torch
     from tensortoolkit_gb300 import workloads
-    from tensortoolkit_gb300.api import Contract, DTensor, Matvec, QR, SVD, Transpose, TransposePlan
+    from tensortoolkit_gb300.api import Contract, DTensor, Lanczos, Matvec, QR, SVD, Transpose, TransposePlan
     pk = peaks()
     out = {"aux": True, "gpu": torch.cuda.get_device_name(local)}
     dev = f"cuda:{local}"
@@ -400,7 +517,7 @@ def run_aux(local: int, part: str = "all"):
         del dt, mats
     # 3. matvec of Config 2 (U(1), D=2000) and Config 5 (fermionic complex128, D=6000), each in
     #    plain FP64 and split precision
-    def mv_time(tensors, mode):
+    def mv_time(tensors, mode, lanczos_steps=0):
         lenv_, psi_, mpo1_, mpo2_, renv_ = tensors
         dl_, dp_, d1_, d2_, dr_ = (DTensor.from_host(x, local) for x in tensors)
         t_create = time.perf_counter()
@@ -411,12 +528,44 @@ def run_aux(local: int, part: str = "all"):
         ms = _time_events(lambda: mv.apply(dp_, o), stream, flush, reps=10)
         mv.device_status()
         f, _ = mv.stats()
-        return {"mode": mode, "ms": round(ms, 4), "gflops": f / (ms / 1e3) / 1e9, "plan_s": round(t_create, 3)}
+        # 8(d): P = FP64 pipe (fp64) or BF16 peak / 28 slice products (split), BW = HBM
+        peak = fp64_peak_tflops(local, stream) if mode == "fp64" else pk["bf16_tflops"] / 28.0
+        _, t_bound = matvec_step_bounds(tensors, local, peak, pk["hbm_gbs"])
+        r = {"mode": mode, "ms": round(ms, 4), "gflops": f / (ms / 1e3) / 1e9, "plan_s": round(t_create, 3),
+             "gflop_per_matvec": round(f / 1e9, 4), "peak_tflops": round(peak, 2),
+             "sum_T_bound_ms": round(t_bound, 4), "frac_sum_T_over_t": round(t_bound / ms, 4)}
+        if lanczos_steps:
+            # the graph-captured Lanczos: one CUDA graph per step (matvec + two-pass complex
+            # Gram-Schmidt + norm); steps captured on a first run, then timed from a restart
+            lz = Lanczos(mv, lanczos_steps)
+            lz.start(dp_)
+            lz.step(lanczos_steps)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            flush.fill_(1.0)
+            lz.start(dp_)
+            e0.record(stream)
+            lz.step(lanczos_steps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            a, b = lz.coeffs()
+            mv.device_status()
+            lms = e0.elapsed_time(e1)
+            r["lanczos"] = {"steps": lanczos_steps, "total_ms": round(lms, 3),
+                            "ms_per_step": round(lms / lanczos_steps, 4),
+                            "lowest_ritz": float(Lanczos.ritz_lowest(a, b)[-1]),
+                            "note": "random complex operands: H is not Hermitian, the Ritz value is the "
+                                    "tridiagonal's lowest eigenvalue of the recurrence"}
+            del lz
+        del mv
+        return r
+    if part in ("all", "proxy"):
+        out["fp64_vs_reference_gpu_pattern_d4000"] = run_proxy(local, stream, flush)
     if part in ("all", "matvec"):
         c2 = workloads.heisenberg(2000, 20, 6.0, 1)
         out["config2_matvec_d2000"] = [mv_time(c2, "fp64"), mv_time(c2, "split")]
         c5 = workloads.hubbard(6000, 10, 4)
-        out["config5_matvec_d6000_complex"] = [mv_time(c5, "fp64"), mv_time(c5, "split")]
+        out["config5_matvec_d6000_complex"] = [mv_time(c5, "fp64", 20), mv_time(c5, "split", 20)]
     print(json.dumps(out))
 
 
@@ -492,7 +641,7 @@ def main():
     ap.add_argument("--aux", action="store_true",
                     help="measurements beside the headline: permute GB/s, batched SVD/QR vs per-block, "
                          "Config 2 and Config 5 matvecs (one JSON line)")
-    ap.add_argument("--aux-part", choices=["all", "transpose", "svd", "matvec"], default="all")
+    ap.add_argument("--aux-part", choices=["all", "transpose", "svd", "matvec", "proxy"], default="all")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: plan the D=4000 matvec, apply it twice, print nothing else")
     args = ap.parse_args()

@@ -57,8 +57,10 @@ enum { QLTG_IN = 0, QLTG_OUT = 1 };       /* TenIndexDirType */
  *                  and each task's sum is rounded to FP64 once. Per element the error is
  *                  below 2^-48 * sum_k |a_ik| |b_kj| scaled by the row / column maxima
  *                  (about 1e-14 relative for random data); the tests and the benchmark
- *                  state the measured relative error against the FP64 result. Real (FP64)
- *                  tensors only; output blocks with n, k <= 8 stay on the FP64 pipe. */
+ *                  state the measured relative error against the FP64 result. Real and
+ *                  complex128 tensors (a complex product runs as the real product of A's
+ *                  interleaved parts with B's 2 x 2 real form); output blocks with n, k <= 8
+ *                  stay on the FP64 pipe. */
 enum { QLTG_MODE_FP64 = 0, QLTG_MODE_SPLIT = 1 };
 
 /* ---------------------------------------------------------------- descriptors */
@@ -358,12 +360,14 @@ QLTG_API int qltg_matvec_device_status(qltg_matvec* mv, void* stream);
 QLTG_API int qltg_matvec_destroy(qltg_matvec* mv);
 
 /* ---------------------------------------------------------------- Lanczos (device vectors)
- * Lanczos on a real FP64 matvec's effective Hamiltonian with every vector operation on the
- * device in FP64: the reference's BSDT vector primitives (Dot / Norm / ScaleByFactor /
- * LinearCombine on the raw buffer: framework/hp_numeric/blas_level1.h,
+ * Lanczos on a matvec's effective Hamiltonian (real FP64 or complex128, either precision
+ * mode of the matvec) with every vector operation on the device in FP64: the reference's
+ * BSDT vector primitives (Dot / Norm / ScaleByFactor / LinearCombine on the raw buffer:
+ * framework/hp_numeric/blas_level1.h, complex forms :381-1080,
  * tensor_manipulation/ten_linear_combine.h:186-459, raw_data_operations.h:225-272) applied to
  * Krylov vectors that share ψ's block topology. Step j: w = H v_j, two passes of classical
- * Gram-Schmidt against v_0..v_j (alpha_j = <v_j, H v_j> with both corrections),
+ * Gram-Schmidt against v_0..v_j with <x, y> = Σ conj(x) y (alpha_j = Re <v_j, H v_j> with
+ * both corrections; real for a Hermitian H),
  * beta_{j+1} = ||w||, v_{j+1} = w / beta_{j+1}; deterministic reductions. Each step is one
  * CUDA graph (built on the step's first use; later starts reuse it). alpha and beta stay on
  * the device until qltg_lanczos_coeffs. The eigenvalues of the tridiagonal matrix are left

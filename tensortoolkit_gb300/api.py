@@ -792,8 +792,9 @@ class Matvec:
 
 
 class Lanczos:
-    """Lanczos on a real FP64 `Matvec` with the Krylov vectors and all vector operations on
-    the device (full reorthogonalisation, FP64); one CUDA graph per step. The lowest Ritz
+    """Lanczos on a `Matvec` (real FP64 or complex128, plain or split precision) with the
+    Krylov vectors and all vector operations on the device (full reorthogonalisation, FP64;
+    complex dots conjugate their first argument); one CUDA graph per step. The lowest Ritz
     value after each step comes from the tridiagonal matrix (host FP64)."""
 
     def __init__(self, mv: Matvec, max_iter: int = 20):
@@ -836,12 +837,15 @@ class Lanczos:
         return self.ritz_lowest(a, b)
 
     def vector(self, i: int) -> torch.Tensor:
-        """Krylov vector v_i as a float64 CUDA tensor viewing the device buffer (no copy)."""
+        """Krylov vector v_i as a float64 (complex128 for a complex matvec) CUDA tensor viewing
+        the device buffer (no copy)."""
         p = C.c_void_p()
         check(lib().qltg_lanczos_vector(self.h, int(i), C.byref(p)))
-        n = self.mv.result.size
+        cplx = self.mv.result.is_complex
+        n = self.mv.result.size * (2 if cplx else 1)
         with torch.cuda.device(self.mv.device):
-            return torch.as_tensor(_DevView(p.value, n), device=f"cuda:{self.mv.device}")
+            v = torch.as_tensor(_DevView(p.value, n), device=f"cuda:{self.mv.device}")
+        return torch.view_as_complex(v.view(-1, 2)) if cplx else v
 
     def __del__(self):
         try:

@@ -285,11 +285,12 @@ inline void fill_heisenberg_mpo(Tensor& w) {
   // channel (sector, degeneracy) ids
   struct Ch { int64_t sct, deg; };
   const Ch start{1, 0}, szc{1, 1}, done{1, 2}, spc{0, 0}, smc{2, 0};
+  const int64_t f = w.is_complex ? 2 : 1;   // doubles per element (real part first)
   auto set = [&](Ch wl, int64_t s_in, int64_t s_out, Ch wr, double v) {
     int64_t b = find_block(w, {wl.sct, s_in, s_out, wr.sct});
     if (b < 0) throw std::runtime_error("heisenberg mpo: block missing");
     const int64_t d3 = w.blk_dim(b, 3);
-    w.data[w.offsets[b] + wl.deg * d3 + wr.deg] = v;   // P dims are 1
+    w.data[(w.offsets[b] + wl.deg * d3 + wr.deg) * f] = v;   // P dims are 1
   };
   for (int s = 0; s < 2; ++s) { set(start, s, s, start, 1.0); set(done, s, s, done, 1.0); }
   set(start, 0, 1, spc, 1.0);          // S+ |down> = |up>
@@ -308,6 +309,54 @@ inline Matvec heisenberg_u1_hermitian(int qmax, double sigma, int64_t D, uint64_
   Matvec m = heisenberg_u1_random(qmax, sigma, D, seed);
   symmetrize_env(m.lenv);
   symmetrize_env(m.renv);
+  fill_heisenberg_mpo(m.mpo1);
+  m.mpo2 = m.mpo1;
+  return m;
+}
+
+// Complex form of symmetrize_env: E(a, w, a') = conj(E(a', wbar, a)) (data interleaved re, im).
+inline void hermitize_env(Tensor& e) {
+  std::vector<double> out(e.data.size());
+  const auto& wleg = e.legs[1];
+  for (int64_t b = 0; b < e.nblk(); ++b) {
+    int64_t c0 = e.coords[b * 3], c1 = e.coords[b * 3 + 1], c2 = e.coords[b * 3 + 2];
+    int64_t p = find_block(e, {c2, wleg.nsct() - 1 - c1, c0});
+    if (p < 0) throw std::runtime_error("hermitize_env: partner block missing");
+    const int64_t d0 = e.blk_dim(b, 0), d1 = e.blk_dim(b, 1), d2 = e.blk_dim(b, 2);
+    const double* x = e.data.data() + 2 * e.offsets[b];
+    const double* y = e.data.data() + 2 * e.offsets[p];
+    double* o = out.data() + 2 * e.offsets[b];
+    for (int64_t i = 0; i < d0; ++i)
+      for (int64_t w = 0; w < d1; ++w)
+        for (int64_t j = 0; j < d2; ++j) {
+          const int64_t u = (i * d1 + w) * d2 + j, v = (j * d1 + w) * d0 + i;
+          o[2 * u] = 0.5 * (x[2 * u] + y[2 * v]);
+          o[2 * u + 1] = 0.5 * (x[2 * u + 1] - y[2 * v + 1]);
+        }
+  }
+  e.data.swap(out);
+}
+
+// Complex128 U(1) chain with a complex-Hermitian effective Hamiltonian (for the complex
+// Lanczos): N(0,1)+iN(0,1) psi and environments, environments made Hermitian per MPO
+// channel pair, the real Heisenberg MPO on both sites.
+inline Matvec heisenberg_u1_hermitian_complex(int qmax, double sigma, int64_t D, uint64_t seed) {
+  auto dims = gauss_dims(qmax, sigma, D);
+  Leg vin = make_u1_leg(-qmax, dims, DIR_IN);
+  Leg pin = make_u1_leg(0, {1, 1}, DIR_IN);
+  Leg min_ = make_u1_leg(-1, {1, 3, 1}, DIR_IN);
+  Matvec m;
+  m.psi = make_tensor({vin, pin, pin, vin.inverse()}, {0}, true);
+  m.lenv = make_tensor({vin.inverse(), min_, vin}, {0}, true);
+  m.mpo1 = make_tensor({min_.inverse(), pin.inverse(), pin, min_}, {0}, true);
+  m.renv = make_tensor({vin, min_.inverse(), vin.inverse()}, {0}, true);
+  Normal rng(seed);
+  fill_normal(m.psi, rng);
+  normalize(m.psi);
+  fill_normal(m.lenv, rng);
+  fill_normal(m.renv, rng);
+  hermitize_env(m.lenv);
+  hermitize_env(m.renv);
   fill_heisenberg_mpo(m.mpo1);
   m.mpo2 = m.mpo1;
   return m;

@@ -24,6 +24,7 @@ const char* qltg_synth_last_error(void) { return g_synth_err.c_str(); }
 //   "cfg1" (seed)                        -> A, B
 //   "matvec_u1" (qmax, sigma, D, seed)   -> lenv, psi, mpo1, mpo2, renv  (random operands)
 //   "matvec_u1h" (qmax, sigma, D, seed)  -> same, real-symmetric effective Hamiltonian
+//   "matvec_u1hc" (qmax, sigma, D, seed) -> same, complex128, complex-Hermitian H_eff
 //   "matvec_f" (half, D, seed)           -> same, fermionic U(1)xU(1) complex128
 //   "svd_u1" (qmax, sigma, D, seed)      -> T  (psi with a controlled block spectrum)
 //   "svd_stress" (nb, lo, hi, seed)      -> T  (rank-2 block-diagonal, sizes lo..hi)
@@ -37,10 +38,14 @@ void* qltg_synth_create(const char* kind, const double* p, int np) {
       need(1);
       auto pr = sy::config1((uint64_t)p[0]);
       w->tensors = {pr.a, pr.b};
-    } else if (k == "matvec_u1" || k == "matvec_u1h" || k == "matvec_f") {
+    } else if (k == "matvec_u1" || k == "matvec_u1h" || k == "matvec_u1hc" || k == "matvec_f") {
       sy::Matvec m;
       if (k == "matvec_u1") { need(4); m = sy::heisenberg_u1_random((int)p[0], p[1], (int64_t)p[2], (uint64_t)p[3]); }
       else if (k == "matvec_u1h") { need(4); m = sy::heisenberg_u1_hermitian((int)p[0], p[1], (int64_t)p[2], (uint64_t)p[3]); }
+      else if (k == "matvec_u1hc") {
+        need(4);
+        m = sy::heisenberg_u1_hermitian_complex((int)p[0], p[1], (int64_t)p[2], (uint64_t)p[3]);
+      }
       else { need(3); m = sy::hubbard_u1u1((int)p[0], (int64_t)p[1], (uint64_t)p[2]); }
       w->tensors = {m.lenv, m.psi, m.mpo1, m.mpo2, m.renv};
     } else if (k == "svd_u1") {

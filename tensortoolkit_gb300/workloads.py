@@ -73,6 +73,12 @@ def heisenberg(D: int, qmax: int, sigma: float, seed: int = 1, hermitian: bool =
     return generate("matvec_u1h" if hermitian else "matvec_u1", qmax, sigma, D, seed, lib=lib)
 
 
+def heisenberg_complex_hermitian(D: int, qmax: int, sigma: float, seed: int = 1):
+    """The U(1) two-site matvec in complex128 with a complex-Hermitian effective Hamiltonian
+    (environments E(a, w, a') = conj(E(a', wbar, a)), the Heisenberg MPO)."""
+    return generate("matvec_u1hc", qmax, sigma, D, seed)
+
+
 def hubbard(D: int, half: int = 10, seed: int = 4):
     """(lenv, psi, mpo1, mpo2, renv) of the fermionic U(1)xU(1) complex128 matvec."""
     return generate("matvec_f", half, D, seed)

@@ -32,3 +32,27 @@ def test_workload_symmetric_and_lanczos_converges():
     assert abs(r[-1] - e0) <= 1e-8 * abs(e0)
     G = V[:-1] @ V[:-1].T
     assert np.abs(G - np.eye(len(G))).max() <= 1e-12
+
+
+def test_complex_workload_hermitian_and_lanczos_converges():
+    """The complex128 U(1) workload's effective Hamiltonian is complex-Hermitian (with a
+    non-trivial imaginary part), and the complex CPU Lanczos reaches its lowest eigenvalue."""
+    lenv, psi, mpo1, mpo2, renv = workloads.heisenberg_complex_hermitian(24, 3, 1.5, 5)
+    ops = (lenv, mpo1, mpo2, renv)
+    n = psi.size
+    H = np.zeros((n, n), np.complex128)
+    for i in range(n):
+        e = np.zeros(n, np.complex128)
+        e[i] = 1.0
+        H[:, i] = oracle_apply(ops, psi, e)
+    assert np.abs(H - H.conj().T).max() <= 1e-12 * np.abs(H).max()
+    assert np.abs(H.imag).max() >= 0.1 * np.abs(H).max()
+    e0 = np.linalg.eigvalsh(H)[0]
+    r = np.random.default_rng(0)
+    x0 = r.standard_normal(n) + 1j * r.standard_normal(n)
+    a, b, V = lanczos(lambda x: oracle_apply(ops, psi, x), x0, min(60, n - 1))
+    rz = ritz_lowest(a, b)
+    assert np.all(np.diff(rz) <= 1e-10 * abs(e0))
+    assert abs(rz[-1] - e0) <= 1e-8 * abs(e0)
+    G = V[:-1].conj() @ V[:-1].T
+    assert np.abs(G - np.eye(len(G))).max() <= 1e-12
