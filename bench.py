@@ -235,6 +235,7 @@ def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
         eb = 16 if a_meta.is_complex else 8
         step_fb.append((p.stats()[0], (a_meta.size + b_meta.size + p.result.size) * eb))
         c = DTensor.empty(p.result, local)
+        p.tune(cur_a, bs[i], c, mode=mode)        # the matvec's own choice, from the tuner's cache
         p.execute(cur_a, bs[i], c, mode=mode)
         args = (p.h, C.c_void_p(cur_a.ptr), C.c_void_p(bs[i].ptr), C.c_void_p(c.ptr), mode_i)
         ms1 = _time_events(lambda: capi.check(lib.qltg_ctrct_exec_stage(*args, 1, sp)), stream, flush)
@@ -242,21 +243,16 @@ def gemm_roofline(mode, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
         ms3 = _time_events(lambda: capi.check(lib.qltg_ctrct_exec_stage(*args, 3, sp)), stream, flush)
         p.device_status()
         f, _ = p.stats()
-        tcf = 0.0
+        tcf, useful = 0.0, None
         if mode == "split":
-            cbs = {}
-            for (_, _, cidx, m, k, n, _, _) in p.tasks():
-                cbs.setdefault(int(cidx), [int(m), int(n), []])[2].append(int(k))
-            for m, n, ks in cbs.values():
-                if n <= 8 and max(ks) <= 8:
-                    continue            # skinny blocks stay on the FP64 pipe
-                tiles = -(-m // 128) * -(-n // 32)
-                stages = sum(-(-k // 32) for k in ks)
-                # 28 slice pairs on 128 x 32 x 32 padded tiles per 32-wide k stage
-                tcf += tiles * stages * 28 * (2 * 128 * 32 * 32)
+            # 28 slice pairs on 128 x 32 x 32 tile stages (padding included), as scheduled
+            stages, useful = p.split_stats()
+            tcf = stages * 28 * (2 * 128 * 32 * 32)
+        sch = p.schedule()
         per.append({"transpose_ms": round(ms1, 4), "stage_ms": round(ms2, 4), "kernel_ms": round(ms3, 4),
                     "gflop": round(f / 1e9, 4),
-                    "tensor_gflop": round(tcf / 1e9, 2)})
+                    "tensor_gflop": round(tcf / 1e9, 2), "useful_share": None if useful is None else round(useful, 4),
+                    "schedule": {"f64_tile_rows": sch["f64_tile_rows"], "split_stack": sch["split_stack"]}})
         stage_ms += ms2
         kern_ms += ms3
         alg_flops += f
@@ -460,6 +456,56 @@ def run_proxy(local: int, stream, flush, reps: int = 5) -> dict:
                     "anything, faster than the reference build)"}
 
 
+def run_adapter_costs(local: int) -> dict:
+    """What one qlten_gb300::Contract costs a caller at D=4000, by the C-ABI calls the adapter
+    makes (device buffers, as in a GPU build of qlten): a first call creates the plan (device
+    sector pairing, task list, transposes' work lists), tunes its schedule and executes; a
+    later call with the same layouts finds the plan in the context's cache and only executes.
+    Wall time on the host, the device synchronised at the end of each call."""
+    import torch
+    from tensortoolkit_gb300 import workloads
+    from tensortoolkit_gb300.api import ContractionPlan, DTensor, Contract
+    tensors = workloads.heisenberg(WORKLOAD["D"], WORKLOAD["qmax"], WORKLOAD["sigma"], WORKLOAD["seed"])
+    lenv, psi, mpo1, mpo2, renv = tensors
+    dl, dp, dr = (DTensor.from_host(x, local) for x in (lenv, psi, renv))
+    t1 = Contract(dl, dp, [[0], [0]])
+    t2 = Contract(t1, DTensor.from_host(mpo1, local), [[0, 2], [0, 1]])
+    t3 = Contract(t2, DTensor.from_host(mpo2, local), [[4, 1], [0, 1]])
+    out = {}
+    for name, a, b, axes in (("L.psi (step 0)", dl, dp, [[0], [0]]), ("t3.R (step 3)", t3, dr, [[4, 1], [1, 0]])):
+        row = {}
+        for mode in ("fp64", "split"):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            plan = ContractionPlan(a.meta, b.meta, axes, local)
+            t_plan = time.perf_counter() - t0
+            c = DTensor.empty(plan.result, local)
+            t0 = time.perf_counter()
+            plan.tune(a, b, c, mode=mode)
+            t_tune = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            plan.execute(a, b, c, mode=mode)
+            torch.cuda.synchronize()
+            t_first = time.perf_counter() - t0
+            ts = []
+            for _ in range(5):
+                t0 = time.perf_counter()
+                plan.execute(a, b, c, mode=mode)
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+            plan.device_status()
+            row[mode] = {"plan_create_ms": round(t_plan * 1e3, 3), "tune_ms": round(t_tune * 1e3, 3),
+                         "first_exec_ms": round(t_first * 1e3, 3),
+                         "cached_call_ms": round(statistics.median(ts) * 1e3, 3),
+                         "schedule": {k: v for k, v in plan.schedule().items() if k != "tuned_ms"}}
+            del plan, c
+        out[name] = row
+    out["note"] = ("C-ABI calls of the adapter's Contract: first call = plan create + tune + execute; cached call = "
+                   "execute on the context's cached plan (result topology export and the qlten-side block "
+                   "insertion are host bookkeeping not timed here)")
+    return out
+
+
 def run_aux(local: int, part: str = "all"):
     """Measurements beside the headline: the batched permute's achieved HBM bandwidth, the
     batched block SVD / QR (Config 3) against a per-block cuSOLVER loop on the same shapes
@@ -532,6 +578,7 @@ def run_aux(local: int, part: str = "all"):
         peak = fp64_peak_tflops(local, stream) if mode == "fp64" else pk["bf16_tflops"] / 28.0
         _, t_bound = matvec_step_bounds(tensors, local, peak, pk["hbm_gbs"])
         r = {"mode": mode, "ms": round(ms, 4), "gflops": f / (ms / 1e3) / 1e9, "plan_s": round(t_create, 3),
+             "schedules": mv.schedules(),
              "gflop_per_matvec": round(f / 1e9, 4), "peak_tflops": round(peak, 2),
              "sum_T_bound_ms": round(t_bound, 4), "frac_sum_T_over_t": round(t_bound / ms, 4)}
         if lanczos_steps:
@@ -561,6 +608,8 @@ def run_aux(local: int, part: str = "all"):
         return r
     if part in ("all", "proxy"):
         out["fp64_vs_reference_gpu_pattern_d4000"] = run_proxy(local, stream, flush)
+    if part in ("all", "adapter"):
+        out["adapter_contract_costs_d4000"] = run_adapter_costs(local)
     if part in ("all", "matvec"):
         c2 = workloads.heisenberg(2000, 20, 6.0, 1)
         out["config2_matvec_d2000"] = [mv_time(c2, "fp64"), mv_time(c2, "split")]
@@ -641,7 +690,7 @@ def main():
     ap.add_argument("--aux", action="store_true",
                     help="measurements beside the headline: permute GB/s, batched SVD/QR vs per-block, "
                          "Config 2 and Config 5 matvecs (one JSON line)")
-    ap.add_argument("--aux-part", choices=["all", "transpose", "svd", "matvec", "proxy"], default="all")
+    ap.add_argument("--aux-part", choices=["all", "transpose", "svd", "matvec", "proxy", "adapter"], default="all")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: plan the D=4000 matvec, apply it twice, print nothing else")
     args = ap.parse_args()
@@ -731,7 +780,7 @@ def main():
         roof = gemm_roofline(m, lenv, psi, d1, d2, dr, dl, dp, local, stream, flush, pk)
         roof["sum_T_over_t"] = roof["sum_T_bound_ms"] / (t_step * 1e3)
         results[m] = {"s_per_iter": t_step, "e2e_s_per_iter": e2e_step, "flops": flops,
-                      "launches_per_step": launches_per_step, "roofline": roof,
+                      "launches_per_step": launches_per_step, "roofline": roof, "schedules": mv.schedules(),
                       "h2d": int(h_in.numel() * 8), "d2h": int(h_out.numel() * 8)}
         del mv, out
 
@@ -771,13 +820,15 @@ def main():
             "gpu_launches": int(head["launches_per_step"] * args.steps),
             "gpu_launches_per_step": int(head["launches_per_step"]),
             "roofline": head["roofline"],
+            "tuned_schedules": head["schedules"],
             "cpu_baseline": cpu,
             "clocks": clk_summary,
         }
         if len(modes) > 1:
             f = results["fp64"]
             res["fp64"] = {"s_per_iter": f["s_per_iter"], "e2e_s_per_iter": f["e2e_s_per_iter"],
-                           "roofline": f["roofline"], "gpu_launches_per_step": int(f["launches_per_step"])}
+                           "roofline": f["roofline"], "gpu_launches_per_step": int(f["launches_per_step"]),
+                           "tuned_schedules": f["schedules"]}
             res["split_speedup_vs_fp64"] = f["s_per_iter"] / head["s_per_iter"]
             res["precision_study"] = precision_study(local)
         print(json.dumps(res))

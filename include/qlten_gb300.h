@@ -22,6 +22,11 @@
  * device memory and are passed straight through. With the CPU build they are staged
  * through device buffers (one copy in, one copy out per call).
  *
+ * Contract keeps its plans: the Context caches one plan per (A layout, B layout, axes) - the
+ * device pairing, task list, operand-transpose work lists and the GEMM schedule the tuner
+ * picked on the plan's first use - so the repeated contractions of a sweep pay the planning
+ * once.
+ *
  * Supported quantum numbers: U1QN, U1U1QN, fU1QN, fU1U1QN (integer-additive components;
  * the fermionic ones take their parity from the particle-number component).
  */
@@ -30,6 +35,8 @@
 
 #include <cuda_runtime.h>
 
+#include <deque>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -122,7 +129,11 @@ class DeviceView {
 #else
     if (bytes_) {
       if (cudaMalloc(&ptr_, bytes_) != cudaSuccess) throw std::runtime_error("qlten_gb300: cudaMalloc failed");
-      if (copy_in) cudaMemcpy(ptr_, bsdt.GetActualRawDataPtr(), bytes_, cudaMemcpyHostToDevice);
+      if (copy_in && cudaMemcpy(ptr_, bsdt.GetActualRawDataPtr(), bytes_, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(ptr_);
+        ptr_ = nullptr;
+        throw std::runtime_error("qlten_gb300: copy of a tensor to the device failed");
+      }
     }
 #endif
   }
@@ -136,7 +147,9 @@ class DeviceView {
   void* get() const { return ptr_; }
   void sync_back() {
 #ifndef USE_GPU
-    if (bytes_) cudaMemcpy(t_.GetBlkSparDataTen().GetActualRawDataPtr(), ptr_, bytes_, cudaMemcpyDeviceToHost);
+    if (bytes_ &&
+        cudaMemcpy(t_.GetBlkSparDataTen().GetActualRawDataPtr(), ptr_, bytes_, cudaMemcpyDeviceToHost) != cudaSuccess)
+      throw std::runtime_error("qlten_gb300: copy of a result to the host failed");
 #endif
   }
 
@@ -148,14 +161,70 @@ class DeviceView {
 
 class Context {
  public:
-  explicit Context(int device = 0) { check(qltg_create(device, &ctx_)); }
-  ~Context() { qltg_destroy(ctx_); }
+  // max_plans: contraction plans kept for reuse (oldest dropped first); autotune: time the
+  // candidate GEMM schedules on a plan's first use
+  explicit Context(int device = 0, size_t max_plans = 256, bool autotune = true)
+      : max_plans_(max_plans), autotune_(autotune) {
+    check(qltg_create(device, &ctx_));
+  }
+  ~Context() {
+    for (auto& kv : plans_) qltg_ctrct_plan_destroy(kv.second);
+    qltg_destroy(ctx_);
+  }
   Context(const Context&) = delete;
   Context& operator=(const Context&) = delete;
   qltg_ctx* get() const { return ctx_; }
+  bool autotune() const { return autotune_; }
+
+  // The cached plan of this (A layout, B layout, axes), or a new one (*fresh = true) that the
+  // cache now owns.
+  qltg_ctrct_plan* plan_for(const qltg_tensor_desc& a, const qltg_tensor_desc& b, const std::vector<int64_t>& axa,
+                            const std::vector<int64_t>& axb, bool* fresh) const {
+    std::vector<int64_t> key;
+    append(key, a);
+    append(key, b);
+    key.push_back((int64_t)axa.size());
+    key.insert(key.end(), axa.begin(), axa.end());
+    key.insert(key.end(), axb.begin(), axb.end());
+    auto it = plans_.find(key);
+    *fresh = it == plans_.end();
+    if (!*fresh) return it->second;
+    qltg_ctrct_plan* plan = nullptr;
+    check(qltg_ctrct_plan_create(ctx_, &a, &b, axa.data(), axb.data(), (int32_t)axa.size(), &plan));
+    if (max_plans_ && plans_.size() >= max_plans_) {
+      auto old = plans_.find(order_.front());
+      qltg_ctrct_plan_destroy(old->second);
+      plans_.erase(old);
+      order_.pop_front();
+    }
+    plans_.emplace(key, plan);
+    order_.push_back(key);
+    return plan;
+  }
+  size_t cached_plans() const { return plans_.size(); }
 
  private:
+  static void append(std::vector<int64_t>& k, const qltg_tensor_desc& d) {
+    k.push_back(d.rank);
+    k.push_back(d.dtype);
+    k.push_back(d.qn_ncomp);
+    k.push_back(d.parity_comp);
+    int64_t ts = 0;
+    for (int l = 0; l < d.rank; ++l) {
+      k.push_back(d.dirs[l]);
+      k.push_back(d.nsct[l]);
+      ts += d.nsct[l];
+    }
+    for (int64_t i = 0; i < ts * d.qn_ncomp; ++i) k.push_back(d.qns[i]);
+    k.insert(k.end(), d.dims, d.dims + ts);
+    k.push_back(d.nblk);
+    k.insert(k.end(), d.coords, d.coords + d.nblk * d.rank);
+  }
   qltg_ctx* ctx_ = nullptr;
+  size_t max_plans_;
+  bool autotune_;
+  mutable std::map<std::vector<int64_t>, qltg_ctrct_plan*> plans_;
+  mutable std::deque<std::vector<int64_t>> order_;
 };
 
 // ------------------------------------------------------------------ Contract
@@ -165,31 +234,26 @@ void Contract(const qlten::QLTensor<ElemT, QNT>* pa, const qlten::QLTensor<ElemT
               const Context& ctx, int mode = QLTG_MODE_FP64) {
   Desc<ElemT, QNT> da(*pa), db(*pb);
   std::vector<int64_t> axa(axes_set[0].begin(), axes_set[0].end()), axb(axes_set[1].begin(), axes_set[1].end());
-  qltg_ctrct_plan* plan = nullptr;
-  check(qltg_ctrct_plan_create(ctx.get(), &da.d, &db.d, axa.data(), axb.data(), (int32_t)axa.size(), &plan));
-  try {
-    // result legs: saved legs of A then saved legs of B (ten_ctrct.h:372-394)
-    auto saved = qlten::TenCtrctGenSavedAxesSet(pa->Rank(), pb->Rank(), axes_set);
-    qlten::TenCtrctInitResTen(pa, pb, saved, pc);
-    int32_t rank = 0;
-    int64_t nblk = 0, size = 0;
-    check(qltg_ctrct_plan_result(plan, &rank, &nblk, &size));
-    std::vector<int64_t> coords((size_t)nblk * rank);
-    check(qltg_ctrct_plan_result_blocks(plan, coords.data(), nullptr));
-    std::vector<qlten::CoorsT> blk_coors(nblk);
-    for (int64_t b = 0; b < nblk; ++b) blk_coors[b].assign(coords.begin() + b * rank, coords.begin() + (b + 1) * rank);
-    if (nblk) pc->GetBlkSparDataTen().DataBlksInsert(blk_coors, true, false);
-    auto& a = const_cast<qlten::QLTensor<ElemT, QNT>&>(*pa);
-    auto& b = const_cast<qlten::QLTensor<ElemT, QNT>&>(*pb);
-    DeviceView<ElemT, QNT> va(a, true), vb(b, true), vc(*pc, false);
-    check(qltg_ctrct_exec(plan, va.get(), vb.get(), vc.get(), mode, nullptr));
-    if (cudaStreamSynchronize(nullptr) != cudaSuccess) throw std::runtime_error("qlten_gb300: contraction failed");
-    vc.sync_back();
-  } catch (...) {
-    qltg_ctrct_plan_destroy(plan);
-    throw;
-  }
-  qltg_ctrct_plan_destroy(plan);
+  bool fresh = false;
+  qltg_ctrct_plan* plan = ctx.plan_for(da.d, db.d, axa, axb, &fresh);   // owned by the context
+  // result legs: saved legs of A then saved legs of B (ten_ctrct.h:372-394)
+  auto saved = qlten::TenCtrctGenSavedAxesSet(pa->Rank(), pb->Rank(), axes_set);
+  qlten::TenCtrctInitResTen(pa, pb, saved, pc);
+  int32_t rank = 0;
+  int64_t nblk = 0, size = 0;
+  check(qltg_ctrct_plan_result(plan, &rank, &nblk, &size));
+  std::vector<int64_t> coords((size_t)nblk * rank);
+  check(qltg_ctrct_plan_result_blocks(plan, coords.data(), nullptr));
+  std::vector<qlten::CoorsT> blk_coors(nblk);
+  for (int64_t b = 0; b < nblk; ++b) blk_coors[b].assign(coords.begin() + b * rank, coords.begin() + (b + 1) * rank);
+  if (nblk) pc->GetBlkSparDataTen().DataBlksInsert(blk_coors, true, false);
+  auto& a = const_cast<qlten::QLTensor<ElemT, QNT>&>(*pa);
+  auto& b = const_cast<qlten::QLTensor<ElemT, QNT>&>(*pb);
+  DeviceView<ElemT, QNT> va(a, true), vb(b, true), vc(*pc, false);
+  if (fresh && ctx.autotune() && size) check(qltg_ctrct_plan_tune(plan, va.get(), vb.get(), vc.get(), mode, nullptr, nullptr));
+  check(qltg_ctrct_exec(plan, va.get(), vb.get(), vc.get(), mode, nullptr));
+  if (cudaStreamSynchronize(nullptr) != cudaSuccess) throw std::runtime_error("qlten_gb300: contraction failed");
+  vc.sync_back();
 }
 
 // ------------------------------------------------------------------ SVD / QR

@@ -149,6 +149,32 @@ QLTG_API int qltg_ctrct_plan_device_status(qltg_ctrct_plan* plan, void* stream);
 
 QLTG_API int qltg_ctrct_plan_destroy(qltg_ctrct_plan* plan);
 
+/* Schedule of a plan's grouped GEMM stage. No counterpart in the reference, which issues one
+ * cublasDgemm per task (framework/hp_numeric/blas_level3.h:797-856) and has no schedule.
+ * f64_tile_rows: rows of the FP64 output tiles, 32 or 64 (x 32 columns); 0 keeps it.
+ * split_stack: split-precision row stacking (output blocks with the same task structure share
+ * 128-row tiles), 1 on, 0 off, -1 keeps it. Rebuilds the affected schedule (allocates and
+ * synchronises `stream`; not inside a stream capture). Results are the same under every
+ * schedule (to rounding). */
+QLTG_API int qltg_ctrct_plan_set_schedule(qltg_ctrct_plan* plan, int32_t f64_tile_rows, int32_t split_stack,
+                                          void* stream);
+/* The current schedule and, per mode (index QLTG_MODE_FP64 / QLTG_MODE_SPLIT), whether the
+ * tuner chose it (tuned[mode] = 1) and the GEMM-stage times it measured for the chosen and
+ * the slowest candidate (ms[2 mode], ms[2 mode + 1]). Any out-pointer may be NULL. */
+QLTG_API int qltg_ctrct_plan_get_schedule(const qltg_ctrct_plan* plan, int32_t* f64_tile_rows, int32_t* split_stack,
+                                          int32_t* tuned, float* ms);
+/* Autotune the schedule of `mode`: every candidate (FP64: 32 x 32 and 64 x 32 tiles; split:
+ * stacking on and off) runs on these operands (c_dev is overwritten), timed with CUDA events
+ * on `stream`, and the fastest is kept. The choice is cached per device and block-structure
+ * signature for the life of the process; a plan with the same signature takes it without
+ * timing (*from_cache = 1). Synchronises `stream`; not inside a stream capture. */
+QLTG_API int qltg_ctrct_plan_tune(qltg_ctrct_plan* plan, const void* a_dev, const void* b_dev, void* c_dev,
+                                  int32_t mode, void* stream, int32_t* from_cache);
+/* Executed tensor work of the plan's split-precision GEMM (after its first split-mode use):
+ * 128 x 32 output-tile stages of 32 k per launch, and the share of them that is not padding
+ * (m n k summed over tasks / (stages 128 32 32)). Zero before the split schedule exists. */
+QLTG_API int qltg_ctrct_plan_split_stats(const qltg_ctrct_plan* plan, int64_t* tile_stages, double* useful_frac);
+
 /* ------------------------------------------------ contiguous-axes contraction, accumulation */
 enum { QLTG_SIDE_HEAD = 0, QLTG_SIDE_TAIL = 1 };
 
@@ -356,6 +382,12 @@ QLTG_API int qltg_matvec_apply_host(qltg_matvec* mv, const void* psi_host, void*
 
 /* Device-side status of the four captured contractions (see qltg_ctrct_plan_device_status). */
 QLTG_API int qltg_matvec_device_status(qltg_matvec* mv, void* stream);
+
+/* The GEMM schedule the tuner chose for contraction `step` (0..3) of the matvec when it was
+ * created, as qltg_ctrct_plan_get_schedule reports it, and that step's split-precision tile
+ * stages and useful share (qltg_ctrct_plan_split_stats; zero in plain FP64 mode). */
+QLTG_API int qltg_matvec_schedule(const qltg_matvec* mv, int32_t step, int32_t* f64_tile_rows, int32_t* split_stack,
+                                  int32_t* tuned, float* ms, int64_t* tile_stages, double* useful_frac);
 
 QLTG_API int qltg_matvec_destroy(qltg_matvec* mv);
 

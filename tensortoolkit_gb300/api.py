@@ -8,7 +8,7 @@ here falls back to the CPU.
 from __future__ import annotations
 
 import ctypes as C
-from typing import Optional, Sequence, Tuple
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 import torch
@@ -163,6 +163,39 @@ class ContractionPlan:
 
     def device_status(self) -> None:
         check(lib().qltg_ctrct_plan_device_status(self.h, stream_ptr(self.device)))
+
+    def set_schedule(self, f64_tile_rows: int = 0, split_stack: int = -1) -> None:
+        """FP64 tile rows (32 or 64; 0 keeps) and split-precision row stacking (1 / 0; -1 keeps)."""
+        check(lib().qltg_ctrct_plan_set_schedule(self.h, int(f64_tile_rows), int(split_stack),
+                                                 stream_ptr(self.device)))
+
+    def schedule(self) -> dict:
+        """The current schedule, whether the tuner chose it per mode, and the GEMM-stage times
+        (ms) it measured for the chosen and the slowest candidate."""
+        rows, stack = C.c_int32(), C.c_int32()
+        tuned = np.zeros(2, np.int32)
+        ms = np.zeros(4, np.float32)
+        check(lib().qltg_ctrct_plan_get_schedule(self.h, C.byref(rows), C.byref(stack), tuned.ctypes.data,
+                                                 ms.ctypes.data))
+        return {"f64_tile_rows": rows.value, "split_stack": bool(stack.value),
+                "tuned": {"fp64": bool(tuned[0]), "split": bool(tuned[1])},
+                "tuned_ms": {"fp64": [float(ms[0]), float(ms[1])], "split": [float(ms[2]), float(ms[3])]}}
+
+    def split_stats(self) -> Tuple[int, float]:
+        """(128 x 32 x 32 tile stages per split GEMM launch, useful share of them)."""
+        n, f = C.c_int64(), C.c_double()
+        check(lib().qltg_ctrct_plan_split_stats(self.h, C.byref(n), C.byref(f)))
+        return n.value, f.value
+
+    def tune(self, a: "DTensor", b: "DTensor", out: Optional["DTensor"] = None, mode="fp64") -> bool:
+        """Autotune the GEMM schedule of `mode` on these operands (out is overwritten); returns
+        True when the choice came from the per-signature cache."""
+        if out is None:
+            out = DTensor.empty(self.result, self.device)
+        cached = C.c_int32()
+        check(lib().qltg_ctrct_plan_tune(self.h, C.c_void_p(a.ptr), C.c_void_p(b.ptr), C.c_void_p(out.ptr),
+                                         _mode(mode), stream_ptr(self.device), C.byref(cached)))
+        return bool(cached.value)
 
     def __del__(self):
         try:
@@ -754,6 +787,23 @@ class Matvec:
         f, n = C.c_double(), C.c_int64()
         check(lib().qltg_matvec_stats(self.h, C.byref(f), C.byref(n)))
         return f.value, n.value
+
+    def schedules(self) -> List[dict]:
+        """Per contraction step, the GEMM schedule the tuner chose at creation."""
+        out = []
+        for step in range(4):
+            rows, stack, st = C.c_int32(), C.c_int32(), C.c_int64()
+            tuned = np.zeros(2, np.int32)
+            ms = np.zeros(4, np.float32)
+            uf = C.c_double()
+            check(lib().qltg_matvec_schedule(self.h, step, C.byref(rows), C.byref(stack), tuned.ctypes.data,
+                                             ms.ctypes.data, C.byref(st), C.byref(uf)))
+            out.append({"f64_tile_rows": rows.value, "split_stack": bool(stack.value),
+                        "tuned": {"fp64": bool(tuned[0]), "split": bool(tuned[1])},
+                        "tuned_ms": {"fp64": [round(float(ms[0]), 4), round(float(ms[1]), 4)],
+                                     "split": [round(float(ms[2]), 4), round(float(ms[3]), 4)]},
+                        "split_tile_stages": st.value, "split_useful_frac": round(uf.value, 4)})
+        return out
 
     def apply(self, psi: DTensor, out: Optional[DTensor] = None) -> DTensor:
         if out is None:

@@ -73,6 +73,12 @@ _SIGS = {
     "qltg_qlten_read_data": ([_P, _P, C.c_int32, _P], C.c_int),
     "qltg_qlten_close": ([_P], C.c_int),
     "qltg_qlten_write": ([C.c_char_p, C.POINTER(TensorDesc), _P, C.c_int32, _P], C.c_int),
+    "qltg_ctrct_plan_set_schedule": ([_P, C.c_int32, C.c_int32, _P], C.c_int),
+    "qltg_ctrct_plan_get_schedule": ([_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P, _P], C.c_int),
+    "qltg_ctrct_plan_tune": ([_P, _P, _P, _P, C.c_int32, _P, C.POINTER(C.c_int32)], C.c_int),
+    "qltg_ctrct_plan_split_stats": ([_P, _I64P, C.POINTER(C.c_double)], C.c_int),
+    "qltg_matvec_schedule": ([_P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P, _P, _I64P,
+                              C.POINTER(C.c_double)], C.c_int),
     "qltg_transpose": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
     "qltg_transpose_noalloc": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),
     "qltg_transpose_plan_create": ([_P, C.POINTER(TensorDesc), _P, _P, C.POINTER(_P)], C.c_int),

@@ -259,6 +259,63 @@ int qltg_ctrct_plan_destroy(qltg_ctrct_plan* plan) {
   return QLTG_OK;
 }
 
+int qltg_ctrct_plan_set_schedule(qltg_ctrct_plan* plan, int32_t f64_tile_rows, int32_t split_stack, void* stream) {
+  return guarded([&] {
+    QLTG_CHECK(plan, QLTG_ERR_INVALID, "null plan");
+    QLTG_CHECK(f64_tile_rows == 0 || f64_tile_rows == 32 || f64_tile_rows == 64, QLTG_ERR_INVALID,
+               "f64_tile_rows must be 0, 32 or 64");
+    QLTG_CHECK(split_stack >= -1 && split_stack <= 1, QLTG_ERR_INVALID, "split_stack must be -1, 0 or 1");
+    QLTG_CUDA(cudaSetDevice(plan->p.ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    CtrctPlan& p = plan->p;
+    if (f64_tile_rows) set_f64_tile(p, f64_tile_rows, 32, s);
+    if (split_stack >= 0) {
+      TuneChoice c;
+      c.f64_bm = p.sched.bm;
+      c.split_stack = split_stack != 0;
+      if (p.split) apply_choice(p, QLTG_MODE_SPLIT, c, s);
+      else p.split_cfg.stack = c.split_stack;
+    }
+  });
+}
+
+int qltg_ctrct_plan_get_schedule(const qltg_ctrct_plan* plan, int32_t* f64_tile_rows, int32_t* split_stack,
+                                 int32_t* tuned, float* ms) {
+  return guarded([&] {
+    QLTG_CHECK(plan, QLTG_ERR_INVALID, "null plan");
+    const CtrctPlan& p = plan->p;
+    if (f64_tile_rows) *f64_tile_rows = p.sched.bm;
+    if (split_stack) *split_stack = p.split_cfg.stack ? 1 : 0;
+    for (int m = 0; m < 2; ++m) {
+      if (tuned) tuned[m] = p.is_tuned[m] ? 1 : 0;
+      if (ms) {
+        ms[2 * m] = p.tuned[m].ms;
+        ms[2 * m + 1] = p.tuned[m].other_ms;
+      }
+    }
+  });
+}
+
+int qltg_ctrct_plan_split_stats(const qltg_ctrct_plan* plan, int64_t* tile_stages, double* useful_frac) {
+  return guarded([&] {
+    QLTG_CHECK(plan, QLTG_ERR_INVALID, "null plan");
+    const bool has = plan->p.split && plan->p.split->built;
+    if (tile_stages) *tile_stages = has ? plan->p.split->tile_stages : 0;
+    if (useful_frac) *useful_frac = has ? plan->p.split->useful_frac : 0.0;
+  });
+}
+
+int qltg_ctrct_plan_tune(qltg_ctrct_plan* plan, const void* a_dev, const void* b_dev, void* c_dev, int32_t mode,
+                         void* stream, int32_t* from_cache) {
+  return guarded([&] {
+    QLTG_CHECK(plan && a_dev && b_dev && c_dev, QLTG_ERR_INVALID, "null plan or buffer");
+    QLTG_CUDA(cudaSetDevice(plan->p.ctx->device));
+    bool cached = false;
+    tune_plan(plan->p, a_dev, b_dev, c_dev, mode, static_cast<cudaStream_t>(stream), &cached);
+    if (from_cache) *from_cache = cached ? 1 : 0;
+  });
+}
+
 int qltg_transpose(qltg_ctx* ctx, const qltg_tensor_desc* a, const void* src_dev, const int32_t* perm,
                    void* dst_dev, void* stream) {
   return guarded([&] {

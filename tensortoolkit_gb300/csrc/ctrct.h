@@ -90,16 +90,27 @@ struct GemmSchedule {
 
 // Split-precision schedule (gemm_split.cu): operand blocks to slice and pack, per-task
 // packed-tile addresses, output tiles of 128 x 32.
+//
+// Row stacking: output blocks whose task lists pair the same B blocks with the same k and
+// signs (the blocks of one "stack") are computed as one taller GEMM - their A blocks are
+// packed one under the other into shared 128-row tiles (each A block at a row offset of a
+// stacked operand), and each output row of a tile finds its place in C through a row map.
+// Short blocks then share tiles instead of each padding its own to 128 rows.
 struct SplitOperand {
   int64_t src_off;        // element offset of the (transposed) FP64 block
-  int64_t pack_off;       // byte offset of its packed slice tiles
+  int64_t pack_off;       // byte offset of its packed slice tiles (A: of its stacked operand)
   int32_t rows, cols;     // A: m x k; B: k x n
   int32_t ktiles;         // 64-wide k tiles
   int32_t exp_off;        // offset of its row (A) / column (B) exponent fields
   int64_t chunk_begin;    // A: prefix over operands of 8-element chunks (row-scale kernel)
   int64_t pchunk_begin;   // A: prefix over operands of rows x ceil(cols / 16) (pack kernel)
   int32_t cplx;           // B: complex block read as its real 2k x 2n form
-  int32_t pad;
+  int32_t row_base;       // A: first row of this block in its stacked operand
+};
+// Schedule choices of one split-precision plan (picked by the tuner, or fixed).
+struct SplitConfig {
+  bool stack = true;      // row stacking of output blocks with the same task structure
+  int max_stack_rows = 4096;
 };
 struct SplitTask {
   int64_t a_pack, b_pack;
@@ -110,16 +121,18 @@ struct SplitTask {
 // One (output tile, task) step of the split GEMM; the steps of one CTA are contiguous, in
 // the order it processes them.
 struct SplitWork {
-  int64_t c_off;          // element offset of the output block
+  int64_t c_off;          // element offset of the first output block of the stack (reporting)
   int64_t a_pack, b_pack; // byte offsets of the operand blocks' packed slice tiles
-  int32_t m, n;           // output block shape
+  int32_t m, n;           // stacked output shape (rows of all blocks of the stack) x n
   int32_t a_exp, b_exp;   // exponent offsets of the operand blocks
   int32_t ktiles;         // 64-wide k tiles of the task
   int32_t k;              // contracted extent of the task
-  int16_t tm, tn;         // 128-row / 32-column tile of the output block
+  int16_t tm, tn;         // 128-row / 32-column tile of the stacked output
   int8_t sign;            // sign of the task
   uint8_t flags;          // bit 0: first task of the tile, bit 1: last task of the tile
-  uint8_t pad[10];
+  uint8_t pad0[2];
+  int32_t row_map;        // first entry of the stack's rows in the row map (C offset per row)
+  uint8_t pad[4];
 };
 static_assert(sizeof(SplitWork) == 64, "SplitWork is one 64-byte record");
 struct SplitPlan {
@@ -127,8 +140,11 @@ struct SplitPlan {
   bool a_static = false, b_static = false;   // operand packed once, unchanged afterwards
   bool a_ready = false, b_ready = false;
   std::vector<SplitOperand> a_ops, b_ops;
-  std::vector<SplitTask> tasks;   // indexed like GemmSchedule::task
-  std::vector<GemmTile> tiles;    // (output block, 128-row tile, 32-col tile), longest first
+  SplitConfig cfg;
+  std::vector<SplitTask> tasks;   // per stack, its task positions (stack_task0 offsets)
+  std::vector<int32_t> stack_task0, stack_m, stack_n, stack_rowmap, stack_cblk0;   // per stack
+  std::vector<int64_t> row_map;   // per stacked output row: its element offset in C
+  std::vector<GemmTile> tiles;    // (stack, 128-row tile, 32-col tile), longest first
   std::vector<SplitWork> work;    // per CTA: tiles blockIdx.x, + grid, ...; each its tasks
   std::vector<int32_t> work_off;  // grid + 1 offsets into work
   int grid = 0;
@@ -137,7 +153,10 @@ struct SplitPlan {
   int64_t n_a_chunks = 0, n_a_pchunks = 0, n_a_rows = 0;
   bool row_warp = false;          // A row scales one warp per row (long rows) or by chunks
   bool a_fields_external = false; // A row scales written by the kernel producing A (matvec)
-  DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_b_col_tiles;
+  DevBuf d_a_ops, d_b_ops, d_work, d_work_off, a_packed, b_packed, a_exps, b_exps, error, d_b_col_tiles, d_row_map;
+  // executed tensor work: 128 x 32 x 32 tile stages per launch, and the useful share of it
+  int64_t tile_stages = 0;
+  double useful_frac = 0.0;
   // a plan with skinny blocks and tiles runs the skinny kernel on a side stream (forked and
   // joined with events, capturable), beside the slicing kernels and the split GEMM
   cudaStream_t side = nullptr;
@@ -152,6 +171,14 @@ struct SplitPlan {
   }
   void build(const struct CtrctPlan& p, cudaStream_t s);
   int64_t launches() const;
+};
+
+// A schedule choice of the tuner (tune.cu): FP64 tile rows and split-precision row stacking,
+// with the timed GEMM stage of the chosen and of the slowest candidate.
+struct TuneChoice {
+  int f64_bm = 32;
+  bool split_stack = true;
+  float ms = 0.f, other_ms = 0.f;
 };
 
 struct CtrctPlan {
@@ -170,12 +197,21 @@ struct CtrctPlan {
   DevBuf a_t, b_t;             // transposed operand scratch
   GemmSchedule sched;
   std::unique_ptr<SplitPlan> split;   // built on first use of QLTG_MODE_SPLIT
+  SplitConfig split_cfg;              // schedule choices the split plan is built with
+  TuneChoice tuned[2];                // per mode (QLTG_MODE_FP64, QLTG_MODE_SPLIT): the tuner's choice
+  bool is_tuned[2] = {false, false};
   DevBuf d_fuse;                      // split mode: SkinnyFuse per output block, or empty
   int32_t* fuse_fields = nullptr;     // the field array those blocks fold into
   int64_t launches_per_exec = 0;
 };
 
 void plan_contraction(CtrctPlan& p, cudaStream_t s);
+// Schedule tuner (tune.cu): time the candidate GEMM schedules of `mode` on these operands
+// and keep the fastest (cached per block-structure signature); *cached = taken from cache.
+TuneChoice tune_plan(CtrctPlan& p, const void* a, const void* b, void* c, int mode, cudaStream_t s, bool* cached);
+void apply_choice(CtrctPlan& p, int mode, const TuneChoice& c, cudaStream_t s);
+uint64_t plan_signature(const CtrctPlan& p, int mode);
+void set_f64_tile(CtrctPlan& p, int bm, int bn, cudaStream_t s);
 // Grouped-GEMM schedule, operand transposes and device buffers of a planned contraction.
 void finalize_plan(CtrctPlan& p, cudaStream_t s);
 int64_t exec_launches_split(const CtrctPlan& p);

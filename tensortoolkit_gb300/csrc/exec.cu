@@ -7,19 +7,14 @@
 
 namespace qltg {
 
-void finalize_plan(CtrctPlan& p, cudaStream_t s) {
-  GemmSchedule& g = p.sched;
+// FP64 output tiles of g.bm x g.bn, longest first (the DFMA kernel takes them in this order).
+static void f64_tile_list(GemmSchedule& g) {
   g.tile.clear();
-  g.skinny.clear();
-  const int rows_per_item = skinny_rows_per_item();
   struct Cand { GemmTile t; int64_t cost; };
   std::vector<Cand> cands;
   for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q) {
     const GemmCBlk& cb = g.cblk[q];
-    if (skinny_cblk(g, q)) {
-      for (int32_t c = 0; c * (int64_t)rows_per_item < cb.m; ++c) g.skinny.push_back(GemmRowChunk{q, c});
-      continue;
-    }
+    if (skinny_cblk(g, q)) continue;
     int64_t ksum = 0;
     for (int32_t t = cb.t0; t < cb.t1; ++t) ksum += g.task[t].k;
     const int tm = (cb.m + g.bm - 1) / g.bm, tn = (cb.n + g.bn - 1) / g.bn;
@@ -33,6 +28,29 @@ void finalize_plan(CtrctPlan& p, cudaStream_t s) {
   std::stable_sort(cands.begin(), cands.end(), [](const Cand& x, const Cand& y) { return x.cost > y.cost; });
   g.tile.reserve(cands.size());
   for (auto& c : cands) g.tile.push_back(c.t);
+}
+
+void set_f64_tile(CtrctPlan& p, int bm, int bn, cudaStream_t s) {
+  QLTG_CHECK((bm == 32 && bn == 32) || (bm == 64 && bn == 32), QLTG_ERR_INVALID, "FP64 tiles are 32 x 32 or 64 x 32");
+  GemmSchedule& g = p.sched;
+  if (g.bm == bm && g.bn == bn && g.d_tile.get()) return;
+  g.bm = bm;
+  g.bn = bn;
+  f64_tile_list(g);
+  g.d_tile = upload(g.tile, s);
+  QLTG_CUDA(cudaStreamSynchronize(s));
+}
+
+void finalize_plan(CtrctPlan& p, cudaStream_t s) {
+  GemmSchedule& g = p.sched;
+  g.skinny.clear();
+  const int rows_per_item = skinny_rows_per_item();
+  for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q) {
+    const GemmCBlk& cb = g.cblk[q];
+    if (skinny_cblk(g, q))
+      for (int32_t c = 0; c * (int64_t)rows_per_item < cb.m; ++c) g.skinny.push_back(GemmRowChunk{q, c});
+  }
+  f64_tile_list(g);
   // Operand transposes. A task reads its operand block from the transposed scratch unless
   // (a) the permutation leaves the block's layout unchanged, or (b) it is a skinny task and
   // the block, read in place, is a strided matrix (rows and columns each one stride); such

@@ -35,8 +35,9 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
-#include <queue>
 #include <cstring>
+#include <map>
+#include <queue>
 
 #include "scaled_int.h"
 #include "split.h"
@@ -251,12 +252,15 @@ __global__ void __launch_bounds__(256) k_pack_a(const double* __restrict__ scr, 
     const int k0 = kp * 16;
     const int e = exp_of_field(__ldg(exps + o.exp_off + row));
     const double* src_row = operand_block(scr, src, o.src_off) + row * o.cols;
+    // the row's place in its stacked operand: 128-row tile vt, row vr inside it
+    const int vrow = o.row_base + (int)row;
+    const int vt = vrow / kTM, vr = vrow - vt * kTM;
     // tile layout [ks][slice][m_core][k_core][8 rows x 16 B]: the 7 slices of a 16-wide k
     // step are contiguous, so a 32-wide stage is one 56 KB copy
     const int kt = k0 / kTK, ks = (k0 % kTK) >> 4;
-    const int64_t tile = (int64_t)rt * o.ktiles + kt;
-    uint8_t* dst = pack + o.pack_off + tile * (int64_t)(kS * kATile) + (int64_t)ks * (kS * 4096) + (r >> 3) * 256 +
-                   (r & 7) * 16;
+    const int64_t tile = (int64_t)vt * o.ktiles + kt;
+    uint8_t* dst = pack + o.pack_off + tile * (int64_t)(kS * kATile) + (int64_t)ks * (kS * 4096) + (vr >> 3) * 256 +
+                   (vr & 7) * 16;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {   // k_core 0 and 1: the two 8-wide chunks of the step
       const int kb = k0 + 8 * half;
@@ -601,8 +605,8 @@ __device__ __forceinline__ void fold_sums(const long long (&z)[kDrainCols], int 
 __global__ void __launch_bounds__(kRoleThreads, 1)
     k_gemm_split(const SplitWork* __restrict__ items, const int32_t* __restrict__ item_off,
                  const uint8_t* __restrict__ apack, const uint8_t* __restrict__ bpack,
-                 const int32_t* __restrict__ aexp, const int32_t* __restrict__ bexp, double* __restrict__ C,
-                 int* __restrict__ err) {
+                 const int32_t* __restrict__ aexp, const int32_t* __restrict__ bexp,
+                 const int64_t* __restrict__ row_map, double* __restrict__ C, int* __restrict__ err) {
   extern __shared__ uint8_t smem_dyn[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
   __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], accf_bar[2], acce_bar[2], fin_bar;
@@ -776,7 +780,7 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
         tmem_ld16(tsum, v);
         asm volatile("tcgen05.wait::ld.sync.aligned;");
         if (row < w.m) {
-          double* out = C + w.c_off + (int64_t)row * w.n;
+          double* out = C + __ldg(row_map + w.row_map + row);
 #pragma unroll
           for (int c = 0; c < kDrainCols; ++c)
             if (col0 + c < w.n)
@@ -796,88 +800,219 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
 }  // namespace
 
 // ------------------------------------------------------------------ host side
+// Row tiles of every stack fit the 16-bit tile index of a work record.
+static bool rtiles_fit(const std::vector<int32_t>& m) {
+  for (const int32_t x : m)
+    if ((x + kTM - 1) / kTM > 32767) return false;
+  return true;
+}
+
 void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   built = false;
+  cfg = p.split_cfg;
   const GemmSchedule& g = p.sched;
-  // operand blocks used by non-skinny output blocks
-  std::vector<int32_t> a_of(p.a.nblk, -1), b_of(p.b.nblk, -1);
   a_ops.clear();
   b_ops.clear();
   tasks.clear();
   tiles.clear();
-  int64_t a_pack = 0, b_pack = 0, a_exp = 0, b_exp = 0, a_chunks = 0, a_pchunks = 0;
+  stack_task0.clear();
+  stack_m.clear();
+  stack_n.clear();
+  stack_rowmap.clear();
+  stack_cblk0.clear();
+  row_map.clear();
   auto a_index = [&](int64_t a_off) {   // block ordinal from its offset
     return (int64_t)(std::lower_bound(p.a.offsets.begin(), p.a.offsets.end(), a_off) - p.a.offsets.begin());
   };
   auto b_index = [&](int64_t b_off) {
     return (int64_t)(std::lower_bound(p.b.offsets.begin(), p.b.offsets.end(), b_off) - p.b.offsets.begin());
   };
-  tasks.resize(g.task.size());
   // complex operands as real ones: A (m x k complex) is the real m x 2k matrix of its
   // interleaved parts, C likewise m x 2n, and B becomes the real 2k x 2n matrix of 2 x 2
   // blocks [[Re, Im], [-Im, Re]] (built by the B slicing kernel), so C' = A' B'
   const int cw = p.a.dtype == QLTG_C128 ? 2 : 1;
   auto real_off = [cw](int64_t off) { return ((off & ~kFromSrc) * cw) | (off & kFromSrc); };
-  for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q) {
-    const GemmCBlk& cb = g.cblk[q];
-    if (skinny_cblk(g, q)) continue;
-    const int cn = cw * cb.n;
-    for (int32_t t = cb.t0; t < cb.t1; ++t) {
-      const GemmTask& gt = g.task[t];
-      const int64_t ia = a_index(gt.a_off & ~kFromSrc), ib = b_index(gt.b_off & ~kFromSrc);
-      const int k = cw * gt.k;
-      const int ktiles = (k + kTK - 1) / kTK;
-      if (a_of[ia] < 0) {
-        SplitOperand o{};
-        o.src_off = real_off(gt.a_off);
-        o.rows = cb.m;
-        o.cols = k;
-        o.ktiles = ktiles;
-        o.exp_off = (int32_t)a_exp;
-        o.pack_off = a_pack;
-        o.chunk_begin = a_chunks;
-        o.pchunk_begin = a_pchunks;
-        QLTG_CHECK((int64_t)cb.m * k < ((int64_t)1 << 31) - 8, QLTG_ERR_UNSUPPORTED, "operand block too large");
-        const int64_t rtiles = (cb.m + kTM - 1) / kTM;
-        a_exp += cb.m;
-        a_chunks += ((int64_t)cb.m * k + 7) / 8;
-        a_pchunks += (int64_t)cb.m * ((k + 15) / 16);
-        a_pack += rtiles * ktiles * kS * (int64_t)kATile;
-        a_of[ia] = (int32_t)a_ops.size();
-        a_ops.push_back(o);
+
+  // ---- stacks: output blocks with the same n and the same (B block, k, sign) task sequence.
+  // Within a stack, the A blocks of task position t form one stacked operand (rows in the
+  // stack's block order). An A block can sit in one stacked operand only (its slices are
+  // packed once), so a stack whose A blocks would also be stacked differently elsewhere is
+  // split back into single blocks, until every A block has one place.
+  std::vector<int32_t> cand;
+  for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q)
+    if (!skinny_cblk(g, q)) cand.push_back(q);
+  std::vector<std::vector<int32_t>> stacks;
+  if (cfg.stack) {
+    std::map<std::vector<int64_t>, int32_t> key_of;
+    for (const int32_t q : cand) {
+      const GemmCBlk& cb = g.cblk[q];
+      std::vector<int64_t> key{cb.n};
+      for (int32_t t = cb.t0; t < cb.t1; ++t) {
+        key.push_back(b_index(g.task[t].b_off & ~kFromSrc));
+        key.push_back(g.task[t].k);
+        key.push_back(g.task[t].sign);
       }
+      auto it = key_of.find(key);
+      if (it == key_of.end()) {
+        key_of.emplace(std::move(key), (int32_t)stacks.size());
+        stacks.push_back({q});
+      } else {
+        stacks[it->second].push_back(q);
+      }
+    }
+    // cap the rows of one stack (greedy in block order; equal keys split identically)
+    std::vector<std::vector<int32_t>> capped;
+    for (auto& st : stacks) {
+      std::vector<int32_t> cur;
+      int64_t rows = 0;
+      for (const int32_t q : st) {
+        if (!cur.empty() && rows + g.cblk[q].m > cfg.max_stack_rows) {
+          capped.push_back(cur);
+          cur.clear();
+          rows = 0;
+        }
+        cur.push_back(q);
+        rows += g.cblk[q].m;
+      }
+      if (!cur.empty()) capped.push_back(cur);
+    }
+    stacks.swap(capped);
+    // demote stacks whose A blocks have more than one stacked place, to a fixed point
+    for (bool changed = true; changed;) {
+      changed = false;
+      std::map<int64_t, std::vector<int64_t>> place;   // A block -> its stacked operand (A blocks)
+      std::vector<uint8_t> bad(stacks.size(), 0);
+      std::map<int64_t, std::vector<int32_t>> users;   // A block -> stacks using it
+      for (int32_t si = 0; si < (int32_t)stacks.size(); ++si) {
+        const auto& st = stacks[si];
+        const int32_t nt = g.cblk[st[0]].t1 - g.cblk[st[0]].t0;
+        for (int32_t pos = 0; pos < nt; ++pos) {
+          std::vector<int64_t> tuple;
+          for (const int32_t q : st) tuple.push_back(a_index(g.task[g.cblk[q].t0 + pos].a_off & ~kFromSrc));
+          for (const int64_t ia : tuple) {
+            users[ia].push_back(si);
+            auto it = place.find(ia);
+            if (it == place.end()) place.emplace(ia, tuple);
+            else if (it->second != tuple) bad[si] = 1;
+          }
+        }
+      }
+      // a conflict marks every stack that uses a conflicting block
+      for (auto& [ia, tuple] : place) {
+        bool conflict = false;
+        for (const int32_t si : users[ia]) conflict |= bad[si] != 0;
+        if (conflict)
+          for (const int32_t si : users[ia]) bad[si] = 1;
+      }
+      std::vector<std::vector<int32_t>> next;
+      for (int32_t si = 0; si < (int32_t)stacks.size(); ++si) {
+        if (bad[si] && stacks[si].size() > 1) {
+          changed = true;
+          for (const int32_t q : stacks[si]) next.push_back({q});
+        } else {
+          next.push_back(stacks[si]);
+        }
+      }
+      stacks.swap(next);
+    }
+  } else {
+    for (const int32_t q : cand) stacks.push_back({q});
+  }
+
+  // ---- stacked A operands (one per distinct tuple of A blocks), B operands per block
+  int64_t a_pack = 0, b_pack = 0, a_exp = 0, b_exp = 0, a_chunks = 0, a_pchunks = 0;
+  std::map<std::vector<int64_t>, std::pair<int64_t, int32_t>> stacked_op;   // tuple -> (pack, exp)
+  std::vector<int32_t> b_of(p.b.nblk, -1);
+  tile_stages = 0;
+  double useful = 0.0;
+  for (const auto& st : stacks) {
+    const GemmCBlk& c0 = g.cblk[st[0]];
+    const int32_t nt = c0.t1 - c0.t0;
+    int64_t m = 0;
+    for (const int32_t q : st) m += g.cblk[q].m;
+    QLTG_CHECK(m < ((int64_t)1 << 22), QLTG_ERR_UNSUPPORTED, "stacked output too tall");
+    const int cn = cw * c0.n;
+    stack_cblk0.push_back(st[0]);
+    stack_task0.push_back((int32_t)tasks.size());
+    stack_m.push_back((int32_t)m);
+    stack_n.push_back(cn);
+    stack_rowmap.push_back((int32_t)row_map.size());
+    QLTG_CHECK(row_map.size() + (size_t)m < ((size_t)1 << 31), QLTG_ERR_UNSUPPORTED, "too many stacked rows");
+    for (const int32_t q : st) {
+      const GemmCBlk& cb = g.cblk[q];
+      for (int32_t r = 0; r < cb.m; ++r) row_map.push_back(cw * cb.c_off + (int64_t)r * cn);
+    }
+    const int64_t rtiles = (m + kTM - 1) / kTM, ctiles = (cn + kTN - 1) / kTN;
+    for (int32_t pos = 0; pos < nt; ++pos) {
+      const GemmTask& gt0 = g.task[c0.t0 + pos];
+      const int k = cw * gt0.k;
+      const int ktiles = (k + kTK - 1) / kTK;
+      std::vector<int64_t> tuple;
+      for (const int32_t q : st) tuple.push_back(a_index(g.task[g.cblk[q].t0 + pos].a_off & ~kFromSrc));
+      auto it = stacked_op.find(tuple);
+      if (it == stacked_op.end()) {
+        const std::pair<int64_t, int32_t> where{a_pack, (int32_t)a_exp};
+        int32_t row_base = 0;
+        for (size_t i = 0; i < st.size(); ++i) {
+          const GemmCBlk& cb = g.cblk[st[i]];
+          const GemmTask& gt = g.task[cb.t0 + pos];
+          QLTG_CHECK((int64_t)cb.m * k < ((int64_t)1 << 31) - 8, QLTG_ERR_UNSUPPORTED, "operand block too large");
+          SplitOperand o{};
+          o.src_off = real_off(gt.a_off);
+          o.rows = cb.m;
+          o.cols = k;
+          o.ktiles = ktiles;
+          o.exp_off = (int32_t)(a_exp + row_base);
+          o.pack_off = a_pack;
+          o.chunk_begin = a_chunks;
+          o.pchunk_begin = a_pchunks;
+          o.row_base = row_base;
+          a_chunks += ((int64_t)cb.m * k + 7) / 8;
+          a_pchunks += (int64_t)cb.m * ((k + 15) / 16);
+          row_base += cb.m;
+          a_ops.push_back(o);
+        }
+        a_exp += m;
+        a_pack += rtiles * ktiles * kS * (int64_t)kATile;
+        it = stacked_op.emplace(tuple, where).first;
+      }
+      const int64_t ib = b_index(gt0.b_off & ~kFromSrc);
       if (b_of[ib] < 0) {
         SplitOperand o{};
-        o.src_off = real_off(gt.b_off);
+        o.src_off = real_off(gt0.b_off);
         o.rows = k;
         o.cols = cn;
         o.ktiles = ktiles;
         o.exp_off = (int32_t)b_exp;
         o.pack_off = b_pack;
         o.cplx = cw == 2 ? 1 : 0;
-        const int64_t ctiles = (cn + kTN - 1) / kTN;
         b_exp += cn;
         b_pack += ctiles * ktiles * kS * (int64_t)kBTile;
         b_of[ib] = (int32_t)b_ops.size();
         b_ops.push_back(o);
       }
-      const SplitOperand& oa = a_ops[a_of[ia]];
       const SplitOperand& ob = b_ops[b_of[ib]];
-      QLTG_CHECK(oa.rows == cb.m && oa.cols == k && ob.rows == k && ob.cols == cn, QLTG_ERR_INVALID,
-                 "internal: inconsistent operand shapes in the split schedule");
-      tasks[t] = SplitTask{oa.pack_off, ob.pack_off, oa.exp_off, ob.exp_off, ktiles, gt.sign};
+      QLTG_CHECK(ob.rows == k && ob.cols == cn, QLTG_ERR_INVALID, "internal: inconsistent operand shapes in the split schedule");
+      tasks.push_back(SplitTask{it->second.first, ob.pack_off, it->second.second, ob.exp_off, ktiles, gt0.sign});
+      tile_stages += rtiles * ctiles * ((k + kKS - 1) / kKS);
+      useful += (double)m * cn * k;
     }
-    const int rtiles = (cb.m + kTM - 1) / kTM, ctiles = (cn + kTN - 1) / kTN;
-    for (int i = 0; i < rtiles; ++i)
-      for (int j = 0; j < ctiles; ++j) tiles.push_back(GemmTile{q, (int16_t)i, (int16_t)j});
+    for (int64_t i = 0; i < rtiles; ++i)
+      for (int64_t j = 0; j < ctiles; ++j)
+        tiles.push_back(GemmTile{(int32_t)(stack_m.size() - 1), (int16_t)i, (int16_t)j});
   }
+  useful_frac = tile_stages ? useful / ((double)tile_stages * kTM * kTN * kKS) : 0.0;
   QLTG_CHECK(tiles.size() < ((size_t)1 << 31), QLTG_ERR_UNSUPPORTED, "too many split tiles");
+  QLTG_CHECK(rtiles_fit(stack_m), QLTG_ERR_UNSUPPORTED, "stacked output has too many row tiles");
   // Per-CTA work lists by longest processing time first: tiles in decreasing cost, each to
   // the CTA with the least work so far. Cost of a tile: 2 per 32-wide k stage plus 1 per
   // task (the drain and rounding that end a task).
-  std::vector<int64_t> cost(g.cblk.size(), 0);
-  for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q)
-    for (int32_t t = g.cblk[q].t0; t < g.cblk[q].t1; ++t) cost[q] += 2 * ((cw * g.task[t].k + 31) / 32) + 1;
+  const int32_t nstacks = (int32_t)stack_m.size();
+  std::vector<int64_t> cost(nstacks, 0);
+  for (int32_t si = 0; si < nstacks; ++si) {
+    const GemmCBlk& c0 = g.cblk[stack_cblk0[si]];
+    for (int32_t t = c0.t0; t < c0.t1; ++t) cost[si] += 2 * ((cw * g.task[t].k + 31) / 32) + 1;
+  }
   std::stable_sort(tiles.begin(), tiles.end(), [&](const GemmTile& x, const GemmTile& y) { return cost[x.cblk] > cost[y.cblk]; });
   grid = (int)std::min<int64_t>((int64_t)tiles.size(), std::max(1, p.ctx->num_sms));
   std::vector<std::vector<int32_t>> owned(grid);
@@ -899,23 +1034,26 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
     work_off[b] = (int32_t)work.size();
     for (const int32_t ti : owned[b]) {
       const GemmTile& tl = tiles[ti];
-      const GemmCBlk& cb = g.cblk[tl.cblk];
-      for (int32_t t = cb.t0; t < cb.t1; ++t) {
-        const SplitTask& tk = tasks[t];
+      const int32_t si = tl.cblk;
+      const GemmCBlk& c0 = g.cblk[stack_cblk0[si]];
+      const int32_t nt = c0.t1 - c0.t0;
+      for (int32_t pos = 0; pos < nt; ++pos) {
+        const SplitTask& tk = tasks[stack_task0[si] + pos];
         SplitWork w{};
-        w.c_off = cw * cb.c_off;
+        w.c_off = cw * c0.c_off;
         w.a_pack = tk.a_pack;
         w.b_pack = tk.b_pack;
-        w.m = cb.m;
-        w.n = cw * cb.n;
+        w.m = stack_m[si];
+        w.n = stack_n[si];
         w.a_exp = tk.a_exp;
         w.b_exp = tk.b_exp;
         w.ktiles = tk.ktiles;
-        w.k = cw * g.task[t].k;
+        w.k = cw * g.task[c0.t0 + pos].k;
         w.tm = tl.tm;
         w.tn = tl.tn;
         w.sign = (int8_t)(tk.sign < 0 ? -1 : 1);
-        w.flags = (uint8_t)((t == cb.t0 ? 1 : 0) | (t + 1 == cb.t1 ? 2 : 0));
+        w.flags = (uint8_t)((pos == 0 ? 1 : 0) | (pos + 1 == nt ? 2 : 0));
+        w.row_map = stack_rowmap[si];
         work.push_back(w);
       }
     }
@@ -955,6 +1093,7 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
   d_b_ops = upload(b_ops, s);
   d_work = upload(work, s);
   d_work_off = upload(work_off, s);
+  d_row_map = upload(row_map, s);
   a_packed.alloc(std::max<int64_t>(a_pack, 16));
   b_packed.alloc(std::max<int64_t>(b_pack, 16));
   // tile padding (rows or columns past the block, k past the task) stays zero: the pack
@@ -1085,7 +1224,7 @@ void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s
   }
   k_gemm_split<<<sp.grid, kRoleThreads, kSmemBytes, s>>>(
       sp.d_work.as<SplitWork>(), sp.d_work_off.as<int32_t>(), sp.a_packed.as<uint8_t>(), sp.b_packed.as<uint8_t>(),
-      sp.a_exps.as<int32_t>(), sp.b_exps.as<int32_t>(),
+      sp.a_exps.as<int32_t>(), sp.b_exps.as<int32_t>(), sp.d_row_map.as<int64_t>(),
       static_cast<double*>(c), sp.error.as<int>());
   QLTG_CUDA(cudaGetLastError());
 }

@@ -87,6 +87,23 @@ int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* 
       p.axb.assign(ax[i][1], ax[i][1] + nax[i]);
       plan_contraction(p, s);
       finalize_plan(p, s);
+      if (i < 3) {
+        h->t[i].alloc(std::max<int64_t>(1, p.c.size) * p.c.elem_bytes());
+        QLTG_CUDA(cudaMemsetAsync(h->t[i].get(), 0, std::max<int64_t>(1, p.c.size) * p.c.elem_bytes(), s));
+      }
+      {
+        // the GEMM schedule of this step from the tuner, timed on the step's own operands
+        // (psi and the result as zero-filled scratch; t0..t2 hold the earlier steps' output)
+        if (i == 0) {
+          h->psi_stage.alloc(std::max<int64_t>(1, mp.size) * mp.elem_bytes());
+          QLTG_CUDA(cudaMemsetAsync(h->psi_stage.get(), 0, std::max<int64_t>(1, mp.size) * mp.elem_bytes(), s));
+        }
+        if (i == 3) h->out_stage.alloc(std::max<int64_t>(1, p.c.size) * p.c.elem_bytes());
+        const void* ta = i == 0 ? h->lenv : h->t[i - 1].get();
+        const void* tb = i == 0 ? h->psi_stage.get() : (i == 1 ? h->mpo1 : (i == 2 ? h->mpo2 : h->renv));
+        void* tc = i < 3 ? h->t[i].get() : h->out_stage.get();
+        tune_plan(p, ta, tb, tc, mode, s, nullptr);
+      }
       if (mode == QLTG_MODE_SPLIT) {
         prepare_split(p, s);
         // lenv (A of the first step), the MPO tensors and renv (B of the later steps) are
@@ -96,7 +113,6 @@ int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* 
         if (i == 2) split_prepack_static(p, nullptr, h->mpo2, s);
         if (i == 3) split_prepack_static(p, nullptr, h->renv, s);
       }
-      if (i < 3) h->t[i].alloc(std::max<int64_t>(1, p.c.size) * p.c.elem_bytes());
     }
     if (mode == QLTG_MODE_SPLIT) link_row_fields(*h, s);
     *mv = h.release();
@@ -115,6 +131,27 @@ int qltg_matvec_result_blocks(const qltg_matvec* mv, int64_t* coords, int64_t* o
   return guarded([&] {
     QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
     mv->step[3].c.export_arrays(nullptr, nullptr, nullptr, nullptr, coords, offsets);
+  });
+}
+
+int qltg_matvec_schedule(const qltg_matvec* mv, int32_t step, int32_t* f64_tile_rows, int32_t* split_stack,
+                         int32_t* tuned, float* ms, int64_t* tile_stages, double* useful_frac) {
+  return guarded([&] {
+    QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
+    QLTG_CHECK(step >= 0 && step < 4, QLTG_ERR_INVALID, "step must be 0 .. 3");
+    const CtrctPlan& p = mv->step[step];
+    if (f64_tile_rows) *f64_tile_rows = p.sched.bm;
+    if (split_stack) *split_stack = p.split_cfg.stack ? 1 : 0;
+    for (int m = 0; m < 2; ++m) {
+      if (tuned) tuned[m] = p.is_tuned[m] ? 1 : 0;
+      if (ms) {
+        ms[2 * m] = p.tuned[m].ms;
+        ms[2 * m + 1] = p.tuned[m].other_ms;
+      }
+    }
+    const bool has = p.split && p.split->built;
+    if (tile_stages) *tile_stages = has ? p.split->tile_stages : 0;
+    if (useful_frac) *useful_frac = has ? p.split->useful_frac : 0.0;
   });
 }
 
