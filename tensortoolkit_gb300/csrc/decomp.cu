@@ -383,6 +383,7 @@ struct QrJob {
   int64_t tau_off;
   int64_t q_off;     // m x k column-major Q
   int32_t m, n;
+  int64_t t_off;     // triangular factors of the panels' block reflectors, 32 x 32 each
 };
 
 template <typename T>
@@ -415,23 +416,71 @@ __device__ __forceinline__ T scaleT(T a, double s) {
   if constexpr (sizeof(T) == 8) return a * s; else return make_double2(a.x * s, a.y * s);
 }
 
-// LAPACK ?geqr2 + ?org2r restated (unblocked Householder), one CTA per block-matrix:
-// reflector j: beta = -sign(Re alpha) * ||(alpha, x)||, tau = (beta - alpha) / beta,
-// v = x / (alpha - beta); R(j,j) = beta; Q = H_1 ... H_k applied to the first k columns of I.
+// ------------------------------------------------------------------ blocked Householder QR
+// LAPACK's Householder QR (?geqrf / ?ungqr) restated in panels of kQrNb columns. Reflector
+// j: beta = -sign(Re alpha) ||(alpha, x)||, tau = (beta - alpha) / beta, v = x / (alpha -
+// beta), R(j, j) = beta (LAPACK's ?larfg convention, so Q and R compare directly with
+// ?geqrf + ?orgqr). A panel is factorised by one CTA column by column (reflectors applied
+// inside the panel only), which then forms the triangular factor T of the panel's block
+// reflector H = H_j0 ... H_j0+nb-1 = I - V T V^H (?larft, forward, columnwise). The rest of
+// the matrix is updated by many CTAs at once, one per 32-column tile of every group:
+// A_tile -= V T^H (V^H A_tile). Q is formed backwards over the panels the same way, with
+// Q_tile -= V T (V^H Q_tile) on the columns j0 .. k-1 of Q = I(:, 0:k). A large group thus
+// spreads its O(m n^2) work over as many SMs as it has column tiles, instead of one.
+constexpr int kQrNb = 32;   // panel width
+// rows per shared-memory chunk of the update kernel (its three 32-column buffers stay within
+// the 48 KB of static shared memory)
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_householder(const QrJob* __restrict__ jobs, T* __restrict__ as,
-                                                          T* __restrict__ taus, T* __restrict__ qs) {
+constexpr int qr_rows_per_chunk() { return sizeof(T) == 8 ? 64 : 16; }
+
+struct QrTile {
+  int32_t job, c0;          // 32-column tile starting at column c0
+};
+
+template <typename T>
+__device__ __forceinline__ T addT(T a, T b) {
+  if constexpr (sizeof(T) == 8) return a + b; else return make_double2(a.x + b.x, a.y + b.y);
+}
+template <typename T>
+__device__ __forceinline__ T fmaT(T a, T b, T c) {   // a b + c
+  if constexpr (sizeof(T) == 8) return fma(a, b, c);
+  else return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+template <typename T>
+__device__ __forceinline__ T fma_conj(T a, T b, T c) {   // conj(a) b + c
+  if constexpr (sizeof(T) == 8) return fma(a, b, c);
+  else return make_double2(fma(a.x, b.x, fma(a.y, b.y, c.x)), fma(a.x, b.y, fma(-a.y, b.x, c.y)));
+}
+template <typename T>
+__device__ __forceinline__ T zeroT() {
+  if constexpr (sizeof(T) == 8) return 0.0; else return make_double2(0.0, 0.0);
+}
+
+// Element (r, l) of panel j0's reflector block V: 1 on its diagonal, the stored reflector
+// below it, 0 above.
+template <typename T>
+__device__ __forceinline__ T v_elem(const T* __restrict__ A, int m, int j0, int nbe, int r, int l) {
+  if (l >= nbe || r >= m) return zeroT<T>();
+  const int d = j0 + l;
+  if (r == d) return mk<T>(1.0, 0.0);
+  return r > d ? A[(int64_t)d * m + r] : zeroT<T>();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_qr_panel(const QrJob* __restrict__ jobs, int j0, T* __restrict__ as,
+                                                       T* __restrict__ taus, T* __restrict__ tfac) {
   const QrJob jb = jobs[blockIdx.x];
+  const int m = jb.m, n = jb.n, k = min(m, n);
+  if (j0 >= k) return;
+  const int nbe = min(kQrNb, k - j0);
   T* A = as + jb.a_off;
   T* tau = taus + jb.tau_off;
-  T* Q = qs + jb.q_off;
-  const int m = jb.m, n = jb.n, k = min(m, n);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __shared__ double red[kWarps];
   __shared__ T s_tau, s_scale;
-  for (int j = 0; j < k; ++j) {
+  __shared__ T sY[kQrNb][kQrNb + 1], sT[kQrNb][kQrNb + 1];
+  for (int j = j0; j < j0 + nbe; ++j) {
     T* col = A + (int64_t)j * m;
-    // ||x||^2 over rows j+1..m-1
     double part = 0;
     for (int r = j + 1 + threadIdx.x; r < m; r += kThreads) part += abs2(col[r]);
     part = warp_sum(part);
@@ -449,7 +498,6 @@ __global__ void __launch_bounds__(kThreads) k_householder(const QrJob* __restric
         const double nrm = sqrt(ar * ar + ai * ai + xn2);
         const double beta = ar >= 0 ? -nrm : nrm;
         s_tau = mk<T>((beta - ar) / beta, -ai / beta);
-        // scale = 1 / (alpha - beta)
         const double dr = ar - beta, di = ai;
         const double den = dr * dr + di * di;
         s_scale = mk<T>(dr / den, -di / den);
@@ -461,11 +509,10 @@ __global__ void __launch_bounds__(kThreads) k_householder(const QrJob* __restric
     const T sc = s_scale;
     for (int r = j + 1 + threadIdx.x; r < m; r += kThreads) col[r] = mulT(col[r], sc);
     __syncthreads();
-    // apply H = I - tau v v^H (v = [1; col[j+1:]]) to columns j+1..n-1 from the left:
-    // a_c -= tau^H ... LAPACK applies H^H = I - conj(tau) v v^H for geqr2
+    // H_j^H on the panel's later columns only (the rest waits for the block update)
     const T tconj = conjT(s_tau);
     if (re_of(s_tau) != 0.0 || im_of(s_tau) != 0.0) {
-      for (int c = j + 1 + warp; c < n; c += kWarps) {
+      for (int c = j + 1 + warp; c < j0 + nbe; c += kWarps) {
         T* ac = A + (int64_t)c * m;
         double wr = 0, wi = 0;
         for (int r = j + lane; r < m; r += 32) {
@@ -485,34 +532,133 @@ __global__ void __launch_bounds__(kThreads) k_householder(const QrJob* __restric
     }
     __syncthreads();
   }
-  // Q: start from the first k columns of I, apply H_j for j = k-1 .. 0 (?org2r)
-  for (int64_t e = threadIdx.x; e < (int64_t)m * k; e += kThreads) {
-    const int64_t c = e / m, r = e % m;
-    Q[e] = mk<T>(r == c ? 1.0 : 0.0, 0.0);
+  // T: y(l, i) = v_l^H v_i for l < i (v_i starts at row j0 + i with a 1)
+  for (int i = 1; i < nbe; ++i) {
+    const T* vi = A + (int64_t)(j0 + i) * m;
+    for (int l = warp; l < i; l += kWarps) {
+      const T* vl = A + (int64_t)(j0 + l) * m;
+      T acc = zeroT<T>();
+      for (int r = j0 + i + 1 + lane; r < m; r += 32) acc = fma_conj(vl[r], vi[r], acc);
+      double ar = warp_sum(re_of(acc)), ai = warp_sum(im_of(acc));
+      if (lane == 0) sY[l][i] = addT(mk<T>(ar, ai), conjT(vl[j0 + i]));
+    }
   }
   __syncthreads();
-  for (int j = k - 1; j >= 0; --j) {
-    const T* col = A + (int64_t)j * m;
-    const T tj = tau[j];
-    if (re_of(tj) == 0.0 && im_of(tj) == 0.0) continue;
-    for (int c = j + warp; c < k; c += kWarps) {
-      T* qc = Q + (int64_t)c * m;
-      double wr = 0, wi = 0;
-      for (int r = j + lane; r < m; r += 32) {
-        const T v = (r == j) ? mk<T>(1.0, 0.0) : col[r];
-        const T prod = mulT(conjT(v), qc[r]);
-        wr += re_of(prod);
-        wi += im_of(prod);
-      }
-      wr = warp_sum(wr);
-      wi = warp_sum(wi);
-      const T w = mulT(tj, mk<T>(wr, wi));
-      for (int r = j + lane; r < m; r += 32) {
-        const T v = (r == j) ? mk<T>(1.0, 0.0) : col[r];
-        qc[r] = subT(qc[r], mulT(v, w));
+  // column by column: T(i, i) = tau_i, T(0:i, i) = -tau_i T(0:i, 0:i) y(0:i, i)
+  for (int i = 0; i < nbe; ++i) {
+    const T ti = tau[j0 + i];
+    if (threadIdx.x < i) {
+      const int l = threadIdx.x;
+      T z = zeroT<T>();
+      for (int lp = l; lp < i; ++lp) z = fmaT(sT[l][lp], sY[lp][i], z);
+      sT[l][i] = mulT(mk<T>(-re_of(ti), -im_of(ti)), z);
+    } else if ((int)threadIdx.x == i) {
+      sT[i][i] = ti;
+    }
+    __syncthreads();
+  }
+  T* Tp = tfac + jb.t_off + (int64_t)(j0 / kQrNb) * kQrNb * kQrNb;
+  for (int e = threadIdx.x; e < kQrNb * kQrNb; e += kThreads) {
+    const int c = e / kQrNb, r = e % kQrNb;
+    Tp[e] = (r < nbe && c < nbe && r <= c) ? sT[r][c] : zeroT<T>();
+  }
+}
+
+// One 32-column tile of every group per CTA: X_tile -= V op(T) (V^H X_tile), op(T) = T^H for
+// the trailing update of A (FORM_Q false, X = A) and T for the backward formation of Q
+// (FORM_Q true, X = Q). Rows j0 .. m-1, streamed through shared memory kQrRc at a time.
+template <typename T, bool FORM_Q>
+__global__ void __launch_bounds__(kThreads) k_qr_update(const QrJob* __restrict__ jobs,
+                                                        const QrTile* __restrict__ tiles, int j0,
+                                                        const T* __restrict__ as, const T* __restrict__ tfac,
+                                                        T* __restrict__ xs) {
+  const QrTile tl = tiles[blockIdx.x];
+  const QrJob jb = jobs[tl.job];
+  const int m = jb.m, n = jb.n, k = min(m, n);
+  const int nbe = min(kQrNb, k - j0);
+  const T* A = as + jb.a_off;
+  T* X = FORM_Q ? xs + jb.q_off : xs + jb.a_off;
+  const int ncols = FORM_Q ? k : n;
+  const int c0 = tl.c0, nc = min(32, ncols - c0);
+  constexpr int kQrRc = qr_rows_per_chunk<T>();
+  __shared__ T sV[kQrRc][kQrNb + 1], sX[kQrRc][33], sW[kQrNb][33];
+  // T(r, c) of this panel, column-major 32 x 32 (read through the cache)
+  const T* Tp = tfac + jb.t_off + (int64_t)(j0 / kQrNb) * kQrNb * kQrNb;
+  const int l = threadIdx.x & 31, cg = threadIdx.x >> 5;   // W entries (l, cg + 8 u)
+  T acc[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) acc[u] = zeroT<T>();
+  auto load_v = [&](int r0) {
+    for (int e = threadIdx.x; e < kQrRc * kQrNb; e += kThreads) {
+      const int rr = e % kQrRc, ll = e / kQrRc;
+      sV[rr][ll] = v_elem(A, m, j0, nbe, r0 + rr, ll);
+    }
+  };
+  for (int r0 = j0; r0 < m; r0 += kQrRc) {
+    load_v(r0);
+    for (int e = threadIdx.x; e < kQrRc * 32; e += kThreads) {
+      const int rr = e % kQrRc, c = e / kQrRc;
+      sX[rr][c] = (r0 + rr < m && c < nc) ? X[(int64_t)(c0 + c) * m + r0 + rr] : zeroT<T>();
+    }
+    __syncthreads();
+    const int rn = min(kQrRc, m - r0);
+    for (int rr = 0; rr < rn; ++rr) {
+      const T v = sV[rr][l];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc[u] = fma_conj(v, sX[rr][cg + 8 * u], acc[u]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) sW[l][cg + 8 * u] = acc[u];
+  __syncthreads();
+  // W2 = T^H W (trailing update) or T W (Q), T upper triangular
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int c = cg + 8 * u;
+    T z = zeroT<T>();
+    if (FORM_Q) {
+      for (int lp = l; lp < kQrNb; ++lp) z = fmaT(__ldg(Tp + lp * kQrNb + l), sW[lp][c], z);
+    } else {
+      for (int lp = 0; lp <= l; ++lp) z = fma_conj(__ldg(Tp + l * kQrNb + lp), sW[lp][c], z);
+    }
+    acc[u] = z;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 4; ++u) sW[l][cg + 8 * u] = acc[u];
+  __syncthreads();
+  // X -= V W2
+  const int c = threadIdx.x & 31, rg = threadIdx.x >> 5;
+  for (int r0 = j0; r0 < m; r0 += kQrRc) {
+    load_v(r0);
+    __syncthreads();
+    if (c < nc) {
+      for (int rr = rg; rr < kQrRc; rr += kThreads / 32) {
+        const int r = r0 + rr;
+        if (r >= m) break;
+        T z = zeroT<T>();
+#pragma unroll 8
+        for (int ll = 0; ll < kQrNb; ++ll) z = fmaT(sV[rr][ll], sW[ll][c], z);
+        T* x = X + (int64_t)(c0 + c) * m + r;
+        *x = subT(*x, z);
       }
     }
     __syncthreads();
+  }
+}
+
+// Q = I(:, 0:k) for every job (the start of the backward formation).
+template <typename T>
+__global__ void k_qr_qinit(const QrJob* __restrict__ jobs, int njobs, T* __restrict__ qs) {
+  for (int g = blockIdx.y; g < njobs; g += gridDim.y) {
+    const QrJob jb = jobs[g];
+    const int k = min(jb.m, jb.n);
+    const int64_t tot = (int64_t)jb.m * k;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t c = e / jb.m, r = e % jb.m;
+      qs[jb.q_off + e] = mk<T>(r == c ? 1.0 : 0.0, 0.0);
+    }
   }
 }
 
@@ -600,6 +746,73 @@ int64_t block_of(const Meta& t, const std::vector<int64_t>& c) {
 
 unsigned grid_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)current_sm_count() * 16)); }
 
+// Blocked Householder QR of every job (A in place, tau, Q): per panel one factorisation
+// launch (one CTA per job) and one trailing-update launch over all jobs' column tiles; then
+// Q = I and one update launch per panel, last panel first. The jobs' t_off are assigned here.
+struct QrBuffers {
+  DevBuf jobs, tiles, tfac;
+};
+template <typename T>
+void launch_blocked_qr(std::vector<QrJob>& jobs, T* A, T* tau, T* Q, cudaStream_t s, QrBuffers& keep) {
+  const int ng = (int)jobs.size();
+  if (!ng) return;
+  int kmax = 0;
+  int64_t toff = 0;
+  for (auto& j : jobs) {
+    const int k = std::min(j.m, j.n);
+    kmax = std::max(kmax, k);
+    j.t_off = toff;
+    toff += (int64_t)((k + kQrNb - 1) / kQrNb) * kQrNb * kQrNb;
+  }
+  const int np = (kmax + kQrNb - 1) / kQrNb;
+  // tiles of panel p: trailing columns of A (p in [0, np)), then columns j0 .. k-1 of Q
+  std::vector<QrTile> tiles;
+  std::vector<int64_t> trail_begin(np + 1), q_begin(np + 1);
+  for (int p = 0; p < np; ++p) {
+    trail_begin[p] = (int64_t)tiles.size();
+    const int j0 = p * kQrNb;
+    for (int g = 0; g < ng; ++g) {
+      const int k = std::min(jobs[g].m, jobs[g].n);
+      if (j0 >= k) continue;
+      for (int c0 = j0 + std::min(kQrNb, k - j0); c0 < jobs[g].n; c0 += 32) tiles.push_back(QrTile{g, c0});
+    }
+  }
+  trail_begin[np] = (int64_t)tiles.size();
+  for (int p = 0; p < np; ++p) {
+    q_begin[p] = (int64_t)tiles.size();
+    const int j0 = p * kQrNb;
+    for (int g = 0; g < ng; ++g) {
+      const int k = std::min(jobs[g].m, jobs[g].n);
+      if (j0 >= k) continue;
+      for (int c0 = j0; c0 < k; c0 += 32) tiles.push_back(QrTile{g, c0});
+    }
+  }
+  q_begin[np] = (int64_t)tiles.size();
+  QLTG_CHECK(tiles.size() < ((size_t)1 << 31), QLTG_ERR_UNSUPPORTED, "too many QR tiles");
+  keep.jobs = upload(jobs, s);
+  keep.tiles = upload(tiles.empty() ? std::vector<QrTile>{QrTile{0, 0}} : tiles, s);
+  keep.tfac.alloc(std::max<int64_t>(1, toff) * sizeof(T));
+  const QrJob* dj = keep.jobs.as<QrJob>();
+  const QrTile* dt = keep.tiles.as<QrTile>();
+  T* tf = keep.tfac.as<T>();
+  for (int p = 0; p < np; ++p) {
+    const int j0 = p * kQrNb;
+    k_qr_panel<T><<<ng, kThreads, 0, s>>>(dj, j0, A, tau, tf);
+    const int64_t nt = trail_begin[p + 1] - trail_begin[p];
+    if (nt) k_qr_update<T, false><<<(unsigned)nt, kThreads, 0, s>>>(dj, dt + trail_begin[p], j0, A, tf, A);
+  }
+  const int64_t total_q = std::accumulate(jobs.begin(), jobs.end(), (int64_t)0, [](int64_t a, const QrJob& j) {
+    return std::max<int64_t>(a, (int64_t)j.m * std::min(j.m, j.n));
+  });
+  k_qr_qinit<T><<<dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>((total_q + 255) / 256, 64)),
+                       (unsigned)std::min(ng, 1024)), 256, 0, s>>>(dj, ng, Q);
+  for (int p = np - 1; p >= 0; --p) {
+    const int64_t nt = q_begin[p + 1] - q_begin[p];
+    if (nt) k_qr_update<T, true><<<(unsigned)nt, kThreads, 0, s>>>(dj, dt + q_begin[p], p * kQrNb, A, tf, Q);
+  }
+  QLTG_CUDA(cudaGetLastError());
+}
+
 template <typename T>
 void launch_gather(const std::vector<CopyDesc>& d, int64_t total, const void* src, void* dst, cudaStream_t s,
                    DevBuf& keep) {
@@ -639,7 +852,7 @@ namespace {
 
 
 // ---- QR preconditioning of the one-sided Jacobi (the Drmac-Veselic scheme, restated):
-// M = Q R (Householder, k_householder), Jacobi on X = R^H, then M = (Q J) S Xn^H with
+// M = Q R (blocked Householder), Jacobi on X = R^H, then M = (Q J) S Xn^H with
 // Xn the normalised columns of X and J the accumulated rotations. On graded spectra (the
 // decaying singular values of a DMRG bond) this cuts the sweeps from ~30 to ~8.
 struct PrecondJob {
@@ -778,9 +991,10 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   }
   DevBuf qbuf(std::max<int64_t>(1, qoff) * eb), taubuf(std::max<int64_t>(1, toff) * eb),
       jbuf(std::max<int64_t>(1, joff) * eb);
-  DevBuf d_qjobs = upload(qjobs, s), d_pre = upload(pre, s), d_qtiles = upload(qtiles, s);
+  DevBuf d_pre = upload(pre, s), d_qtiles = upload(qtiles, s);
+  QrBuffers qr_keep;
   if (ng) {
-    k_householder<T><<<ng, kThreads, 0, s>>>(d_qjobs.as<QrJob>(), ws.as<T>(), taubuf.as<T>(), qbuf.as<T>());
+    launch_blocked_qr<T>(qjobs, ws.as<T>(), taubuf.as<T>(), qbuf.as<T>(), s, qr_keep);
     k_r_to_x<T><<<ng, kThreads, 0, s>>>(d_pre.as<PrecondJob>(), ng, ws.as<T>(), ws.as<T>());
     QLTG_CUDA(cudaGetLastError());
   }
@@ -1055,11 +1269,8 @@ void qr_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int3
   DevBuf keep_g;
   if (aoff) QLTG_CUDA(cudaMemsetAsync(A.get(), 0, aoff * eb, s));
   launch_gather<T>(cd, eoff, t_dev, A.get(), s, keep_g);
-  DevBuf d_jobs = upload(jobs, s);
-  if (ng) {
-    k_householder<T><<<ng, kThreads, 0, s>>>(d_jobs.as<QrJob>(), A.as<T>(), tau.as<T>(), Qd.as<T>());
-    QLTG_CUDA(cudaGetLastError());
-  }
+  QrBuffers qr_keep;
+  if (ng) launch_blocked_qr<T>(jobs, A.as<T>(), tau.as<T>(), Qd.as<T>(), s, qr_keep);
   // result metadata (reference ten_qr.h:199-291): mid dim min(rows, cols) per group
   std::vector<int32_t> mid_q;
   std::vector<int64_t> mid_d;

@@ -41,6 +41,89 @@ __device__ __forceinline__ double flip(double x, unsigned long long m) {
 __device__ __forceinline__ double2 flip(double2 x, unsigned long long m) { return make_double2(flip(x.x, m), flip(x.y, m)); }
 __device__ __forceinline__ unsigned long long sign_mask(int sign) { return sign < 0 ? 0x8000000000000000ull : 0ull; }
 
+constexpr int BM = 32, BN = 32, BK = 32;
+
+// 32 x 32 output tiles (BM = BN = 32): one output tile per work item; 16 x 16 threads, each 2 x 2 outputs at
+// (ty + 16 i, tx + 16 j). Operand tiles are staged through shared memory (A transposed so
+// a warp reads one broadcast row); outputs outside the block are predicated off so no FP64
+// issue slot is spent on padding. Work items are taken longest-first from an atomic
+// counter (the plan zeroes it before each launch), so the few very long tiles start first
+// and the rest fill in behind them.
+template <typename T>
+__global__ void __launch_bounds__(NT) k_gemm_dfma32(const GemmCBlk* __restrict__ cblk, const GemmTask* __restrict__ task,
+                                                  const GemmTile* __restrict__ tiles, int ntiles,
+                                                  const T* __restrict__ A, const T* __restrict__ As,
+                                                  const T* __restrict__ B, const T* __restrict__ Bs,
+                                                  T* __restrict__ C, int* __restrict__ counter) {
+  __shared__ T sA[BK][BM + 1];
+  __shared__ T sB[BK][BN];
+  __shared__ int s_ti;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  while (true) {
+    if (threadIdx.x == 0) s_ti = atomicAdd(counter, 1);
+    __syncthreads();
+    const int ti = s_ti;
+    __syncthreads();
+    if (ti >= ntiles) break;
+    const GemmTile tl = tiles[ti];
+    const GemmCBlk cb = cblk[tl.cblk];
+    const int r0 = tl.tm * BM, c0 = tl.tn * BN;
+    const int m = cb.m, n = cb.n;
+    T acc[2][2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) acc[i][j] = zero_of(T());
+    bool rv[2], cv[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) { rv[i] = r0 + ty + 16 * i < m; cv[i] = c0 + tx + 16 * i < n; }
+    for (int t = cb.t0; t < cb.t1; ++t) {
+      const GemmTask tk = task[t];
+      const int k = tk.k;
+      const T* a = operand_block(A, As, tk.a_off);
+      const T* b = operand_block(B, Bs, tk.b_off);
+      const unsigned long long sg = sign_mask(tk.sign);
+      for (int k0 = 0; k0 < k; k0 += BK) {
+        const int kc = min(BK, k - k0);
+#pragma unroll
+        for (int e = threadIdx.x; e < BM * BK; e += NT) {
+          const int row = e / BK, kk = e % BK;
+          T v = zero_of(T());
+          if (kk < kc && r0 + row < m) v = flip(a[(int64_t)(r0 + row) * k + k0 + kk], sg);
+          sA[kk][row] = v;
+        }
+#pragma unroll
+        for (int e = threadIdx.x; e < BK * BN; e += NT) {
+          const int kk = e / BN, col = e % BN;
+          T v = zero_of(T());
+          if (kk < kc && c0 + col < n) v = b[(int64_t)(k0 + kk) * n + c0 + col];
+          sB[kk][col] = v;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < kc; ++kk) {
+          const T a0 = sA[kk][ty], a1 = sA[kk][ty + 16];
+          const T b0 = sB[kk][tx], b1 = sB[kk][tx + 16];
+          if (rv[0]) {
+            if (cv[0]) fma_acc(acc[0][0], a0, b0);
+            if (cv[1]) fma_acc(acc[0][1], a0, b1);
+          }
+          if (rv[1]) {
+            if (cv[0]) fma_acc(acc[1][0], a1, b0);
+            if (cv[1]) fma_acc(acc[1][1], a1, b1);
+          }
+        }
+        __syncthreads();
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j)
+        if (rv[i] && cv[j]) C[cb.c_off + (int64_t)(r0 + ty + 16 * i) * n + c0 + tx + 16 * j] = acc[i][j];
+  }
+}
+
 // k depth of one shared-memory stage: 32, or 16 where the two operand tiles would pass the
 // 48 KB of static shared memory (complex 64-row tiles).
 template <typename T, int BM, int BN>
@@ -51,9 +134,9 @@ constexpr int dfma_bk() { return (int)sizeof(T) * 32 * (BM + 1 + BN) <= 48 * 102
 // (A transposed so a warp reads one broadcast row); outputs outside the block are predicated
 // off so no FP64 issue slot is spent on padding. Work items are taken longest-first from an
 // atomic counter (the plan zeroes it before each launch), so the few very long tiles start
-// first and the rest fill in behind them. The tile shape is chosen per plan (32 x 32 or
-// 64 x 32: the larger tile reads each staged operand value for twice the FMAs, the smaller
-// one pads less on small blocks).
+// first and the rest fill in behind them. Used for 64 x 32 tiles (TM = 4, TN = 2): the
+// taller tile reads each staged operand value for twice the FMAs; the 32 x 32 tile above
+// pads less on small blocks. The tuner picks between them per plan.
 template <typename T, int TM, int TN>
 __global__ void __launch_bounds__(NT, TM * TN <= 4 ? 4 : 2) k_gemm_dfma(const GemmCBlk* __restrict__ cblk, const GemmTask* __restrict__ task,
                                                   const GemmTile* __restrict__ tiles, int ntiles,
@@ -317,10 +400,14 @@ void launch_dfma_tile(const GemmSchedule& g, const Operands& op, void* c, int gr
 
 template <typename T>
 void launch_dfma_t(const GemmSchedule& g, const Operands& op, void* c, int grid, cudaStream_t s) {
-  if (g.bm == 64)
+  if (g.bm == 64) {
     launch_dfma_tile<T, 4, 2>(g, op, c, grid, s);
-  else
-    launch_dfma_tile<T, 2, 2>(g, op, c, grid, s);
+  } else {
+    k_gemm_dfma32<T><<<grid, NT, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(), g.d_tile.as<GemmTile>(),
+                                         (int)g.tile.size(), static_cast<const T*>(op.a),
+                                         static_cast<const T*>(op.a_src), static_cast<const T*>(op.b),
+                                         static_cast<const T*>(op.b_src), static_cast<T*>(c), g.d_counter.as<int>());
+  }
 }
 
 // CTAs of one full wave: the grid-stride loop then has no partial second wave.

@@ -11,13 +11,12 @@
 //   the row (column) maximum.
 // Products (the Ozaki scheme, restated): C_ij = 2^(ea_i + eb_j) sum over the 28 slice pairs
 //   p + q <= 8 of (A_p B_q)_ij. Level L = p + q sums L - 1 pairs, each an integer multiple
-//   of 2^(-7L) below 2^14 of those units, so over at most 128 k the FP32 sum of one level
-//   is exact (4 * 128 * 127^2 < 2^24 for L <= 5). Levels 2, 3, 4 and 5 get their own
-//   128 x 32 FP32 accumulator in tensor memory; levels 6..8 share a fifth one, where FP32
-//   rounding costs at most 2^-24 of a quantity below 2^-26 of the leading level. Every
-//   128 k the accumulators are drained into int32 level sums (and a float for 6..8); at
-//   the end of a task C (+)= sign 2^(ea+eb-42) Z with Z = sum_L i_L 2^(7(6-L)) + fm 2^42 as one
-//   int64, rounded to FP64 with integer operations.
+//   of 2^(-7L) below 2^14 of those units. Each level has its own 128 x 32 FP32 accumulator
+//   in tensor memory (levels 2..8: 224 columns per set, two sets). Over 256 k the sums of
+//   levels 2..5 stay below 2^24 and are exact; levels 6..8 may round in FP32, at most
+//   2^-24 of a quantity 2^-28 below the leading level. Every 256 k the drain warps read the
+//   levels and fold them into one int64 per output (units 2^-49); at the end of a task
+//   C (+)= sign 2^(ea + eb - 49) z, rounded to FP64 with integer operations.
 //
 // Layout for the tensor cores: both operands K-major, no swizzle, in 8 x 16-byte core
 // matrices (leading-byte offset 128 B between the two core matrices of a 16-wide k step,
@@ -25,10 +24,11 @@
 // k tile, slice) as one contiguous tile in exactly that layout, zero-padded, so the GEMM
 // stages operands with bulk copies and points the descriptors at them.
 //
-// GEMM: one persistent CTA per SM, warp-specialised (see k_gemm_split). Per 16-wide k step
-// the 7 A slices are copied once into tensor memory and the 28 MMAs (M = 128, N = 32,
-// K = 16) read A from there and only B from shared memory: shared-memory traffic per step
-// is 7 A + 28 B reads of a slice instead of 28 + 28.
+// GEMM: one persistent CTA per SM, warp-specialised (see k_gemm_split): a producer warp
+// streams 32-wide k slabs of all A and B slices into shared memory, an MMA warp issues per
+// 16-wide k step 7 MMAs (A slice p against B slices 1..8-p concatenated along N), sixteen
+// drain warps fold the accumulators. Output rows reach C through a row map, so the A blocks
+// of several output blocks can share one 128-row tile (row stacking).
 // Every wait on an mbarrier is bounded; on expiry the CTA sets the plan's error word,
 // waits (bounded) for its own copies and tensor-core work, frees its tensor memory and
 // returns.
@@ -50,7 +50,7 @@ constexpr int kLevels = 7;                 // accumulators: levels 2..8
 constexpr int kTM = 128, kTN = 32, kTK = 64;
 constexpr int kATile = kTM * kTK * 2;      // bytes of one (row tile, k tile, slice): 16 KB
 constexpr int kBTile = kTN * kTK * 2;      // 4 KB
-constexpr int kDrainK = 128;               // k between drains (exactness bound)
+constexpr int kDrainK = 256;               // k between drains (exactness bound of levels 2..5)
 
 // ------------------------------------------------------------------ slicing
 // Work distribution of the slicing kernels: CTA b takes the contiguous item range
@@ -407,7 +407,7 @@ constexpr int kAccCols = kLevels * kTN;         // 224
 constexpr int kSumCol = 2 * kAccCols;           // 448
 constexpr uint32_t kTmemAlloc = 512;
 static_assert(kSumCol + 2 * kTN <= (int)kTmemAlloc, "tensor memory budget");
-constexpr int kFlushDrains = 64;                // the int64 sum of a chunk stays below 2^63
+constexpr int kFlushDrains = 32;                // the int64 sum of a chunk stays below 2^63
 constexpr float kMagic = 12582912.0f;           // 1.5 * 2^23: x + kMagic has the integer x in its low bits
 constexpr int kMagicBits = 0x4B400000;          // for |x| < 2^22
 
@@ -513,9 +513,12 @@ __global__ void __launch_bounds__(32) k_wait_selftest(long long limit, int* __re
 }
 
 // Fold one drained accumulator set into the int64 sums z (units 2^-49) of this thread's
-// row and 8 columns. Level L holds integers times 2^(-7L) below 2^24 (exact in FP32);
-// levels 2 and 3 stay below 2^22 and convert with the magic-number add, the others with
-// F2I; level 8 is rounded to units of 2^-49.
+// row and 8 columns. Over 256 k, level L sums (L - 1) slice pairs of 256 products below
+// 127^2 each, integers times 2^(-7L): levels 2..5 stay below 2^24 and are exact in FP32;
+// levels 6..8 may pass 2^24 and carry an FP32 rounding there, at most 2^-24 of a quantity
+// 2^-28 below the leading level (2^-52 of the result: below the 2^-49 slice truncation).
+// Level 2 stays below 2^22 and converts with the magic-number add, the others with F2I;
+// level 8 is rounded to units of 2^-49.
 __device__ __forceinline__ void drain_set(uint32_t lb, long long (&z)[kDrainCols]) {
   uint32_t r[kDrainCols];
   int32_t u[kDrainCols];
@@ -528,7 +531,7 @@ __device__ __forceinline__ void drain_set(uint32_t lb, long long (&z)[kDrainCols
   asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
   for (int c = 0; c < kDrainCols; ++c) {
-    u[c] += __float_as_int(fmaf(__uint_as_float(r[c]), 0x1p21f, kMagic)) - kMagicBits;
+    u[c] += __float2int_rn(__uint_as_float(r[c]) * 0x1p21f);
     z[c] += (long long)u[c] << 28;
   }
   tmem_ld8(lb + 2 * kTN, r);                             // level 4
@@ -542,14 +545,14 @@ __device__ __forceinline__ void drain_set(uint32_t lb, long long (&z)[kDrainCols
     u[c] += __float2int_rn(__uint_as_float(r[c]) * 0x1p35f);
     z[c] += (long long)u[c] << 14;
   }
-  tmem_ld8(lb + 4 * kTN, r);                             // level 6
+  tmem_ld8(lb + 4 * kTN, r);                             // level 6 (in int64: it may pass 2^24)
   asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-  for (int c = 0; c < kDrainCols; ++c) u[c] = __float2int_rn(__uint_as_float(r[c]) * 0x1p42f) * 128;
+  for (int c = 0; c < kDrainCols; ++c) z[c] += (long long)__float2int_rn(__uint_as_float(r[c]) * 0x1p42f) * 128;
   tmem_ld8(lb + 5 * kTN, r);                             // level 7
   asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-  for (int c = 0; c < kDrainCols; ++c) u[c] += __float2int_rn(__uint_as_float(r[c]) * 0x1p49f);
+  for (int c = 0; c < kDrainCols; ++c) u[c] = __float2int_rn(__uint_as_float(r[c]) * 0x1p49f);
   tmem_ld8(lb + 6 * kTN, r);                             // level 8
   asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
