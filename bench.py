@@ -506,6 +506,37 @@ def run_adapter_costs(local: int) -> dict:
     return out
 
 
+def run_profile_case(case: str, tensors, dev, local: int) -> None:
+    """Profiling drivers (one small, fixed piece of work each, for ncu captures): the split GEMM
+    of the D=4000 matvec's first (step0) or last (step3) contraction, stacked schedule, run
+    twice; Config 3's batched SVD; the stress QR (41 square blocks 10..800)."""
+    import torch
+    from tensortoolkit_gb300 import workloads
+    from tensortoolkit_gb300.api import Contract, ContractionPlan, DTensor, QR, SVD
+    lenv, psi, mpo1, mpo2, renv = tensors
+    dl, dp, d1, d2, dr = dev
+    if case in ("step0", "step3"):
+        if case == "step0":
+            p, a, b = ContractionPlan(lenv, psi, [[0], [0]], local), dl, dp
+        else:
+            t1 = Contract(dl, dp, [[0], [0]])
+            t2 = Contract(t1, d1, [[0, 2], [0, 1]])
+            t3 = Contract(t2, d2, [[4, 1], [0, 1]])
+            p, a, b = ContractionPlan(t3.meta, renv, [[4, 1], [1, 0]], local), t3, dr
+        p.set_schedule(split_stack=1)
+        c = DTensor.empty(p.result, local)
+        for _ in range(2):
+            p.execute(a, b, c, mode="split")
+        torch.cuda.synchronize()
+        p.device_status()
+    elif case == "svd":
+        SVD(DTensor.from_host(workloads.svd_psi(2000, 20, 6.0, 3), local), 2, [0], 1e-9, 1, 2000)
+    else:
+        QR(DTensor.from_host(workloads.svd_stress(41, 10, 800, 3), local), 1, [0])
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_run": True, "case": case}))
+
+
 def run_aux(local: int, part: str = "all"):
     """Measurements beside the headline: the batched permute's achieved HBM bandwidth, the
     batched block SVD / QR (Config 3) against a per-block cuSOLVER loop on the same shapes
@@ -693,6 +724,9 @@ def main():
     ap.add_argument("--aux-part", choices=["all", "transpose", "svd", "matvec", "proxy", "adapter"], default="all")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: plan the D=4000 matvec, apply it twice, print nothing else")
+    ap.add_argument("--profile-case", choices=["matvec", "step0", "step3", "svd", "qr"], default="matvec",
+                    help="with --profile: the matvec (default); one of its split-precision GEMM steps "
+                         "(stacked schedule, executed twice); Config 3's batched SVD; the stress QR")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -723,6 +757,9 @@ def main():
 
     if args.aux:
         return run_aux(local, args.aux_part)
+
+    if args.profile and args.profile_case != "matvec":
+        return run_profile_case(args.profile_case, tensors, (dl, dp, d1, d2, dr), local)
 
     if args.profile:
         for m in modes:

@@ -53,7 +53,7 @@ enum { QLTG_IN = 0, QLTG_OUT = 1 };       /* TenIndexDirType */
  * QLTG_MODE_SPLIT: FP64 emulated with BF16 slices on the tcgen05 tensor cores: every row
  *                  of A / column of B is scaled by a power of two and cut into seven 7-bit
  *                  integer slices, the 28 slice products of weight >= 2^-56 accumulate
- *                  exactly (FP32 integers in tensor memory, drained every 128 k into int64),
+ *                  exactly (FP32 integers in tensor memory, drained every 256 k into int64),
  *                  and each task's sum is rounded to FP64 once. Per element the error is
  *                  below 2^-48 * sum_k |a_ik| |b_kj| scaled by the row / column maxima
  *                  (about 1e-14 relative for random data); the tests and the benchmark
@@ -382,6 +382,17 @@ QLTG_API int qltg_matvec_apply_host(qltg_matvec* mv, const void* psi_host, void*
 
 /* Device-side status of the four captured contractions (see qltg_ctrct_plan_device_status). */
 QLTG_API int qltg_matvec_device_status(qltg_matvec* mv, void* stream);
+
+/* The form of the matvec's MPO part. No counterpart in the reference, whose chain is four
+ * Contract calls. With W12 = W1 . W2 contracted over the middle MPO bond once at creation,
+ * the two MPO steps become one, t3 = t1 . W12: the same result to rounding, without the
+ * intermediate t2. qltg_matvec_create times both forms and keeps the faster one.
+ * qltg_matvec_mpo_form reports: *fused (1 = the fused form runs), *fusable (0 when W12 cannot
+ * replace the two steps) and ms[0], ms[1] = the MPO part timed at creation in the two-step and
+ * the fused form. qltg_matvec_set_mpo_form forces a form (QLTG_ERR_UNSUPPORTED when not
+ * fusable); only before the matvec's first apply and before a Lanczos is created on it. */
+QLTG_API int qltg_matvec_mpo_form(const qltg_matvec* mv, int32_t* fused, int32_t* fusable, float* ms);
+QLTG_API int qltg_matvec_set_mpo_form(qltg_matvec* mv, int32_t fused, void* stream);
 
 /* The GEMM schedule the tuner chose for contraction `step` (0..3) of the matvec when it was
  * created, as qltg_ctrct_plan_get_schedule reports it, and that step's split-precision tile

@@ -788,6 +788,18 @@ class Matvec:
         check(lib().qltg_matvec_stats(self.h, C.byref(f), C.byref(n)))
         return f.value, n.value
 
+    def mpo_form(self) -> dict:
+        """Whether the two MPO steps run fused (t1 . W12), whether they can, and the MPO part's
+        time in both forms as measured at creation (ms)."""
+        fused, fusable = C.c_int32(), C.c_int32()
+        ms = np.zeros(2, np.float32)
+        check(lib().qltg_matvec_mpo_form(self.h, C.byref(fused), C.byref(fusable), ms.ctypes.data))
+        return {"fused": bool(fused.value), "fusable": bool(fusable.value),
+                "ms_two_steps": round(float(ms[0]), 4), "ms_fused": round(float(ms[1]), 4)}
+
+    def set_mpo_form(self, fused: bool) -> None:
+        check(lib().qltg_matvec_set_mpo_form(self.h, 1 if fused else 0, stream_ptr(self.device)))
+
     def schedules(self) -> List[dict]:
         """Per contraction step, the GEMM schedule the tuner chose at creation."""
         out = []

@@ -77,6 +77,8 @@ _SIGS = {
     "qltg_ctrct_plan_get_schedule": ([_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P, _P], C.c_int),
     "qltg_ctrct_plan_tune": ([_P, _P, _P, _P, C.c_int32, _P, C.POINTER(C.c_int32)], C.c_int),
     "qltg_ctrct_plan_split_stats": ([_P, _I64P, C.POINTER(C.c_double)], C.c_int),
+    "qltg_matvec_mpo_form": ([_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P], C.c_int),
+    "qltg_matvec_set_mpo_form": ([_P, C.c_int32, _P], C.c_int),
     "qltg_matvec_schedule": ([_P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P, _P, _I64P,
                               C.POINTER(C.c_double)], C.c_int),
     "qltg_transpose": ([_P, C.POINTER(TensorDesc), _P, _P, _P, _P], C.c_int),

@@ -10,10 +10,11 @@
 // Here: grouping is host metadata; one gather launch densifies every group; one batched
 // launch decomposes all groups - one-sided (Hestenes) Jacobi in FP64 with round-robin pair
 // ordering for the SVD, Householder with LAPACK's reflector convention for the QR - where a
-// large group is spread over a thread-block cluster of up to 8 CTAs (one SM each) that
-// step through the rotation rounds together on the cluster barrier; one scatter launch
-// builds the result blocks. Only the singular values cross to the host (for the global
-// truncation sort, as in the reference).
+// group is spread over a thread-block cluster of up to 16 CTAs (one SM each, in proportion
+// to its share of the work) that step through the rotation rounds together on the cluster
+// barrier, and the QR runs in panels whose updates spread over every group's column tiles;
+// one scatter launch builds the result blocks. Only the singular values cross to the host
+// (for the global truncation sort, as in the reference).
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -32,7 +33,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxSweeps = 60;
-constexpr int kBigCluster = 8;
+constexpr int kMaxCluster = 16;   // CTAs of the largest Jacobi cluster (non-portable size)
 constexpr int kJacobiSmem = 200 * 1024;   // dynamic shared memory of k_jacobi (two column blocks)
 
 // ------------------------------------------------------------------ complex helpers
@@ -199,14 +200,14 @@ struct JacobiShape {
 };
 
 template <typename T>
-__host__ __device__ inline JacobiShape jacobi_shape(int p, int q, int smem_bytes) {
+__host__ __device__ inline JacobiShape jacobi_shape(int p, int q, int smem_bytes, int cl) {
   const int L = p + q;
   int nb = smem_bytes / (2 * L * (int)sizeof(T));
   if (nb < 1) nb = 1;
-  if (2 * nb >= q) return JacobiShape{(q + 1) / 2, 1};
+  if (cl == 1 && 2 * nb >= q) return JacobiShape{(q + 1) / 2, 1};
   // block pairs per step: a multiple of the cluster size, so no CTA of the cluster idles
   int M = (q + 2 * nb - 1) / (2 * nb);
-  M = (M + kBigCluster - 1) / kBigCluster * kBigCluster;
+  M = (M + cl - 1) / cl * cl;
   return JacobiShape{(q + 2 * M - 1) / (2 * M), M};
 }
 
@@ -250,7 +251,7 @@ __global__ void __launch_bounds__(kThreads) k_jacobi(const JacobiJob* __restrict
     if (rank == 0 && threadIdx.x == 0) status[job] = 0;
     return;
   }
-  const JacobiShape sh = jacobi_shape<T>(p, q, smem_bytes);
+  const JacobiShape sh = jacobi_shape<T>(p, q, smem_bytes, cl);
   const int nb = sh.nb, M = sh.M, nblk = 2 * sh.M;
   // global column c of block `blk` and its count
   auto block_cols = [&](int blk, int& c0) {
@@ -998,11 +999,29 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
     k_r_to_x<T><<<ng, kThreads, 0, s>>>(d_pre.as<PrecondJob>(), ng, ws.as<T>(), ws.as<T>());
     QLTG_CUDA(cudaGetLastError());
   }
-  // groups whose columns all fit in one CTA's shared memory: one CTA each; the others on
-  // 8-CTA clusters stepping through block pairs
-  std::vector<JacobiJob> big, small;
-  for (int g = 0; g < ng; ++g)
-    (jacobi_shape<T>(xjobs[g].p, xjobs[g].q, kJacobiSmem).M > 1 ? big : small).push_back(xjobs[g]);
+  // Jacobi jobs by cluster size: each job gets a share of the SMs in proportion to its work
+  // per sweep (q^2 (p + q) multiply-adds), rounded down to 1, 2, 4, 8 or 16 CTAs (at least
+  // two columns per CTA); each size is one launch, all launches run side by side on streams
+  // forked from s and joined back. A one-CTA job whose columns fit in shared memory keeps
+  // them there for all sweeps; the others step through block pairs on the cluster barrier.
+  const int nsm = current_sm_count();
+  std::vector<double> jwork(ng);
+  double wsum = 0;
+  for (int g = 0; g < ng; ++g) {
+    jwork[g] = (double)xjobs[g].q * xjobs[g].q * (xjobs[g].p + xjobs[g].q);
+    wsum += jwork[g];
+  }
+  constexpr int kClasses = 5;   // 1, 2, 4, 8, 16 CTAs
+  std::vector<JacobiJob> cls_jobs[kClasses];
+  for (int g = 0; g < ng; ++g) {
+    const double share = wsum > 0 ? nsm * jwork[g] / wsum : 1.0;
+    int c = 1, ci = 0;
+    while (2 * c <= kMaxCluster && 2 * c <= share && 4 * c <= xjobs[g].q) {
+      c *= 2;
+      ++ci;
+    }
+    cls_jobs[ci].push_back(xjobs[g]);
+  }
   {
     static std::mutex mu;
     static bool done[2][64] = {};
@@ -1015,56 +1034,58 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
       if (dev >= 0 && dev < 64) done[sizeof(T) == 16][dev] = true;
     }
   }
-  DevBuf d_big = upload(big, s), d_small = upload(small, s);
-  DevBuf st_big(std::max<size_t>(1, big.size()) * 4), st_small(std::max<size_t>(1, small.size()) * 4);
-  DevBuf sr_big(std::max<size_t>(1, big.size()) * kMaxSweeps * 4);
-  DevBuf sr_small(std::max<size_t>(1, small.size()) * kMaxSweeps * 4);
-  QLTG_CUDA(cudaMemsetAsync(sr_big.get(), 0, sr_big.bytes(), s));
-  QLTG_CUDA(cudaMemsetAsync(sr_small.get(), 0, sr_small.bytes(), s));
+  DevBuf d_cls[kClasses], st_cls[kClasses], sr_cls[kClasses];
+  for (int ci = 0; ci < kClasses; ++ci) {
+    if (cls_jobs[ci].empty()) continue;
+    d_cls[ci] = upload(cls_jobs[ci], s);
+    st_cls[ci].alloc(cls_jobs[ci].size() * 4);
+    sr_cls[ci].alloc(cls_jobs[ci].size() * kMaxSweeps * 4);
+    QLTG_CUDA(cudaMemsetAsync(sr_cls[ci].get(), 0, sr_cls[ci].bytes(), s));
+  }
   // rotate while |<wi, wj>| > tol ||wi|| ||wj||: columns orthogonal to a few ulps
   const double tol = 64.0 * 2.220446049250313e-16;
-  // the single-CTA jobs run beside the clusters: on a second stream forked before the
-  // cluster launch and joined after it
-  cudaStream_t s2 = s;
-  cudaEvent_t fork = nullptr, join = nullptr;
-  const bool two = !big.empty() && !small.empty();
-  if (two) {
-    QLTG_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
-    QLTG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
-    QLTG_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
-    QLTG_CUDA(cudaEventRecord(fork, s));
-    QLTG_CUDA(cudaStreamWaitEvent(s2, fork, 0));
-  }
+  cudaEvent_t fork = nullptr;
+  QLTG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  QLTG_CUDA(cudaEventRecord(fork, s));
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> joins;
   cudaError_t le = cudaSuccess;
-  if (!small.empty()) {
-    k_jacobi<T><<<(unsigned)small.size(), kThreads, kJacobiSmem, s2>>>(d_small.as<const JacobiJob>(), 1, ws.as<T>(),
-                                                                        jbuf.as<T>(), sr_small.as<int>(),
-                                                                        st_small.as<int>(), tol, (int)kJacobiSmem);
-    le = cudaGetLastError();
-  }
-  if (!big.empty() && le == cudaSuccess) {
+  for (int ci = 0; ci < kClasses && le == cudaSuccess; ++ci) {
+    if (cls_jobs[ci].empty()) continue;
+    const int cl = 1 << ci;
+    cudaStream_t sx = nullptr;
+    le = cudaStreamCreateWithFlags(&sx, cudaStreamNonBlocking);
+    if (le != cudaSuccess) break;
+    side.push_back(sx);
+    le = cudaStreamWaitEvent(sx, fork, 0);
+    if (le != cudaSuccess) break;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(big.size() * kBigCluster));
+    cfg.gridDim = dim3((unsigned)(cls_jobs[ci].size() * cl));
     cfg.blockDim = dim3(kThreads);
     cfg.dynamicSmemBytes = kJacobiSmem;
-    cfg.stream = s;
+    cfg.stream = sx;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kBigCluster;
+    attr[0].val.clusterDim.x = cl;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    le = cudaLaunchKernelEx(&cfg, k_jacobi<T>, d_big.as<const JacobiJob>(), (int)kBigCluster, ws.as<T>(),
-                            jbuf.as<T>(), sr_big.as<int>(), st_big.as<int>(), tol, (int)kJacobiSmem);
+    cfg.numAttrs = cl > 1 ? 1 : 0;
+    le = cudaLaunchKernelEx(&cfg, k_jacobi<T>, d_cls[ci].as<const JacobiJob>(), cl, ws.as<T>(), jbuf.as<T>(),
+                            sr_cls[ci].as<int>(), st_cls[ci].as<int>(), tol, (int)kJacobiSmem);
+    if (le != cudaSuccess) break;
+    cudaEvent_t j = nullptr;
+    le = cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
+    if (le != cudaSuccess) break;
+    joins.push_back(j);
+    le = cudaEventRecord(j, sx);
   }
-  if (two) {
-    cudaEventRecord(join, s2);
-    cudaStreamWaitEvent(s, join, 0);
-    cudaEventDestroy(fork);
-    cudaEventDestroy(join);
-    cudaStreamDestroy(s2);   // released by the driver once its work is done
+  for (auto j : joins) {
+    cudaStreamWaitEvent(s, j, 0);
+    cudaEventDestroy(j);
   }
+  cudaEventDestroy(fork);
+  for (auto sx : side) cudaStreamDestroy(sx);   // released by the driver once its work is done
   QLTG_CUDA(le);
   // singular values and the right vectors from X; the left vectors W = Q J
   DevBuf d_jobs = upload(xjobs, s);
@@ -1078,14 +1099,22 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   }
   std::vector<double> h_sv(sv_off[ng]);
   std::vector<int32_t> h_ord(sv_off[ng]);
-  std::vector<int> h_st(big.size() + small.size());
+  std::vector<int> h_st;
   if (!h_sv.empty()) {
     QLTG_CUDA(cudaMemcpyAsync(h_sv.data(), sv.get(), h_sv.size() * 8, cudaMemcpyDeviceToHost, s));
     QLTG_CUDA(cudaMemcpyAsync(h_ord.data(), order.get(), h_ord.size() * 4, cudaMemcpyDeviceToHost, s));
   }
-  if (!big.empty()) QLTG_CUDA(cudaMemcpyAsync(h_st.data(), st_big.get(), big.size() * 4, cudaMemcpyDeviceToHost, s));
-  if (!small.empty())
-    QLTG_CUDA(cudaMemcpyAsync(h_st.data() + big.size(), st_small.get(), small.size() * 4, cudaMemcpyDeviceToHost, s));
+  {
+    size_t total_jobs = 0;
+    for (int ci = 0; ci < kClasses; ++ci) total_jobs += cls_jobs[ci].size();
+    h_st.resize(total_jobs);
+    size_t at = 0;
+    for (int ci = 0; ci < kClasses; ++ci) {
+      if (cls_jobs[ci].empty()) continue;
+      QLTG_CUDA(cudaMemcpyAsync(h_st.data() + at, st_cls[ci].get(), cls_jobs[ci].size() * 4, cudaMemcpyDeviceToHost, s));
+      at += cls_jobs[ci].size();
+    }
+  }
   QLTG_CUDA(cudaStreamSynchronize(s));
   for (int x : h_st) QLTG_CHECK(x >= 0, QLTG_ERR_NOCONV, "one-sided Jacobi did not converge within 60 sweeps");
 

@@ -211,6 +211,7 @@ int qltg_lanczos_create(qltg_matvec* mv, int32_t max_iter, qltg_lanczos** lz) {
     QLTG_CUDA(cudaSetDevice(mv->ctx->device));
     auto h = std::make_unique<qltg_lanczos>();
     h->mv = mv;
+    mv->frozen = true;   // the step graphs capture the matvec's current form
     h->max_iter = max_iter;
     h->cplx = mv->step[3].c.dtype == QLTG_C128;
     h->n = mv->psi_size;

@@ -7,6 +7,7 @@
 // topology of a Lanczos matvec never changes, so here the four plans (device pairing,
 // schedules, operand scratch) are built once, the intermediates t1..t3 live in HBM for
 // the life of the object, and the whole chain replays as one graph launch.
+#include <algorithm>
 #include <map>
 #include <memory>
 
@@ -15,8 +16,6 @@
 
 using namespace qltg;
 
-extern "C" {
-
 namespace {
 
 // Split mode: when every A block of the last step's slices is written by the second MPO
@@ -24,7 +23,13 @@ namespace {
 // a multiple of the skinny block's n), that kernel folds the row scales while it writes them
 // and the last step skips its row-scale pass.
 void link_row_fields(qltg_matvec& mv, cudaStream_t s) {
-  CtrctPlan& p2 = mv.step[2];
+  for (CtrctPlan* q : {&mv.step[2], &mv.mpo12}) {   // unlink both possible producers first
+    q->d_fuse.release();
+    q->fuse_fields = nullptr;
+  }
+  if (mv.step[3].split) mv.step[3].split->a_fields_external = false;
+  mv.fused_fields = false;
+  CtrctPlan& p2 = mv.mpo_producer();
   CtrctPlan& p3 = mv.step[3];
   if (!p2.split || !p3.split || p3.split->a_ops.empty() || p3.split->a_static) return;
   if (p3.a.dtype != QLTG_F64) return;   // the skinny kernel folds real outputs only
@@ -53,7 +58,63 @@ void link_row_fields(qltg_matvec& mv, cudaStream_t s) {
   mv.fused_fields = true;
 }
 
+// Median ms of `reps` runs of fn on s (after one unmeasured run).
+template <typename F>
+float time_ms(F&& fn, cudaStream_t s, int reps = 5) {
+  fn();
+  std::vector<cudaEvent_t> ev(2 * reps);
+  for (auto& e : ev) QLTG_CUDA(cudaEventCreate(&e));
+  for (int r = 0; r < reps; ++r) {
+    QLTG_CUDA(cudaEventRecord(ev[2 * r], s));
+    fn();
+    QLTG_CUDA(cudaEventRecord(ev[2 * r + 1], s));
+  }
+  QLTG_CUDA(cudaStreamSynchronize(s));
+  std::vector<float> ms(reps);
+  for (int r = 0; r < reps; ++r) cudaEventElapsedTime(&ms[r], ev[2 * r], ev[2 * r + 1]);
+  for (auto e : ev) cudaEventDestroy(e);
+  std::sort(ms.begin(), ms.end());
+  return ms[reps / 2];
+}
+
+// Plan the fused MPO form (W12 = W1 . W2 on the device, then t1 . W12 over t1's (w, p1, p2)
+// legs), check that it yields t3's exact layout, and time it against the two MPO steps.
+void plan_mpo_fusion(qltg_matvec& mv, cudaStream_t s) {
+  CtrctPlan wp;
+  wp.ctx = mv.ctx;
+  wp.a = mv.step[1].b;
+  wp.b = mv.step[2].b;
+  wp.axa = {3};
+  wp.axb = {0};
+  plan_contraction(wp, s);
+  finalize_plan(wp, s);
+  if (wp.c.rank != 6 || wp.c.size == 0) return;
+  mv.w12.alloc(wp.c.size * wp.c.elem_bytes());
+  exec_contraction(wp, mv.mpo1, mv.mpo2, mv.w12.get(), QLTG_MODE_FP64, s);
+  QLTG_CUDA(cudaStreamSynchronize(s));   // W12 is final before its plan's buffers go
+  CtrctPlan& f = mv.mpo12;
+  f.ctx = mv.ctx;
+  f.a = mv.step[0].c;
+  f.b = wp.c;
+  f.axa = {0, 2, 3};
+  f.axb = {0, 1, 3};
+  plan_contraction(f, s);
+  finalize_plan(f, s);
+  const Meta& t3 = mv.step[2].c;
+  if (f.c.size != t3.size || f.c.nblk != t3.nblk || f.c.coords != t3.coords || f.c.offsets != t3.offsets) return;
+  tune_plan(f, mv.t[0].get(), mv.w12.get(), mv.t[2].get(), mv.mode, s, nullptr);
+  if (mv.mode == QLTG_MODE_SPLIT) prepare_split(f, s);
+  mv.mpo_fusable = true;
+  mv.mpo_fused = false;
+  mv.mid_ms[0] = time_ms([&] { mv.enqueue_mid(s); }, s);
+  mv.mpo_fused = true;
+  mv.mid_ms[1] = time_ms([&] { mv.enqueue_mid(s); }, s);
+  mv.mpo_fused = mv.mid_ms[1] < mv.mid_ms[0];
+}
+
 }  // namespace
+
+extern "C" {
 
 int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* lenv_dev,
                        const qltg_tensor_desc* psi, const qltg_tensor_desc* mpo1, const void* mpo1_dev,
@@ -114,6 +175,8 @@ int qltg_matvec_create(qltg_ctx* ctx, const qltg_tensor_desc* lenv, const void* 
         if (i == 3) split_prepack_static(p, nullptr, h->renv, s);
       }
     }
+    plan_mpo_fusion(*h, s);
+    if (h->mpo_fused) h->t[1].release();   // t2 is never written in the fused form
     if (mode == QLTG_MODE_SPLIT) link_row_fields(*h, s);
     *mv = h.release();
   });
@@ -155,12 +218,48 @@ int qltg_matvec_schedule(const qltg_matvec* mv, int32_t step, int32_t* f64_tile_
   });
 }
 
+int qltg_matvec_mpo_form(const qltg_matvec* mv, int32_t* fused, int32_t* fusable, float* ms) {
+  return guarded([&] {
+    QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
+    if (fused) *fused = mv->mpo_fused ? 1 : 0;
+    if (fusable) *fusable = mv->mpo_fusable ? 1 : 0;
+    if (ms) {
+      ms[0] = mv->mid_ms[0];
+      ms[1] = mv->mid_ms[1];
+    }
+  });
+}
+
+int qltg_matvec_set_mpo_form(qltg_matvec* mv, int32_t fused, void* stream) {
+  return guarded([&] {
+    QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
+    QLTG_CHECK(fused == 0 || fused == 1, QLTG_ERR_INVALID, "fused must be 0 or 1");
+    QLTG_CHECK(!fused || mv->mpo_fusable, QLTG_ERR_UNSUPPORTED, "the MPO steps of this matvec cannot be fused");
+    QLTG_CHECK(!mv->frozen && mv->graphs.empty(), QLTG_ERR_INVALID,
+               "the MPO form is fixed once the matvec was applied or a Lanczos was created on it");
+    if ((fused != 0) == mv->mpo_fused) return;
+    QLTG_CUDA(cudaSetDevice(mv->ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    mv->mpo_fused = fused != 0;
+    if (!mv->mpo_fused && !mv->t[1].get())
+      mv->t[1].alloc(std::max<int64_t>(1, mv->step[1].c.size) * mv->step[1].c.elem_bytes());
+    if (mv->mode == QLTG_MODE_SPLIT) link_row_fields(*mv, s);
+  });
+}
+
 int qltg_matvec_stats(const qltg_matvec* mv, double* flops, int64_t* launches) {
   return guarded([&] {
     QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
     double f = 0;
     int64_t l = 0;
-    for (auto& p : mv->step) {
+    const CtrctPlan* plans[4] = {&mv->step[0], &mv->step[1], &mv->step[2], &mv->step[3]};
+    const int np = mv->mpo_fused ? 3 : 4;
+    if (mv->mpo_fused) {
+      plans[1] = &mv->mpo12;
+      plans[2] = &mv->step[3];
+    }
+    for (int i = 0; i < np; ++i) {
+      const CtrctPlan& p = *plans[i];
       f += p.flops;
       l += mv->mode == QLTG_MODE_SPLIT && p.split ? exec_launches_split(p) : p.launches_per_exec;
     }
@@ -207,8 +306,8 @@ int qltg_matvec_device_status(qltg_matvec* mv, void* stream) {
   return guarded([&] {
     QLTG_CHECK(mv, QLTG_ERR_INVALID, "null matvec");
     QLTG_CUDA(cudaSetDevice(mv->ctx->device));
-    for (auto& p : mv->step)
-      QLTG_CHECK(split_device_error(p, static_cast<cudaStream_t>(stream)) == 0, QLTG_ERR_TIMEOUT,
+    for (const CtrctPlan* p : {&mv->step[0], &mv->step[1], &mv->step[2], &mv->step[3], &mv->mpo12})
+      QLTG_CHECK(split_device_error(*p, static_cast<cudaStream_t>(stream)) == 0, QLTG_ERR_TIMEOUT,
                  "a bounded tensor-core wait expired in the split-precision GEMM");
   });
 }
