@@ -429,6 +429,10 @@ __device__ __forceinline__ T scaleT(T a, double s) {
 // Q_tile -= V T (V^H Q_tile) on the columns j0 .. k-1 of Q = I(:, 0:k). A large group thus
 // spreads its O(m n^2) work over as many SMs as it has column tiles, instead of one.
 constexpr int kQrNb = 32;   // panel width
+// the panel kernel's CTA: 32 warps, so each of a panel's columns has a warp for the in-panel
+// updates and the column norms reduce over 1024 threads
+constexpr int kPanelThreads = 1024;
+constexpr int kPanelWarps = kPanelThreads / 32;
 // rows per shared-memory chunk of the update kernel (its three 32-column buffers stay within
 // the 48 KB of static shared memory)
 template <typename T>
@@ -468,7 +472,7 @@ __device__ __forceinline__ T v_elem(const T* __restrict__ A, int m, int j0, int 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_qr_panel(const QrJob* __restrict__ jobs, int j0, T* __restrict__ as,
+__global__ void __launch_bounds__(kPanelThreads) k_qr_panel(const QrJob* __restrict__ jobs, int j0, T* __restrict__ as,
                                                        T* __restrict__ taus, T* __restrict__ tfac) {
   const QrJob jb = jobs[blockIdx.x];
   const int m = jb.m, n = jb.n, k = min(m, n);
@@ -477,19 +481,19 @@ __global__ void __launch_bounds__(kThreads) k_qr_panel(const QrJob* __restrict__
   T* A = as + jb.a_off;
   T* tau = taus + jb.tau_off;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __shared__ double red[kWarps];
+  __shared__ double red[kPanelWarps];
   __shared__ T s_tau, s_scale;
   __shared__ T sY[kQrNb][kQrNb + 1], sT[kQrNb][kQrNb + 1];
   for (int j = j0; j < j0 + nbe; ++j) {
     T* col = A + (int64_t)j * m;
     double part = 0;
-    for (int r = j + 1 + threadIdx.x; r < m; r += kThreads) part += abs2(col[r]);
+    for (int r = j + 1 + threadIdx.x; r < m; r += kPanelThreads) part += abs2(col[r]);
     part = warp_sum(part);
     if (lane == 0) red[warp] = part;
     __syncthreads();
     if (threadIdx.x == 0) {
       double xn2 = 0;
-      for (int w = 0; w < kWarps; ++w) xn2 += red[w];
+      for (int w = 0; w < kPanelWarps; ++w) xn2 += red[w];
       const T alpha = col[j];
       const double ar = re_of(alpha), ai = im_of(alpha);
       if (xn2 == 0.0 && ai == 0.0) {
@@ -508,12 +512,12 @@ __global__ void __launch_bounds__(kThreads) k_qr_panel(const QrJob* __restrict__
     }
     __syncthreads();
     const T sc = s_scale;
-    for (int r = j + 1 + threadIdx.x; r < m; r += kThreads) col[r] = mulT(col[r], sc);
+    for (int r = j + 1 + threadIdx.x; r < m; r += kPanelThreads) col[r] = mulT(col[r], sc);
     __syncthreads();
     // H_j^H on the panel's later columns only (the rest waits for the block update)
     const T tconj = conjT(s_tau);
     if (re_of(s_tau) != 0.0 || im_of(s_tau) != 0.0) {
-      for (int c = j + 1 + warp; c < j0 + nbe; c += kWarps) {
+      for (int c = j + 1 + warp; c < j0 + nbe; c += kPanelWarps) {
         T* ac = A + (int64_t)c * m;
         double wr = 0, wi = 0;
         for (int r = j + lane; r < m; r += 32) {
@@ -536,7 +540,7 @@ __global__ void __launch_bounds__(kThreads) k_qr_panel(const QrJob* __restrict__
   // T: y(l, i) = v_l^H v_i for l < i (v_i starts at row j0 + i with a 1)
   for (int i = 1; i < nbe; ++i) {
     const T* vi = A + (int64_t)(j0 + i) * m;
-    for (int l = warp; l < i; l += kWarps) {
+    for (int l = warp; l < i; l += kPanelWarps) {
       const T* vl = A + (int64_t)(j0 + l) * m;
       T acc = zeroT<T>();
       for (int r = j0 + i + 1 + lane; r < m; r += 32) acc = fma_conj(vl[r], vi[r], acc);
@@ -559,7 +563,7 @@ __global__ void __launch_bounds__(kThreads) k_qr_panel(const QrJob* __restrict__
     __syncthreads();
   }
   T* Tp = tfac + jb.t_off + (int64_t)(j0 / kQrNb) * kQrNb * kQrNb;
-  for (int e = threadIdx.x; e < kQrNb * kQrNb; e += kThreads) {
+  for (int e = threadIdx.x; e < kQrNb * kQrNb; e += kPanelThreads) {
     const int c = e / kQrNb, r = e % kQrNb;
     Tp[e] = (r < nbe && c < nbe && r <= c) ? sT[r][c] : zeroT<T>();
   }
@@ -798,7 +802,7 @@ void launch_blocked_qr(std::vector<QrJob>& jobs, T* A, T* tau, T* Q, cudaStream_
   T* tf = keep.tfac.as<T>();
   for (int p = 0; p < np; ++p) {
     const int j0 = p * kQrNb;
-    k_qr_panel<T><<<ng, kThreads, 0, s>>>(dj, j0, A, tau, tf);
+    k_qr_panel<T><<<ng, kPanelThreads, 0, s>>>(dj, j0, A, tau, tf);
     const int64_t nt = trail_begin[p + 1] - trail_begin[p];
     if (nt) k_qr_update<T, false><<<(unsigned)nt, kThreads, 0, s>>>(dj, dt + trail_begin[p], j0, A, tf, A);
   }
@@ -999,29 +1003,30 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
     k_r_to_x<T><<<ng, kThreads, 0, s>>>(d_pre.as<PrecondJob>(), ng, ws.as<T>(), ws.as<T>());
     QLTG_CUDA(cudaGetLastError());
   }
-  // Jacobi jobs by cluster size: each job gets a share of the SMs in proportion to its work
-  // per sweep (q^2 (p + q) multiply-adds), rounded down to 1, 2, 4, 8 or 16 CTAs (at least
-  // two columns per CTA); each size is one launch, all launches run side by side on streams
-  // forked from s and joined back. A one-CTA job whose columns fit in shared memory keeps
-  // them there for all sweeps; the others step through block pairs on the cluster barrier.
+  // Jacobi jobs by cluster size: starting from one CTA each, the job with the most work per
+  // CTA (q^2 (p + q) multiply-adds per sweep / CTAs) gets one CTA more, until the SMs are
+  // used up (clusters of at most 16 CTAs, at least two columns per CTA), so the largest
+  // groups finish about together. Each cluster size is one launch on its own stream, forked
+  // from s and joined back, largest clusters first. A one-CTA job whose columns fit in shared
+  // memory keeps them there for all sweeps; the others step through block pairs on the
+  // cluster barrier.
   const int nsm = current_sm_count();
   std::vector<double> jwork(ng);
-  double wsum = 0;
-  for (int g = 0; g < ng; ++g) {
-    jwork[g] = (double)xjobs[g].q * xjobs[g].q * (xjobs[g].p + xjobs[g].q);
-    wsum += jwork[g];
+  std::vector<int> jcl(ng, 1);
+  for (int g = 0; g < ng; ++g) jwork[g] = (double)xjobs[g].q * xjobs[g].q * (xjobs[g].p + xjobs[g].q);
+  for (int used = ng; used < nsm;) {
+    int best = -1;
+    for (int g = 0; g < ng; ++g)
+      if (jcl[g] < kMaxCluster && 2 * (jcl[g] + 1) <= xjobs[g].q &&
+          (best < 0 || jwork[g] / jcl[g] > jwork[best] / jcl[best]))
+        best = g;
+    if (best < 0) break;
+    ++jcl[best];
+    ++used;
   }
-  constexpr int kClasses = 5;   // 1, 2, 4, 8, 16 CTAs
+  constexpr int kClasses = kMaxCluster;   // class ci holds the jobs on clusters of ci + 1 CTAs
   std::vector<JacobiJob> cls_jobs[kClasses];
-  for (int g = 0; g < ng; ++g) {
-    const double share = wsum > 0 ? nsm * jwork[g] / wsum : 1.0;
-    int c = 1, ci = 0;
-    while (2 * c <= kMaxCluster && 2 * c <= share && 4 * c <= xjobs[g].q) {
-      c *= 2;
-      ++ci;
-    }
-    cls_jobs[ci].push_back(xjobs[g]);
-  }
+  for (int g = 0; g < ng; ++g) cls_jobs[jcl[g] - 1].push_back(xjobs[g]);
   {
     static std::mutex mu;
     static bool done[2][64] = {};
@@ -1050,9 +1055,9 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> joins;
   cudaError_t le = cudaSuccess;
-  for (int ci = 0; ci < kClasses && le == cudaSuccess; ++ci) {
+  for (int ci = kClasses - 1; ci >= 0 && le == cudaSuccess; --ci) {
     if (cls_jobs[ci].empty()) continue;
-    const int cl = 1 << ci;
+    const int cl = ci + 1;
     cudaStream_t sx = nullptr;
     le = cudaStreamCreateWithFlags(&sx, cudaStreamNonBlocking);
     if (le != cudaSuccess) break;

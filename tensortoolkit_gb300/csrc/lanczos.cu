@@ -67,23 +67,58 @@ struct ComplexOps {
   }
 };
 
+// N sums at once: one warp shuffle tree each, one shared-memory round for all (valid in
+// thread 0). The per-value order is fixed, as in block_sum.
+template <int N>
+__device__ __forceinline__ void block_sum_n(double (&v)[N], double* red) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    if (lane == 0) red[i * (kVecThreads / 32) + warp] = v[i];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      double t = lane < nw ? red[i * (kVecThreads / 32) + lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      v[i] = t;
+    }
+  }
+  __syncthreads();
+}
+
 // part[(i * gridDim.x + b) * kParts + r] = part r of the sum over CTA b's chunk of conj(V_i[e]) w[e].
+// Four vectors per pass over the chunk: w is loaded once for them, and the four load streams
+// keep more reads in flight than one vector at a time.
 template <class Ops>
 __global__ void __launch_bounds__(kVecThreads) k_multi_dot(const typename Ops::T* __restrict__ V, int nv, int64_t ld,
                                                            const typename Ops::T* __restrict__ w, int64_t n,
                                                            double* __restrict__ part) {
-  __shared__ double red[kVecThreads / 32];
+  constexpr int kG = 4, kN = kG * Ops::kParts;
+  __shared__ double red[kN * (kVecThreads / 32)];
   const int64_t per = (n + gridDim.x - 1) / gridDim.x;
   const int64_t e0 = (int64_t)blockIdx.x * per, e1 = min(n, e0 + per);
-  for (int i = 0; i < nv; ++i) {
-    const typename Ops::T* v = V + (int64_t)i * ld;
-    double acc[Ops::kParts] = {};
-    for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) Ops::dot_acc(__ldg(v + e), __ldg(w + e), acc);
+  for (int i0 = 0; i0 < nv; i0 += kG) {
+    const int g = min(kG, nv - i0);
+    double acc[kG][Ops::kParts] = {};
+    for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+      const typename Ops::T x = __ldg(w + e);
 #pragma unroll
-    for (int r = 0; r < Ops::kParts; ++r) {
-      const double t = block_sum(acc[r], red);
-      if (threadIdx.x == 0) part[((int64_t)i * gridDim.x + blockIdx.x) * Ops::kParts + r] = t;
+      for (int u = 0; u < kG; ++u)
+        if (u < g) Ops::dot_acc(__ldg(V + (int64_t)(i0 + u) * ld + e), x, acc[u]);
     }
+    double flat[kN];
+#pragma unroll
+    for (int u = 0; u < kG; ++u)
+#pragma unroll
+      for (int r = 0; r < Ops::kParts; ++r) flat[u * Ops::kParts + r] = acc[u][r];
+    block_sum_n<kN>(flat, red);
+    if (threadIdx.x == 0)
+      for (int u = 0; u < g; ++u)
+        for (int r = 0; r < Ops::kParts; ++r)
+          part[((int64_t)(i0 + u) * gridDim.x + blockIdx.x) * Ops::kParts + r] = flat[u * Ops::kParts + r];
   }
 }
 
