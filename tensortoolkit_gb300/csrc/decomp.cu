@@ -433,13 +433,22 @@ constexpr int kQrNb = 32;   // panel width
 // updates and the column norms reduce over 1024 threads
 constexpr int kPanelThreads = 1024;
 constexpr int kPanelWarps = kPanelThreads / 32;
+// dynamic shared memory for a panel held on chip (beside the kernel's static 17 / 34 KB)
+template <typename T>
+constexpr int qr_panel_smem() { return sizeof(T) == 8 ? 200 * 1024 : 184 * 1024; }
 // rows per shared-memory chunk of the update kernel (its three 32-column buffers stay within
 // the 48 KB of static shared memory)
 template <typename T>
 constexpr int qr_rows_per_chunk() { return sizeof(T) == 8 ? 64 : 16; }
 
+// One work item of the block-reflector updates: rows [r0, r1) of the 32-column tile that
+// starts at column c0. The row chunks of one tile are consecutive items, the first at index
+// `first`, `nchunks` of them; they share the tile's W = V^H X through partial sums.
+constexpr int kQrRowChunk = 128;
 struct QrTile {
-  int32_t job, c0;          // 32-column tile starting at column c0
+  int32_t job, c0;
+  int32_t r0, r1;
+  int32_t first, nchunks;
 };
 
 template <typename T>
@@ -471,9 +480,13 @@ __device__ __forceinline__ T v_elem(const T* __restrict__ A, int m, int j0, int 
   return r > d ? A[(int64_t)d * m + r] : zeroT<T>();
 }
 
+// The panel (rows j0 .. m-1 of its 32 columns) is worked on in shared memory when it fits
+// (panel_rows_cap rows; the launch provides the space), else in place in global memory.
 template <typename T>
 __global__ void __launch_bounds__(kPanelThreads) k_qr_panel(const QrJob* __restrict__ jobs, int j0, T* __restrict__ as,
-                                                       T* __restrict__ taus, T* __restrict__ tfac) {
+                                                       T* __restrict__ taus, T* __restrict__ tfac,
+                                                       int panel_rows_cap) {
+  extern __shared__ __align__(16) uint8_t panel_smem[];
   const QrJob jb = jobs[blockIdx.x];
   const int m = jb.m, n = jb.n, k = min(m, n);
   if (j0 >= k) return;
@@ -481,20 +494,33 @@ __global__ void __launch_bounds__(kPanelThreads) k_qr_panel(const QrJob* __restr
   T* A = as + jb.a_off;
   T* tau = taus + jb.tau_off;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int pr = m - j0;                       // panel rows
+  const bool in_smem = pr <= panel_rows_cap;
+  T* sp = reinterpret_cast<T*>(panel_smem);
+  // column c of the panel, indexed by (row - j0)
+  auto pcol = [&](int c) -> T* { return in_smem ? sp + (int64_t)c * pr : A + (int64_t)(j0 + c) * m + j0; };
+  if (in_smem) {
+    for (int64_t e = threadIdx.x; e < (int64_t)nbe * pr; e += kPanelThreads) {
+      const int c = (int)(e / pr), r = (int)(e - (int64_t)c * pr);
+      sp[e] = A[(int64_t)(j0 + c) * m + j0 + r];
+    }
+    __syncthreads();
+  }
   __shared__ double red[kPanelWarps];
   __shared__ T s_tau, s_scale;
   __shared__ T sY[kQrNb][kQrNb + 1], sT[kQrNb][kQrNb + 1];
-  for (int j = j0; j < j0 + nbe; ++j) {
-    T* col = A + (int64_t)j * m;
+  for (int jc = 0; jc < nbe; ++jc) {
+    const int j = j0 + jc;
+    T* col = pcol(jc);
     double part = 0;
-    for (int r = j + 1 + threadIdx.x; r < m; r += kPanelThreads) part += abs2(col[r]);
+    for (int r = jc + 1 + threadIdx.x; r < pr; r += kPanelThreads) part += abs2(col[r]);
     part = warp_sum(part);
     if (lane == 0) red[warp] = part;
     __syncthreads();
     if (threadIdx.x == 0) {
       double xn2 = 0;
       for (int w = 0; w < kPanelWarps; ++w) xn2 += red[w];
-      const T alpha = col[j];
+      const T alpha = col[jc];
       const double ar = re_of(alpha), ai = im_of(alpha);
       if (xn2 == 0.0 && ai == 0.0) {
         s_tau = mk<T>(0.0, 0.0);
@@ -506,22 +532,23 @@ __global__ void __launch_bounds__(kPanelThreads) k_qr_panel(const QrJob* __restr
         const double dr = ar - beta, di = ai;
         const double den = dr * dr + di * di;
         s_scale = mk<T>(dr / den, -di / den);
-        col[j] = mk<T>(beta, 0.0);
+        col[jc] = mk<T>(beta, 0.0);
       }
       tau[j] = s_tau;
     }
     __syncthreads();
     const T sc = s_scale;
-    for (int r = j + 1 + threadIdx.x; r < m; r += kPanelThreads) col[r] = mulT(col[r], sc);
+    for (int r = jc + 1 + threadIdx.x; r < pr; r += kPanelThreads) col[r] = mulT(col[r], sc);
     __syncthreads();
     // H_j^H on the panel's later columns only (the rest waits for the block update)
     const T tconj = conjT(s_tau);
     if (re_of(s_tau) != 0.0 || im_of(s_tau) != 0.0) {
-      for (int c = j + 1 + warp; c < j0 + nbe; c += kPanelWarps) {
-        T* ac = A + (int64_t)c * m;
+      for (int c = jc + 1 + warp; c < nbe; c += kPanelWarps) {
+        T* ac = pcol(c);
         double wr = 0, wi = 0;
-        for (int r = j + lane; r < m; r += 32) {
-          const T v = (r == j) ? mk<T>(1.0, 0.0) : col[r];
+#pragma unroll 4
+        for (int r = jc + lane; r < pr; r += 32) {
+          const T v = (r == jc) ? mk<T>(1.0, 0.0) : col[r];
           const T prod = mulT(conjT(v), ac[r]);
           wr += re_of(prod);
           wi += im_of(prod);
@@ -529,23 +556,24 @@ __global__ void __launch_bounds__(kPanelThreads) k_qr_panel(const QrJob* __restr
         wr = warp_sum(wr);
         wi = warp_sum(wi);
         const T w = mulT(tconj, mk<T>(wr, wi));
-        for (int r = j + lane; r < m; r += 32) {
-          const T v = (r == j) ? mk<T>(1.0, 0.0) : col[r];
+#pragma unroll 4
+        for (int r = jc + lane; r < pr; r += 32) {
+          const T v = (r == jc) ? mk<T>(1.0, 0.0) : col[r];
           ac[r] = subT(ac[r], mulT(v, w));
         }
       }
     }
     __syncthreads();
   }
-  // T: y(l, i) = v_l^H v_i for l < i (v_i starts at row j0 + i with a 1)
+  // T: y(l, i) = v_l^H v_i for l < i (v_i starts at panel row i with a 1)
   for (int i = 1; i < nbe; ++i) {
-    const T* vi = A + (int64_t)(j0 + i) * m;
+    const T* vi = pcol(i);
     for (int l = warp; l < i; l += kPanelWarps) {
-      const T* vl = A + (int64_t)(j0 + l) * m;
+      const T* vl = pcol(l);
       T acc = zeroT<T>();
-      for (int r = j0 + i + 1 + lane; r < m; r += 32) acc = fma_conj(vl[r], vi[r], acc);
+      for (int r = i + 1 + lane; r < pr; r += 32) acc = fma_conj(vl[r], vi[r], acc);
       double ar = warp_sum(re_of(acc)), ai = warp_sum(im_of(acc));
-      if (lane == 0) sY[l][i] = addT(mk<T>(ar, ai), conjT(vl[j0 + i]));
+      if (lane == 0) sY[l][i] = addT(mk<T>(ar, ai), conjT(vl[i]));
     }
   }
   __syncthreads();
@@ -567,16 +595,67 @@ __global__ void __launch_bounds__(kPanelThreads) k_qr_panel(const QrJob* __restr
     const int c = e / kQrNb, r = e % kQrNb;
     Tp[e] = (r < nbe && c < nbe && r <= c) ? sT[r][c] : zeroT<T>();
   }
+  if (in_smem) {
+    for (int64_t e = threadIdx.x; e < (int64_t)nbe * pr; e += kPanelThreads) {
+      const int c = (int)(e / pr), r = (int)(e - (int64_t)c * pr);
+      A[(int64_t)(j0 + c) * m + j0 + r] = sp[e];
+    }
+  }
 }
 
-// One 32-column tile of every group per CTA: X_tile -= V op(T) (V^H X_tile), op(T) = T^H for
-// the trailing update of A (FORM_Q false, X = A) and T for the backward formation of Q
-// (FORM_Q true, X = Q). Rows j0 .. m-1, streamed through shared memory kQrRc at a time.
+// The block-reflector update X_tile -= V op(T) (V^H X_tile), op(T) = T^H for the trailing
+// columns of A (FORM_Q false, X = A) and T for the backward formation of Q (FORM_Q true,
+// X = Q), in two launches over (tile, row chunk) items so a tall group spreads over many
+// CTAs: k_qr_wpart writes each item's partial W = V^H X over its rows, k_qr_apply sums the
+// partials of its tile in chunk order (deterministic), forms op(T) W and updates its rows.
+// Rows are streamed through shared memory kQrRc at a time.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_qr_wpart(const QrJob* __restrict__ jobs,
+                                                       const QrTile* __restrict__ tiles, int j0, bool form_q,
+                                                       const T* __restrict__ as, const T* __restrict__ xs,
+                                                       T* __restrict__ part) {
+  const QrTile tl = tiles[blockIdx.x];
+  const QrJob jb = jobs[tl.job];
+  const int m = jb.m, n = jb.n, k = min(m, n);
+  const int nbe = min(kQrNb, k - j0);
+  const T* A = as + jb.a_off;
+  const T* X = form_q ? xs + jb.q_off : xs + jb.a_off;
+  const int ncols = form_q ? k : n;
+  const int c0 = tl.c0, nc = min(32, ncols - c0);
+  constexpr int kQrRc = qr_rows_per_chunk<T>();
+  __shared__ T sV[kQrRc][kQrNb + 1], sX[kQrRc][33];
+  const int l = threadIdx.x & 31, cg = threadIdx.x >> 5;   // W entries (l, cg + 8 u)
+  T acc[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) acc[u] = zeroT<T>();
+  for (int r0 = tl.r0; r0 < tl.r1; r0 += kQrRc) {
+    for (int e = threadIdx.x; e < kQrRc * kQrNb; e += kThreads) {
+      const int rr = e % kQrRc, ll = e / kQrRc;
+      sV[rr][ll] = r0 + rr < tl.r1 ? v_elem(A, m, j0, nbe, r0 + rr, ll) : zeroT<T>();
+    }
+    for (int e = threadIdx.x; e < kQrRc * 32; e += kThreads) {
+      const int rr = e % kQrRc, c = e / kQrRc;
+      sX[rr][c] = (r0 + rr < tl.r1 && c < nc) ? X[(int64_t)(c0 + c) * m + r0 + rr] : zeroT<T>();
+    }
+    __syncthreads();
+    const int rn = min(kQrRc, tl.r1 - r0);
+    for (int rr = 0; rr < rn; ++rr) {
+      const T v = sV[rr][l];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc[u] = fma_conj(v, sX[rr][cg + 8 * u], acc[u]);
+    }
+    __syncthreads();
+  }
+  T* pw = part + (int64_t)blockIdx.x * kQrNb * 32;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) pw[l * 32 + cg + 8 * u] = acc[u];
+}
+
 template <typename T, bool FORM_Q>
-__global__ void __launch_bounds__(kThreads) k_qr_update(const QrJob* __restrict__ jobs,
-                                                        const QrTile* __restrict__ tiles, int j0,
-                                                        const T* __restrict__ as, const T* __restrict__ tfac,
-                                                        T* __restrict__ xs) {
+__global__ void __launch_bounds__(kThreads) k_qr_apply(const QrJob* __restrict__ jobs,
+                                                       const QrTile* __restrict__ tiles, int j0,
+                                                       const T* __restrict__ as, const T* __restrict__ tfac,
+                                                       const T* __restrict__ part, T* __restrict__ xs) {
   const QrTile tl = tiles[blockIdx.x];
   const QrJob jb = jobs[tl.job];
   const int m = jb.m, n = jb.n, k = min(m, n);
@@ -586,38 +665,20 @@ __global__ void __launch_bounds__(kThreads) k_qr_update(const QrJob* __restrict_
   const int ncols = FORM_Q ? k : n;
   const int c0 = tl.c0, nc = min(32, ncols - c0);
   constexpr int kQrRc = qr_rows_per_chunk<T>();
-  __shared__ T sV[kQrRc][kQrNb + 1], sX[kQrRc][33], sW[kQrNb][33];
+  __shared__ T sV[kQrRc][kQrNb + 1], sW[kQrNb][33];
   // T(r, c) of this panel, column-major 32 x 32 (read through the cache)
   const T* Tp = tfac + jb.t_off + (int64_t)(j0 / kQrNb) * kQrNb * kQrNb;
-  const int l = threadIdx.x & 31, cg = threadIdx.x >> 5;   // W entries (l, cg + 8 u)
-  T acc[4];
+  const int l = threadIdx.x & 31, cg = threadIdx.x >> 5;
+  // W of the tile: its chunks' partials summed in chunk order
 #pragma unroll
-  for (int u = 0; u < 4; ++u) acc[u] = zeroT<T>();
-  auto load_v = [&](int r0) {
-    for (int e = threadIdx.x; e < kQrRc * kQrNb; e += kThreads) {
-      const int rr = e % kQrRc, ll = e / kQrRc;
-      sV[rr][ll] = v_elem(A, m, j0, nbe, r0 + rr, ll);
-    }
-  };
-  for (int r0 = j0; r0 < m; r0 += kQrRc) {
-    load_v(r0);
-    for (int e = threadIdx.x; e < kQrRc * 32; e += kThreads) {
-      const int rr = e % kQrRc, c = e / kQrRc;
-      sX[rr][c] = (r0 + rr < m && c < nc) ? X[(int64_t)(c0 + c) * m + r0 + rr] : zeroT<T>();
-    }
-    __syncthreads();
-    const int rn = min(kQrRc, m - r0);
-    for (int rr = 0; rr < rn; ++rr) {
-      const T v = sV[rr][l];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) acc[u] = fma_conj(v, sX[rr][cg + 8 * u], acc[u]);
-    }
-    __syncthreads();
+  for (int u = 0; u < 4; ++u) {
+    T w = zeroT<T>();
+    for (int ch = 0; ch < tl.nchunks; ++ch) w = addT(w, part[((int64_t)(tl.first + ch) * kQrNb + l) * 32 + cg + 8 * u]);
+    sW[l][cg + 8 * u] = w;
   }
-#pragma unroll
-  for (int u = 0; u < 4; ++u) sW[l][cg + 8 * u] = acc[u];
   __syncthreads();
   // W2 = T^H W (trailing update) or T W (Q), T upper triangular
+  T acc[4];
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
     const int c = cg + 8 * u;
@@ -633,15 +694,18 @@ __global__ void __launch_bounds__(kThreads) k_qr_update(const QrJob* __restrict_
 #pragma unroll
   for (int u = 0; u < 4; ++u) sW[l][cg + 8 * u] = acc[u];
   __syncthreads();
-  // X -= V W2
+  // X -= V W2 over this item's rows
   const int c = threadIdx.x & 31, rg = threadIdx.x >> 5;
-  for (int r0 = j0; r0 < m; r0 += kQrRc) {
-    load_v(r0);
+  for (int r0 = tl.r0; r0 < tl.r1; r0 += kQrRc) {
+    for (int e = threadIdx.x; e < kQrRc * kQrNb; e += kThreads) {
+      const int rr = e % kQrRc, ll = e / kQrRc;
+      sV[rr][ll] = r0 + rr < tl.r1 ? v_elem(A, m, j0, nbe, r0 + rr, ll) : zeroT<T>();
+    }
     __syncthreads();
     if (c < nc) {
       for (int rr = rg; rr < kQrRc; rr += kThreads / 32) {
         const int r = r0 + rr;
-        if (r >= m) break;
+        if (r >= tl.r1) break;
         T z = zeroT<T>();
 #pragma unroll 8
         for (int ll = 0; ll < kQrNb; ++ll) z = fmaT(sV[rr][ll], sW[ll][c], z);
@@ -755,7 +819,7 @@ unsigned grid_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<in
 // launch (one CTA per job) and one trailing-update launch over all jobs' column tiles; then
 // Q = I and one update launch per panel, last panel first. The jobs' t_off are assigned here.
 struct QrBuffers {
-  DevBuf jobs, tiles, tfac;
+  DevBuf jobs, tiles, tfac, part;
 };
 template <typename T>
 void launch_blocked_qr(std::vector<QrJob>& jobs, T* A, T* tau, T* Q, cudaStream_t s, QrBuffers& keep) {
@@ -773,14 +837,25 @@ void launch_blocked_qr(std::vector<QrJob>& jobs, T* A, T* tau, T* Q, cudaStream_
   // tiles of panel p: trailing columns of A (p in [0, np)), then columns j0 .. k-1 of Q
   std::vector<QrTile> tiles;
   std::vector<int64_t> trail_begin(np + 1), q_begin(np + 1);
+  // one item per (tile, chunk of kQrRowChunk rows from j0); item indices are relative to the
+  // launch that runs them (the partial sums of a launch start at 0)
+  int64_t max_items = 1;
+  auto add_tile = [&](int g, int c0, int j0, int64_t begin) {
+    const int m = jobs[g].m;
+    const int nch = (m - j0 + kQrRowChunk - 1) / kQrRowChunk;
+    const int first = (int)((int64_t)tiles.size() - begin);
+    for (int ch = 0; ch < nch; ++ch)
+      tiles.push_back(QrTile{g, c0, j0 + ch * kQrRowChunk, std::min(m, j0 + (ch + 1) * kQrRowChunk), first, nch});
+  };
   for (int p = 0; p < np; ++p) {
     trail_begin[p] = (int64_t)tiles.size();
     const int j0 = p * kQrNb;
     for (int g = 0; g < ng; ++g) {
       const int k = std::min(jobs[g].m, jobs[g].n);
       if (j0 >= k) continue;
-      for (int c0 = j0 + std::min(kQrNb, k - j0); c0 < jobs[g].n; c0 += 32) tiles.push_back(QrTile{g, c0});
+      for (int c0 = j0 + std::min(kQrNb, k - j0); c0 < jobs[g].n; c0 += 32) add_tile(g, c0, j0, trail_begin[p]);
     }
+    max_items = std::max<int64_t>(max_items, (int64_t)tiles.size() - trail_begin[p]);
   }
   trail_begin[np] = (int64_t)tiles.size();
   for (int p = 0; p < np; ++p) {
@@ -789,22 +864,45 @@ void launch_blocked_qr(std::vector<QrJob>& jobs, T* A, T* tau, T* Q, cudaStream_
     for (int g = 0; g < ng; ++g) {
       const int k = std::min(jobs[g].m, jobs[g].n);
       if (j0 >= k) continue;
-      for (int c0 = j0; c0 < k; c0 += 32) tiles.push_back(QrTile{g, c0});
+      for (int c0 = j0; c0 < k; c0 += 32) add_tile(g, c0, j0, q_begin[p]);
     }
+    max_items = std::max<int64_t>(max_items, (int64_t)tiles.size() - q_begin[p]);
   }
   q_begin[np] = (int64_t)tiles.size();
-  QLTG_CHECK(tiles.size() < ((size_t)1 << 31), QLTG_ERR_UNSUPPORTED, "too many QR tiles");
+  QLTG_CHECK(tiles.size() < ((size_t)1 << 31), QLTG_ERR_UNSUPPORTED, "too many QR work items");
   keep.jobs = upload(jobs, s);
   keep.tiles = upload(tiles.empty() ? std::vector<QrTile>{QrTile{0, 0}} : tiles, s);
   keep.tfac.alloc(std::max<int64_t>(1, toff) * sizeof(T));
+  keep.part.alloc(max_items * kQrNb * 32 * sizeof(T));
+  T* pw = keep.part.as<T>();
+  {
+    static std::mutex mu;
+    static bool done[2][64] = {};
+    int dev = 0;
+    QLTG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0 || dev >= 64 || !done[sizeof(T) == 16][dev]) {
+      QLTG_CUDA(cudaFuncSetAttribute(k_qr_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, qr_panel_smem<T>()));
+      if (dev >= 0 && dev < 64) done[sizeof(T) == 16][dev] = true;
+    }
+  }
   const QrJob* dj = keep.jobs.as<QrJob>();
   const QrTile* dt = keep.tiles.as<QrTile>();
   T* tf = keep.tfac.as<T>();
   for (int p = 0; p < np; ++p) {
     const int j0 = p * kQrNb;
-    k_qr_panel<T><<<ng, kPanelThreads, 0, s>>>(dj, j0, A, tau, tf);
+    // the panel in shared memory when the tallest active one fits
+    int rows_max = 0;
+    for (auto& j : jobs)
+      if (j0 < std::min(j.m, j.n)) rows_max = std::max(rows_max, j.m - j0);
+    const int cap = qr_panel_smem<T>() / (kQrNb * (int)sizeof(T));
+    const size_t smem = rows_max <= cap ? (size_t)rows_max * kQrNb * sizeof(T) : 0;
+    k_qr_panel<T><<<ng, kPanelThreads, smem, s>>>(dj, j0, A, tau, tf, smem ? rows_max : 0);
     const int64_t nt = trail_begin[p + 1] - trail_begin[p];
-    if (nt) k_qr_update<T, false><<<(unsigned)nt, kThreads, 0, s>>>(dj, dt + trail_begin[p], j0, A, tf, A);
+    if (nt) {
+      k_qr_wpart<T><<<(unsigned)nt, kThreads, 0, s>>>(dj, dt + trail_begin[p], j0, false, A, A, pw);
+      k_qr_apply<T, false><<<(unsigned)nt, kThreads, 0, s>>>(dj, dt + trail_begin[p], j0, A, tf, pw, A);
+    }
   }
   const int64_t total_q = std::accumulate(jobs.begin(), jobs.end(), (int64_t)0, [](int64_t a, const QrJob& j) {
     return std::max<int64_t>(a, (int64_t)j.m * std::min(j.m, j.n));
@@ -813,7 +911,10 @@ void launch_blocked_qr(std::vector<QrJob>& jobs, T* A, T* tau, T* Q, cudaStream_
                        (unsigned)std::min(ng, 1024)), 256, 0, s>>>(dj, ng, Q);
   for (int p = np - 1; p >= 0; --p) {
     const int64_t nt = q_begin[p + 1] - q_begin[p];
-    if (nt) k_qr_update<T, true><<<(unsigned)nt, kThreads, 0, s>>>(dj, dt + q_begin[p], p * kQrNb, A, tf, Q);
+    if (nt) {
+      k_qr_wpart<T><<<(unsigned)nt, kThreads, 0, s>>>(dj, dt + q_begin[p], p * kQrNb, true, A, Q, pw);
+      k_qr_apply<T, true><<<(unsigned)nt, kThreads, 0, s>>>(dj, dt + q_begin[p], p * kQrNb, A, tf, pw, Q);
+    }
   }
   QLTG_CUDA(cudaGetLastError());
 }

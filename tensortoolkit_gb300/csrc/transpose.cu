@@ -26,7 +26,8 @@ namespace qltg {
 namespace {
 
 constexpr int kTile = 32;
-constexpr int kTileMax = 4096;    // elements per batched tile (Tp * Tq * Tu)
+constexpr int kTileMax = 2048;    // elements per batched tile (Tp * Tq * Tu): 24 KB of shared
+                                  // memory for FP64, so eight 256-thread CTAs fit on an SM
 constexpr int kRunChunk = 4096;   // elements per copy-mode / gather-mode work item
 constexpr int kPermThreads = 256;
 constexpr int kLoadBatch = 8;     // tile-mode loads issued per thread before storing
@@ -234,9 +235,15 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
         if (slot[i] >= 0) tile[slot[i]] = v[i];
     }
     __syncthreads();
-    // write: q fastest (stride 1 in the destination)
+    // write: q fastest (stride 1 in the destination), then whichever of u and p has the
+    // smaller destination stride, so consecutive threads write consecutive addresses where the
+    // destination has them (a short q dim with u next to it in the destination)
+    const int lu = __ffs(tu) - 1;
+    const bool u_next = d.u >= 0 && du < dp;
     for (int e = threadIdx.x; e < n; e += kPermThreads) {
-      const int qi = e & (tq - 1), pi = (e >> lq) & (tp - 1), ui = e >> (lp + lq);
+      const int qi = e & (tq - 1);
+      const int pi = u_next ? (e >> (lq + lu)) & (tp - 1) : (e >> lq) & (tp - 1);
+      const int ui = u_next ? (e >> lq) & (tu - 1) : e >> (lp + lq);
       if (p0 + pi < np_ && q0 + qi < nq && ui < ulim)
         o[(q0 + qi) + (p0 + pi) * dp + ui * du] = flip(tile[ui * plane + qi * row + pi], sg);
     }
