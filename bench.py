@@ -639,6 +639,16 @@ def run_aux(local: int, part: str = "all"):
         return r
     if part in ("all", "proxy"):
         out["fp64_vs_reference_gpu_pattern_d4000"] = run_proxy(local, stream, flush)
+    if part in ("all", "fp64rates"):
+        import ctypes as C
+        from tensortoolkit_gb300 import capi
+        from tensortoolkit_gb300.api import context, stream_ptr
+        f, m = C.c_double(), C.c_double()
+        capi.check(capi.lib().qltg_selftest_fp64_rates(context(local).h, C.byref(f), C.byref(m), stream_ptr(local)))
+        out["fp64_rates"] = {"dfma_tflops": round(f.value, 3), "dmma_mma_sync_m8n8k4_tflops": round(m.value, 3),
+                             "cublas_dgemm_8192_tflops": round(fp64_peak_tflops(local, stream), 3),
+                             "note": "qltg_selftest_fp64_rates: DFMA loop (8 chains per thread) and mma.sync "
+                                     "m8n8k4 f64 loop (4 fragments per warp, 512 flops each) over 8 CTAs per SM"}
     if part in ("all", "adapter"):
         out["adapter_contract_costs_d4000"] = run_adapter_costs(local)
     if part in ("all", "matvec"):
@@ -721,7 +731,7 @@ def main():
     ap.add_argument("--aux", action="store_true",
                     help="measurements beside the headline: permute GB/s, batched SVD/QR vs per-block, "
                          "Config 2 and Config 5 matvecs (one JSON line)")
-    ap.add_argument("--aux-part", choices=["all", "transpose", "svd", "matvec", "proxy", "adapter"], default="all")
+    ap.add_argument("--aux-part", choices=["all", "transpose", "svd", "matvec", "proxy", "adapter", "fp64rates"], default="all")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: plan the D=4000 matvec, apply it twice, print nothing else")
     ap.add_argument("--profile-case", choices=["matvec", "step0", "step3", "svd", "qr"], default="matvec",

@@ -98,6 +98,12 @@ QLTG_API const char* qltg_last_error(void);
  * the context stays usable), QLTG_OK if it had completed. Synchronises `stream`. */
 QLTG_API int qltg_selftest_bounded_wait(qltg_ctx* ctx, int64_t limit_cycles, void* stream);
 
+/* Measured FP64 throughput of the device in TFLOP/s: a DFMA loop and an mma.sync m8n8k4 f64
+ * (DMMA) loop over the whole GPU, timed with CUDA events (the reason the FP64 GEMM kernels use
+ * DFMA: equal rates, and DMMA pads blocks to 8 x 8 x 4 fragments). No counterpart in the
+ * reference. Synchronises `stream`. */
+QLTG_API int qltg_selftest_fp64_rates(qltg_ctx* ctx, double* dfma_tflops, double* dmma_tflops, void* stream);
+
 /* ---------------------------------------------------------------- contraction */
 typedef struct qltg_ctrct_plan qltg_ctrct_plan;
 

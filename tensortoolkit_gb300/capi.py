@@ -95,6 +95,7 @@ _SIGS = {
     "qltg_matvec_apply": ([_P, _P, _P, _P], C.c_int),
     "qltg_matvec_apply_host": ([_P, _P, _P, _P], C.c_int),
     "qltg_selftest_bounded_wait": ([_P, C.c_int64, _P], C.c_int),
+    "qltg_selftest_fp64_rates": ([_P, C.POINTER(C.c_double), C.POINTER(C.c_double), _P], C.c_int),
     "qltg_matvec_device_status": ([_P, _P], C.c_int),
     "qltg_matvec_destroy": ([_P], C.c_int),
     "qltg_lanczos_create": ([_P, C.c_int32, C.POINTER(_P)], C.c_int),

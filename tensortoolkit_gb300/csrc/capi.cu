@@ -424,3 +424,11 @@ extern "C" int qltg_selftest_bounded_wait(qltg_ctx* ctx, int64_t limit_cycles, v
     QLTG_CHECK(!expired, QLTG_ERR_TIMEOUT, "the bounded wait expired after its limit, as intended");
   });
 }
+
+extern "C" int qltg_selftest_fp64_rates(qltg_ctx* ctx, double* dfma_tflops, double* dmma_tflops, void* stream) {
+  return qltg::guarded([&] {
+    QLTG_CHECK(ctx && dfma_tflops && dmma_tflops, QLTG_ERR_INVALID, "null ctx or out-pointer");
+    QLTG_CUDA(cudaSetDevice(ctx->device));
+    qltg::fp64_rates(ctx->num_sms, static_cast<cudaStream_t>(stream), dfma_tflops, dmma_tflops);
+  });
+}

@@ -235,6 +235,9 @@ void launch_gemm_f64(const GemmSchedule& g, const Operands& op, void* c, bool cp
 void launch_gemm_f64_skinny(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms,
                             cudaStream_t s, const SkinnyFuse* fuse = nullptr, int32_t* fields = nullptr);
 
+// FP64 rate self-test (gemm_f64.cu): DFMA and mma.sync f64 throughput of this GPU, TFLOP/s.
+void fp64_rates(int num_sms, cudaStream_t s, double* dfma_tflops, double* dmma_tflops);
+
 // Block order, destination offsets and fermionic block signs of QLTensor::Transpose.
 void transpose_layout(const Meta& m, const std::vector<int>& order, std::vector<double>& signs,
                       std::vector<int64_t>& dst_off);

@@ -451,4 +451,65 @@ void launch_gemm_f64(const GemmSchedule& g, const Operands& op, void* c, bool cp
   }
 }
 
+// ------------------------------------------------------------------ FP64 rate self-test
+// The two FP64 arithmetic paths of this GPU side by side, measured rather than assumed: a
+// DFMA loop (8 independent chains per thread) and an mma.sync m8n8k4 f64 loop (4 independent
+// accumulator fragments per warp; 8 x 8 x 4 multiply-adds = 512 flops per instruction). The
+// FP64 GEMM kernels above use DFMA because the two run at the same rate here while the MMA
+// path pads every block to 8 x 8 x 4 fragments.
+constexpr int kRateIters = 4096;
+__global__ void __launch_bounds__(256) k_rate_dfma(double* out, double seed) {
+  double a[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) a[i] = seed + threadIdx.x + i;
+  const double b = 1.0 + 1e-12 * seed, c = 1e-300;
+  for (int it = 0; it < kRateIters; ++it)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = fma(a[i], b, c);
+  double t = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) t += a[i];
+  if (t == 1.2345) out[0] = t;   // keeps the loop; never true for these inputs
+}
+__global__ void __launch_bounds__(256) k_rate_dmma(double* out, double seed) {
+  const double av = seed + (threadIdx.x & 31), bv = 1.0 + 1e-12 * seed;
+  double d[4][2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) d[i][0] = d[i][1] = 0.0;
+  for (int it = 0; it < kRateIters; ++it)
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                   : "+d"(d[i][0]), "+d"(d[i][1])
+                   : "d"(av), "d"(bv));
+  double t = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) t += d[i][0] + d[i][1];
+  if (t == 1.2345) out[0] = t;
+}
+
+void fp64_rates(int num_sms, cudaStream_t s, double* dfma_tflops, double* dmma_tflops) {
+  DevBuf sink(sizeof(double));
+  const int grid = std::max(1, num_sms) * 8;
+  cudaEvent_t e[4];
+  for (auto& x : e) QLTG_CUDA(cudaEventCreate(&x));
+  k_rate_dfma<<<grid, 256, 0, s>>>(sink.as<double>(), 1.0);   // warm-up
+  k_rate_dmma<<<grid, 256, 0, s>>>(sink.as<double>(), 1.0);
+  QLTG_CUDA(cudaEventRecord(e[0], s));
+  k_rate_dfma<<<grid, 256, 0, s>>>(sink.as<double>(), 2.0);
+  QLTG_CUDA(cudaEventRecord(e[1], s));
+  QLTG_CUDA(cudaEventRecord(e[2], s));
+  k_rate_dmma<<<grid, 256, 0, s>>>(sink.as<double>(), 2.0);
+  QLTG_CUDA(cudaEventRecord(e[3], s));
+  QLTG_CUDA(cudaGetLastError());
+  QLTG_CUDA(cudaEventSynchronize(e[3]));
+  float ms_f = 0, ms_m = 0;
+  QLTG_CUDA(cudaEventElapsedTime(&ms_f, e[0], e[1]));
+  QLTG_CUDA(cudaEventElapsedTime(&ms_m, e[2], e[3]));
+  for (auto x : e) cudaEventDestroy(x);
+  const double threads = (double)grid * 256, warps = threads / 32;
+  *dfma_tflops = threads * kRateIters * 8 * 2 / (ms_f * 1e-3) / 1e12;
+  *dmma_tflops = warps * kRateIters * 4 * 512 / (ms_m * 1e-3) / 1e12;
+}
+
 }  // namespace qltg
