@@ -436,13 +436,15 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
   if (elect_one())
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
 }
-// D (+)= A B, both operands from shared memory.
-__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t da, uint64_t db, uint32_t id, uint32_t acc) {
-  if (elect_one())
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-        "l"(da), "l"(db), "r"(id), "r"(acc));
+// The same, issued by the calling thread alone (the caller elects it).
+__device__ __forceinline__ void tc_commit_issue(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
+}
+__device__ __forceinline__ void mma_bf16_issue(uint32_t d, uint64_t da, uint64_t db, uint32_t id, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+      "l"(da), "l"(db), "r"(id), "r"(acc));
 }
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -700,19 +702,26 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
           asm volatile("tcgen05.fence::after_thread_sync;");
           const uint64_t soff = (uint64_t)((s * kStageBytes) >> 4);
           const uint32_t dbuf = tmem + (uint32_t)(buf * kAccCols);
+          // one elected lane issues the stage's 14 MMAs and its commits: the warp shares its
+          // scheduler with four busy drain warps, so the fewer instructions between two MMAs,
+          // the less the tensor pipe waits for the next one
+          if (elect_one()) {
 #pragma unroll
-          for (int ks = 0; ks < kKS / 16; ++ks) {
-            const uint64_t bdesc = sd0 + soff + (uint64_t)((kABytes + ks * kBStep) >> 4);
+            for (int ks = 0; ks < kKS / 16; ++ks) {
+              const uint64_t bdesc = sd0 + soff + (uint64_t)((kABytes + ks * kBStep) >> 4);
 #pragma unroll
-            for (int p = 1; p <= kS; ++p) {
-              const uint64_t adesc = sd0 + soff + (uint64_t)((ks * kAStep + (p - 1) * kTM * 32) >> 4);
-              // the first MMA of a period (p = 1, all 224 columns) overwrites the set
-              const uint32_t acc = (first && ks == 0 && p == 1) ? 0u : 1u;
-              mma_bf16(dbuf + (uint32_t)((p - 1) * kTN), adesc, bdesc, idesc_bf16(kTN * (kS + 1 - p)), acc);
+              for (int p = 1; p <= kS; ++p) {
+                const uint64_t adesc = sd0 + soff + (uint64_t)((ks * kAStep + (p - 1) * kTM * 32) >> 4);
+                // the first MMA of a period (p = 1, all 224 columns) overwrites the set
+                const uint32_t acc = (first && ks == 0 && p == 1) ? 0u : 1u;
+                mma_bf16_issue(dbuf + (uint32_t)((p - 1) * kTN), adesc, bdesc, idesc_bf16(kTN * (kS + 1 - p)), acc);
+              }
             }
+            tc_commit_issue(smem_u32(&empty_bar[s]));
+            if (drain) tc_commit_issue(smem_u32(&accf_bar[buf]));
           }
-          tc_commit(smem_u32(&empty_bar[s]));
-          if (drain) { tc_commit(smem_u32(&accf_bar[buf])); ++d; }
+          __syncwarp();
+          if (drain) ++d;
         }
       }
     }

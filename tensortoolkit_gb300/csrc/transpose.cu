@@ -26,8 +26,7 @@ namespace qltg {
 namespace {
 
 constexpr int kTile = 32;
-constexpr int kTileMax = 2048;    // elements per batched tile (Tp * Tq * Tu): 24 KB of shared
-                                  // memory for FP64, so eight 256-thread CTAs fit on an SM
+constexpr int kTileMax = 4096;    // elements per batched tile (Tp * Tq * Tu)
 constexpr int kRunChunk = 4096;   // elements per copy-mode / gather-mode work item
 constexpr int kPermThreads = 256;
 constexpr int kLoadBatch = 8;     // tile-mode loads issued per thread before storing
