@@ -440,6 +440,22 @@ def run_proxy(local: int, stream, flush, reps: int = 5) -> dict:
     got = bufs[-1][2][: ours.size].cpu().numpy()
     err = float(np.linalg.norm(got - ours.data) / np.linalg.norm(ours.data))
     t_proxy = _time_events(proxy_matvec, stream, flush, reps=reps)
+    # the same launches captured once into a CUDA graph and replayed: kernels only, without the
+    # host's per-call dispatch (a lower bound for the pattern however it is issued)
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream(device=f"cuda:{local}")
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        proxy_matvec()
+    torch.cuda.current_stream().wait_stream(side)
+    with torch.cuda.graph(graph):
+        proxy_matvec()
+    bufs[-1][2].zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    got_g = bufs[-1][2][: ours.size].cpu().numpy()
+    err_g = float(np.linalg.norm(got_g - ours.data) / np.linalg.norm(ours.data))
+    t_graph = _time_events(graph.replay, stream, flush, reps=reps)
     per_step = []
     for st, (a, b, c) in zip(steps, bufs):
         per_step.append(round(_time_events(lambda: st.run(a, b, c), stream, flush, reps=reps), 3))
@@ -447,13 +463,16 @@ def run_proxy(local: int, stream, flush, reps: int = 5) -> dict:
     t_ours = _time_events(lambda: mv.apply(dp, o), stream, flush, reps=10)
     ntasks = sum(len(st.tasks) for st in steps)
     return {"proxy_fp64_ms_per_matvec": round(t_proxy, 3), "proxy_ms_per_step": per_step,
+            "proxy_graph_ms_per_matvec": round(t_graph, 3), "proxy_graph_vs_ours_rel_err": err_g,
             "ours_fp64_ms_per_matvec": round(t_ours, 4), "ours_vs_proxy_speedup": round(t_proxy / t_ours, 2),
+            "ours_vs_proxy_graph_speedup": round(t_graph / t_ours, 2),
             "proxy_vs_ours_rel_err": err, "gemm_calls_per_matvec": ntasks,
             "note": "labelled proxy of the reference CUDA build's pattern (the build itself needs cuTENSOR, "
                     "absent on this host): per operand block one strided-copy permute, then one cuBLAS "
                     "DGEMM per task in task order on one stream, with torch's caching allocator in place "
                     "of the reference's cudaMalloc / cudaFree per transposed block (so the proxy is, if "
-                    "anything, faster than the reference build)"}
+                    "anything, faster than the reference build); proxy_graph = the same launches "
+                    "replayed from one CUDA graph (no per-call host dispatch: a lower bound)"}
 
 
 def run_adapter_costs(local: int) -> dict:
@@ -509,7 +528,8 @@ def run_adapter_costs(local: int) -> dict:
 def run_profile_case(case: str, tensors, dev, local: int) -> None:
     """Profiling drivers (one small, fixed piece of work each, for ncu captures): the split GEMM
     of the D=4000 matvec's first (step0) or last (step3) contraction, stacked schedule, run
-    twice; Config 3's batched SVD; the stress QR (41 square blocks 10..800)."""
+    twice; three applies of the Config 5 split matvec (fU(1) x U(1) complex, D=6000); Config 3's
+    batched SVD; the stress QR (41 square blocks 10..800)."""
     import torch
     from tensortoolkit_gb300 import workloads
     from tensortoolkit_gb300.api import Contract, ContractionPlan, DTensor, QR, SVD
@@ -529,6 +549,16 @@ def run_profile_case(case: str, tensors, dev, local: int) -> None:
             p.execute(a, b, c, mode="split")
         torch.cuda.synchronize()
         p.device_status()
+    elif case == "matvec5":
+        from tensortoolkit_gb300.api import Matvec
+        lenv5, psi5, m15, m25, renv5 = workloads.hubbard(6000, 10, 4)
+        d5 = [DTensor.from_host(x, local) for x in (lenv5, psi5, m15, m25, renv5)]
+        mv = Matvec(d5[0], psi5, d5[2], d5[3], d5[4], mode="split")
+        o = DTensor.empty(mv.result, local)
+        for _ in range(3):
+            mv.apply(d5[1], o)
+        torch.cuda.synchronize()
+        mv.device_status()
     elif case == "svd":
         SVD(DTensor.from_host(workloads.svd_psi(2000, 20, 6.0, 3), local), 2, [0], 1e-9, 1, 2000)
     else:
@@ -734,7 +764,7 @@ def main():
     ap.add_argument("--aux-part", choices=["all", "transpose", "svd", "matvec", "proxy", "adapter", "fp64rates"], default="all")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: plan the D=4000 matvec, apply it twice, print nothing else")
-    ap.add_argument("--profile-case", choices=["matvec", "step0", "step3", "svd", "qr"], default="matvec",
+    ap.add_argument("--profile-case", choices=["matvec", "matvec5", "step0", "step3", "svd", "qr"], default="matvec",
                     help="with --profile: the matvec (default); one of its split-precision GEMM steps "
                          "(stacked schedule, executed twice); Config 3's batched SVD; the stress QR")
     args = ap.parse_args()

@@ -126,72 +126,68 @@ __device__ __forceinline__ int rr_player(int slot, int r, int qq) {
   return slot == 0 ? 0 : ((slot - 1 + r) % (qq - 1)) + 1;
 }
 
-// Rotate stacked columns xi, xj (length L: the p entries of W, then the q of V) so that
-// their first p entries become orthogonal, unless they already are to `tol` (relative).
-// Convergence: a pair is rotated only if |<wi, wj>| > tol ||wi|| ||wj|| (relative
-// orthogonality) and |<wi, wj>| > tol ||A||_F max(||wi||, ||wj||) (absolute floor: pairs whose
-// inner product is at the rounding level of the whole matrix are left alone, which bounds the
-// singular-value change to about tol ||A|| absolute - the accuracy LAPACK's ?gesvd gives).
+// ---- one-sided Jacobi: a round of disjoint column pairs in shared memory ----------------
+// Columns are held scaled: the true column i is sc[i] * x_i (x_i in shared memory), its
+// squared 2-norm (of the first p entries) tracked in dn[i]. A rotation that makes columns i
+// and j orthogonal (the Jacobi angle of their 2 x 2 Gram matrix [[a, g], [conj g, b]],
+// zeta = (b - a) / 2|g|, t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)), c = 1 / sqrt(1 + t^2),
+// tau = t conj(g) / |g|) becomes two multiply-adds per entry,
+//   x_i <- x_i - (tau sc_j / sc_i) x_j,   x_j <- x_j + (conj(tau) sc_i / sc_j) x_i,
+// with sc_i, sc_j <- c sc_i, c sc_j, and the norms follow a <- a - t|g|, b <- b + t|g|.
+// A norm that fell below half its value is recomputed from the data the next time its
+// column is in a pair; every column is recomputed when it is loaded. A round runs in three
+// phases between barriers: (1) one warp per pair forms <x_i, x_j>; (2) warp 0 decides and
+// computes the rotations, one lane per pair, and lists the rotated ones; (3) all warps
+// apply them over (pair, 32-entry chunk) items.
+constexpr int kJacThreads = 256;
+constexpr int kJacWarps = kJacThreads / 32;
+constexpr int kJacAuxPerCol = 64;    // shared-memory bytes per column for the bookkeeping below
+constexpr int kJacAuxFixed = 256;
+
 template <typename T>
-__device__ __forceinline__ void rotate_cols(T* __restrict__ xi, T* __restrict__ xj, int p, int L, double tol,
-                                            double tol_abs, int lane, int* rotated) {
-  double a = 0, b = 0;
-  T g;
+struct JacRot {
+  int32_t i, j;
+  T alpha, beta;
+};
+
+template <typename T>
+__device__ __forceinline__ T jac_conj(T x) {
+  if constexpr (sizeof(T) == 8) return x; else return make_double2(x.x, -x.y);
+}
+template <typename T>
+__device__ __forceinline__ T jac_scale(T x, double s) {
+  if constexpr (sizeof(T) == 8) return x * s; else return make_double2(x.x * s, x.y * s);
+}
+// x - a y and y + b x, fused
+template <typename T>
+__device__ __forceinline__ void jac_apply(T& x, T& y, T a, T b) {
   if constexpr (sizeof(T) == 8) {
-    double gg = 0;
-    for (int e = lane; e < p; e += 32) {
-      const double x = xi[e], y = xj[e];
-      a = fma(x, x, a); b = fma(y, y, b); gg = fma(x, y, gg);
-    }
-    g = warp_sum(gg);
+    const double x0 = x;
+    x = fma(-a, y, x0);
+    y = fma(b, x0, y);
   } else {
-    double gr = 0, gi = 0;
-    for (int e = lane; e < p; e += 32) {
-      const double2 x = xi[e], y = xj[e];
-      a += abs2(x); b += abs2(y);
-      const double2 t = cconjmul(x, y);
-      gr += t.x; gi += t.y;
-    }
-    g = make_double2(warp_sum(gr), warp_sum(gi));
-  }
-  a = warp_sum(a);
-  b = warp_sum(b);
-  const double gabs = sqrt(abs2(g));
-  if (!(gabs > tol * sqrt(a) * sqrt(b)) || !(gabs > tol_abs * sqrt(fmax(a, b))) || gabs == 0.0) return;
-  if (lane == 0) *rotated = 1;
-  const double zeta = (b - a) / (2.0 * gabs);
-  const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-  const double c = 1.0 / sqrt(1.0 + t * t);
-  const double sn = c * t;
-  if constexpr (sizeof(T) == 8) {
-    const double sg = g >= 0 ? sn : -sn;   // e^{i phi} = sign(g)
-    for (int e = lane; e < L; e += 32) {
-      const double x = xi[e], y = xj[e];
-      xi[e] = c * x - sg * y;
-      xj[e] = sg * x + c * y;
-    }
-  } else {
-    // [xi', xj'] = [xi, xj] [[c, s e^{i phi}], [-s e^{-i phi}, c]],  e^{i phi} = g / |g|
-    const double2 ph = make_double2(g.x / gabs, g.y / gabs);
-    const double2 sp = make_double2(sn * ph.x, sn * ph.y);          // s e^{i phi}
-    const double2 sm = make_double2(sn * ph.x, -sn * ph.y);         // s e^{-i phi}
-    for (int e = lane; e < L; e += 32) {
-      const double2 x = xi[e], y = xj[e];
-      const double2 a1 = cmul(sm, y), b1 = cmul(sp, x);
-      xi[e] = make_double2(c * x.x - a1.x, c * x.y - a1.y);
-      xj[e] = make_double2(b1.x + c * y.x, b1.y + c * y.y);
-    }
+    const double2 x0 = x;
+    x = make_double2(fma(-a.x, y.x, fma(a.y, y.y, x0.x)), fma(-a.x, y.y, fma(-a.y, y.x, x0.y)));
+    y = make_double2(fma(b.x, x0.x, fma(-b.y, x0.y, y.x)), fma(b.x, x0.y, fma(b.y, x0.x, y.y)));
   }
 }
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src));
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src));
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // Blocked one-sided Jacobi. The q columns of the stacked matrix [W; V] (W: p x q, V: q x q
 // accumulated rotations, both vector-major in global memory) are cut into 2M blocks of nb
-// columns, nb chosen so that two blocks fit in shared memory. A sweep is the 2M - 1 steps
-// of a round-robin tournament over the blocks; in each step a CTA takes block pairs
-// (a, b), loads their columns into shared memory, runs a full round-robin sweep over those
-// columns there (only __syncthreads between rounds) and writes them back. With M = 1 all
-// columns stay in shared memory for every sweep. One cluster of cl CTAs per job; the
-// cluster barrier separates steps, so a sweep costs 2M - 1 barriers instead of q - 1.
+// columns, nb chosen so that two blocks (and their bookkeeping) fit in shared memory. A sweep
+// is the 2M - 1 steps of a round-robin tournament over the blocks; in each step a CTA takes
+// block pairs (a, b), loads their columns into shared memory, runs all pairs between them
+// there (the first step of a sweep also all pairs inside the two blocks) and writes them
+// back. With M = 1 all columns stay in shared memory for every sweep. One cluster of cl
+// CTAs per job; the cluster barrier separates steps, so a sweep costs 2M - 1 barriers.
 // Sweeps stop after one without a rotation (bounded by kMaxSweeps; status[job] = sweeps
 // used, or -1 if not converged).
 struct JacobiShape {
@@ -202,7 +198,7 @@ struct JacobiShape {
 template <typename T>
 __host__ __device__ inline JacobiShape jacobi_shape(int p, int q, int smem_bytes, int cl) {
   const int L = p + q;
-  int nb = smem_bytes / (2 * L * (int)sizeof(T));
+  int nb = (smem_bytes - kJacAuxFixed) / (2 * (L * (int)sizeof(T) + kJacAuxPerCol));
   if (nb < 1) nb = 1;
   if (cl == 1 && 2 * nb >= q) return JacobiShape{(q + 1) / 2, 1};
   // block pairs per step: a multiple of the cluster size, so no CTA of the cluster idles
@@ -212,11 +208,10 @@ __host__ __device__ inline JacobiShape jacobi_shape(int p, int q, int smem_bytes
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_jacobi(const JacobiJob* __restrict__ jobs, int cl, T* __restrict__ ws,
-                                                     T* __restrict__ vs, int* __restrict__ sweep_rot,
-                                                     int* __restrict__ status, double tol, int smem_bytes) {
+__global__ void __launch_bounds__(kJacThreads) k_jacobi(const JacobiJob* __restrict__ jobs, int cl, T* __restrict__ ws,
+                                                        T* __restrict__ vs, int* __restrict__ sweep_rot,
+                                                        int* __restrict__ status, double tol, int smem_bytes) {
   extern __shared__ __align__(16) uint8_t jac_smem[];
-  T* X = reinterpret_cast<T*>(jac_smem);
   cg::cluster_group cluster = cg::this_cluster();
   const int job = blockIdx.x / cl;
   const int rank = blockIdx.x % cl;
@@ -225,7 +220,7 @@ __global__ void __launch_bounds__(kThreads) k_jacobi(const JacobiJob* __restrict
   T* V = vs + jb.v_off;
   const int p = jb.p, q = jb.q, L = p + q;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __shared__ int rotated;
+  __shared__ int rotated, nrot_s;
   T one, zero;
   if constexpr (sizeof(T) == 8) { one = 1.0; zero = 0.0; } else { one = make_double2(1, 0); zero = make_double2(0, 0); }
   auto barrier = [&]() {
@@ -233,19 +228,23 @@ __global__ void __launch_bounds__(kThreads) k_jacobi(const JacobiJob* __restrict
     if (cl > 1) cluster.sync(); else __syncthreads();
   };
   // V = identity
-  for (int64_t e = (int64_t)rank * kThreads + threadIdx.x; e < (int64_t)q * q; e += (int64_t)cl * kThreads)
+  for (int64_t e = (int64_t)rank * kJacThreads + threadIdx.x; e < (int64_t)q * q; e += (int64_t)cl * kJacThreads)
     V[e] = (e / q == e % q) ? one : zero;
   // ||A||_F (every CTA of the cluster computes it, in the same order)
-  __shared__ double red[kWarps];
+  __shared__ double red[kJacWarps];
   double f2 = 0.0;
-  for (int64_t e = threadIdx.x; e < (int64_t)p * q; e += kThreads) f2 += abs2(W[e]);
+  for (int64_t e = threadIdx.x; e < (int64_t)p * q; e += kJacThreads) f2 += abs2(W[e]);
   f2 = warp_sum(f2);
   if (lane == 0) red[warp] = f2;
   __syncthreads();
   double normA = 0.0;
-  for (int w = 0; w < kWarps; ++w) normA += red[w];
+  for (int w = 0; w < kJacWarps; ++w) normA += red[w];
   normA = sqrt(normA);
-  const double tol_abs = tol * normA;
+  // rotate while |<wi, wj>| > tol ||wi|| ||wj|| (relative orthogonality) and
+  // |<wi, wj>| > tol ||A||_F max(||wi||, ||wj||) (absolute floor: pairs whose inner product
+  // is at the rounding level of the whole matrix are left alone, which bounds the
+  // singular-value change to about tol ||A|| absolute - the accuracy LAPACK's ?gesvd gives)
+  const double tol2 = tol * tol, tola2 = (tol * normA) * (tol * normA);
   barrier();
   if (q < 2) {
     if (rank == 0 && threadIdx.x == 0) status[job] = 0;
@@ -253,59 +252,208 @@ __global__ void __launch_bounds__(kThreads) k_jacobi(const JacobiJob* __restrict
   }
   const JacobiShape sh = jacobi_shape<T>(p, q, smem_bytes, cl);
   const int nb = sh.nb, M = sh.M, nblk = 2 * sh.M;
+  const int cols_cap = M == 1 ? q : 2 * nb;
+  // shared memory: columns, then scales, norms, flags, pair inner products, rotations
+  T* X = reinterpret_cast<T*>(jac_smem);
+  size_t off = (size_t)cols_cap * L * sizeof(T);
+  double* sc = reinterpret_cast<double*>(jac_smem + off);
+  off += (size_t)cols_cap * sizeof(double);
+  double* dn = reinterpret_cast<double*>(jac_smem + off);
+  off += (size_t)cols_cap * sizeof(double);
+  int* fl = reinterpret_cast<int*>(jac_smem + off);
+  off += (size_t)cols_cap * sizeof(int);
+  off = (off + 15) & ~size_t(15);
+  T* G = reinterpret_cast<T*>(jac_smem + off);
+  off += (size_t)(cols_cap / 2 + 1) * sizeof(T);
+  off = (off + 15) & ~size_t(15);
+  JacRot<T>* R = reinterpret_cast<JacRot<T>*>(jac_smem + off);
+
   // global column c of block `blk` and its count
   auto block_cols = [&](int blk, int& c0) {
     c0 = blk * nb;
     return max(0, min(q, c0 + nb) - c0);
   };
-  auto load = [&](int c0, int n, int x0) {   // columns c0 .. c0+n-1 into shared slots x0 ..
-    for (int e = threadIdx.x; e < n * L; e += kThreads) {
-      const int c = e / L, r = e - c * L;
-      X[(int64_t)(x0 + c) * L + r] = r < p ? W[(int64_t)(c0 + c) * p + r] : V[(int64_t)(c0 + c) * q + (r - p)];
+  // columns c0 .. c0+n-1 into shared slots x0 .. (asynchronous; cp_async_wait_all + barrier after)
+  auto load = [&](int c0, int n, int x0) {
+    for (int c = warp; c < n; c += kJacWarps) {
+      T* dst = X + (int64_t)(x0 + c) * L;
+      const T* sw = W + (int64_t)(c0 + c) * p;
+      const T* sv = V + (int64_t)(c0 + c) * q;
+      for (int r = lane; r < p; r += 32) cp_async_elem(dst + r, sw + r);
+      for (int r = lane; r < q; r += 32) cp_async_elem(dst + p + r, sv + r);
+      if (lane == 0) {
+        sc[x0 + c] = 1.0;
+        fl[x0 + c] = 1;
+      }
     }
   };
+  // true columns (scale applied) back to global memory
   auto store = [&](int c0, int n, int x0) {
-    for (int e = threadIdx.x; e < n * L; e += kThreads) {
-      const int c = e / L, r = e - c * L;
-      const T x = X[(int64_t)(x0 + c) * L + r];
-      if (r < p) W[(int64_t)(c0 + c) * p + r] = x; else V[(int64_t)(c0 + c) * q + (r - p)] = x;
+    for (int c = warp; c < n; c += kJacWarps) {
+      const T* src = X + (int64_t)(x0 + c) * L;
+      const double s = sc[x0 + c];
+      for (int r = lane; r < p; r += 32) W[(int64_t)(c0 + c) * p + r] = jac_scale(src[r], s);
+      for (int r = lane; r < q; r += 32) V[(int64_t)(c0 + c) * q + r] = jac_scale(src[p + r], s);
     }
   };
-  // one full round-robin sweep over the lc columns in shared memory
-  auto local_sweep = [&](int lc) {
-    const int lcc = lc + (lc & 1);
-    for (int r = 0; r < lcc - 1; ++r) {
-      for (int k = warp; k < lcc / 2; k += kWarps) {
-        int i = rr_player(k, r, lcc), j = rr_player(lcc - 1 - k, r, lcc);
+  // The pairs of one round. kind 0: round r of a round-robin over lc columns (slots lcc / 2,
+  // slot k pairs players k and lcc - 1 - k; a pair with the bye column lc is skipped);
+  // kind 1: round r of all pairs between columns 0..na-1 and na..na+nbb-1 (slot k pairs k with
+  // na + (k + r) mod max(na, nbb)).
+  auto run_round = [&](int kind, int r, int n0, int n1) {
+    int nslots;
+    if (kind == 0) nslots = (n0 + (n0 & 1)) / 2; else nslots = max(n0, n1);
+    auto slot_pair = [&](int k, int& i, int& j) -> bool {
+      if (kind == 0) {
+        const int lcc = n0 + (n0 & 1);
+        i = rr_player(k, r, lcc);
+        j = rr_player(lcc - 1 - k, r, lcc);
         if (i > j) { const int t = i; i = j; j = t; }
-        if (j < lc) rotate_cols<T>(X + (int64_t)i * L, X + (int64_t)j * L, p, L, tol, tol_abs, lane, &rotated);
+        return j < n0;
       }
-      __syncthreads();
-    }
-  };
-  // every pair (i in the first na columns, j in the next nbb): max(na, nbb) rounds in which
-  // column i meets column (i + r) mod max of the other block
-  auto cross_sweep = [&](int na, int nbb) {
-    const int nm = max(na, nbb);
-    for (int r = 0; r < nm; ++r) {
-      for (int i = warp; i < nm; i += kWarps) {
-        const int j = (i + r) % nm;
-        if (i < na && j < nbb)
-          rotate_cols<T>(X + (int64_t)i * L, X + (int64_t)(na + j) * L, p, L, tol, tol_abs, lane, &rotated);
+      const int nm = max(n0, n1);
+      const int jj = (k + r) % nm;
+      i = k;
+      j = n0 + jj;
+      return k < n0 && jj < n1;
+    };
+    // (1) inner products (and the norms of flagged columns)
+    for (int k = warp; k < nslots; k += kJacWarps) {
+      int i, j;
+      if (!slot_pair(k, i, j)) continue;
+      const T* xi = X + (int64_t)i * L;
+      const T* xj = X + (int64_t)j * L;
+      const bool fi = fl[i] != 0, fj = fl[j] != 0;
+      double a = 0, b = 0;
+      T g;
+      if constexpr (sizeof(T) == 8) {
+        double gg = 0;
+        if (fi || fj) {
+          for (int e = lane; e < p; e += 32) {
+            const double x = xi[e], y = xj[e];
+            a = fma(x, x, a); b = fma(y, y, b); gg = fma(x, y, gg);
+          }
+        } else {
+          for (int e = lane; e < p; e += 32) gg = fma(xi[e], xj[e], gg);
+        }
+        g = warp_sum(gg);
+      } else {
+        double gr = 0, gi = 0;
+        if (fi || fj) {
+          for (int e = lane; e < p; e += 32) {
+            const double2 x = xi[e], y = xj[e];
+            a += abs2(x); b += abs2(y);
+            gr = fma(x.x, y.x, fma(x.y, y.y, gr));
+            gi = fma(x.x, y.y, fma(-x.y, y.x, gi));
+          }
+        } else {
+          for (int e = lane; e < p; e += 32) {
+            const double2 x = xi[e], y = xj[e];
+            gr = fma(x.x, y.x, fma(x.y, y.y, gr));
+            gi = fma(x.x, y.y, fma(-x.y, y.x, gi));
+          }
+        }
+        g = make_double2(warp_sum(gr), warp_sum(gi));
       }
-      __syncthreads();
+      if (fi || fj) {
+        a = warp_sum(a);
+        b = warp_sum(b);
+      }
+      if (lane == 0) {
+        const double si = sc[i], sj = sc[j];
+        G[k] = jac_scale(g, si * sj);
+        if (fi) { dn[i] = a * si * si; fl[i] = 0; }
+        if (fj) { dn[j] = b * sj * sj; fl[j] = 0; }
+      }
     }
+    __syncthreads();
+    // (2) rotations, one lane per pair
+    if (warp == 0) {
+      int base = 0;
+      for (int k0 = 0; k0 < nslots; k0 += 32) {
+        const int k = k0 + lane;
+        int i = 0, j = 0;
+        bool rot = false;
+        T alpha = zero, beta = zero;
+        if (k < nslots && slot_pair(k, i, j)) {
+          const T g = G[k];
+          const double a = dn[i], b = dn[j];
+          const double g2 = abs2(g);
+          rot = g2 > tol2 * a * b && g2 > tola2 * fmax(a, b) && g2 > 0.0;
+          if (rot) {
+            const double gabs = sqrt(g2);
+            const double zeta = (b - a) / (2.0 * gabs);
+            const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+            const double c = rsqrt(1.0 + t * t);
+            const double si = sc[i], sj = sc[j];
+            T tau;
+            if constexpr (sizeof(T) == 8) tau = g >= 0 ? t : -t;
+            else tau = make_double2(t * g.x / gabs, -t * g.y / gabs);
+            alpha = jac_scale(tau, sj / si);
+            beta = jac_scale(jac_conj(tau), si / sj);
+            sc[i] = c * si;
+            sc[j] = c * sj;
+            const double an = a - t * gabs, bn = b + t * gabs;
+            dn[i] = an;
+            dn[j] = bn;
+            if (!(an >= 0.5 * a)) fl[i] = 1;
+            if (!(bn >= 0.5 * b)) fl[j] = 1;
+          }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, rot);
+        if (rot) {
+          JacRot<T> e;
+          e.i = i;
+          e.j = j;
+          e.alpha = alpha;
+          e.beta = beta;
+          R[base + __popc(m & ((1u << lane) - 1u))] = e;
+        }
+        base += __popc(m);
+      }
+      if (lane == 0) {
+        nrot_s = base;
+        if (base) rotated = 1;
+      }
+    }
+    __syncthreads();
+    // (3) updates over (rotation, 32-entry chunk) items
+    const int nrot = nrot_s;
+    const int nch = (L + 31) >> 5;
+    for (int it = warp; it < nrot * nch; it += kJacWarps) {
+      const int k = it / nch, e = (it - k * nch) * 32 + lane;
+      if (e < L) {
+        const JacRot<T> rr = R[k];
+        T* xi = X + (int64_t)rr.i * L + e;
+        T* xj = X + (int64_t)rr.j * L + e;
+        T x = *xi, y = *xj;
+        jac_apply(x, y, rr.alpha, rr.beta);
+        *xi = x;
+        *xj = y;
+      }
+    }
+    __syncthreads();
   };
+
   int sweep = 0;
   if (M == 1) {
     // every column in shared memory for all sweeps (one CTA: cl == 1 for these jobs)
     load(0, q, 0);
+    cp_async_wait_all();
     __syncthreads();
+    const int lcc = q + (q & 1);
     for (; sweep < kMaxSweeps; ++sweep) {
       if (threadIdx.x == 0) rotated = 0;
       __syncthreads();
-      local_sweep(q);
+      for (int r = 0; r < lcc - 1; ++r) run_round(0, r, q, 0);
       const int any = rotated;
+      // fold the scales into the columns; norms are recomputed in the next sweep
+      for (int idx = threadIdx.x; idx < q * L; idx += kJacThreads) X[idx] = jac_scale(X[idx], sc[idx / L]);
+      __syncthreads();
+      for (int c = threadIdx.x; c < q; c += kJacThreads) {
+        sc[c] = 1.0;
+        fl[c] = 1;
+      }
       __syncthreads();
       if (!any) break;
     }
@@ -323,9 +471,16 @@ __global__ void __launch_bounds__(kThreads) k_jacobi(const JacobiJob* __restrict
           if (na + nbb < 2) continue;
           load(ca, na, 0);
           load(cb, nbb, na);
+          cp_async_wait_all();
           __syncthreads();
-          // the first step of a sweep also orthogonalises the columns inside each block
-          if (st == 0) local_sweep(na + nbb); else cross_sweep(na, nbb);
+          if (st == 0) {
+            // the first step of a sweep also orthogonalises the columns inside each block
+            const int lc = na + nbb, lcc = lc + (lc & 1);
+            for (int r = 0; r < lcc - 1; ++r) run_round(0, r, lc, 0);
+          } else {
+            const int nm = max(na, nbb);
+            for (int r = 0; r < nm; ++r) run_round(1, r, na, nbb);
+          }
           store(ca, na, 0);
           store(cb, nbb, na);
           __syncthreads();
@@ -1167,7 +1322,7 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
     if (le != cudaSuccess) break;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(cls_jobs[ci].size() * cl));
-    cfg.blockDim = dim3(kThreads);
+    cfg.blockDim = dim3(kJacThreads);
     cfg.dynamicSmemBytes = kJacobiSmem;
     cfg.stream = sx;
     cudaLaunchAttribute attr[1];
