@@ -559,6 +559,7 @@ def run_profile_case(case: str, tensors, dev, local: int) -> None:
             mv.apply(d5[1], o)
         torch.cuda.synchronize()
         mv.device_status()
+        print(json.dumps({"mpo_form": mv.mpo_form()}))
     elif case == "svd":
         SVD(DTensor.from_host(workloads.svd_psi(2000, 20, 6.0, 3), local), 2, [0], 1e-9, 1, 2000)
     else:

@@ -135,10 +135,11 @@ __device__ __forceinline__ int rr_player(int slot, int r, int qq) {
 //   x_i <- x_i - (tau sc_j / sc_i) x_j,   x_j <- x_j + (conj(tau) sc_i / sc_j) x_i,
 // with sc_i, sc_j <- c sc_i, c sc_j, and the norms follow a <- a - t|g|, b <- b + t|g|.
 // A norm that fell below half its value is recomputed from the data the next time its
-// column is in a pair; every column is recomputed when it is loaded. A round runs in three
-// phases between barriers: (1) one warp per pair forms <x_i, x_j>; (2) warp 0 decides and
-// computes the rotations, one lane per pair, and lists the rotated ones; (3) all warps
-// apply them over (pair, 32-entry chunk) items.
+// column is in a pair; every column is recomputed when it is loaded. The reciprocal of every
+// scale is kept beside it, so the rotation needs no division. A round runs in three phases
+// between barriers: (1) one warp per pair forms <x_i, x_j>; (2) warps 0-3 (one per
+// scheduler) decide and compute the rotations, one lane per pair, and list the rotated ones;
+// (3) all warps apply them over (pair, 32-entry chunk) items.
 constexpr int kJacThreads = 256;
 constexpr int kJacWarps = kJacThreads / 32;
 constexpr int kJacAuxPerCol = 64;    // shared-memory bytes per column for the bookkeeping below
@@ -253,10 +254,13 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const JacobiJob* __restr
   const JacobiShape sh = jacobi_shape<T>(p, q, smem_bytes, cl);
   const int nb = sh.nb, M = sh.M, nblk = 2 * sh.M;
   const int cols_cap = M == 1 ? q : 2 * nb;
-  // shared memory: columns, then scales, norms, flags, pair inner products, rotations
+  // shared memory: columns, then scales and their reciprocals, norms, flags, pair inner
+  // products, rotations
   T* X = reinterpret_cast<T*>(jac_smem);
   size_t off = (size_t)cols_cap * L * sizeof(T);
   double* sc = reinterpret_cast<double*>(jac_smem + off);
+  off += (size_t)cols_cap * sizeof(double);
+  double* isc = reinterpret_cast<double*>(jac_smem + off);
   off += (size_t)cols_cap * sizeof(double);
   double* dn = reinterpret_cast<double*>(jac_smem + off);
   off += (size_t)cols_cap * sizeof(double);
@@ -283,6 +287,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const JacobiJob* __restr
       for (int r = lane; r < q; r += 32) cp_async_elem(dst + p + r, sv + r);
       if (lane == 0) {
         sc[x0 + c] = 1.0;
+        isc[x0 + c] = 1.0;
         fl[x0 + c] = 1;
       }
     }
@@ -318,6 +323,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const JacobiJob* __restr
       return k < n0 && jj < n1;
     };
     // (1) inner products (and the norms of flagged columns)
+    if (threadIdx.x == 0) nrot_s = 0;
     for (int k = warp; k < nslots; k += kJacWarps) {
       int i, j;
       if (!slot_pair(k, i, j)) continue;
@@ -367,11 +373,10 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const JacobiJob* __restr
       }
     }
     __syncthreads();
-    // (2) rotations, one lane per pair
-    if (warp == 0) {
-      int base = 0;
-      for (int k0 = 0; k0 < nslots; k0 += 32) {
-        const int k = k0 + lane;
+    // (2) rotations: warp w < 4 takes slots w, w + 4, ... one lane per slot
+    if (warp < 4) {
+      for (int k0 = 0; k0 < nslots; k0 += 128) {
+        const int k = k0 + 4 * lane + warp;
         int i = 0, j = 0;
         bool rot = false;
         T alpha = zero, beta = zero;
@@ -381,18 +386,23 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const JacobiJob* __restr
           const double g2 = abs2(g);
           rot = g2 > tol2 * a * b && g2 > tola2 * fmax(a, b) && g2 > 0.0;
           if (rot) {
-            const double gabs = sqrt(g2);
-            const double zeta = (b - a) / (2.0 * gabs);
-            const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-            const double c = rsqrt(1.0 + t * t);
-            const double si = sc[i], sj = sc[j];
+            const double rg = rsqrt(g2);                  // 1 / |g|
+            const double gabs = g2 * rg;
+            const double zeta = (b - a) * (0.5 * rg);
+            const double z1 = fma(zeta, zeta, 1.0);
+            const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + z1 * rsqrt(z1));
+            const double t1 = fma(t, t, 1.0);
+            const double c = rsqrt(t1), ic = t1 * c;       // cos, 1 / cos
+            const double si = sc[i], sj = sc[j], isi = isc[i], isj = isc[j];
             T tau;
             if constexpr (sizeof(T) == 8) tau = g >= 0 ? t : -t;
-            else tau = make_double2(t * g.x / gabs, -t * g.y / gabs);
-            alpha = jac_scale(tau, sj / si);
-            beta = jac_scale(jac_conj(tau), si / sj);
+            else tau = make_double2(t * g.x * rg, -t * g.y * rg);
+            alpha = jac_scale(tau, sj * isi);
+            beta = jac_scale(jac_conj(tau), si * isj);
             sc[i] = c * si;
             sc[j] = c * sj;
+            isc[i] = ic * isi;
+            isc[j] = ic * isj;
             const double an = a - t * gabs, bn = b + t * gabs;
             dn[i] = an;
             dn[j] = bn;
@@ -401,6 +411,9 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const JacobiJob* __restr
           }
         }
         const unsigned m = __ballot_sync(0xffffffffu, rot);
+        int base = 0;
+        if (lane == 0 && m) base = atomicAdd(&nrot_s, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
         if (rot) {
           JacRot<T> e;
           e.i = i;
@@ -409,11 +422,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const JacobiJob* __restr
           e.beta = beta;
           R[base + __popc(m & ((1u << lane) - 1u))] = e;
         }
-        base += __popc(m);
-      }
-      if (lane == 0) {
-        nrot_s = base;
-        if (base) rotated = 1;
+        if (lane == 0 && m) rotated = 1;
       }
     }
     __syncthreads();
@@ -452,6 +461,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const JacobiJob* __restr
       __syncthreads();
       for (int c = threadIdx.x; c < q; c += kJacThreads) {
         sc[c] = 1.0;
+        isc[c] = 1.0;
         fl[c] = 1;
       }
       __syncthreads();

@@ -452,6 +452,13 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
                : "r"(taddr));
 }
 
+// 16 lanes x 256 bits: thread t gets 32-bit columns 2 (t % 4) and 2 (t % 4) + 1 of lanes t / 4
+// (r[0], r[1]) and t / 4 + 8 (r[2], r[3]) - one FP64 value of each of two rows
+__device__ __forceinline__ void tmem_ld_16x256b(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.16x256b.x1.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -749,6 +756,8 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
         written = false;
         poison = 0;
       }
+      // this row's place in C, fetched early for the tile's store
+      const long long rmap = (w.flags & 2) && row < w.m ? __ldg(row_map + w.row_map + row) : -1ll;
       // scale exponents, fetched while the first period is still on the tensor cores
       const int fa = row < w.m ? aexp[w.a_exp + row] : 0;
       const int ea = exp_of_field(fa);
@@ -786,19 +795,39 @@ __global__ void __launch_bounds__(kRoleThreads, 1)
         if (stop) break;
         fold_sums(z, ea, eb, w.sign < 0, tsum, written);
       }
-      // one store per tile after its last task (a C tile belongs to exactly one CTA)
+      // one store per tile after its last task (a C tile belongs to exactly one CTA). The sums
+      // are read back in the 16 x 256-bit shape, so that four consecutive lanes hold four
+      // consecutive columns of one row and each store instruction writes 32-byte pieces of 8
+      // rows (a lane-per-row store would write 32 separate 8-byte pieces). Row places and
+      // non-finite masks come from the lane that owns the row.
       if (!stop && (w.flags & 2)) {
-        uint32_t v[2 * kDrainCols];
-        tmem_ld16(tsum, v);
+        uint32_t v[4 * kDrainCols];
+        const uint32_t tb = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(kSumCol + 2 * cpart * kDrainCols);
+        tmem_ld_16x256b(tb, v);
+        tmem_ld_16x256b(tb + 8u, v + 4);
+        tmem_ld_16x256b(tb + (16u << 16), v + 8);
+        tmem_ld_16x256b(tb + (16u << 16) + 8u, v + 12);
         asm volatile("tcgen05.wait::ld.sync.aligned;");
-        if (row < w.m) {
-          double* out = C + __ldg(row_map + w.row_map + row);
+        const int cq = lane & 3, rq = lane >> 2;
 #pragma unroll
-          for (int c = 0; c < kDrainCols; ++c)
-            if (col0 + c < w.n)
-              out[col0 + c] = (poison >> c) & 1u ? __longlong_as_double(0x7FF8000000000000ll)
-                                                 : __hiloint2double((int)v[2 * c + 1], (int)v[2 * c]);
-        }
+        for (int lh = 0; lh < 2; ++lh)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int rl = 16 * lh + 8 * h + rq;       // the row's lane in this warp
+            const long long rm = __shfl_sync(0xffffffffu, rmap, rl);
+            const uint32_t pz = __shfl_sync(0xffffffffu, poison, rl);
+            if (rm >= 0) {
+#pragma unroll
+              for (int ch = 0; ch < 2; ++ch) {
+                const int c = 4 * ch + cq;
+                if (col0 + c < w.n) {
+                  const uint32_t* x = v + 8 * lh + 4 * ch + 2 * h;
+                  C[rm + col0 + c] = (pz >> c) & 1u ? __longlong_as_double(0x7FF8000000000000ll)
+                                                    : __hiloint2double((int)x[1], (int)x[0]);
+                }
+              }
+            }
+          }
       }
     }
   }

@@ -28,9 +28,10 @@ using namespace qltg;
 namespace {
 
 constexpr int kVecThreads = 256;
-// fixed grid (independent of the device): the partial-sum order, and so every α and β, is
-// the same on every run
-constexpr int kVecBlocks = 152 * 4;
+// fixed grid, deliberately independent of the device's SM count: the partial-sum order, and
+// so every α and β, is the same on every run and every GPU (608 CTAs = four per SM on a
+// 152-SM GB300)
+constexpr int kVecBlocks = 608;
 
 __device__ __forceinline__ double block_sum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
