@@ -148,10 +148,11 @@ class ClockSampler:
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture of
-# `python bench.py --profile --mode <mode>` (summaries: profiles/k_gemm_split_d4000.txt,
-# profiles/k_gemm_dfma_d4000.txt). Keyed by matvec step.
+# `python bench.py --profile --profile-case step0|step3` (split) and `--profile --mode fp64`
+# (summaries: profiles/k_gemm_split_d4000.txt, profiles/k_gemm_dfma_d4000.txt). Keyed by
+# matvec step.
 NCU_TRAFFIC = {
-    "split": {0: 133.3e6, 3: 312.0e6},
+    "split": {0: 117.4e6, 3: 228.9e6},
     "fp64": {0: 84.6e6, 3: 167.7e6},
 }
 

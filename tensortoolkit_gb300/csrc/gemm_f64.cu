@@ -230,7 +230,7 @@ __device__ __forceinline__ int out_field(double v) {
   const uint32_t hi = (uint32_t)__double2hiint(v) & 0x7FFFFFFFu, lo = (uint32_t)__double2loint(v);
   return (hi | lo) ? max(1, (int)(hi >> 20)) : 0;
 }
-__device__ __forceinline__ int out_field(double2) { return 0; }
+__device__ __forceinline__ int out_field(double2 v) { return max(out_field(v.x), out_field(v.y)); }
 
 template <typename T, int NN>
 __device__ __forceinline__ void skinny_row(const GemmCBlk& cb, const GemmTask* __restrict__ task, int row,

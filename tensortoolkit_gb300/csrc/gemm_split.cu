@@ -529,39 +529,35 @@ __global__ void __launch_bounds__(32) k_wait_selftest(long long limit, int* __re
 // Level 2 stays below 2^22 and converts with the magic-number add, the others with F2I;
 // level 8 is rounded to units of 2^-49.
 __device__ __forceinline__ void drain_set(uint32_t lb, long long (&z)[kDrainCols]) {
-  uint32_t r[kDrainCols];
+  // levels are read two at a time, one wait per pair
+  uint32_t r[kDrainCols], q[kDrainCols];
   int32_t u[kDrainCols];
   tmem_ld8(lb, r);                                       // level 2
-  asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-  for (int c = 0; c < kDrainCols; ++c)
-    u[c] = (__float_as_int(fmaf(__uint_as_float(r[c]), 0x1p14f, kMagic)) - kMagicBits) * 128;
-  tmem_ld8(lb + kTN, r);                                 // level 3
+  tmem_ld8(lb + kTN, q);                                 // level 3
   asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
   for (int c = 0; c < kDrainCols; ++c) {
-    u[c] += __float2int_rn(__uint_as_float(r[c]) * 0x1p21f);
+    u[c] = (__float_as_int(fmaf(__uint_as_float(r[c]), 0x1p14f, kMagic)) - kMagicBits) * 128;
+    u[c] += __float2int_rn(__uint_as_float(q[c]) * 0x1p21f);
     z[c] += (long long)u[c] << 28;
   }
   tmem_ld8(lb + 2 * kTN, r);                             // level 4
-  asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-  for (int c = 0; c < kDrainCols; ++c) u[c] = __float2int_rn(__uint_as_float(r[c]) * 0x1p28f) * 128;
-  tmem_ld8(lb + 3 * kTN, r);                             // level 5
+  tmem_ld8(lb + 3 * kTN, q);                             // level 5
   asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
   for (int c = 0; c < kDrainCols; ++c) {
-    u[c] += __float2int_rn(__uint_as_float(r[c]) * 0x1p35f);
+    u[c] = __float2int_rn(__uint_as_float(r[c]) * 0x1p28f) * 128;
+    u[c] += __float2int_rn(__uint_as_float(q[c]) * 0x1p35f);
     z[c] += (long long)u[c] << 14;
   }
   tmem_ld8(lb + 4 * kTN, r);                             // level 6 (in int64: it may pass 2^24)
+  tmem_ld8(lb + 5 * kTN, q);                             // level 7
   asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-  for (int c = 0; c < kDrainCols; ++c) z[c] += (long long)__float2int_rn(__uint_as_float(r[c]) * 0x1p42f) * 128;
-  tmem_ld8(lb + 5 * kTN, r);                             // level 7
-  asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-  for (int c = 0; c < kDrainCols; ++c) u[c] = __float2int_rn(__uint_as_float(r[c]) * 0x1p49f);
+  for (int c = 0; c < kDrainCols; ++c) {
+    z[c] += (long long)__float2int_rn(__uint_as_float(r[c]) * 0x1p42f) * 128;
+    u[c] = __float2int_rn(__uint_as_float(q[c]) * 0x1p49f);
+  }
   tmem_ld8(lb + 6 * kTN, r);                             // level 8
   asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
@@ -1239,7 +1235,7 @@ void launch_gemm_split(CtrctPlan& p, const Operands& op, void* c, cudaStream_t s
   // pipe); everything else goes through the slices. With both present the skinny kernel
   // runs on the side stream (it writes other output blocks) and joins after the split GEMM.
   const bool fork = !p.sched.skinny.empty() && !sp.tiles.empty() && sp.side;
-  const SkinnyFuse* fuse = p.fuse_fields && !cplx ? p.d_fuse.as<SkinnyFuse>() : nullptr;
+  const SkinnyFuse* fuse = p.fuse_fields ? p.d_fuse.as<SkinnyFuse>() : nullptr;
   if (fork) {
     QLTG_CUDA(cudaEventRecord(sp.fork, s));
     QLTG_CUDA(cudaStreamWaitEvent(sp.side, sp.fork, 0));

@@ -32,8 +32,9 @@ void link_row_fields(qltg_matvec& mv, cudaStream_t s) {
   CtrctPlan& p2 = mv.mpo_producer();
   CtrctPlan& p3 = mv.step[3];
   if (!p2.split || !p3.split || p3.split->a_ops.empty() || p3.split->a_static) return;
-  if (p3.a.dtype != QLTG_F64) return;   // the skinny kernel folds real outputs only
   if (p3.a_tl.ntiles || !p2.split->tiles.empty()) return;
+  // a complex operand row of the last step is the real 2k-wide view of k complex values
+  const int cw = p3.a.dtype == QLTG_C128 ? 2 : 1;
   const auto& ops = p3.split->a_ops;
   std::map<int64_t, int> op_of;
   for (int i = 0; i < (int)ops.size(); ++i) op_of[ops[i].src_off & ~qltg::kFromSrc] = i;
@@ -41,13 +42,13 @@ void link_row_fields(qltg_matvec& mv, cudaStream_t s) {
   std::vector<qltg::SkinnyFuse> fz(std::max<size_t>(g.cblk.size(), 1), qltg::SkinnyFuse{-1, 1});
   size_t covered = 0;
   for (size_t q = 0; q < g.cblk.size(); ++q) {
-    auto it = op_of.find(g.cblk[q].c_off);
+    auto it = op_of.find(cw * g.cblk[q].c_off);   // operand offsets count real values
     if (it == op_of.end()) continue;
     const qltg::SplitOperand& o = ops[it->second];
-    if (!qltg::skinny_cblk(g, (int32_t)q) || o.cols % g.cblk[q].n != 0 ||
-        (int64_t)o.rows * o.cols != (int64_t)g.cblk[q].m * g.cblk[q].n)
+    if (!qltg::skinny_cblk(g, (int32_t)q) || o.cols % (cw * g.cblk[q].n) != 0 ||
+        (int64_t)o.rows * o.cols != (int64_t)cw * g.cblk[q].m * g.cblk[q].n)
       return;
-    fz[q] = qltg::SkinnyFuse{o.exp_off, o.cols};
+    fz[q] = qltg::SkinnyFuse{o.exp_off, o.cols / cw};
     ++covered;
   }
   if (covered != ops.size()) return;

@@ -26,7 +26,10 @@ struct PairParams {
   int64_t c_w[kMaxRank];         // block-index weights of C's legs
   int a_leg_off[kMaxRank], b_leg_off[kMaxRank];   // per-leg offsets into flattened sector arrays
   int fermionic;
-  int a_ctrct_in[kMaxRank];      // A's i-th contracted leg is IN
+  // the contracted pairs in the caller's order, for the exchange sign (the pairing and the
+  // operand transposes may use another order of the same pairs)
+  int sgn_axa[kMaxRank], sgn_axb[kMaxRank];
+  int a_ctrct_in[kMaxRank];      // A's i-th contracted leg (caller's order) is IN
 };
 
 __global__ void k_keys_a(const int32_t* __restrict__ coords, int64_t n, const int64_t* __restrict__ dims,
@@ -137,7 +140,7 @@ __global__ void k_emit(const int32_t* __restrict__ ca, const int32_t* __restrict
     int sign = 1;
     if (P.fermionic) {
       for (int l = 0; l < P.rb; ++l) pb_l[l] = par_b[P.b_leg_off[l] + c2[l]];
-      sign = exchange_sign(pa_l, P.ra, pb_l, P.rb, P.axa, P.axb, P.nax, P.a_ctrct_in) *
+      sign = exchange_sign(pa_l, P.ra, pb_l, P.rb, P.sgn_axa, P.sgn_axb, P.nax, P.a_ctrct_in) *
              saved_order_sign(pa_l, P.sa, P.nsa) * saved_order_sign(pb_l, P.sb, P.nsb);
     }
     pa[p] = (int32_t)i;
@@ -241,11 +244,13 @@ void plan_contraction(CtrctPlan& p, cudaStream_t s) {
 
   // The order of the contracted pairs (a_i, b_i) is internal to the contraction: any
   // consistent reordering of the pairs gives the same C (the k index of every block pair
-  // is only permuted, in A and B alike). For bosonic tensors pick, among the given order and
-  // the orders sorted by A's or by B's leg numbers, the one whose operand transposes move
-  // the fewest bytes (blocks whose layout a transpose leaves unchanged move none). For
-  // fermionic tensors the exchange sign depends on the order, so the given order stays.
-  if (A.parity_comp < 0 && nax >= 2) {
+  // is only permuted, in A and B alike; the operand transposes carry no signs). Pick, among
+  // the given order and the orders sorted by A's or by B's leg numbers, the one whose operand
+  // transposes move the fewest bytes (blocks whose layout a transpose leaves unchanged move
+  // none). The fermionic exchange sign of a block pair depends on the order the caller gave,
+  // so it is computed from that order (sgn_axa / sgn_axb below), whatever order is used here.
+  const std::vector<int64_t> given_axa = p.axa, given_axb = p.axb;
+  if (nax >= 2) {
     auto order_of = [&](const std::vector<int64_t>& axa, const std::vector<int64_t>& axb, std::vector<int>& oa,
                         std::vector<int>& ob) {
       oa.assign(p.sa.begin(), p.sa.end());
@@ -301,7 +306,13 @@ void plan_contraction(CtrctPlan& p, cudaStream_t s) {
   PairParams P{};
   P.ra = A.rank; P.rb = B.rank; P.rc = rc; P.nax = nax;
   P.nsa = (int)p.sa.size(); P.nsb = (int)p.sb.size();
-  for (int t = 0; t < nax; ++t) { P.axa[t] = (int)p.axa[t]; P.axb[t] = (int)p.axb[t]; P.a_ctrct_in[t] = A.dirs[p.axa[t]] == QLTG_IN; }
+  for (int t = 0; t < nax; ++t) {
+    P.axa[t] = (int)p.axa[t];
+    P.axb[t] = (int)p.axb[t];
+    P.sgn_axa[t] = (int)given_axa[t];
+    P.sgn_axb[t] = (int)given_axb[t];
+    P.a_ctrct_in[t] = A.dirs[given_axa[t]] == QLTG_IN;
+  }
   for (int t = 0; t < P.nsa; ++t) P.sa[t] = (int)p.sa[t];
   for (int t = 0; t < P.nsb; ++t) P.sb[t] = (int)p.sb[t];
   // key weights over the contracted legs (sector counts of A's contracted legs)

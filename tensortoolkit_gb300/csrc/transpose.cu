@@ -427,21 +427,16 @@ namespace {
 
 __device__ __align__(256) PermDesc g_noalloc_perm[kNoAllocPermBlocks];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-PermDesc* g_noalloc_addr[kMaxDevices] = {};
-
-// Device address of the table for `device`, looked up once per device with that device
-// current (host code may not use the symbol itself as a device pointer).
+// Device address of the table on the current device, looked up on every call (host code
+// may not use the symbol itself as a device pointer; the lookup allocates nothing, and not
+// caching it keeps the address right after a device reset or a reload of the module).
 PermDesc* noalloc_table(int device) {
-  QLTG_CHECK(device >= 0 && device < kMaxDevices, QLTG_ERR_UNSUPPORTED, "device ordinal above 63");
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[device]) {
-    void* p = nullptr;
-    QLTG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_perm));
-    g_noalloc_addr[device] = static_cast<PermDesc*>(p);
-  }
-  return g_noalloc_addr[device];
+  int cur = -1;
+  QLTG_CUDA(cudaGetDevice(&cur));
+  QLTG_CHECK(cur == device, QLTG_ERR_INVALID, "the no-allocation permute runs on the current device");
+  void* p = nullptr;
+  QLTG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_perm));
+  return static_cast<PermDesc*>(p);
 }
 
 }  // namespace
