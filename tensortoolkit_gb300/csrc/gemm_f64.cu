@@ -431,7 +431,7 @@ void launch_gemm_f64_skinny(const GemmSchedule& g, const Operands& op, void* c, 
   if (!ns) return;
   const int grid = skinny_grid(ns, cplx, num_sms);
   if (cplx)
-    launch_skinny_t<double2>(g, op, c, grid, s, nullptr, nullptr);
+    launch_skinny_t<double2>(g, op, c, grid, s, fuse, fields);
   else
     launch_skinny_t<double>(g, op, c, grid, s, fuse, fields);
   QLTG_CUDA(cudaGetLastError());
