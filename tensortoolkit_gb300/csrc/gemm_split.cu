@@ -1065,6 +1065,18 @@ void SplitPlan::build(const CtrctPlan& p, cudaStream_t s) {
       heap.push(l);
     }
   }
+  // Each CTA's tiles alternate long and short (its list is in decreasing cost): a short
+  // tile's drain, fold and store then overlap a long tile's MMAs instead of the short tiles
+  // all coming last, where the drain warps would set the pace.
+  for (auto& v : owned) {
+    std::vector<int32_t> mixed;
+    mixed.reserve(v.size());
+    for (size_t i = 0, j = v.size(); i < j;) {
+      mixed.push_back(v[i++]);
+      if (i < j) mixed.push_back(v[--j]);
+    }
+    v.swap(mixed);
+  }
   work.clear();
   work_off.assign(grid + 1, 0);
   for (int b = 0; b < grid; ++b) {
