@@ -86,6 +86,7 @@ struct GemmSchedule {
   std::vector<GemmRowChunk> skinny;     // row chunks of skinny blocks (n, k <= 8)
   DevBuf d_cblk, d_task, d_tile, d_skinny, d_counter;
   int bm = 32, bn = 32;
+  int skinny_maxn = 8;                  // largest n of the skinny blocks (kernel variant)
 };
 
 // Split-precision schedule (gemm_split.cu): operand blocks to slice and pack, per-task
@@ -222,7 +223,7 @@ bool skinny_cblk(const GemmSchedule& g, int32_t q);
 int skinny_rows_per_item();
 // Grid of the skinny kernel: one full wave of resident CTAs (the first call queries the
 // occupancy; call it once outside any stream capture).
-int skinny_grid(int items, bool cplx, int num_sms);
+int skinny_grid(int items, bool cplx, int maxn, int num_sms);
 // Operand buffers of one execution: scratch (transposed blocks) and source (the operands as
 // passed in, for blocks flagged kFromSrc).
 struct Operands {

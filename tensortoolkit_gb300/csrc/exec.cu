@@ -44,11 +44,14 @@ void set_f64_tile(CtrctPlan& p, int bm, int bn, cudaStream_t s) {
 void finalize_plan(CtrctPlan& p, cudaStream_t s) {
   GemmSchedule& g = p.sched;
   g.skinny.clear();
+  g.skinny_maxn = 1;
   const int rows_per_item = skinny_rows_per_item();
   for (int32_t q = 0; q < (int32_t)g.cblk.size(); ++q) {
     const GemmCBlk& cb = g.cblk[q];
-    if (skinny_cblk(g, q))
+    if (skinny_cblk(g, q)) {
+      g.skinny_maxn = std::max(g.skinny_maxn, (int)cb.n);
       for (int32_t c = 0; c * (int64_t)rows_per_item < cb.m; ++c) g.skinny.push_back(GemmRowChunk{q, c});
+    }
   }
   f64_tile_list(g);
   // Operand transposes. A task reads its operand block from the transposed scratch unless
@@ -128,7 +131,7 @@ void finalize_plan(CtrctPlan& p, cudaStream_t s) {
       if (p.b_tl.identity[block_of(p.b, tk.b_off)]) tk.b_off |= kFromSrc;
     if (p.b_tl.ntiles) p.b_t.alloc(p.b.size * eb);
   }
-  if (!g.skinny.empty()) (void)skinny_grid((int)g.skinny.size(), p.a.dtype == QLTG_C128, p.ctx->num_sms);
+  if (!g.skinny.empty()) (void)skinny_grid((int)g.skinny.size(), p.a.dtype == QLTG_C128, g.skinny_maxn, p.ctx->num_sms);
   g.d_cblk = upload(g.cblk, s);
   g.d_task = upload(g.task, s);
   g.d_tile = upload(g.tile, s);

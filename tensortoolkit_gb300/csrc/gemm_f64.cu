@@ -331,12 +331,13 @@ __device__ __forceinline__ void fold_field(unsigned mask, int key, int v, int32_
 }
 
 // Resident CTAs per SM the kernel is compiled for: 8 for real operands (64 registers, no
-// spills at two rows per thread); complex ones need their registers (2).
-template <typename T> struct SkinnyMinBlocks { static constexpr int value = 2; };
-template <> struct SkinnyMinBlocks<double> { static constexpr int value = 8; };
+// spills at two rows per thread); complex ones need their registers, the more the wider the
+// blocks (the kernel is instantiated for the plan's largest n: MAXN = 2, 4 or 8).
+template <typename T, int MAXN> struct SkinnyMinBlocks { static constexpr int value = MAXN <= 2 ? 6 : MAXN <= 4 ? 4 : 2; };
+template <int MAXN> struct SkinnyMinBlocks<double, MAXN> { static constexpr int value = 8; };
 
-template <typename T>
-__global__ void __launch_bounds__(kSkinnyThreads, SkinnyMinBlocks<T>::value) k_gemm_skinny(
+template <typename T, int MAXN>
+__global__ void __launch_bounds__(kSkinnyThreads, SkinnyMinBlocks<T, MAXN>::value) k_gemm_skinny(
     const GemmCBlk* __restrict__ cblk, const GemmTask* __restrict__ task, const GemmRowChunk* __restrict__ items,
     int nitems, const T* __restrict__ A, const T* __restrict__ As, const T* __restrict__ B, const T* __restrict__ Bs,
     T* __restrict__ C, const SkinnyFuse* __restrict__ fuse, int32_t* __restrict__ fields) {
@@ -348,15 +349,27 @@ __global__ void __launch_bounds__(kSkinnyThreads, SkinnyMinBlocks<T>::value) k_g
     const SkinnyFuse fz = fuse ? fuse[item.cblk] : SkinnyFuse{-1, 1};
     const bool want = fz.exp_base >= 0;   // uniform over the item
     int f0 = 0, f1 = -1;
-    switch (cb.n) {
-      case 1: skinny_rows<T, 1>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
-      case 2: skinny_rows<T, 2>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
-      case 3: skinny_rows<T, 3>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
-      case 4: skinny_rows<T, 4>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
-      case 5: skinny_rows<T, 5>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
-      case 6: skinny_rows<T, 6>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
-      case 7: skinny_rows<T, 7>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
-      default: skinny_rows<T, 8>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+    if (MAXN <= 2) {
+      if (cb.n == 1) skinny_rows<T, 1>(cb, task, row, A, As, B, Bs, C, want, f0, f1);
+      else skinny_rows<T, 2>(cb, task, row, A, As, B, Bs, C, want, f0, f1);
+    } else if (MAXN <= 4) {
+      switch (cb.n) {
+        case 1: skinny_rows<T, 1>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+        case 2: skinny_rows<T, 2>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+        case 3: skinny_rows<T, 3>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+        default: skinny_rows<T, 4>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+      }
+    } else {
+      switch (cb.n) {
+        case 1: skinny_rows<T, 1>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+        case 2: skinny_rows<T, 2>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+        case 3: skinny_rows<T, 3>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+        case 4: skinny_rows<T, 4>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+        case 5: skinny_rows<T, 5>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+        case 6: skinny_rows<T, 6>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+        case 7: skinny_rows<T, 7>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+        default: skinny_rows<T, 8>(cb, task, row, A, As, B, Bs, C, want, f0, f1); break;
+      }
     }
     if (want) {
       // a row's n outputs lie in one row of the later operand (k3 is a multiple of n)
@@ -380,10 +393,10 @@ bool skinny_cblk(const GemmSchedule& g, int32_t q) {
 
 int skinny_rows_per_item() { return kSkinnyRows; }
 
-template <typename T>
+template <typename T, int MAXN>
 void launch_skinny_t(const GemmSchedule& g, const Operands& op, void* c, int grid, cudaStream_t s,
                      const SkinnyFuse* fuse, int32_t* fields) {
-  k_gemm_skinny<T><<<grid, kSkinnyThreads, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
+  k_gemm_skinny<T, MAXN><<<grid, kSkinnyThreads, 0, s>>>(g.d_cblk.as<GemmCBlk>(), g.d_task.as<GemmTask>(),
                                                    g.d_skinny.as<GemmRowChunk>(), (int)g.skinny.size(),
                                                    static_cast<const T*>(op.a), static_cast<const T*>(op.a_src),
                                                    static_cast<const T*>(op.b), static_cast<const T*>(op.b_src),
@@ -411,29 +424,42 @@ void launch_dfma_t(const GemmSchedule& g, const Operands& op, void* c, int grid,
 }
 
 // CTAs of one full wave: the grid-stride loop then has no partial second wave.
-template <typename T>
+template <typename T, int MAXN>
 int skinny_wave(int num_sms) {
   static int per_sm = [] {
     int n = 0;
-    QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_gemm_skinny<T>, kSkinnyThreads, 0));
+    QLTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_gemm_skinny<T, MAXN>, kSkinnyThreads, 0));
     return std::max(1, n);
   }();
   return std::max(1, num_sms) * per_sm;
 }
 
-int skinny_grid(int items, bool cplx, int num_sms) {
-  return std::max(1, std::min(items, cplx ? skinny_wave<double2>(num_sms) : skinny_wave<double>(num_sms)));
+// the kernel variant of a plan: real operands always use MAXN = 8 (64 registers either way);
+// complex ones the narrowest that covers the plan's blocks
+int skinny_variant(bool cplx, int maxn) { return !cplx ? 8 : maxn <= 2 ? 2 : maxn <= 4 ? 4 : 8; }
+
+int skinny_grid(int items, bool cplx, int maxn, int num_sms) {
+  int wave = 0;
+  switch (skinny_variant(cplx, maxn)) {
+    case 2: wave = skinny_wave<double2, 2>(num_sms); break;
+    case 4: wave = skinny_wave<double2, 4>(num_sms); break;
+    default: wave = cplx ? skinny_wave<double2, 8>(num_sms) : skinny_wave<double, 8>(num_sms); break;
+  }
+  return std::max(1, std::min(items, wave));
 }
 
 void launch_gemm_f64_skinny(const GemmSchedule& g, const Operands& op, void* c, bool cplx, int num_sms,
                             cudaStream_t s, const SkinnyFuse* fuse, int32_t* fields) {
   const int ns = (int)g.skinny.size();
   if (!ns) return;
-  const int grid = skinny_grid(ns, cplx, num_sms);
-  if (cplx)
-    launch_skinny_t<double2>(g, op, c, grid, s, fuse, fields);
-  else
-    launch_skinny_t<double>(g, op, c, grid, s, fuse, fields);
+  const int grid = skinny_grid(ns, cplx, g.skinny_maxn, num_sms);
+  switch (skinny_variant(cplx, g.skinny_maxn)) {
+    case 2: launch_skinny_t<double2, 2>(g, op, c, grid, s, fuse, fields); break;
+    case 4: launch_skinny_t<double2, 4>(g, op, c, grid, s, fuse, fields); break;
+    default:
+      if (cplx) launch_skinny_t<double2, 8>(g, op, c, grid, s, fuse, fields);
+      else launch_skinny_t<double, 8>(g, op, c, grid, s, fuse, fields);
+  }
   QLTG_CUDA(cudaGetLastError());
 }
 
