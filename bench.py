@@ -595,9 +595,24 @@ def run_aux(local: int, part: str = "all"):
         plan.execute(t0, dst)
         ms = _time_events(lambda: plan.execute(t0, dst), stream, flush)
         ms_api = _time_events(lambda: Transpose(t0, perm), stream, flush)
+        # the same launch after a flush that leaves L2 clean (write > L2, then read 256 MiB):
+        # the write flush leaves L2 full of dirty lines whose write-back the next kernel pays
+        clean = []
+        for r in range(5):
+            flush.fill_(float(r))
+            flush[: flush.numel() // 2].sum()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.execute(t0, dst)
+            e1.record(stream)
+            clean.append((e0, e1))
+        torch.cuda.synchronize()
+        ms_clean = statistics.median(a.elapsed_time(b) for a, b in clean)
         nbytes = 2 * 8 * t0.meta.size
         out.setdefault("transpose", []).append(
             {"case": name, "mbytes_moved": nbytes / 1e6, "kernel_ms": round(ms, 4),
+             "kernel_ms_clean_l2": round(ms_clean, 4),
+             "frac_of_hbm_clean_l2": nbytes / (ms_clean / 1e3) / 1e9 / pk["hbm_gbs"],
              "gbs": nbytes / (ms / 1e3) / 1e9, "frac_of_hbm": nbytes / (ms / 1e3) / 1e9 / pk["hbm_gbs"],
              "api_call_ms": round(ms_api, 4),
              "note": "kernel_ms: qltg_transpose_plan_exec (one launch); api_call_ms: qltg_transpose, which "

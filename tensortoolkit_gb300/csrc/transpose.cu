@@ -10,12 +10,14 @@
 // source, the block is a set of contiguous runs copied with 16-byte vector accesses;
 // otherwise tiles over (source-innermost dim p, destination-innermost dim q) are staged
 // through shared memory so both the read (along p) and the write (along q) are coalesced.
-// Tiles are 32 x 32, or Tp x Tq with Tp Tq <= 1024 when one of the two dims is short (an
-// inner dim of 4 elements gets 4 x 256 tiles, whose reads and writes are still long
-// contiguous runs). Only blocks whose two inner dims are both short fall back to a
-// destination-ordered gather. The +-1 block sign is applied by flipping the sign bit (no
-// floating-point multiply). Each CTA takes a contiguous range of work items, so it looks up
-// its first block once and then walks forward.
+// Tiles are 32 x 32, or Tp x Tq (x Tu of one batched outer dim) up to 32 KB of data when one
+// of the two dims is short (an inner dim of 4 elements gets 4 x 256 tiles, whose reads and
+// writes are still long contiguous runs). A CTA reads its next tile into a second shared
+// buffer (cp.async, no staging registers) while it writes the current one out, so a tile's
+// worth of loads is always in flight. Only blocks whose two inner dims are both short fall
+// back to a destination-ordered gather. The +-1 block sign is applied by flipping the sign
+// bit (no floating-point multiply). Each CTA takes a contiguous range of work items, so it
+// looks up its first block once and then walks forward.
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -26,23 +28,130 @@ namespace qltg {
 namespace {
 
 constexpr int kTile = 32;
-constexpr int kTileMax = 4096;    // elements per batched tile (Tp * Tq * Tu)
+constexpr int kTileMax = 4096;    // elements per batched tile (Tp * Tq * Tu), 8-byte elements
 constexpr int kRunChunk = 4096;   // elements per copy-mode / gather-mode work item
 constexpr int kPermThreads = 256;
-constexpr int kLoadBatch = 8;     // tile-mode loads issued per thread before storing
+constexpr int kLoadBatch = 8;     // copy-mode loads issued per thread before storing
+
+// Tile budget in elements: the same 32 KB of data per tile for real and complex elements.
+__host__ __device__ constexpr int tile_budget(int elem_bytes) { return elem_bytes == 16 ? kTileMax / 2 : kTileMax; }
+// One tile buffer in elements: Tu planes of Tq rows of Tp + 1 (Tp >= 2): at most 1.5x the tile.
+__host__ __device__ constexpr int tile_buf_elems(int elem_bytes) { return tile_budget(elem_bytes) * 3 / 2; }
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src));
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src));
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ __forceinline__ double flip(double x, uint64_t m) {
   return __longlong_as_double(__double_as_longlong(x) ^ (long long)m);
 }
 __device__ __forceinline__ double2 flip(double2 x, uint64_t m) { return make_double2(flip(x.x, m), flip(x.y, m)); }
 
+// A tile-mode work item, decoded: a Tp x Tq x Tu tile over (p, q, u) (u: one outer dim batched
+// so a tile holds up to the budget even when the inner dims are short).
+template <typename T>
+struct TileJob {
+  const T* s;
+  T* o;
+  uint32_t sq, su, dp, du;
+  int np, nq, ulim, ip0, iq0;
+  int tp, tq, tu, lp, lq, lu, n;
+  bool u_next;
+  uint64_t sg;
+};
+
+__host__ __device__ inline bool is_tile_item(const PermDesc& d) { return d.rank > 0 && d.p >= 0 && d.p != d.rank - 1; }
+
+template <typename T>
+__device__ __forceinline__ TileJob<T> tile_job(const PermDesc& d, int64_t local, const T* src, T* dst) {
+  TileJob<T> j;
+  const int r = d.rank, q = r - 1;
+  j.tp = d.tp;
+  j.tq = d.tq;
+  j.tu = d.tu;
+  const uint32_t per_outer = (uint32_t)d.tiles_p * (uint32_t)d.tiles_q * (uint32_t)d.tiles_u;
+  const uint32_t outer = (uint32_t)local / per_outer;
+  uint32_t tt = (uint32_t)local - outer * per_outer;
+  const uint32_t tui = tt / ((uint32_t)d.tiles_p * (uint32_t)d.tiles_q);
+  tt -= tui * ((uint32_t)d.tiles_p * (uint32_t)d.tiles_q);
+  const uint32_t tpi = tt / (uint32_t)d.tiles_q;
+  j.ip0 = (int)(tpi * (uint32_t)j.tp);
+  j.iq0 = (int)((tt - tpi * (uint32_t)d.tiles_q) * (uint32_t)j.tq);
+  const int u0 = (int)(tui * (uint32_t)j.tu);
+  uint32_t rem = outer, soff = 0, doff = 0, dstr = 1, dp = 0, du = 0;
+  for (int i = r - 1; i >= 0; --i) {
+    const uint32_t di = (uint32_t)d.dims[i];
+    if (i == d.p) dp = dstr;
+    if (i == d.u) du = dstr;
+    if (i != d.p && i != q && i != d.u) {
+      const uint32_t qq = rem / di;
+      const uint32_t x = rem - qq * di;
+      rem = qq;
+      soff += x * (uint32_t)d.sstride[i];
+      doff += x * dstr;
+    }
+    dstr *= di;
+  }
+  const int nu = d.u >= 0 ? d.dims[d.u] : 1;
+  j.su = d.u >= 0 ? (uint32_t)d.sstride[d.u] : 0u;
+  j.dp = dp;
+  j.du = du;
+  j.s = src + d.src_off + soff + (uint32_t)u0 * j.su;
+  j.o = dst + d.dst_off + doff + (uint32_t)u0 * du;
+  j.np = d.dims[d.p];
+  j.nq = d.dims[q];
+  j.sq = (uint32_t)d.sstride[q];
+  j.lp = __ffs(j.tp) - 1;   // tile extents are powers of two
+  j.lq = __ffs(j.tq) - 1;
+  j.lu = __ffs(j.tu) - 1;
+  j.n = j.tp * j.tq * j.tu;
+  j.ulim = nu - u0;
+  // write order: q fastest (stride 1 in the destination), then whichever of u and p has the
+  // smaller destination stride (a short q dim with u next to it in the destination)
+  j.u_next = d.u >= 0 && du < dp;
+  j.sg = d.sign_mask;
+  return j;
+}
+
+// read into a tile buffer: p fastest (stride 1 in the source), straight into shared memory
+// (cp.async), so a whole tile is in flight per CTA without staging registers
+template <typename T>
+__device__ __forceinline__ void tile_loads(const TileJob<T>& j, T* buf) {
+  const int row = j.tp + 1, plane = j.tq * row;
+  for (int e = threadIdx.x; e < j.n; e += kPermThreads) {
+    const int pi = e & (j.tp - 1), qi = (e >> j.lp) & (j.tq - 1), ui = e >> (j.lp + j.lq);
+    if (j.ip0 + pi < j.np && j.iq0 + qi < j.nq && ui < j.ulim)
+      cp_async_elem(buf + (ui * plane + qi * row + pi),
+                    j.s + ((uint32_t)(j.ip0 + pi) + (uint32_t)(j.iq0 + qi) * j.sq + (uint32_t)ui * j.su));
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_stores(const TileJob<T>& j, const T* buf) {
+  const int row = j.tp + 1, plane = j.tq * row;
+  for (int e = threadIdx.x; e < j.n; e += kPermThreads) {
+    const int qi = e & (j.tq - 1);
+    const int pi = j.u_next ? (e >> (j.lq + j.lu)) & (j.tp - 1) : (e >> j.lq) & (j.tp - 1);
+    const int ui = j.u_next ? (e >> j.lq) & (j.tu - 1) : e >> (j.lp + j.lq);
+    if (j.ip0 + pi < j.np && j.iq0 + qi < j.nq && ui < j.ulim)
+      j.o[(uint32_t)(j.iq0 + qi) + (uint32_t)(j.ip0 + pi) * j.dp + (uint32_t)ui * j.du] =
+          flip(buf[ui * plane + qi * row + pi], j.sg);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __restrict__ descs, int nd, int64_t ntiles,
                                                           const T* __restrict__ src, T* __restrict__ dst) {
-  // tile buffer: Tu planes of Tq rows of Tp + 1 (Tp a power of two, so the row stride is
-  // odd); Tp >= 2, so Tu Tq (Tp + 1) <= 1.5 Tp Tq Tu
+  // two tile buffers: Tu planes of Tq rows of Tp + 1 (Tp a power of two, so the row stride
+  // is odd); tile t + 1 is read into one while tile t is written out of the other
   extern __shared__ __align__(16) uint8_t perm_smem[];
-  T* tile = reinterpret_cast<T*>(perm_smem);
+  T* const bufs = reinterpret_cast<T*>(perm_smem);
+  constexpr int kBuf = tile_buf_elems((int)sizeof(T));
   const int64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
   const int64_t t_begin = (int64_t)blockIdx.x * per, t_end = min(ntiles, t_begin + per);
   if (t_begin >= t_end) return;
@@ -55,6 +164,8 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
   // the current block's descriptor, staged in shared memory when the walk reaches a new block
   __shared__ PermDesc sdesc;
   int cur = -1;
+  int b = 0;              // the buffer of the current tile item
+  bool pending = false;   // its loads were issued by the previous item
   for (int64_t t = t_begin; t < t_end; ++t) {
     while (lo + 1 < nd && descs[lo + 1].tile_begin <= t) ++lo;
     if (lo != cur) {   // uniform across the CTA: every thread walks the same items
@@ -72,10 +183,9 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
       if (threadIdx.x == 0) dst[d.dst_off] = flip(src[d.src_off], sg);
       continue;
     }
-    // destination strides
-    int64_t dstride[kMaxRank];
-    dstride[r - 1] = 1;
-    for (int i = r - 2; i >= 0; --i) dstride[i] = dstride[i + 1] * d.dims[i + 1];
+    // Offsets inside a block are below 2^31 (checked on the host), so the index arithmetic
+    // below is 32-bit; destination strides are running products (no per-thread stride array,
+    // which kept the kernel at 128 registers).
     if (d.p < 0) {
       // gather mode (both inner dims short): 1024 consecutive destination elements per work
       // item, each thread decodes its source offset; block sizes are below 2^31 (checked on
@@ -84,12 +194,11 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
       const uint32_t e0 = (uint32_t)local * kRunChunk;
       const uint32_t e1 = min(e0 + (uint32_t)kRunChunk, total);
       for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        uint32_t rem = e;
-        int64_t soff = 0;
+        uint32_t rem = e, soff = 0;
         for (int i = r - 1; i >= 0; --i) {
           const uint32_t di = (uint32_t)d.dims[i];
           const uint32_t qq = rem / di;
-          soff += (int64_t)(rem - qq * di) * d.sstride[i];
+          soff += (rem - qq * di) * (uint32_t)d.sstride[i];
           rem = qq;
         }
         dst[d.dst_off + e] = flip(src[d.src_off + soff], sg);
@@ -105,15 +214,15 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
       const uint32_t r1 = min(nruns, r0 + (uint32_t)d.tq);
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
       for (uint32_t run = r0 + warp; run < r1; run += kPermThreads / 32) {
-        uint32_t rem = run;
-        int64_t soff = 0, doff = 0;
+        uint32_t rem = run, soff = 0, doff = 0, dstr = len;
         for (int i = r - 2; i >= 0; --i) {
           const uint32_t di = (uint32_t)d.dims[i];
           const uint32_t qq = rem / di;
           const uint32_t x = rem - qq * di;
           rem = qq;
-          soff += (int64_t)x * d.sstride[i];
-          doff += (int64_t)x * dstride[i];
+          soff += x * (uint32_t)d.sstride[i];
+          doff += x * dstr;
+          dstr *= di;
         }
         const T* s = src + d.src_off + soff;
         T* o = dst + d.dst_off + doff;
@@ -134,15 +243,15 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
       const uint32_t chunks_per_run = ((uint32_t)d.dims[q] + kRunChunk - 1) / kRunChunk;
       const uint32_t run = (uint32_t)local / chunks_per_run;
       const int64_t c0 = (int64_t)((uint32_t)local - run * chunks_per_run) * kRunChunk;
-      uint32_t rem = run;
-      int64_t soff = 0, doff = 0;
+      uint32_t rem = run, soff = 0, doff = 0, dstr = (uint32_t)d.dims[q];
       for (int i = r - 2; i >= 0; --i) {
         const uint32_t di = (uint32_t)d.dims[i];
         const uint32_t qq = rem / di;
         const uint32_t x = rem - qq * di;
         rem = qq;
-        soff += (int64_t)x * d.sstride[i];
-        doff += (int64_t)x * dstride[i];
+        soff += x * (uint32_t)d.sstride[i];
+        doff += x * dstr;
+        dstr *= di;
       }
       const T* s = src + d.src_off + soff;
       T* o = dst + d.dst_off + doff;
@@ -183,75 +292,32 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
       }
       continue;
     }
-    // tile mode over (p, q, u) with Tp x Tq x Tu tiles (u: one outer dim batched so a tile
-    // holds up to kTileMax elements even when the inner dims are short)
-    const int tp = d.tp, tq = d.tq, tu = d.tu;
-    const uint32_t per_outer = (uint32_t)d.tiles_p * (uint32_t)d.tiles_q * (uint32_t)d.tiles_u;
-    const uint32_t outer = (uint32_t)local / per_outer;
-    uint32_t tt = (uint32_t)local - outer * per_outer;
-    const uint32_t tui = tt / ((uint32_t)d.tiles_p * (uint32_t)d.tiles_q);
-    tt -= tui * ((uint32_t)d.tiles_p * (uint32_t)d.tiles_q);
-    const uint32_t tpi = tt / (uint32_t)d.tiles_q;
-    const int64_t p0 = (int64_t)tpi * tp, q0 = (int64_t)(tt - tpi * (uint32_t)d.tiles_q) * tq;
-    const int64_t u0 = (int64_t)tui * tu;
-    uint32_t rem = outer;
-    int64_t soff = 0, doff = 0;
-    for (int i = r - 1; i >= 0; --i) {
-      if (i == d.p || i == q || i == d.u) continue;
-      const uint32_t di = (uint32_t)d.dims[i];
-      const uint32_t qq = rem / di;
-      const uint32_t x = rem - qq * di;
-      rem = qq;
-      soff += (int64_t)x * d.sstride[i];
-      doff += (int64_t)x * dstride[i];
-    }
-    const int64_t nu = d.u >= 0 ? d.dims[d.u] : 1;
-    const int64_t su = d.u >= 0 ? d.sstride[d.u] : 0, du = d.u >= 0 ? dstride[d.u] : 0;
-    const T* s = src + d.src_off + soff + u0 * su;
-    T* o = dst + d.dst_off + doff + u0 * du;
-    const int64_t np_ = d.dims[d.p], nq = d.dims[q];
-    const int64_t sq = d.sstride[q], dp = dstride[d.p];
-    const int lp = __ffs(tp) - 1, lq = __ffs(tq) - 1;   // tile extents are powers of two
-    const int n = tp * tq * tu, row = tp + 1, plane = tq * row;
-    const int64_t ulim = nu - u0;
-    // read: p fastest (stride 1 in the source); kLoadBatch independent loads in flight per
-    // thread before any of them is stored to shared memory
-    for (int e0 = threadIdx.x; e0 < n; e0 += kPermThreads * kLoadBatch) {
-      T v[kLoadBatch];
-      int slot[kLoadBatch];
-#pragma unroll
-      for (int i = 0; i < kLoadBatch; ++i) {
-        const int e = e0 + i * kPermThreads;
-        const int pi = e & (tp - 1), qi = (e >> lp) & (tq - 1), ui = e >> (lp + lq);
-        slot[i] = -1;
-        if (e < n && p0 + pi < np_ && q0 + qi < nq && ui < ulim) {
-          v[i] = __ldg(s + (p0 + pi) + (q0 + qi) * sq + ui * su);
-          slot[i] = ui * plane + qi * row + pi;
-        }
+    // tile mode
+    T* cb = bufs + b * kBuf;
+    const TileJob<T> j = tile_job<T>(d, local, src, dst);
+    if (!pending) tile_loads(j, cb);
+    cp_async_wait_all();
+    __syncthreads();
+    // the next item's tile goes into the other buffer while this one is written out
+    pending = false;
+    if (t + 1 < t_end) {
+      int ln = lo;
+      while (ln + 1 < nd && descs[ln + 1].tile_begin <= t + 1) ++ln;
+      const PermDesc& dn = ln == lo ? sdesc : descs[ln];
+      if (is_tile_item(dn)) {
+        tile_loads(tile_job<T>(dn, t + 1 - dn.tile_begin, src, dst), bufs + (b ^ 1) * kBuf);
+        pending = true;
       }
-#pragma unroll
-      for (int i = 0; i < kLoadBatch; ++i)
-        if (slot[i] >= 0) tile[slot[i]] = v[i];
     }
+    tile_stores(j, cb);
     __syncthreads();
-    // write: q fastest (stride 1 in the destination), then whichever of u and p has the
-    // smaller destination stride, so consecutive threads write consecutive addresses where the
-    // destination has them (a short q dim with u next to it in the destination)
-    const int lu = __ffs(tu) - 1;
-    const bool u_next = d.u >= 0 && du < dp;
-    for (int e = threadIdx.x; e < n; e += kPermThreads) {
-      const int qi = e & (tq - 1);
-      const int pi = u_next ? (e >> (lq + lu)) & (tp - 1) : (e >> lq) & (tp - 1);
-      const int ui = u_next ? (e >> lq) & (tu - 1) : e >> (lp + lq);
-      if (p0 + pi < np_ && q0 + qi < nq && ui < ulim)
-        o[(q0 + qi) + (p0 + pi) * dp + ui * du] = flip(tile[ui * plane + qi * row + pi], sg);
-    }
-    __syncthreads();
+    b ^= 1;
   }
+  cp_async_wait_all();
 }
 
 // dynamic shared memory of k_permute (also set as the kernel's maximum, per device)
-size_t perm_smem_bytes(int elem_bytes) { return (size_t)(kTileMax + kTileMax / 2) * elem_bytes; }
+size_t perm_smem_bytes(int elem_bytes) { return (size_t)2 * tile_buf_elems(elem_bytes) * elem_bytes; }
 
 // once per device (the attribute belongs to the current device's copy of the kernel)
 void perm_set_smem_attr() {
@@ -268,9 +334,9 @@ void perm_set_smem_attr() {
   if (dev >= 0 && dev < 64) done[dev] = true;
 }
 
-int pow2_at_least(int64_t x) {
+int pow2_at_least(int64_t x, int cap) {
   int v = 1;
-  while (v < x && v < kTileMax) v <<= 1;
+  while (v < x && v < cap) v <<= 1;
   return v;
 }
 
@@ -283,6 +349,7 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
   identity.assign(t.nblk, 0);
   ntiles = 0;
   const int r = t.rank;
+  const int budget = tile_budget((int)t.elem_bytes());   // elements per tile (32 KB of data)
   for (int64_t b = 0; b < t.nblk; ++b) {
     PermDesc d{};
     d.src_off = t.offsets[b];
@@ -345,15 +412,15 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
       // tile extents: 32 x 32, or stretched along the longer dim when the other is short
       int tp = -1, tq = -1;
       if (d.p >= 0) {
-        const int a = pow2_at_least(dd[d.p]), c = pow2_at_least(dd[m - 1]);
+        const int a = pow2_at_least(dd[d.p], budget), c = pow2_at_least(dd[m - 1], budget);
         if (a >= kTile && c >= kTile) {
           tp = tq = kTile;
         } else if (a < kTile) {
           tp = a;
-          tq = std::min(c, kTileMax / a);
+          tq = std::min(c, budget / a);
         } else {
           tq = c;
-          tp = std::min(a, kTileMax / c);
+          tp = std::min(a, budget / c);
         }
       }
       if (tp < 0 || tp * tq < 64) {
@@ -373,9 +440,9 @@ void TransposeList::describe(const Meta& t, const std::vector<int>& order, const
         int64_t best = 1;
         for (int i = 0; i < m - 1; ++i)
           if (i != d.p && dd[i] > best) { best = dd[i]; d.u = i; }
-        if (d.u >= 0 && valid < kTileMax / 2) {
+        if (d.u >= 0 && valid < budget / 2) {
           int tu = 1;
-          while (tu * 2 <= kTileMax / (tp * tq) && tu * 2 * valid <= kTileMax && tu < dd[d.u]) tu *= 2;
+          while (tu * 2 <= budget / (tp * tq) && tu * 2 * valid <= budget && tu < dd[d.u]) tu *= 2;
           d.tu = tu;
         } else {
           d.u = -1;
