@@ -17,6 +17,10 @@
  *     -> the same names with (..., C, ctx [, mode])  (contract_contiguous_axes.h:953-1040)
  *   qlten::LinearCombine(coefs, tens, beta, &res)   (ten_linear_combine.h:186-197)
  *     -> qlten_gb300::LinearCombine(coefs, tens, beta, &res, ctx)
+ *   qlten::dmrg::ApplyAxisDiagonal / ProjectAxis / ApplyAxisMonomial / ApplyRank2ToAxis... /
+ *   the composed ApplyRank2Then... / ApplyTwoRank2Then... forms / MoveHeadAxisToTail
+ *   (tensor_manipulation/dmrg/axis_ops.h:2391-3678)
+ *     -> qlten_gb300::dmrg::<same name>(<same arguments>, ctx [, mode]) (bosonic tensors)
  *
  * With the reference built for the GPU (USE_GPU) the QLTensor raw buffers already live in
  * device memory and are passed straight through. With the CPU build they are staged
@@ -43,6 +47,7 @@
 #include <vector>
 
 #include "qltg.h"
+#include "qlten/tensor_manipulation/dmrg/axis_ops.h"
 
 namespace qlten_gb300 {
 
@@ -534,6 +539,412 @@ void LinearCombine(const std::vector<ElemT>& coefs, const std::vector<qlten::QLT
   }
   qltg_lincomb_plan_destroy(lc);
 }
+
+// ------------------------------------------------------------------ qlten::dmrg axis operations
+// The bosonic axis-local operators of qlten::dmrg (tensor_manipulation/dmrg/axis_ops.h) with
+// the reference's signatures plus a Context. The work counters (AxisOpStats and friends) are
+// reset and left at zero: the device path has no loop of host GEMM calls to count. The
+// composed forms run as the device primitives in sequence (the reference's "Fused" forms avoid
+// a CPU intermediate; here the intermediate is one device tensor).
+namespace dmrg {
+
+namespace detail {
+
+template <typename ElemT>
+void append_value(std::vector<double>& v, const ElemT& x) {
+  double p[2];
+  qlten_gb300::detail::scalar_pair(x, p);
+  v.push_back(p[0]);
+  if (dtype_of<ElemT>() == QLTG_C128) v.push_back(p[1]);
+}
+
+inline void sync_or_throw(const char* what) {
+  if (cudaStreamSynchronize(nullptr) != cudaSuccess) throw std::runtime_error(std::string("qlten_gb300: ") + what);
+}
+
+// A tensor with `idxs` and the blocks an axis plan reports.
+template <typename ElemT, typename QNT>
+qlten::QLTensor<ElemT, QNT> from_axis_plan(const qlten::IndexVec<QNT>& idxs, qltg_axis_plan* plan) {
+  qlten::QLTensor<ElemT, QNT> out;
+  qlten_gb300::detail::init_from_plan(&out, idxs, plan, qltg_axis_plan_result, qltg_axis_plan_result_blocks);
+  return out;
+}
+
+// Destroys an axis plan on every way out.
+struct AxisPlan {
+  qltg_axis_plan* h = nullptr;
+  ~AxisPlan() {
+    if (h) qltg_axis_plan_destroy(h);
+  }
+};
+
+template <typename ElemT, typename QNT>
+qlten::QLTensor<ElemT, QNT> rank2(const qlten::QLTensor<ElemT, QNT>& in, const qlten::QLTensor<ElemT, QNT>& op1,
+                                  size_t axis1, const qlten::QLTensor<ElemT, QNT>* op2, size_t axis2,
+                                  const Context& ctx, int mode) {
+  Desc<ElemT, QNT> dt(in), d1(op1);
+  AxisPlan plan;
+  qlten::IndexVec<QNT> idxs = in.GetIndexes();
+  idxs[axis1] = op1.GetIndex(1);
+  if (op2) {
+    Desc<ElemT, QNT> d2(*op2);
+    check(qltg_axis_two_rank2_plan_create(ctx.get(), &dt.d, &d1.d, (int32_t)axis1, &d2.d, (int32_t)axis2, &plan.h));
+    idxs[axis2] = op2->GetIndex(1);
+  } else {
+    check(qltg_axis_rank2_plan_create(ctx.get(), &dt.d, &d1.d, (int32_t)axis1, &plan.h));
+  }
+  auto out = from_axis_plan<ElemT, QNT>(idxs, plan.h);
+  auto& mi = const_cast<qlten::QLTensor<ElemT, QNT>&>(in);
+  auto& m1 = const_cast<qlten::QLTensor<ElemT, QNT>&>(op1);
+  DeviceView<ElemT, QNT> vi(mi, true), v1(m1, true), vo(out, false);
+  std::unique_ptr<DeviceView<ElemT, QNT>> v2;
+  if (op2) v2 = std::make_unique<DeviceView<ElemT, QNT>>(const_cast<qlten::QLTensor<ElemT, QNT>&>(*op2), true);
+  check(qltg_axis_plan_exec(plan.h, vi.get(), v1.get(), v2 ? v2->get() : nullptr, vo.get(), mode, nullptr));
+  check(qltg_axis_plan_device_status(plan.h, nullptr));
+  vo.sync_back();
+  return out;
+}
+
+template <typename ElemT, typename QNT>
+void sector_scalars(const qlten::QLTensor<ElemT, QNT>& in, size_t axis, const std::vector<ElemT>& values,
+                    qlten::QLTensor<ElemT, QNT>& out, const Context& ctx) {
+  Desc<ElemT, QNT> dt(in);
+  std::vector<double> v;
+  for (const auto& x : values) append_value(v, x);
+  auto& mi = const_cast<qlten::QLTensor<ElemT, QNT>&>(in);
+  if (&out != &in) {
+    out = qlten::QLTensor<ElemT, QNT>(in.GetIndexes());
+    std::vector<qlten::CoorsT> coors;
+    for (const auto& kv : in.GetBlkSparDataTen().GetBlkIdxDataBlkMap()) coors.push_back(kv.second.blk_coors);
+    if (!coors.empty()) out.GetBlkSparDataTen().DataBlksInsert(coors, true, false);
+  }
+  DeviceView<ElemT, QNT> vi(mi, true);
+  if (&out == &in) {
+    check(qltg_axis_sector_scalars(ctx.get(), &dt.d, (int32_t)axis, v.data(), vi.get(), vi.get(), nullptr));
+    sync_or_throw("axis sector scalars failed");
+    vi.sync_back();
+  } else {
+    DeviceView<ElemT, QNT> vo(out, false);
+    check(qltg_axis_sector_scalars(ctx.get(), &dt.d, (int32_t)axis, v.data(), vi.get(), vo.get(), nullptr));
+    sync_or_throw("axis sector scalars failed");
+    vo.sync_back();
+  }
+}
+
+}  // namespace detail
+
+// output = beta output + alpha D(input) (axis_ops.h:2391-2466); output = input with alpha 1,
+// beta 0 is ApplyAxisDiagonalInPlace.
+template <typename ElemT, typename QNT>
+void ApplyAxisDiagonal(const qlten::QLTensor<ElemT, QNT>& input, size_t axis,
+                       const qlten::dmrg::AxisDiagonalOp<ElemT, QNT>& op, qlten::QLTensor<ElemT, QNT>& output,
+                       const Context& ctx, ElemT alpha = ElemT(1), ElemT beta = ElemT(0)) {
+  Desc<ElemT, QNT> dt(input);
+  std::vector<double> v;
+  for (const auto& sector : op.values)
+    for (const auto& x : sector) detail::append_value(v, x);
+  double al[2], be[2];
+  qlten_gb300::detail::scalar_pair(alpha, al);
+  qlten_gb300::detail::scalar_pair(beta, be);
+  auto& mi = const_cast<qlten::QLTensor<ElemT, QNT>&>(input);
+  if (&output == &input) {
+    DeviceView<ElemT, QNT> vi(mi, true);
+    check(qltg_axis_diagonal(ctx.get(), &dt.d, (int32_t)axis, v.data(), vi.get(), vi.get(), al, be, nullptr));
+    detail::sync_or_throw("axis diagonal failed");
+    vi.sync_back();
+    return;
+  }
+  const bool keep = be[0] != 0.0 || be[1] != 0.0;
+  if (!keep) {
+    output = qlten::QLTensor<ElemT, QNT>(input.GetIndexes());
+    std::vector<qlten::CoorsT> coors;
+    for (const auto& kv : input.GetBlkSparDataTen().GetBlkIdxDataBlkMap()) coors.push_back(kv.second.blk_coors);
+    if (!coors.empty()) output.GetBlkSparDataTen().DataBlksInsert(coors, true, false);
+  }
+  DeviceView<ElemT, QNT> vi(mi, true), vo(output, keep);
+  check(qltg_axis_diagonal(ctx.get(), &dt.d, (int32_t)axis, v.data(), vi.get(), vo.get(), al, be, nullptr));
+  detail::sync_or_throw("axis diagonal failed");
+  vo.sync_back();
+}
+
+// axis_ops.h:2548-2582
+template <typename ElemT, typename QNT>
+void ApplyAxisDiagonalInPlace(qlten::QLTensor<ElemT, QNT>& tensor, size_t axis,
+                              const qlten::dmrg::AxisDiagonalOp<ElemT, QNT>& op, const Context& ctx) {
+  ApplyAxisDiagonal(tensor, axis, op, tensor, ctx);
+}
+
+// axis_ops.h:2583-2637 (either storage mode gives the same result here; kConsumeOwnedInPlace
+// with output aliasing input scales in place)
+template <typename ElemT, typename QNT>
+void ApplyAxisDiagonalPreserveOrder(const qlten::QLTensor<ElemT, QNT>& input, size_t axis,
+                                    const qlten::dmrg::AxisDiagonalOp<ElemT, QNT>& op,
+                                    qlten::QLTensor<ElemT, QNT>& output, qlten::dmrg::AxisApplyStorageMode,
+                                    const Context& ctx, qlten::dmrg::AxisOpStats* stats = nullptr) {
+  if (stats) *stats = qlten::dmrg::AxisOpStats{};
+  ApplyAxisDiagonal(input, axis, op, output, ctx);
+}
+
+// axis_ops.h:2638-2675
+template <typename ElemT, typename QNT>
+void ScaleAxisSectorsInPlace(qlten::QLTensor<ElemT, QNT>& tensor, const qlten::dmrg::AxisSectorScalar<ElemT, QNT>& scale,
+                             const Context& ctx) {
+  detail::sector_scalars(tensor, scale.axis, scale.values_by_sector, tensor, ctx);
+}
+
+// axis_ops.h:2676-2744
+template <typename ElemT, typename QNT>
+void ApplyAxisSectorScalarsPreserveOrder(const qlten::QLTensor<ElemT, QNT>& input,
+                                         const qlten::dmrg::AxisSectorScalar<ElemT, QNT>& scale,
+                                         qlten::QLTensor<ElemT, QNT>& output, qlten::dmrg::AxisApplyStorageMode,
+                                         const Context& ctx, qlten::dmrg::AxisOpStats* stats = nullptr) {
+  if (stats) *stats = qlten::dmrg::AxisOpStats{};
+  detail::sector_scalars(input, scale.axis, scale.values_by_sector, output, ctx);
+}
+
+// output = beta output + alpha M(input) (axis_ops.h:2772-2860); beta != 0 needs an output with
+// the result's topology.
+template <typename ElemT, typename QNT>
+void ApplyAxisMonomial(const qlten::QLTensor<ElemT, QNT>& input, size_t axis,
+                       const qlten::dmrg::AxisMonomialOp<ElemT, QNT>& op, qlten::QLTensor<ElemT, QNT>& output,
+                       const Context& ctx, ElemT alpha = ElemT(1), ElemT beta = ElemT(0)) {
+  Desc<ElemT, QNT> dt(input);
+  std::vector<int32_t> oq;
+  std::vector<int64_t> od, ent;
+  for (const auto& s : op.output_index.GetQNScts()) {
+    int32_t v[4];
+    qn_values(s.GetQn(), v);
+    oq.insert(oq.end(), v, v + QNTraits<QNT>::ncomp);
+    od.push_back((int64_t)s.GetDegeneracy());
+  }
+  int32_t flux[4];
+  qn_values(op.flux, flux);
+  std::vector<double> cf;
+  for (const auto& e : op.entries) {
+    ent.insert(ent.end(), {(int64_t)e.in_sector, (int64_t)e.in_offset, (int64_t)e.out_sector, (int64_t)e.out_offset});
+    detail::append_value(cf, e.coef);
+  }
+  detail::AxisPlan plan;
+  check(qltg_axis_monomial_plan_create(ctx.get(), &dt.d, (int32_t)axis, (int32_t)od.size(), oq.data(), od.data(),
+                                       flux, (int64_t)op.entries.size(), ent.empty() ? nullptr : ent.data(),
+                                       cf.empty() ? nullptr : cf.data(), &plan.h));
+  double al[2], be[2];
+  qlten_gb300::detail::scalar_pair(alpha, al);
+  qlten_gb300::detail::scalar_pair(beta, be);
+  const bool keep = be[0] != 0.0 || be[1] != 0.0;
+  qlten::IndexVec<QNT> idxs = input.GetIndexes();
+  idxs[axis] = op.output_index;
+  if (!keep) output = detail::from_axis_plan<ElemT, QNT>(idxs, plan.h);
+  auto& mi = const_cast<qlten::QLTensor<ElemT, QNT>&>(input);
+  DeviceView<ElemT, QNT> vi(mi, true), vo(output, keep);
+  check(qltg_axis_monomial_exec(plan.h, vi.get(), vo.get(), al, be, nullptr));
+  detail::sync_or_throw("axis monomial failed");
+  vo.sync_back();
+}
+
+// axis_ops.h:2468-2532
+template <typename ElemT, typename QNT>
+void ProjectAxis(const qlten::QLTensor<ElemT, QNT>& input, size_t axis, const qlten::dmrg::AxisProjector<QNT>& projector,
+                 qlten::QLTensor<ElemT, QNT>& output, const Context& ctx) {
+  Desc<ElemT, QNT> dt(input);
+  std::vector<int64_t> counts, kept;
+  std::vector<qlten::QNSector<QNT>> scts;
+  const auto& in_scts = input.GetIndex(axis).GetQNScts();
+  for (size_t s = 0; s < projector.kept_degeneracies.size(); ++s) {
+    const auto& k = projector.kept_degeneracies[s];
+    counts.push_back((int64_t)k.size());
+    for (auto x : k) kept.push_back((int64_t)x);
+    if (!k.empty()) scts.emplace_back(in_scts.at(s).GetQn(), k.size());
+  }
+  detail::AxisPlan plan;
+  check(qltg_axis_project_plan_create(ctx.get(), &dt.d, (int32_t)axis, counts.data(), kept.empty() ? nullptr : kept.data(),
+                                      &plan.h));
+  qlten::IndexVec<QNT> idxs = input.GetIndexes();
+  idxs[axis] = qlten::Index<QNT>(scts, input.GetIndex(axis).GetDir());
+  output = detail::from_axis_plan<ElemT, QNT>(idxs, plan.h);
+  double al[2] = {1.0, 0.0}, be[2] = {0.0, 0.0};
+  auto& mi = const_cast<qlten::QLTensor<ElemT, QNT>&>(input);
+  DeviceView<ElemT, QNT> vi(mi, true), vo(output, false);
+  check(qltg_axis_monomial_exec(plan.h, vi.get(), vo.get(), al, be, nullptr));
+  detail::sync_or_throw("axis projection failed");
+  vo.sync_back();
+}
+
+// axis_ops.h:2889-2993 (rank2_op index 0 contracts with `target_axis`, index 1 takes its place)
+template <typename ElemT, typename QNT>
+void ApplyRank2ToAxisPreserveOrder(const qlten::QLTensor<ElemT, QNT>& input, const qlten::QLTensor<ElemT, QNT>& rank2_op,
+                                   size_t target_axis, qlten::QLTensor<ElemT, QNT>& out, const Context& ctx,
+                                   qlten::dmrg::Rank2AxisApplyStats* stats = nullptr, int mode = QLTG_MODE_FP64) {
+  if (stats) *stats = qlten::dmrg::Rank2AxisApplyStats{};
+  out = detail::rank2(input, rank2_op, target_axis, (const qlten::QLTensor<ElemT, QNT>*)nullptr, 0, ctx, mode);
+}
+
+// axis_ops.h:2994-3126
+template <typename ElemT, typename QNT>
+void ApplyTwoRank2ToAxesPreserveOrder(const qlten::QLTensor<ElemT, QNT>& input, const qlten::QLTensor<ElemT, QNT>& op1,
+                                      size_t axis1, const qlten::QLTensor<ElemT, QNT>& op2, size_t axis2,
+                                      qlten::QLTensor<ElemT, QNT>& out, const Context& ctx,
+                                      qlten::dmrg::AxisOpStats* stats = nullptr, int mode = QLTG_MODE_FP64) {
+  if (stats) *stats = qlten::dmrg::AxisOpStats{};
+  out = detail::rank2(input, op1, axis1, &op2, axis2, ctx, mode);
+}
+
+// axis_ops.h:3127-3151
+template <typename ElemT, typename QNT>
+void ApplyRank2ThenAxisDiagonalPreserveOrder(const qlten::QLTensor<ElemT, QNT>& input,
+                                             const qlten::QLTensor<ElemT, QNT>& rank2_op, size_t rank2_axis,
+                                             size_t diagonal_axis, const qlten::dmrg::AxisDiagonalOp<ElemT, QNT>& diagonal,
+                                             qlten::QLTensor<ElemT, QNT>& out, const Context& ctx,
+                                             qlten::dmrg::AxisOpStats* stats = nullptr, int mode = QLTG_MODE_FP64) {
+  if (stats) *stats = qlten::dmrg::AxisOpStats{};
+  out = detail::rank2(input, rank2_op, rank2_axis, (const qlten::QLTensor<ElemT, QNT>*)nullptr, 0, ctx, mode);
+  ApplyAxisDiagonal(out, diagonal_axis, diagonal, out, ctx);
+}
+
+// axis_ops.h:3152-3180
+template <typename ElemT, typename QNT>
+void ApplyRank2ThenAxisSectorScalarsPreserveOrder(const qlten::QLTensor<ElemT, QNT>& input,
+                                                  const qlten::QLTensor<ElemT, QNT>& rank2_op, size_t rank2_axis,
+                                                  const qlten::dmrg::AxisSectorScalar<ElemT, QNT>& scale,
+                                                  qlten::QLTensor<ElemT, QNT>& out, const Context& ctx,
+                                                  qlten::dmrg::AxisOpStats* stats = nullptr, int mode = QLTG_MODE_FP64) {
+  if (stats) *stats = qlten::dmrg::AxisOpStats{};
+  out = detail::rank2(input, rank2_op, rank2_axis, (const qlten::QLTensor<ElemT, QNT>*)nullptr, 0, ctx, mode);
+  detail::sector_scalars(out, scale.axis, scale.values_by_sector, out, ctx);
+}
+
+// out = beta out + alpha S(R(input)) with R on axis 0 or the last axis (axis_ops.h:3181-3283):
+// an existing out keeps its blocks and gains the ones R produces; a default out needs beta 0.
+template <typename ElemT, typename QNT>
+void ApplyBoundaryRank2ThenAxisSectorScalarsAccumulatePreserveOrder(
+    const qlten::QLTensor<ElemT, QNT>& input, const qlten::QLTensor<ElemT, QNT>& rank2_op, size_t rank2_axis,
+    const qlten::dmrg::AxisSectorScalar<ElemT, QNT>& scale, const ElemT alpha, const ElemT beta,
+    qlten::QLTensor<ElemT, QNT>& out, const Context& ctx, qlten::dmrg::AxisOpStats* stats = nullptr,
+    int mode = QLTG_MODE_FP64) {
+  if (stats) *stats = qlten::dmrg::AxisOpStats{};
+  if (rank2_axis != 0 && rank2_axis + 1 != input.Rank())
+    throw std::invalid_argument("qlten_gb300: rank2_axis must be axis 0 or the last axis");
+  double be[2];
+  qlten_gb300::detail::scalar_pair(beta, be);
+  const bool has_out = !out.IsDefault();
+  if (!has_out && (be[0] != 0.0 || be[1] != 0.0))
+    throw std::invalid_argument("qlten_gb300: beta != 0 needs an existing output");
+  qlten::QLTensor<ElemT, QNT> r =
+      detail::rank2(input, rank2_op, rank2_axis, (const qlten::QLTensor<ElemT, QNT>*)nullptr, 0, ctx, mode);
+  detail::sector_scalars(r, scale.axis, scale.values_by_sector, r, ctx);
+  // out = alpha r + beta out over the union of both block sets, out's blocks kept
+  Desc<ElemT, QNT> dr(r);
+  std::vector<Desc<ElemT, QNT>> dout;
+  if (has_out) dout.emplace_back(out);
+  const qltg_tensor_desc* dp = &dr.d;
+  std::vector<double> cf;
+  detail::append_value(cf, alpha);
+  qltg_lincomb_plan* lc = nullptr;
+  check(qltg_lincomb_plan_create(ctx.get(), 1, &dp, cf.data(), has_out ? &dout[0].d : nullptr, be, has_out ? 1 : 0, &lc));
+  try {
+    qlten::QLTensor<ElemT, QNT> res;
+    qlten_gb300::detail::init_from_plan(&res, r.GetIndexes(), lc, qltg_lincomb_plan_result,
+                                        qltg_lincomb_plan_result_blocks);
+    DeviceView<ElemT, QNT> vr(r, true), vo(res, false);
+    const void* src = vr.get();
+    if (has_out) {
+      DeviceView<ElemT, QNT> vold(out, true);
+      check(qltg_lincomb_exec(lc, &src, vold.get(), vo.get(), nullptr));
+      detail::sync_or_throw("accumulate failed");
+    } else {
+      check(qltg_lincomb_exec(lc, &src, nullptr, vo.get(), nullptr));
+      detail::sync_or_throw("accumulate failed");
+    }
+    vo.sync_back();
+    out = std::move(res);
+  } catch (...) {
+    qltg_lincomb_plan_destroy(lc);
+    throw;
+  }
+  qltg_lincomb_plan_destroy(lc);
+}
+
+// axis_ops.h:3284-3302: the accumulate form with alpha 1, beta 0, as in the reference
+template <typename ElemT, typename QNT>
+void ApplyBoundaryRank2ThenAxisSectorScalarsFusedPreserveOrder(
+    const qlten::QLTensor<ElemT, QNT>& input, const qlten::QLTensor<ElemT, QNT>& rank2_op, size_t rank2_axis,
+    const qlten::dmrg::AxisSectorScalar<ElemT, QNT>& scale, qlten::QLTensor<ElemT, QNT>& out, const Context& ctx,
+    qlten::dmrg::AxisOpStats* stats = nullptr, int mode = QLTG_MODE_FP64) {
+  ApplyBoundaryRank2ThenAxisSectorScalarsAccumulatePreserveOrder(input, rank2_op, rank2_axis, scale, ElemT(1), ElemT(0),
+                                                                 out, ctx, stats, mode);
+}
+
+// axis_ops.h:3319-3503: the rank-2 operator, then the monomial on the result
+template <typename ElemT, typename QNT>
+void ApplyRank2ThenAxisMonomialFusedPreserveOrder(const qlten::QLTensor<ElemT, QNT>& input,
+                                                  const qlten::QLTensor<ElemT, QNT>& rank2_op, size_t rank2_axis,
+                                                  size_t monomial_axis,
+                                                  const qlten::dmrg::AxisMonomialOp<ElemT, QNT>& monomial,
+                                                  qlten::QLTensor<ElemT, QNT>& out, const Context& ctx,
+                                                  qlten::dmrg::AxisOpStats* stats = nullptr, int mode = QLTG_MODE_FP64) {
+  if (stats) *stats = qlten::dmrg::AxisOpStats{};
+  if (&input == &out || &rank2_op == &out) throw std::invalid_argument("qlten_gb300: output aliasing is not allowed");
+  const qlten::QLTensor<ElemT, QNT> r =
+      detail::rank2(input, rank2_op, rank2_axis, (const qlten::QLTensor<ElemT, QNT>*)nullptr, 0, ctx, mode);
+  ApplyAxisMonomial(r, monomial_axis, monomial, out, ctx);
+}
+
+// axis_ops.h:3504-3532
+template <typename ElemT, typename QNT>
+void ApplyTwoRank2ThenAxisDiagonalPreserveOrder(const qlten::QLTensor<ElemT, QNT>& input,
+                                                const qlten::QLTensor<ElemT, QNT>& op1, size_t axis1,
+                                                const qlten::QLTensor<ElemT, QNT>& op2, size_t axis2,
+                                                size_t diagonal_axis,
+                                                const qlten::dmrg::AxisDiagonalOp<ElemT, QNT>& diagonal,
+                                                qlten::QLTensor<ElemT, QNT>& out, const Context& ctx,
+                                                qlten::dmrg::AxisOpStats* stats = nullptr, int mode = QLTG_MODE_FP64) {
+  if (stats) *stats = qlten::dmrg::AxisOpStats{};
+  out = detail::rank2(input, op1, axis1, &op2, axis2, ctx, mode);
+  ApplyAxisDiagonal(out, diagonal_axis, diagonal, out, ctx);
+}
+
+// axis_ops.h:3533-3577
+template <typename ElemT, typename QNT>
+void ApplyTwoRank2ThenAxisSectorScalarsPreserveOrder(const qlten::QLTensor<ElemT, QNT>& input,
+                                                     const qlten::QLTensor<ElemT, QNT>& op1, size_t axis1,
+                                                     const qlten::QLTensor<ElemT, QNT>& op2, size_t axis2,
+                                                     const qlten::dmrg::AxisSectorScalar<ElemT, QNT>& scale,
+                                                     qlten::QLTensor<ElemT, QNT>& out, const Context& ctx,
+                                                     qlten::dmrg::AxisOpStats* stats = nullptr,
+                                                     int mode = QLTG_MODE_FP64) {
+  if (stats) *stats = qlten::dmrg::AxisOpStats{};
+  out = detail::rank2(input, op1, axis1, &op2, axis2, ctx, mode);
+  detail::sector_scalars(out, scale.axis, scale.values_by_sector, out, ctx);
+}
+
+// axis_ops.h:3578-3678: axis 0 moved to the end (a bosonic transpose)
+template <typename ElemT, typename QNT>
+void MoveHeadAxisToTail(const qlten::QLTensor<ElemT, QNT>& input, qlten::QLTensor<ElemT, QNT>& out, const Context& ctx,
+                        qlten::dmrg::AxisLayoutMoveStats* stats = nullptr) {
+  if (stats) *stats = qlten::dmrg::AxisLayoutMoveStats{};
+  const size_t r = input.Rank();
+  std::vector<int32_t> perm;
+  for (size_t i = 1; i < r; ++i) perm.push_back((int32_t)i);
+  perm.push_back(0);
+  qlten::IndexVec<QNT> idxs;
+  for (auto i : perm) idxs.push_back(input.GetIndex(i));
+  out = qlten::QLTensor<ElemT, QNT>(idxs);
+  std::vector<qlten::CoorsT> coors;
+  for (const auto& kv : input.GetBlkSparDataTen().GetBlkIdxDataBlkMap()) {
+    qlten::CoorsT c;
+    for (auto i : perm) c.push_back(kv.second.blk_coors[i]);
+    coors.push_back(c);
+  }
+  if (!coors.empty()) out.GetBlkSparDataTen().DataBlksInsert(coors, true, false);
+  Desc<ElemT, QNT> dt(input);
+  auto& mi = const_cast<qlten::QLTensor<ElemT, QNT>&>(input);
+  DeviceView<ElemT, QNT> vi(mi, true), vo(out, false);
+  check(qltg_transpose(ctx.get(), &dt.d, vi.get(), perm.data(), vo.get(), nullptr));
+  detail::sync_or_throw("axis move failed");
+  vo.sync_back();
+}
+
+}  // namespace dmrg
 
 }  // namespace qlten_gb300
 

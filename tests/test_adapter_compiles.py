@@ -1,6 +1,7 @@
 """The drop-in adapter include/qlten_gb300.h compiles against the reference's own headers
 (U1QN / FP64 and fU1U1QN / complex128 instantiations of Contract, SVD, QR,
-ContractContiguousAxes, the contiguous accumulate forms and LinearCombine). Runs where
+ContractContiguousAxes, the contiguous accumulate forms and LinearCombine; real and complex
+U1QN instantiations of every qlten::dmrg axis entry point). Runs where
 the reference tree is available and named by the environment variable QLTEN_REF_TREE;
 skipped elsewhere."""
 import os
