@@ -140,7 +140,7 @@ __device__ __forceinline__ int rr_player(int slot, int r, int qq) {
 // between barriers: (1) one warp per pair forms <x_i, x_j>; (2) warps 0-3 (one per
 // scheduler) decide and compute the rotations, one lane per pair, and list the rotated ones;
 // (3) all warps apply them over (pair, 32-entry chunk) items.
-constexpr int kJacThreads = 256;
+constexpr int kJacThreads = 512;
 constexpr int kJacWarps = kJacThreads / 32;
 constexpr int kJacAuxPerCol = 64;    // shared-memory bytes per column for the bookkeeping below
 constexpr int kJacAuxFixed = 256;
