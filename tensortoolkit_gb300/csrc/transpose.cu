@@ -207,14 +207,18 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
     }
     if (d.p == q && d.tq > 1) {
       // copy mode with short runs: a work item is d.tq consecutive runs (of dims[q] elements,
-      // contiguous on both sides); each warp copies whole runs, decoding one run's offsets
+      // contiguous on both sides). The runs' offsets are decoded once, one thread per run,
+      // into shared memory (the tile buffers are idle: only tile items prefetch into them);
+      // then the item's elements are copied as one flat range, kLoadBatch loads in flight
+      // per thread before the stores.
       const uint32_t len = (uint32_t)d.dims[q];
       const uint32_t nruns = (uint32_t)(d.nouter);
       const uint32_t r0 = (uint32_t)local * (uint32_t)d.tq;
-      const uint32_t r1 = min(nruns, r0 + (uint32_t)d.tq);
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      for (uint32_t run = r0 + warp; run < r1; run += kPermThreads / 32) {
-        uint32_t rem = run, soff = 0, doff = 0, dstr = len;
+      const uint32_t nr = min(nruns, r0 + (uint32_t)d.tq) - r0;
+      uint32_t* run_s = reinterpret_cast<uint32_t*>(perm_smem);
+      uint32_t* run_d = run_s + nr;
+      for (uint32_t j = threadIdx.x; j < nr; j += kPermThreads) {
+        uint32_t rem = r0 + j, soff = 0, doff = 0, dstr = len;
         for (int i = r - 2; i >= 0; --i) {
           const uint32_t di = (uint32_t)d.dims[i];
           const uint32_t qq = rem / di;
@@ -224,18 +228,37 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
           doff += x * dstr;
           dstr *= di;
         }
-        const T* s = src + d.src_off + soff;
-        T* o = dst + d.dst_off + doff;
-        for (uint32_t e0 = lane; e0 < len; e0 += 32 * 4) {
-          T v[4];
+        run_s[j] = soff;
+        run_d[j] = doff;
+      }
+      __syncthreads();
+      const uint32_t total = nr * len;
+      const float rlen = 1.0f / (float)len;
+      const T* s = src + d.src_off;
+      T* o = dst + d.dst_off;
+      for (uint32_t e0 = threadIdx.x; e0 < total; e0 += kPermThreads * kLoadBatch) {
+        T v[kLoadBatch];
+        uint32_t at[kLoadBatch];
 #pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (e0 + 32 * i < len) v[i] = __ldg(s + e0 + 32 * i);
+        for (int i = 0; i < kLoadBatch; ++i) {
+          const uint32_t e = e0 + (uint32_t)i * kPermThreads;
+          if (e < total) {
+            // run = e / len: the float quotient, corrected to the exact one
+            uint32_t run = (uint32_t)((float)e * rlen);
+            if (run * len > e) --run;
+            else if ((run + 1) * len <= e) ++run;
+            const uint32_t off = e - run * len;
+            v[i] = __ldg(s + run_s[run] + off);
+            at[i] = run_d[run] + off;
+          }
+        }
 #pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (e0 + 32 * i < len) o[e0 + 32 * i] = flip(v[i], sg);
+        for (int i = 0; i < kLoadBatch; ++i) {
+          const uint32_t e = e0 + (uint32_t)i * kPermThreads;
+          if (e < total) o[at[i]] = flip(v[i], sg);
         }
       }
+      __syncthreads();   // the run tables are rewritten by the next item
       continue;
     }
     if (d.p == q) {
