@@ -166,8 +166,14 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
   int cur = -1;
   int b = 0;              // the buffer of the current tile item
   bool pending = false;   // its loads were issued by the previous item
+  // first work item of the next block, read from global memory only when the walk moves on
+  constexpr int64_t kNone = 0x7FFFFFFFFFFFFFFFll;
+  int64_t next_begin = lo + 1 < nd ? descs[lo + 1].tile_begin : kNone;
   for (int64_t t = t_begin; t < t_end; ++t) {
-    while (lo + 1 < nd && descs[lo + 1].tile_begin <= t) ++lo;
+    while (t >= next_begin) {
+      ++lo;
+      next_begin = lo + 1 < nd ? descs[lo + 1].tile_begin : kNone;
+    }
     if (lo != cur) {   // uniform across the CTA: every thread walks the same items
       __syncthreads();
       if (threadIdx.x == 0) sdesc = descs[lo];
@@ -325,7 +331,10 @@ __global__ void __launch_bounds__(kPermThreads) k_permute(const PermDesc* __rest
     pending = false;
     if (t + 1 < t_end) {
       int ln = lo;
-      while (ln + 1 < nd && descs[ln + 1].tile_begin <= t + 1) ++ln;
+      if (t + 1 >= next_begin) {
+        ++ln;
+        while (ln + 1 < nd && descs[ln + 1].tile_begin <= t + 1) ++ln;
+      }
       const PermDesc& dn = ln == lo ? sdesc : descs[ln];
       if (is_tile_item(dn)) {
         tile_loads(tile_job<T>(dn, t + 1 - dn.tile_begin, src, dst), bufs + (b ^ 1) * kBuf);
