@@ -119,10 +119,24 @@ __device__ __forceinline__ TileJob<T> tile_job(const PermDesc& d, int64_t local,
 }
 
 // read into a tile buffer: p fastest (stride 1 in the source), straight into shared memory
-// (cp.async), so a whole tile is in flight per CTA without staging registers
+// (cp.async), so a whole tile is in flight per CTA without staging registers. With Tp <= the
+// CTA size a thread keeps one column pi and walks the (q, u) rows of the tile, so the index
+// arithmetic per element is a few integer operations.
 template <typename T>
 __device__ __forceinline__ void tile_loads(const TileJob<T>& j, T* buf) {
   const int row = j.tp + 1, plane = j.tq * row;
+  if (j.tp <= kPermThreads) {
+    const int pi = threadIdx.x & (j.tp - 1);
+    if (j.ip0 + pi >= j.np) return;
+    const T* sb = j.s + (uint32_t)(j.ip0 + pi);
+    const int rstep = kPermThreads >> j.lp, nrows = j.tq * j.tu;
+    for (int ri = threadIdx.x >> j.lp; ri < nrows; ri += rstep) {
+      const int qi = ri & (j.tq - 1), ui = ri >> j.lq;
+      if (j.iq0 + qi < j.nq && ui < j.ulim)
+        cp_async_elem(buf + (ui * plane + qi * row + pi), sb + ((uint32_t)(j.iq0 + qi) * j.sq + (uint32_t)ui * j.su));
+    }
+    return;
+  }
   for (int e = threadIdx.x; e < j.n; e += kPermThreads) {
     const int pi = e & (j.tp - 1), qi = (e >> j.lp) & (j.tq - 1), ui = e >> (j.lp + j.lq);
     if (j.ip0 + pi < j.np && j.iq0 + qi < j.nq && ui < j.ulim)
@@ -131,9 +145,24 @@ __device__ __forceinline__ void tile_loads(const TileJob<T>& j, T* buf) {
   }
 }
 
+// write out of a tile buffer in the write order (q fastest, then u or p); with Tq <= the CTA
+// size a thread keeps one q and walks the (p, u) columns
 template <typename T>
 __device__ __forceinline__ void tile_stores(const TileJob<T>& j, const T* buf) {
   const int row = j.tp + 1, plane = j.tq * row;
+  if (j.tq <= kPermThreads) {
+    const int qi = threadIdx.x & (j.tq - 1);
+    if (j.iq0 + qi >= j.nq) return;
+    T* ob = j.o + (uint32_t)(j.iq0 + qi);
+    const int cstep = kPermThreads >> j.lq, ncols = j.tp * j.tu;
+    for (int ci = threadIdx.x >> j.lq; ci < ncols; ci += cstep) {
+      const int pi = j.u_next ? ci >> j.lu : ci & (j.tp - 1);
+      const int ui = j.u_next ? ci & (j.tu - 1) : ci >> j.lp;
+      if (j.ip0 + pi < j.np && ui < j.ulim)
+        ob[(uint32_t)(j.ip0 + pi) * j.dp + (uint32_t)ui * j.du] = flip(buf[ui * plane + qi * row + pi], j.sg);
+    }
+    return;
+  }
   for (int e = threadIdx.x; e < j.n; e += kPermThreads) {
     const int qi = e & (j.tq - 1);
     const int pi = j.u_next ? (e >> (j.lq + j.lu)) & (j.tp - 1) : (e >> j.lq) & (j.tp - 1);
