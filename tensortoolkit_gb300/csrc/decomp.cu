@@ -13,11 +13,14 @@
 // group is spread over a thread-block cluster of up to 16 CTAs (one SM each, in proportion
 // to its share of the work) that step through the rotation rounds together on the cluster
 // barrier, and the QR runs in panels whose updates spread over every group's column tiles;
-// one scatter launch builds the result blocks. Only the singular values cross to the host
-// (for the global truncation sort, as in the reference).
+// one scatter launch builds the result blocks. The truncation (the reference's global sort
+// of the singular values, kept dimension and error) runs on the device too; the host reads
+// back only the kept dimension, the error and the kept count per group, which size the
+// result tensors.
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -38,9 +41,6 @@ constexpr int kJacobiSmem = 200 * 1024;   // dynamic shared memory of k_jacobi (
 
 // ------------------------------------------------------------------ complex helpers
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-__device__ __forceinline__ double2 cconjmul(double2 a, double2 b) {   // conj(a) * b
-  return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
-}
 __device__ __forceinline__ double abs2(double a) { return a * a; }
 __device__ __forceinline__ double abs2(double2 a) { return a.x * a.x + a.y * a.y; }
 
@@ -507,11 +507,11 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const JacobiJob* __restr
 }
 
 // Singular values = vector norms, sorted descending; left vectors normalised in place.
-// order[job][k] = vector index of the k-th largest singular value.
+// order[job][k] = vector index of the k-th largest singular value, svs[job][k] its value.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_svd_finish(const JacobiJob* __restrict__ jobs, T* __restrict__ ws,
                                                          double* __restrict__ sv, const int64_t* __restrict__ sv_off,
-                                                         int32_t* __restrict__ order) {
+                                                         int32_t* __restrict__ order, double* __restrict__ svs) {
   const JacobiJob jb = jobs[blockIdx.x];
   T* W = ws + jb.w_off;
   const int p = jb.p, q = jb.q;
@@ -540,6 +540,125 @@ __global__ void __launch_bounds__(kThreads) k_svd_finish(const JacobiJob* __rest
       rk += (y > x) || (y == x && u < v);
     }
     ord[rk] = v;
+    svs[sv_off[blockIdx.x] + rk] = x;
+  }
+}
+
+// ---- truncation on the device, the reference's rule (tensor_manipulation/ten_decomp/
+// ten_svd.h:281-372): all groups' nonzero singular values in descending order (ties by group,
+// then rank: a strict total order, so the result does not depend on how it is sorted), keep
+// Dmin of them, then one more while the kept weight sum s^2 is <= (1 - eps) of the total and
+// the count stays <= Dmax. Each group's values sit in rank order (descending, zeros last), so
+// an entry's place in the global order is a sum of counts:
+//   place(g, i) = i + sum_{h < g} #{s_h >= v} + sum_{h > g} #{s_h > v}.
+struct SvCut {
+  int64_t kept;    // kept dimension D
+  double err;      // truncation error 1 - kept weight / total weight (0 when nothing is cut)
+  int32_t nnz;     // nonzero singular values over all groups
+  int32_t pad;
+};
+
+__global__ void __launch_bounds__(256) k_sv_place(const double* __restrict__ svs, const int64_t* __restrict__ sv_off,
+                                                  int ng, double* __restrict__ sorted_v, int32_t* __restrict__ sorted_g,
+                                                  SvCut* __restrict__ cut) {
+  const int64_t n = sv_off[ng];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const double v = svs[e];
+    if (v == 0.0) continue;
+    int lo = 0, hi = ng - 1;   // the group holding entry e: the last one starting at or before e
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sv_off[mid] <= e) lo = mid; else hi = mid - 1;
+    }
+    const int g = lo;
+    int64_t place = e - sv_off[g];
+    for (int h = 0; h < ng; ++h) {
+      if (h == g) continue;
+      const double* sh = svs + sv_off[h];
+      int a = 0, b = (int)(sv_off[h + 1] - sv_off[h]);   // first entry of h that comes after v
+      while (a < b) {
+        const int m = (a + b) >> 1;
+        if (h < g ? sh[m] >= v : sh[m] > v) a = m + 1; else b = m;
+      }
+      place += a;
+    }
+    sorted_v[place] = v;   // place <= n - 1: at most (size_g - 1) + the other groups' sizes
+    sorted_g[place] = g;
+    atomicAdd(&cut->nnz, 1);
+  }
+}
+
+// One CTA. The weights s^2 are summed in one thread in the sorted order (the order the
+// reference sums in; each square is rounded before its addition), chunk by chunk through
+// shared memory, keeping every prefix W(k) = weight of the first k values. The reference's
+// loop (keep Dmin, add one while W(kept) <= (1 - eps) W(total) and kept < min(total, Dmax))
+// ends at the smallest k in [Dmin, min(total, Dmax)) with W(k) > (1 - eps) W(total), else at
+// min(total, Dmax): the threads search for it. Then the kept entries are counted per group.
+constexpr int kCutChunk = 2048;
+
+__global__ void __launch_bounds__(256) k_sv_cut(const double* __restrict__ sorted_v, const int32_t* __restrict__ sorted_g,
+                                                double* __restrict__ prefix, double trunc, int64_t dmin, int64_t dmax,
+                                                int ng, SvCut* __restrict__ cut, int* __restrict__ kcnt) {
+  __shared__ double buf[kCutChunk];
+  __shared__ unsigned long long kept_s;
+  __shared__ double target_s;
+  const int64_t total = cut->nnz;
+  const bool cuts = total > dmin;
+  const int64_t lim = cuts ? (total < dmax ? total : dmax) : total;
+  if (threadIdx.x == 0) kept_s = (unsigned long long)lim;
+  if (cuts) {
+    double run = 0;   // thread 0's running sum
+    for (int64_t base = 0; base < total; base += kCutChunk) {
+      const int n = (int)(total - base < kCutChunk ? total - base : kCutChunk);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) buf[i] = __dmul_rn(sorted_v[base + i], sorted_v[base + i]);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+#pragma unroll 16
+        for (int i = 0; i < n; ++i) {
+          run = __dadd_rn(run, buf[i]);
+          buf[i] = run;
+        }
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x) prefix[base + i] = buf[i];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) target_s = __dmul_rn(run, __dsub_rn(1.0, trunc));
+    __syncthreads();   // also orders the prefix stores before the reads below
+    for (int64_t k = dmin + threadIdx.x; k < lim; k += blockDim.x) {
+      const double w = k == 0 ? 0.0 : prefix[k - 1];
+      if (w > target_s) atomicMin(&kept_s, (unsigned long long)k);
+    }
+  }
+  __syncthreads();
+  const int64_t kept = (int64_t)kept_s;
+  if (threadIdx.x == 0) {
+    double err = 0;
+    if (cuts) {
+      const double w = kept == 0 ? 0.0 : prefix[kept - 1];
+      const double x = __dsub_rn(1.0, __ddiv_rn(w, prefix[total - 1]));
+      err = x > 0 ? x : 0;
+    }
+    cut->kept = kept;
+    cut->err = err;
+  }
+  // (a NaN among the values leaves places unfilled: the group index is checked)
+  for (int64_t j = threadIdx.x; j < kept; j += blockDim.x) {
+    const int g = sorted_g[j];
+    if (g >= 0 && g < ng) atomicAdd(kcnt + g, 1);
+  }
+}
+
+// S blocks: the kept values of a group on the diagonal of its (zero-filled) kd x kd block
+struct SvDiag {
+  int64_t dst_off, src_off;
+  int32_t kd, pad;
+};
+
+__global__ void k_sv_diag(const SvDiag* __restrict__ d, int nd, const double* __restrict__ svs, double* __restrict__ S) {
+  for (int b = blockIdx.x; b < nd; b += gridDim.x) {
+    const SvDiag x = d[b];
+    for (int i = threadIdx.x; i < x.kd; i += blockDim.x) S[x.dst_off + (int64_t)i * x.kd + i] = svs[x.src_off + i];
   }
 }
 
@@ -1095,14 +1214,21 @@ void launch_gather(const std::vector<CopyDesc>& d, int64_t total, const void* sr
 }
 
 template <typename T>
+void launch_scatter(const std::vector<ScatterDesc>& d, int64_t total, const int32_t* list_dev, const void* src,
+                    void* dst, cudaStream_t s, DevBuf& keep_d) {
+  if (total == 0) return;
+  keep_d = upload(d, s);
+  k_scatter<T><<<grid_for(total), 256, 0, s>>>(keep_d.as<ScatterDesc>(), (int)d.size(), total, list_dev,
+                                                static_cast<const T*>(src), static_cast<T*>(dst));
+  QLTG_CUDA(cudaGetLastError());
+}
+
+template <typename T>
 void launch_scatter(const std::vector<ScatterDesc>& d, int64_t total, const std::vector<int32_t>& list,
                     const void* src, void* dst, cudaStream_t s, DevBuf& keep_d, DevBuf& keep_l) {
   if (total == 0) return;
-  keep_d = upload(d, s);
   keep_l = upload(list.empty() ? std::vector<int32_t>{0} : list, s);
-  k_scatter<T><<<grid_for(total), 256, 0, s>>>(keep_d.as<ScatterDesc>(), (int)d.size(), total, keep_l.as<int32_t>(),
-                                                static_cast<const T*>(src), static_cast<T*>(dst));
-  QLTG_CUDA(cudaGetLastError());
+  launch_scatter<T>(d, total, keep_l.as<int32_t>(), src, dst, s, keep_d);
 }
 
 }  // namespace
@@ -1238,7 +1364,11 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   for (int g = 0; g < ng; ++g) { jobs[g].v_off = voff; voff += (int64_t)jobs[g].q * jobs[g].q; }
   const size_t eb = sizeof(T);
   DevBuf ws(std::max<int64_t>(1, voff) * eb), keep_g;
-  DevBuf sv(std::max<int64_t>(1, sv_off[ng]) * 8), order(std::max<int64_t>(1, sv_off[ng]) * 4);
+  const int64_t nsv = sv_off[ng];
+  QLTG_CHECK(nsv < ((int64_t)1 << 31), QLTG_ERR_INVALID, "more than 2^31 singular values");
+  DevBuf sv(std::max<int64_t>(1, nsv) * 8), order(std::max<int64_t>(1, nsv) * 4);
+  DevBuf svs(std::max<int64_t>(1, nsv) * 8), sorted_v(std::max<int64_t>(1, nsv) * 8),
+      sorted_g(std::max<int64_t>(1, nsv) * 4);
   DevBuf d_svoff = upload(sv_off, s);
   if (woff) QLTG_CUDA(cudaMemsetAsync(ws.get(), 0, woff * eb, s));
   launch_gather<T>(cd, eoff, t_dev, ws.get(), s, keep_g);
@@ -1365,16 +1495,27 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
         d_pre.as<PrecondJob>(), d_qtiles.as<QjTile>(), (int)qtiles.size(), qbuf.as<T>(), jbuf.as<T>(), ws.as<T>());
     QLTG_CUDA(cudaGetLastError());
     k_svd_finish<T><<<ng, kThreads, 0, s>>>(d_jobs.as<JacobiJob>(), ws.as<T>(), sv.as<double>(),
-                                             d_svoff.as<int64_t>(), order.as<int32_t>());
+                                             d_svoff.as<int64_t>(), order.as<int32_t>(), svs.as<double>());
     QLTG_CUDA(cudaGetLastError());
   }
-  std::vector<double> h_sv(sv_off[ng]);
-  std::vector<int32_t> h_ord(sv_off[ng]);
-  std::vector<int> h_st;
-  if (!h_sv.empty()) {
-    QLTG_CUDA(cudaMemcpyAsync(h_sv.data(), sv.get(), h_sv.size() * 8, cudaMemcpyDeviceToHost, s));
-    QLTG_CUDA(cudaMemcpyAsync(h_ord.data(), order.get(), h_ord.size() * 4, cudaMemcpyDeviceToHost, s));
+  // truncation on the device; only the kept dimension, the error and the kept count of each
+  // group come back (they size the result tensors)
+  const size_t cut_bytes = sizeof(SvCut) + (size_t)ng * 4;
+  DevBuf cutbuf(cut_bytes);
+  QLTG_CUDA(cudaMemsetAsync(cutbuf.get(), 0, cut_bytes, s));
+  SvCut* d_cut = cutbuf.as<SvCut>();
+  int* d_kcnt = reinterpret_cast<int*>(static_cast<char*>(cutbuf.get()) + sizeof(SvCut));
+  if (nsv) {
+    k_sv_place<<<grid_for(nsv), 256, 0, s>>>(svs.as<double>(), d_svoff.as<int64_t>(), ng, sorted_v.as<double>(),
+                                             sorted_g.as<int32_t>(), d_cut);
+    QLTG_CUDA(cudaGetLastError());
   }
+  k_sv_cut<<<1, 256, 0, s>>>(sorted_v.as<double>(), sorted_g.as<int32_t>(), sv.as<double>(), trunc, dmin, dmax, ng,
+                             d_cut, d_kcnt);   // sv (by vector index) is free again: the prefix sums
+  QLTG_CUDA(cudaGetLastError());
+  std::vector<char> h_cut(cut_bytes);
+  QLTG_CUDA(cudaMemcpyAsync(h_cut.data(), cutbuf.get(), cut_bytes, cudaMemcpyDeviceToHost, s));
+  std::vector<int> h_st;
   {
     size_t total_jobs = 0;
     for (int ci = 0; ci < kClasses; ++ci) total_jobs += cls_jobs[ci].size();
@@ -1389,55 +1530,25 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   QLTG_CUDA(cudaStreamSynchronize(s));
   for (int x : h_st) QLTG_CHECK(x >= 0, QLTG_ERR_NOCONV, "one-sided Jacobi did not converge within 60 sweeps");
 
-  // ---- truncation, as the reference (ten_svd.h:281-372) ----------------------------
-  struct SV { double v; int g; int i; double v2; };   // i = rank inside the group (descending)
-  std::vector<SV> info;
-  for (int g = 0; g < ng; ++g)
-    for (int i = 0; i < jobs[g].q; ++i) {
-      const double v = h_sv[sv_off[g] + h_ord[sv_off[g] + i]];
-      if (v != 0.0) info.push_back({v, g, i, v * v});
-    }
-  const int64_t total = (int64_t)info.size();
-  if (total <= dmin) {
-    out.err = 0;
-    out.D = total;
-  } else {
-    std::stable_sort(info.begin(), info.end(), [](const SV& a, const SV& b) { return a.v > b.v; });
-    double tot2 = 0;
-    for (auto& x : info) tot2 += x.v2;
-    const double target = tot2 * (1 - trunc);
-    int64_t kept = dmin;
-    double kept2 = 0;
-    for (int64_t i = 0; i < kept; ++i) kept2 += info[i].v2;
-    while (true) {
-      if (kept2 > target) break;
-      const int64_t nx = kept + 1;
-      if (nx > total) break;
-      const double nx2 = kept2 + info[nx - 1].v2;
-      if (nx > dmax) break;
-      kept = nx;
-      kept2 = nx2;
-    }
-    const double e = 1 - kept2 / tot2;
-    out.err = e > 0 ? e : 0;
-    out.D = kept;
-    info.resize(kept);
-    std::stable_sort(info.begin(), info.end(),
-                     [](const SV& a, const SV& b) { return a.g < b.g || (a.g == b.g && a.i < b.i); });
-  }
-  QLTG_CHECK(!info.empty(), QLTG_ERR_EMPTY_SVD,
+  SvCut hc;
+  std::memcpy(&hc, h_cut.data(), sizeof(SvCut));
+  std::vector<int> kcnt(ng);
+  if (ng) std::memcpy(kcnt.data(), h_cut.data() + sizeof(SvCut), (size_t)ng * 4);
+  out.err = hc.err;
+  out.D = hc.kept;
+  QLTG_CHECK(hc.kept > 0, QLTG_ERR_EMPTY_SVD,
              "SVD failed: empty result. The input tensor has no data blocks compatible with the specified "
              "quantum number divergence (lqndiv).");
-  std::map<int, std::vector<int>> kept_rank;   // group -> kept ranks (ascending)
-  std::map<int, std::vector<double>> kept_val;
-  for (auto& x : info) { kept_rank[x.g].push_back(x.i); kept_val[x.g].push_back(x.v); }
+  std::map<int, int> kept_n;   // group -> kept count (its leading ranks)
+  for (int g = 0; g < ng; ++g)
+    if (kcnt[g] > 0) kept_n[g] = kcnt[g];
 
   // ---- result metadata (reference ten_svd.h:467-582) --------------------------------
   std::vector<int32_t> mid_q;
   std::vector<int64_t> mid_d;
-  for (auto& kv : kept_rank) {
+  for (auto& kv : kept_n) {
     for (auto q : groups[kv.first].mid) mid_q.push_back(q);
-    mid_d.push_back((int64_t)kv.second.size());
+    mid_d.push_back((int64_t)kv.second);
   }
   Meta U = leg_subset(t, 0, ldims), Vt = leg_subset(t, ldims, t.rank), S = leg_subset(t, 0, 0);
   U.rank += 1;
@@ -1451,7 +1562,7 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   S.dims = {mid_d, mid_d};
   std::vector<std::vector<int64_t>> uc, vc, sc;
   int64_t mc = 0;
-  for (auto& kv : kept_rank) {
+  for (auto& kv : kept_n) {
     const Group& G = groups[kv.first];
     sc.push_back({mc, mc});
     for (auto& rk : G.rkeys) { auto c = rk; c.push_back(mc); uc.push_back(c); }
@@ -1466,23 +1577,23 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   out.buf[1].alloc(std::max<int64_t>(1, S.size) * 8);
   out.buf[2].alloc(std::max<int64_t>(1, Vt.size) * eb);
 
-  // ---- scatter U / Vt from the dense factors (one launch each); S from the host -----
+  // ---- scatter U / Vt from the dense factors (one launch each), S's diagonals ---------
   // With M = A (rows >= cols) or A^T (rows < cols) factorised as M = W S G^H (W = Q J in the
   // W region, G = the normalised X in the V region):
   // rows >= cols: U = W and Vt = G^H.
   // rows <  cols: A = conj(G) S W^T: U = conj(G) and Vt = W^T.
+  // The kept vectors of a group are its leading ranks: the column list is the group's
+  // part of the rank order on the device.
   std::vector<ScatterDesc> su, sd;
-  std::vector<int32_t> list;
+  std::vector<SvDiag> sdg;
   int64_t eu = 0, ev = 0;
-  std::vector<double> s_host(S.size, 0.0);
   mc = 0;
-  for (auto& kv : kept_rank) {
+  for (auto& kv : kept_n) {
     const int g = kv.first;
     const Group& G = groups[g];
     const JacobiJob& j = jobs[g];
-    const int kd = (int)kv.second.size();
-    const int32_t lbase = (int32_t)list.size();
-    for (int r : kv.second) list.push_back(h_ord[sv_off[g] + r]);
+    const int kd = kv.second;
+    const int32_t lbase = (int32_t)sv_off[g];
     for (size_t ri = 0; ri < G.rkeys.size(); ++ri) {
       auto c = G.rkeys[ri];
       c.push_back(mc);
@@ -1517,14 +1628,19 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
       ev += (int64_t)d.rows * d.cols;
       sd.push_back(d);
     }
-    const int64_t sb = block_of(S, {mc, mc});
-    for (int i = 0; i < kd; ++i) s_host[S.offsets[sb] + (int64_t)i * kd + i] = kept_val[g][i];
+    sdg.push_back({S.offsets[block_of(S, {mc, mc})], sv_off[g], kd, 0});
     ++mc;
   }
-  DevBuf k1, k2, k3, k4;
-  launch_scatter<T>(su, eu, list, ws.get(), out.buf[0].get(), s, k1, k2);
-  launch_scatter<T>(sd, ev, list, ws.get(), out.buf[2].get(), s, k3, k4);
-  if (S.size) QLTG_CUDA(cudaMemcpyAsync(out.buf[1].get(), s_host.data(), S.size * 8, cudaMemcpyHostToDevice, s));
+  DevBuf k1, k3, k5;
+  launch_scatter<T>(su, eu, order.as<int32_t>(), ws.get(), out.buf[0].get(), s, k1);
+  launch_scatter<T>(sd, ev, order.as<int32_t>(), ws.get(), out.buf[2].get(), s, k3);
+  if (S.size) {
+    QLTG_CUDA(cudaMemsetAsync(out.buf[1].get(), 0, S.size * 8, s));
+    k5 = upload(sdg, s);
+    k_sv_diag<<<(unsigned)std::min<size_t>(sdg.size(), 1024), 128, 0, s>>>(k5.as<SvDiag>(), (int)sdg.size(),
+                                                                         svs.as<double>(), out.buf[1].as<double>());
+    QLTG_CUDA(cudaGetLastError());
+  }
   QLTG_CUDA(cudaStreamSynchronize(s));
   out.t[0] = U;
   out.t[1] = S;
