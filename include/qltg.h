@@ -444,7 +444,8 @@ typedef struct qltg_decomp qltg_decomp;
  * qlten::SVD (tensor_manipulation/ten_decomp/ten_svd.h:244-263): block-matrices grouped by
  * (left flux, right flux) (ten_decomp/ten_decomp_basic.h:68-106), all block-matrices
  * decomposed in one batched one-sided Jacobi launch, truncation keeping from Dmin while
- * the kept weight <= (1 - trunc_err) of the total and <= Dmax (ten_svd.h:281-372),
+ * the kept weight <= (1 - trunc_err) of the total and <= Dmax (ten_svd.h:281-372) - on the
+ * device, over all values in descending order with ties by block-matrix, then rank -,
  * U with a new OUT leg, S = (IN, OUT) diagonal, Vt with a new IN leg (ten_svd.h:467-582).
  * `lqndiv` has qn_ncomp components. Returns QLTG_ERR_EMPTY_SVD when nothing is kept. */
 QLTG_API int qltg_svd(qltg_ctx* ctx, const qltg_tensor_desc* t, const void* t_dev, int32_t ldims,
