@@ -1486,7 +1486,7 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
     cudaEventDestroy(j);
   }
   cudaEventDestroy(fork);
-  for (auto sx : side) cudaStreamDestroy(sx);   // released by the driver once its work is done
+  for (auto sx : side) cudaStreamDestroy(sx);   // freed by CUDA once its queued work is done
   QLTG_CUDA(le);
   // singular values and the right vectors from X; the left vectors W = Q J
   DevBuf d_jobs = upload(xjobs, s);
