@@ -530,12 +530,23 @@ def run_profile_case(case: str, tensors, dev, local: int) -> None:
     """Profiling drivers (one small, fixed piece of work each, for ncu captures): the split GEMM
     of the D=4000 matvec's first (step0) or last (step3) contraction, stacked schedule, run
     twice; three applies of the Config 5 split matvec (fU(1) x U(1) complex, D=6000); Config 3's
-    batched SVD; the stress QR (41 square blocks 10..800)."""
+    batched SVD; the stress QR (41 square blocks 10..800); the three batched permutes of t0
+    (D=4000, 80 MB) measured by --aux, one launch each after t0 is made."""
     import torch
     from tensortoolkit_gb300 import workloads
-    from tensortoolkit_gb300.api import Contract, ContractionPlan, DTensor, QR, SVD
+    from tensortoolkit_gb300.api import Contract, ContractionPlan, DTensor, QR, SVD, TransposePlan
     lenv, psi, mpo1, mpo2, renv = tensors
     dl, dp, d1, d2, dr = dev
+    if case == "permute":
+        t0 = Contract(dl, dp, [[0], [0]])
+        plans = [TransposePlan(t0.meta, perm, local) for perm in ((1, 3, 4, 0, 2), (4, 3, 2, 1, 0), (1, 0, 4, 2, 3))]
+        outs = [DTensor.empty(pl.result, local) for pl in plans]
+        torch.cuda.synchronize()
+        for pl, o in zip(plans, outs):
+            pl.execute(t0, o)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_run": True, "case": case}))
+        return
     if case in ("step0", "step3"):
         if case == "step0":
             p, a, b = ContractionPlan(lenv, psi, [[0], [0]], local), dl, dp
@@ -781,7 +792,7 @@ def main():
     ap.add_argument("--aux-part", choices=["all", "transpose", "svd", "matvec", "proxy", "adapter", "fp64rates"], default="all")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: plan the D=4000 matvec, apply it twice, print nothing else")
-    ap.add_argument("--profile-case", choices=["matvec", "matvec5", "step0", "step3", "svd", "qr"], default="matvec",
+    ap.add_argument("--profile-case", choices=["matvec", "matvec5", "step0", "step3", "svd", "qr", "permute"], default="matvec",
                     help="with --profile: the matvec (default); one of its split-precision GEMM steps "
                          "(stacked schedule, executed twice); Config 3's batched SVD; the stress QR")
     args = ap.parse_args()
