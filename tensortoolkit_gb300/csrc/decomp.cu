@@ -18,6 +18,7 @@
 // back only the kept dimension, the error and the kept count per group, which size the
 // result tensors.
 #include <cooperative_groups.h>
+#include <cub/cub.cuh>
 
 #include <algorithm>
 #include <cstring>
@@ -546,11 +547,11 @@ __global__ void __launch_bounds__(kThreads) k_svd_finish(const JacobiJob* __rest
 
 // ---- truncation on the device, the reference's rule (tensor_manipulation/ten_decomp/
 // ten_svd.h:281-372): all groups' nonzero singular values in descending order (ties by group,
-// then rank: a strict total order, so the result does not depend on how it is sorted), keep
-// Dmin of them, then one more while the kept weight sum s^2 is <= (1 - eps) of the total and
-// the count stays <= Dmax. Each group's values sit in rank order (descending, zeros last), so
-// an entry's place in the global order is a sum of counts:
-//   place(g, i) = i + sum_{h < g} #{s_h >= v} + sum_{h > g} #{s_h > v}.
+// then rank), keep Dmin of them, then one more while the kept weight sum s^2 is <= (1 - eps)
+// of the total and the count stays <= Dmax. The order comes from a stable radix sort of the
+// entries - held group by group in rank order - keyed by the complement of the value's bits
+// (for values >= 0 the bit patterns order like the values, so ascending keys are descending
+// values, equal values keep their group-then-rank order, zeros sort last).
 struct SvCut {
   int64_t kept;    // kept dimension D
   double err;      // truncation error 1 - kept weight / total weight (0 when nothing is cut)
@@ -558,33 +559,29 @@ struct SvCut {
   int32_t pad;
 };
 
-__global__ void __launch_bounds__(256) k_sv_place(const double* __restrict__ svs, const int64_t* __restrict__ sv_off,
-                                                  int ng, double* __restrict__ sorted_v, int32_t* __restrict__ sorted_g,
-                                                  SvCut* __restrict__ cut) {
-  const int64_t n = sv_off[ng];
+__global__ void __launch_bounds__(256) k_sv_keys(const double* __restrict__ svs, int64_t n, uint64_t* __restrict__ key,
+                                                 int32_t* __restrict__ idx, SvCut* __restrict__ cut) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     const double v = svs[e];
-    if (v == 0.0) continue;
-    int lo = 0, hi = ng - 1;   // the group holding entry e: the last one starting at or before e
+    key[e] = v == 0.0 ? ~0ull : ~(uint64_t)__double_as_longlong(v);
+    idx[e] = (int32_t)e;
+    if (v != 0.0) atomicAdd(&cut->nnz, 1);
+  }
+}
+
+// sorted entries -> their values and groups (the group: the last one starting at or before e)
+__global__ void __launch_bounds__(256) k_sv_sorted(const double* __restrict__ svs, const int64_t* __restrict__ sv_off,
+                                                   int ng, const int32_t* __restrict__ idx, int64_t n,
+                                                   double* __restrict__ sorted_v, int32_t* __restrict__ sorted_g) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = idx[j];
+    int lo = 0, hi = ng - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
       if (sv_off[mid] <= e) lo = mid; else hi = mid - 1;
     }
-    const int g = lo;
-    int64_t place = e - sv_off[g];
-    for (int h = 0; h < ng; ++h) {
-      if (h == g) continue;
-      const double* sh = svs + sv_off[h];
-      int a = 0, b = (int)(sv_off[h + 1] - sv_off[h]);   // first entry of h that comes after v
-      while (a < b) {
-        const int m = (a + b) >> 1;
-        if (h < g ? sh[m] >= v : sh[m] > v) a = m + 1; else b = m;
-      }
-      place += a;
-    }
-    sorted_v[place] = v;   // place <= n - 1: at most (size_g - 1) + the other groups' sizes
-    sorted_g[place] = g;
-    atomicAdd(&cut->nnz, 1);
+    sorted_v[j] = svs[e];
+    sorted_g[j] = lo;
   }
 }
 
@@ -642,7 +639,6 @@ __global__ void __launch_bounds__(256) k_sv_cut(const double* __restrict__ sorte
     cut->kept = kept;
     cut->err = err;
   }
-  // (a NaN among the values leaves places unfilled: the group index is checked)
   for (int64_t j = threadIdx.x; j < kept; j += blockDim.x) {
     const int g = sorted_g[j];
     if (g >= 0 && g < ng) atomicAdd(kcnt + g, 1);
@@ -1368,7 +1364,9 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   QLTG_CHECK(nsv < ((int64_t)1 << 31), QLTG_ERR_INVALID, "more than 2^31 singular values");
   DevBuf sv(std::max<int64_t>(1, nsv) * 8), order(std::max<int64_t>(1, nsv) * 4);
   DevBuf svs(std::max<int64_t>(1, nsv) * 8), sorted_v(std::max<int64_t>(1, nsv) * 8),
-      sorted_g(std::max<int64_t>(1, nsv) * 4);
+      sorted_g(std::max<int64_t>(1, nsv) * 4), sv_key(std::max<int64_t>(1, nsv) * 8),
+      sv_key_s(std::max<int64_t>(1, nsv) * 8), sv_idx(std::max<int64_t>(1, nsv) * 4),
+      sv_idx_s(std::max<int64_t>(1, nsv) * 4);
   DevBuf d_svoff = upload(sv_off, s);
   if (woff) QLTG_CUDA(cudaMemsetAsync(ws.get(), 0, woff * eb, s));
   launch_gather<T>(cd, eoff, t_dev, ws.get(), s, keep_g);
@@ -1505,9 +1503,18 @@ void svd_impl(const Meta& t, const void* t_dev, int ldims, const std::vector<int
   QLTG_CUDA(cudaMemsetAsync(cutbuf.get(), 0, cut_bytes, s));
   SvCut* d_cut = cutbuf.as<SvCut>();
   int* d_kcnt = reinterpret_cast<int*>(static_cast<char*>(cutbuf.get()) + sizeof(SvCut));
+  DevBuf sort_tmp;
   if (nsv) {
-    k_sv_place<<<grid_for(nsv), 256, 0, s>>>(svs.as<double>(), d_svoff.as<int64_t>(), ng, sorted_v.as<double>(),
-                                             sorted_g.as<int32_t>(), d_cut);
+    k_sv_keys<<<grid_for(nsv), 256, 0, s>>>(svs.as<double>(), nsv, sv_key.as<uint64_t>(), sv_idx.as<int32_t>(), d_cut);
+    QLTG_CUDA(cudaGetLastError());
+    size_t tmp_bytes = 0;
+    QLTG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, sv_key.as<uint64_t>(), sv_key_s.as<uint64_t>(),
+                                              sv_idx.as<int32_t>(), sv_idx_s.as<int32_t>(), (int)nsv, 0, 64, s));
+    sort_tmp.alloc(std::max<size_t>(tmp_bytes, 16));
+    QLTG_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp.get(), tmp_bytes, sv_key.as<uint64_t>(), sv_key_s.as<uint64_t>(),
+                                              sv_idx.as<int32_t>(), sv_idx_s.as<int32_t>(), (int)nsv, 0, 64, s));
+    k_sv_sorted<<<grid_for(nsv), 256, 0, s>>>(svs.as<double>(), d_svoff.as<int64_t>(), ng, sv_idx_s.as<int32_t>(), nsv,
+                                              sorted_v.as<double>(), sorted_g.as<int32_t>());
     QLTG_CUDA(cudaGetLastError());
   }
   k_sv_cut<<<1, 256, 0, s>>>(sorted_v.as<double>(), sorted_g.as<int32_t>(), sv.as<double>(), trunc, dmin, dmax, ng,

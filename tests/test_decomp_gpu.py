@@ -62,6 +62,30 @@ def test_svd_stress_vs_oracle(gpu):
     check_svd(t, u.to_host(), s.to_host(), vt.to_host(), err, Dk, ru, rs, rvt, rerr, rD, 1)
 
 
+@pytest.mark.parametrize("D,trunc,dmax", [(1200, 1e-12, 100000), (3000, 1e-8, 2000)])
+def test_svd_complex_fermionic_vs_oracle(gpu, D, trunc, dmax):
+    """The complex128 fU(1) x U(1) psi of the Hubbard workload (5544 blocks, a thousand and
+    more block-matrices): the complex Jacobi path, whole and cut at Dmax."""
+    _, psi, *_ = workloads.hubbard(D)
+    div = [0] * psi.ncomp
+    ru, rs, rvt, rerr, rD = oracle.svd(psi, 2, div, trunc, 1, dmax)
+    u, s, vt, err, Dk = SVD(DTensor.from_host(psi), 2, div, trunc, 1, dmax)
+    check_svd(psi, u.to_host(), s.to_host(), vt.to_host(), err, Dk, ru, rs, rvt, rerr, rD, 2)
+
+
+def test_qr_complex_fermionic_vs_oracle(gpu):
+    """Complex Householder (LAPACK's zlarfg convention: real diagonal of R), so Q and R
+    compare directly."""
+    _, psi, *_ = workloads.hubbard(3000)
+    div = [0] * psi.ncomp
+    rq, rr = oracle.qr(psi, 2, div)
+    q, r = QR(DTensor.from_host(psi), 2, div)
+    q, r = q.to_host(), r.to_host()
+    assert same_topology(q, rq) and same_topology(r, rr)
+    assert rel_frob(q.data, rq.data) <= 1e-11
+    assert rel_frob(r.data, rr.data) <= 1e-11
+
+
 def test_qr_psi_vs_oracle(gpu):
     lenv, psi, *_ = workloads.heisenberg(2000, 20, 6.0, 5)
     rq, rr = oracle.qr(psi, 2, [0])
